@@ -1,0 +1,64 @@
+"""Regenerates tests/golden/reference_fixtures.json from the MolDS test suite.
+
+Reads the reference's own golden input/output pairs (test/<case>.in and
+test/<case>.dat of the MolDS tree, registered in test/Test_Of_MolDS.rb) and
+keeps, per case, the input text and the printed values that pin the NDDO SCF
+path: the per-iteration RMS density and DIIS error, MO energies, electronic
+energy (incl. core repulsion), core repulsion, Mulliken charges and, for MNDO,
+the heat of formation.  MolDS prints these with %e (7 significant digits,
+src/cndo/Cndo2.cpp:1087-1089, 1193-1198), so they pin results to ~5e-7 relative.
+
+Usage:  python tests/golden/make_golden.py [/path/to/molds/test]
+"""
+import json
+import os
+import re
+import sys
+
+CASES = [f"{m}_{t}" for m in ("ch4", "c2h6", "ch3f", "ch3cl") for t in ("mndo", "am1", "pm3")]
+# SCF blocks printed before a frequency run: the first SCF of each pins PM3 for
+# O (with the H-O core-core rule) and for C=C.
+EXTRA = ["h2o_pm3_freq_num_proj_s1", "c2h4_pm3_freq_num_proj"]
+
+
+def parse_dat(text, natoms):
+    """Values of the first SCF block (frequency runs print several)."""
+    start = text.find("-SCF  **********")
+    body = text[start:]
+    end = body.find("**********  DONE:")
+    body = body[:end] if end >= 0 else body
+    trace = []
+    for a, b, c, rest in re.findall(r"SCF iter (\d+)\t(\S+)\t(\S+)([^\n]*)", body):
+        trace.append({"iter": int(a), "rms": float(b), "diis_error": float(c),
+                      "diis_on": rest.strip().startswith("on")})
+    mo = [float(x) for x in re.findall(r"Energy of MO:\t\d+\t\S+\t(\S+)", body)]
+    e = float(re.search(r"Electronic energy\(SCF\):\t(\S+)", body).group(1))
+    ec = float(re.search(r"Core repulsion energy:\t(\S+)", body).group(1))
+    q = [float(x) for x in re.findall(r"Mulliken charge\(SCF\):\t0\t\d+\t\S+\t\S+\t(\S+)", body)][:natoms]
+    hof = re.search(r"Heats of formation:\t(\S+)", body)
+    out = {"trace": trace, "mo_energies": mo, "energy": e, "core_repulsion": ec,
+           "mulliken": q}
+    if hof:
+        out["heat_of_formation"] = float(hof.group(1))
+    return out
+
+
+def main():
+    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test"
+    fixtures = []
+    for name in CASES + EXTRA:
+        inp = open(os.path.join(src, name + ".in")).read()
+        dat = open(os.path.join(src, name + ".dat")).read()
+        natoms = int(re.search(r"Total number of atoms: (\d+)", dat).group(1))
+        nao = int(re.search(r"Total number of valence AOs: (\d+)", dat).group(1))
+        rec = {"name": name, "input": inp, "natoms": natoms, "n_ao": nao}
+        rec.update(parse_dat(dat, natoms))
+        fixtures.append(rec)
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "reference_fixtures.json"), "w") as f:
+        json.dump({"source": "MolDS test/*.in, test/*.dat", "cases": fixtures}, f, indent=1)
+    print(f"wrote {len(fixtures)} cases")
+
+
+if __name__ == "__main__":
+    main()
