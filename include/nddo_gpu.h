@@ -1,0 +1,114 @@
+/*
+ * C ABI of the GB300 NDDO (MNDO / AM1 / PM3) closed-shell SCF.
+ *
+ * Plain C types only: a MolDS build (or any FFI) binds these entry points in
+ * place of its CPU Fock build and LAPACK eigensolver on the SCF path.  Each
+ * declaration names the MolDS interface it stands in for (paths relative to
+ * the MolDS source tree).
+ *
+ * Conventions
+ *   - Coordinates are in bohr (MolDS converts Angstrom input at parse time,
+ *     src/base/InputParser.cpp:545-547).
+ *   - Orbital order per atom is s, py, pz, px (src/base/Enums.h:98-108).
+ *   - Return codes: 0 = OK, 1 = SCF not converged, negative = error; the text
+ *     of the last error is returned by nddo_last_error().
+ *   - Buffers are caller-owned; inputs are copied in, results copied out.
+ *   - One context per host thread.
+ */
+#ifndef MOLDS_GB300_NDDO_GPU_H
+#define MOLDS_GB300_NDDO_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nddo_ctx nddo_ctx;
+
+enum { NDDO_THEORY_MNDO = 0, NDDO_THEORY_AM1 = 1, NDDO_THEORY_PM3 = 2 };
+enum { NDDO_PRECISION_FP64 = 0, NDDO_PRECISION_MIXED = 1 };
+enum {
+  NDDO_OK = 0,
+  NDDO_NOT_CONVERGED = 1,
+  NDDO_ERR_ARGUMENT = -1,
+  NDDO_ERR_CUDA = -2,
+  NDDO_ERR_BUDGET = -3,
+  NDDO_ERR_STATE = -4
+};
+enum { NDDO_STATUS_ACTIVE = 0, NDDO_STATUS_CONVERGED = 1, NDDO_STATUS_NOT_CONVERGED = 2 };
+
+/* SCF block of the MolDS input (src/base/InputParser.cpp:646-734) plus the
+ * precision choice of this implementation. */
+typedef struct {
+  int max_iter;                /* max_iter                                  */
+  double rms_density;          /* rms_density                               */
+  double damping_thresh;       /* damping_thresh                            */
+  double damping_weight;       /* damping_weight                            */
+  int diis_num_error_vect;     /* diis_num_error_vect (0..8)                */
+  double diis_start_error;     /* diis_start_error                          */
+  double diis_end_error;       /* diis_end_error                            */
+  int precision;               /* NDDO_PRECISION_FP64 or NDDO_PRECISION_MIXED */
+  double fp64_switch_error;    /* mixed: FP64 phase once the DIIS error is below this */
+} nddo_scf_params;
+
+typedef struct {
+  int status;                  /* NDDO_STATUS_*                              */
+  int iterations;              /* SCF iterations run (MolDS prints 0..iterations-1) */
+  double energy;               /* electronic energy incl. core repulsion [Eh] */
+  double core_repulsion;       /* [Eh]                                       */
+  double heat_of_formation;    /* [Eh]; meaningful for MNDO only             */
+  double final_rms;            /* last RMS density change                    */
+  double final_diis_error;     /* last DIIS error (max |P_new - P_old|)      */
+} nddo_scf_result;
+
+/* Defaults of src/base/Parameters.cpp:133-139 (precision = FP64). */
+void nddo_default_params(nddo_scf_params* p);
+
+/* Engine on one GPU.  hbm_budget_bytes = 0 means no limit; MolDS's analogue is
+ * the MEMORY limit_heap check (src/base/MallocerFreer.cpp:62-72). */
+int nddo_create(int device, size_t hbm_budget_bytes, nddo_ctx** out);
+void nddo_destroy(nddo_ctx* ctx);
+const char* nddo_last_error(const nddo_ctx* ctx);
+
+/* ElectronicStructure::SetMolecule (src/base/ElectronicStructure.h:27,
+ * Mndo::SetMolecule src/mndo/Mndo.cpp:110-138).  Validates the elements and
+ * the electron count (odd -> error, src/cndo/Cndo2.cpp:351-357) and computes
+ * the one-time pair integrals, overlap and core-core terms. */
+int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* atomic_numbers, const double* xyz_bohr);
+int nddo_num_aos(const nddo_ctx* ctx);
+int nddo_num_atoms(const nddo_ctx* ctx);
+
+/* ElectronicStructure::DoSCF(bool requiresGuess) (src/base/ElectronicStructure.h:28,
+ * Cndo2::DoSCF src/cndo/Cndo2.cpp:585-729).  Returns NDDO_NOT_CONVERGED when
+ * max_iter is reached (MolDS throws "SCF did not met convergence criterion"). */
+int nddo_scf(nddo_ctx* ctx, const nddo_scf_params* params, int requires_guess, nddo_scf_result* result);
+
+/* Getters after nddo_scf (src/base/ElectronicStructure.h:30-39). */
+int nddo_get_energies_mo(nddo_ctx* ctx, double* out_n);          /* GetEnergiesMO: N ascending      */
+int nddo_get_fock_matrix(nddo_ctx* ctx, double* out_nn);         /* GetFockMatrix: eigenvector rows */
+int nddo_get_density(nddo_ctx* ctx, double* out_nn);             /* orbital electron population P   */
+int nddo_get_mulliken(nddo_ctx* ctx, double* out_natoms);        /* Mulliken charges (Cndo2.cpp:1187-1199) */
+int nddo_get_core_hamiltonian(nddo_ctx* ctx, double* out_nn);    /* H = F(P = 0) (Cndo2.cpp:1359-1367) */
+/* Per-iteration log of Cndo2::SatisfyConvergenceCriterion (Cndo2.cpp:1505-1510). */
+int nddo_get_trace(nddo_ctx* ctx, int max_entries, double* rms, double* diis_error, int* diis_on, int* damp_on);
+/* Packed space-frame (mu nu|la si) blocks of all atom pairs a < b, row-major
+ * pair order; 10x10 (sp-sp), 10x1, 1x10 or 1x1 doubles per pair.  With
+ * out == NULL only *count is set.  Replaces the A x A x 4^4 twoElecsTwoAtomCores
+ * store of Mndo::CalcTwoElecsTwoAtomCores (src/mndo/Mndo.cpp:3703-3820). */
+int nddo_get_pair_blocks(nddo_ctx* ctx, double* out, size_t* count);
+
+/* Many independent molecules in one batched, device-resident SCF: the
+ * repeated-DoSCF callers (RPMD beads, src/rpmd/RPMD.cpp:78-84; MD/MC/optimiser
+ * steps) and throughput runs.  Molecule i has n_atoms[i] atoms; Z and xyz are
+ * concatenated over molecules.  results has n_mol entries, charges has
+ * sum(n_atoms) entries (may be NULL). */
+int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, const int* atomic_numbers,
+                   const double* xyz_bohr, const nddo_scf_params* params, nddo_scf_result* results,
+                   double* charges);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOLDS_GB300_NDDO_GPU_H */

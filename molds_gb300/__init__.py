@@ -1,0 +1,279 @@
+"""GB300-native closed-shell NDDO (MNDO / AM1 / PM3) SCF.
+
+The compute path is the CUDA library ``molds_gb300/_build/libnddo_gb300.so``
+(sm_103a), reached through its C ABI (``include/nddo_gpu.h``).  This module is
+the Python mirror of MolDS's ``ElectronicStructure`` interface
+(src/base/ElectronicStructure.h:23-53) on top of that ABI.  There is no CPU
+fallback: when the library is missing the import of the engine fails with an
+error telling how to build it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .inputfile import (ANG2AU, THEORIES, THEORY_NAMES, InputError, InputFile, Molecule, SCFParams,  # noqa: F401
+                        parse)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libnddo_gb300.so")
+
+NDDO_OK, NDDO_NOT_CONVERGED = 0, 1
+ERR_ARGUMENT, ERR_CUDA, ERR_BUDGET, ERR_STATE = -1, -2, -3, -4
+STATUS_CONVERGED = 1
+
+
+class NddoError(RuntimeError):
+    """Error raised across the C ABI (MolDS raises MolDSException)."""
+
+    def __init__(self, code, message):
+        super().__init__(message)
+        self.code = code
+
+
+class SCFNotConverged(NddoError):
+    pass
+
+
+class BudgetExceeded(NddoError):
+    pass
+
+
+class ScfParamsC(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("rms_density", ctypes.c_double),
+                ("damping_thresh", ctypes.c_double), ("damping_weight", ctypes.c_double),
+                ("diis_num_error_vect", ctypes.c_int), ("diis_start_error", ctypes.c_double),
+                ("diis_end_error", ctypes.c_double), ("precision", ctypes.c_int),
+                ("fp64_switch_error", ctypes.c_double)]
+
+
+class ScfResultC(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("energy", ctypes.c_double),
+                ("core_repulsion", ctypes.c_double), ("heat_of_formation", ctypes.c_double),
+                ("final_rms", ctypes.c_double), ("final_diis_error", ctypes.c_double)]
+
+
+# every entry point of include/nddo_gpu.h with its argument types
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+_CTX = ctypes.c_void_p
+SIGNATURES = {
+    "nddo_default_params": (None, [ctypes.POINTER(ScfParamsC)]),
+    "nddo_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+    "nddo_destroy": (None, [_CTX]),
+    "nddo_last_error": (ctypes.c_char_p, [_CTX]),
+    "nddo_set_molecule": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _DP]),
+    "nddo_num_aos": (ctypes.c_int, [_CTX]),
+    "nddo_num_atoms": (ctypes.c_int, [_CTX]),
+    "nddo_scf": (ctypes.c_int, [_CTX, ctypes.POINTER(ScfParamsC), ctypes.c_int, ctypes.POINTER(ScfResultC)]),
+    "nddo_get_energies_mo": (ctypes.c_int, [_CTX, _DP]),
+    "nddo_get_fock_matrix": (ctypes.c_int, [_CTX, _DP]),
+    "nddo_get_density": (ctypes.c_int, [_CTX, _DP]),
+    "nddo_get_mulliken": (ctypes.c_int, [_CTX, _DP]),
+    "nddo_get_core_hamiltonian": (ctypes.c_int, [_CTX, _DP]),
+    "nddo_get_trace": (ctypes.c_int, [_CTX, ctypes.c_int, _DP, _DP, _IP, _IP]),
+    "nddo_get_pair_blocks": (ctypes.c_int, [_CTX, _DP, ctypes.POINTER(ctypes.c_size_t)]),
+    "nddo_batch_scf": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, ctypes.POINTER(ScfParamsC),
+                                      ctypes.POINTER(ScfResultC), _DP]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m molds_gb300.build` "
+                          "(or __graft_entry__.build()); there is no CPU fallback")
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP)
+
+
+def to_c_params(p: SCFParams) -> ScfParamsC:
+    c = ScfParamsC()
+    c.max_iter = int(p.max_iter)
+    c.rms_density = float(p.rms_density)
+    c.damping_thresh = float(p.damping_thresh)
+    c.damping_weight = float(p.damping_weight)
+    c.diis_num_error_vect = int(p.diis_num_error_vect)
+    c.diis_start_error = float(p.diis_start_error)
+    c.diis_end_error = float(p.diis_end_error)
+    c.precision = 1 if str(p.precision).lower() == "mixed" else 0
+    c.fp64_switch_error = float(p.fp64_switch_error)
+    return c
+
+
+class Context:
+    """An engine on one GPU (nddo_create / nddo_destroy)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.nddo_create(device, hbm_budget_bytes, ctypes.byref(h))
+        self.h = h
+        if rc != NDDO_OK:
+            msg = self.lib.nddo_last_error(h).decode() if h.value else "nddo_create failed"
+            if h.value:
+                self.lib.nddo_destroy(h)
+            self.h = None
+            raise NddoError(rc, msg)
+
+    def check(self, rc):
+        if rc >= 0 and rc != NDDO_NOT_CONVERGED:
+            return rc
+        msg = self.lib.nddo_last_error(self.h).decode()
+        if rc == NDDO_NOT_CONVERGED:
+            raise SCFNotConverged(rc, msg)
+        if rc == ERR_BUDGET:
+            raise BudgetExceeded(rc, msg)
+        raise NddoError(rc, msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nddo_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ElectronicStructure:
+    """MolDS ElectronicStructure for MNDO / AM1 / PM3 on one GB300.
+
+    Same call sequence as the reference (src/base/MolDS.cpp:165-178):
+    SetMolecule(molecule) once, DoSCF(requiresGuess) any number of times, then
+    the getters.  Errors are raised as NddoError (SCFNotConverged when
+    max_iter is reached, as Cndo2::DoSCF throws at src/cndo/Cndo2.cpp:700-704).
+    """
+
+    def __init__(self, theory, params: SCFParams | None = None, device: int = 0, hbm_budget_bytes: int = 0,
+                 context: Context | None = None):
+        self.theory = THEORIES[theory.lower()] if isinstance(theory, str) else int(theory)
+        self.params = params or SCFParams()
+        self.ctx = context or Context(device, hbm_budget_bytes)
+        self.molecule = None
+        self.result = None
+
+    def GetTheoryType(self):
+        return THEORY_NAMES[self.theory]
+
+    def SetMolecule(self, molecule: Molecule):
+        Z = np.ascontiguousarray(molecule.Z, dtype=np.int32)
+        xyz = np.ascontiguousarray(molecule.xyz, dtype=np.float64).reshape(-1, 3)
+        self.ctx.check(self.ctx.lib.nddo_set_molecule(self.ctx.h, self.theory, int(Z.shape[0]), _ip(Z), _dp(xyz)))
+        self.molecule = molecule
+        self.n = self.ctx.lib.nddo_num_aos(self.ctx.h)
+        self.result = None
+
+    def DoSCF(self, requiresGuess: bool = True, params: SCFParams | None = None):
+        p = to_c_params(params or self.params)
+        r = ScfResultC()
+        rc = self.ctx.lib.nddo_scf(self.ctx.h, ctypes.byref(p), 1 if requiresGuess else 0, ctypes.byref(r))
+        self.result = r
+        self.ctx.check(rc)
+        return r
+
+    def _vec(self, fn, n):
+        out = np.zeros(n)
+        self.ctx.check(fn(self.ctx.h, _dp(out)))
+        return out
+
+    def GetElectronicEnergy(self, elecState: int = 0) -> float:
+        if elecState != 0:
+            raise NddoError(ERR_ARGUMENT, "only the ground state is computed on this path")
+        return self.result.energy
+
+    def GetCoreRepulsionEnergy(self) -> float:
+        return self.result.core_repulsion
+
+    def GetHeatsFormation(self) -> float:
+        return self.result.heat_of_formation
+
+    def GetIterations(self) -> int:
+        return self.result.iterations
+
+    def GetEnergiesMO(self) -> np.ndarray:
+        return self._vec(self.ctx.lib.nddo_get_energies_mo, self.n)
+
+    def GetFockMatrix(self) -> np.ndarray:
+        """After DoSCF: eigenvectors as rows (as MolDS returns them)."""
+        return self._vec(self.ctx.lib.nddo_get_fock_matrix, self.n * self.n).reshape(self.n, self.n)
+
+    def GetOrbitalElectronPopulation(self) -> np.ndarray:
+        return self._vec(self.ctx.lib.nddo_get_density, self.n * self.n).reshape(self.n, self.n)
+
+    def GetMullikenCharges(self) -> np.ndarray:
+        return self._vec(self.ctx.lib.nddo_get_mulliken, self.molecule.natoms)
+
+    def GetCoreHamiltonian(self) -> np.ndarray:
+        return self._vec(self.ctx.lib.nddo_get_core_hamiltonian, self.n * self.n).reshape(self.n, self.n)
+
+    def GetPairBlocks(self) -> np.ndarray:
+        cnt = ctypes.c_size_t()
+        self.ctx.check(self.ctx.lib.nddo_get_pair_blocks(self.ctx.h, None, ctypes.byref(cnt)))
+        out = np.zeros(cnt.value)
+        self.ctx.check(self.ctx.lib.nddo_get_pair_blocks(self.ctx.h, _dp(out), ctypes.byref(cnt)))
+        return out
+
+    def GetTrace(self):
+        n = self.result.iterations
+        rms, de = np.zeros(n), np.zeros(n)
+        on, dm = np.zeros(n, dtype=np.int32), np.zeros(n, dtype=np.int32)
+        k = self.ctx.check(self.ctx.lib.nddo_get_trace(self.ctx.h, n, _dp(rms), _dp(de), _ip(on), _ip(dm)))
+        return [(i, float(rms[i]), float(de[i]), bool(on[i]), bool(dm[i])) for i in range(k)]
+
+
+class ElectronicStructureFactory:
+    """ElectronicStructureFactory::Create (src/base/factories/ElectronicStructureFactory.cpp:58-98)
+    for the theories this package implements."""
+
+    @staticmethod
+    def Create(theory, **kw) -> ElectronicStructure:
+        name = theory.lower() if isinstance(theory, str) else THEORY_NAMES[int(theory)].lower()
+        if name not in THEORIES:
+            raise NddoError(ERR_ARGUMENT, f"theory {theory} is not implemented on the GB300 path")
+        return ElectronicStructure(name, **kw)
+
+
+def batch_scf(theory, molecules, params: SCFParams | None = None, context: Context | None = None):
+    """Batched SCF of many molecules in one device-resident launch sequence.
+
+    Returns (results, charges): a list of dicts and a list of per-molecule
+    Mulliken charge arrays."""
+    ctx = context or Context()
+    th = THEORIES[theory.lower()] if isinstance(theory, str) else int(theory)
+    nat = np.array([m.natoms for m in molecules], dtype=np.int32)
+    Z = np.ascontiguousarray(np.concatenate([m.Z for m in molecules]), dtype=np.int32)
+    xyz = np.ascontiguousarray(np.concatenate([np.asarray(m.xyz).reshape(-1, 3) for m in molecules]))
+    res = (ScfResultC * len(molecules))()
+    ch = np.zeros(int(nat.sum()))
+    p = to_c_params(params or SCFParams())
+    rc = ctx.lib.nddo_batch_scf(ctx.h, th, len(molecules), _ip(nat), _ip(Z), _dp(xyz), ctypes.byref(p), res, _dp(ch))
+    if rc < 0:
+        ctx.check(rc)
+    out = [dict(status=r.status, iterations=r.iterations, energy=r.energy, core_repulsion=r.core_repulsion,
+                heat_of_formation=r.heat_of_formation, final_rms=r.final_rms,
+                final_diis_error=r.final_diis_error) for r in res]
+    offs = np.concatenate([[0], np.cumsum(nat)])
+    return out, [ch[offs[i]:offs[i + 1]] for i in range(len(molecules))]

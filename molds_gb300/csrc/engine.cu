@@ -1,0 +1,483 @@
+// Host engine of the batched NDDO SCF.
+//
+// The SCF of every molecule in a batch follows MolDS Cndo2::DoSCF
+// (src/cndo/Cndo2.cpp:585-729) step for step:
+//   iteration:  P_old <- P;  F <- guess Fock (iteration 0) or H + G(P);
+//               diagonalise F;  P <- 2 C_occ^T C_occ;  RMS test;  DIIS;  damping
+//   after convergence:  F(P), H  ->  E = 1/2 sum P (F + H) + E_core, Mulliken charges.
+// Each step is one launch over all active molecules of the batch; a converged
+// molecule drops out of every later launch by its own state flag.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+
+#include "nddo_tables.h"
+
+namespace nddo {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+static T* dalloc(size_t count, size_t* total) {
+  T* p = nullptr;
+  if (count == 0) count = 1;
+  cuda_check(cudaMalloc(&p, count * sizeof(T)), "cudaMalloc");
+  *total += count * sizeof(T);
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+__global__ void init_state_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, int n,
+                                  MolState* __restrict__ st, double* __restrict__ C, double* __restrict__ P,
+                                  int requires_guess, int reset_density) {
+  const int m = list[blockIdx.x];
+  const DevMol mol = mols[m];
+  const long long n2 = (long long)mol.nao * mol.nao;
+  if (threadIdx.x == 0) {
+    MolState s;
+    memset(&s, 0, sizeof(s));
+    s.status = kActive;
+    s.requires_guess = requires_guess;
+    s.ecore = st[m].ecore;   // computed by the integral pass
+    st[m] = s;
+  }
+  for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
+    const long long r = i / mol.nao, c = i % mol.nao;
+    C[mol.mat0 + i] = (r == c) ? 1.0 : 0.0;
+    if (reset_density) P[mol.mat0 + i] = 0.0;
+  }
+}
+
+__global__ void count_active_kernel(const int* __restrict__ list, int n, const MolState* __restrict__ st,
+                                    int* __restrict__ out) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  int c = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) c += (st[list[i]].status == kActive);
+  atomicAdd(&cnt, c);
+  __syncthreads();
+  if (threadIdx.x == 0) *out = cnt;
+}
+
+// ---------------------------------------------------------------------------
+Engine::Engine(int device) : device_(device) {
+  cuda_check(cudaSetDevice(device), "cudaSetDevice");
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  static EriTable eri;
+  static OverlapTable ovt;
+  static bool built = false;
+  if (!built) { build_eri_table(&eri); build_overlap_table(&ovt); built = true; }
+  cuda_check(cudaMalloc(&d_eri_, sizeof(EriTable)), "cudaMalloc eri");
+  cuda_check(cudaMalloc(&d_ovt_, sizeof(OverlapTable)), "cudaMalloc ovt");
+  cuda_check(cudaMemcpyAsync(d_eri_, &eri, sizeof(EriTable), cudaMemcpyHostToDevice, stream_), "copy eri");
+  cuda_check(cudaMemcpyAsync(d_ovt_, &ovt, sizeof(OverlapTable), cudaMemcpyHostToDevice, stream_), "copy ovt");
+  nddo_atom_params params[kNumParamSlots];
+  std::memset(params, 0, sizeof(params));
+  static const int zs[NDDO_NUM_ELEMENTS] = {1, 6, 7, 8, 9, 16, 17};
+  for (int t = 0; t < NDDO_NUM_THEORIES; ++t)
+    for (int e = 0; e < NDDO_NUM_ELEMENTS; ++e) nddo_fill_atom_params(t, zs[e], &params[t * NDDO_NUM_ELEMENTS + e]);
+  upload_params(params, stream_);
+  cuda_check(cudaStreamSynchronize(stream_), "engine init");
+}
+
+Engine::~Engine() {
+  cudaFree(d_eri_);
+  cudaFree(d_ovt_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+// ---------------------------------------------------------------------------
+Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
+    : eng_(eng), stream_(eng->stream()), diis_m_(diis_m) {
+  if (diis_m_ < 0 || diis_m_ > kMaxDiis) throw std::invalid_argument("diis_num_error_vect out of range (0..8)");
+  if (mols.empty()) throw std::invalid_argument("empty batch");
+  long long mat = 0, vec = 0;
+  for (size_t m = 0; m < mols.size(); ++m) {
+    const MoleculeInput& in = mols[m];
+    const int na = (int)in.Z.size();
+    if (na < 1) throw std::invalid_argument("molecule without atoms");
+    if ((int)in.xyz.size() != 3 * na) throw std::invalid_argument("coordinate count does not match atom count");
+    if (in.theory < 0 || in.theory >= NDDO_NUM_THEORIES) throw std::invalid_argument("unknown theory");
+    DevMol dm;
+    std::memset(&dm, 0, sizeof(dm));
+    dm.natoms = na;
+    dm.theory = in.theory;
+    dm.atom0 = (int)h_atoms.size();
+    dm.pair0 = (int)h_pairs.size();
+    int ao = 0, nelec = 0;
+    for (int a = 0; a < na; ++a) {
+      const int e = nddo_element_index(in.Z[a]);
+      if (e < 0) throw std::invalid_argument("element " + std::to_string(in.Z[a]) + " has no NDDO parameters");
+      for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(in.xyz[3 * a + k])) throw std::invalid_argument("non-finite coordinate");
+      DevAtom at;
+      at.x = in.xyz[3 * a]; at.y = in.xyz[3 * a + 1]; at.z = in.xyz[3 * a + 2];
+      at.pidx = in.theory * NDDO_NUM_ELEMENTS + e;
+      at.ao0 = ao;
+      at.nao = nddo_elements[e].n_ao;
+      at.mol = (int)m;
+      ao += at.nao;
+      nelec += nddo_elements[e].core_charge;
+      h_atoms.push_back(at);
+    }
+    if (nelec % 2) throw std::invalid_argument("Total number of valence electrons is odd. totalNumberValenceElectrons=" + std::to_string(nelec));
+    dm.nao = ao;
+    dm.nocc = nelec / 2;
+    for (int a = 0; a < na; ++a)
+      for (int b = a + 1; b < na; ++b) {
+        const DevAtom& A = h_atoms[dm.atom0 + a];
+        const DevAtom& B = h_atoms[dm.atom0 + b];
+        const double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+        if (dx == 0.0 && dy == 0.0 && dz == 0.0) throw std::invalid_argument("two atoms at the same position");
+        DevPair p;
+        p.a = dm.atom0 + a; p.b = dm.atom0 + b; p.mol = (int)m; p.pad = 0;
+        p.blk = blk_total_;
+        blk_total_ += (long long)(A.nao == 4 ? 10 : 1) * (B.nao == 4 ? 10 : 1);
+        h_pairs.push_back(p);
+      }
+    dm.npairs = (int)h_pairs.size() - dm.pair0;
+    dm.mat0 = mat;
+    dm.vec0 = vec;
+    mat += ((long long)ao * ao + 31) / 32 * 32;
+    vec += ((long long)ao + 31) / 32 * 32;
+    max_n_ = std::max(max_n_, ao);
+    h_mols.push_back(dm);
+  }
+  mat_total_ = mat;
+  vec_total_ = vec;
+  const int nm = (int)h_mols.size();
+  d_atoms = dalloc<DevAtom>(h_atoms.size(), &bytes_);
+  d_pairs = dalloc<DevPair>(h_pairs.size(), &bytes_);
+  d_mols = dalloc<DevMol>(nm, &bytes_);
+  d_list = dalloc<int>(nm, &bytes_);
+  d_blocks = dalloc<double>(blk_total_, &bytes_);
+  d_ecore_pair = dalloc<double>(h_pairs.size(), &bytes_);
+  d_H = dalloc<double>(mat, &bytes_);
+  d_F = dalloc<double>(mat, &bytes_);
+  d_P = dalloc<double>(mat, &bytes_);
+  d_Pold = dalloc<double>(mat, &bytes_);
+  d_C = dalloc<double>(mat, &bytes_);
+  d_eps = dalloc<double>(vec, &bytes_);
+  d_hist_dens = dalloc<double>((size_t)std::max(diis_m_, 1) * mat, &bytes_);
+  d_hist_err = dalloc<double>((size_t)std::max(diis_m_, 1) * mat, &bytes_);
+  d_G32 = dalloc<float>(mat, &bytes_);
+  d_T32 = dalloc<float>(mat, &bytes_);
+  d_G64 = dalloc<double>(mat, &bytes_);
+  d_T64 = dalloc<double>(mat, &bytes_);
+  for (int i = 0; i < 6; ++i) d_S[i] = dalloc<double>(mat, &bytes_);
+  d_state = dalloc<MolState>(nm, &bytes_);
+  d_charges = dalloc<double>(h_atoms.size(), &bytes_);
+  d_sweeps = dalloc<int>(nm, &bytes_);
+  d_count = dalloc<int>(1, &bytes_);
+  cuda_check(cudaMemcpyAsync(d_atoms, h_atoms.data(), h_atoms.size() * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_), "upload atoms");
+  if (!h_pairs.empty())
+    cuda_check(cudaMemcpyAsync(d_pairs, h_pairs.data(), h_pairs.size() * sizeof(DevPair), cudaMemcpyHostToDevice, stream_), "upload pairs");
+  cuda_check(cudaMemcpyAsync(d_mols, h_mols.data(), nm * sizeof(DevMol), cudaMemcpyHostToDevice, stream_), "upload mols");
+  cuda_check(cudaMemsetAsync(d_state, 0, nm * sizeof(MolState), stream_), "memset state");
+  cuda_check(cudaMemsetAsync(d_H, 0, mat * sizeof(double), stream_), "memset H");
+  cuda_check(cudaMemsetAsync(d_P, 0, mat * sizeof(double), stream_), "memset P");
+  cuda_check(cudaMemsetAsync(d_hist_dens, 0, std::max(diis_m_, 1) * mat * sizeof(double), stream_), "memset hist");
+  cuda_check(cudaMemsetAsync(d_hist_err, 0, std::max(diis_m_, 1) * mat * sizeof(double), stream_), "memset hist");
+  // Jacobi workspaces for molecules too large for shared memory
+  bool ag, vg;
+  const long long np = (max_n_ + 1) & ~1;
+  jws_stride_ = np * np;
+  if (jacobi_needs_workspace(max_n_, 4, &ag, &vg)) {
+    d_jA32 = dalloc<float>(ag ? (size_t)nm * jws_stride_ : 1, &bytes_);
+    d_jV32 = dalloc<float>((size_t)nm * jws_stride_, &bytes_);
+  }
+  if (jacobi_needs_workspace(max_n_, 8, &ag, &vg)) {
+    d_jA64 = dalloc<double>(ag ? (size_t)nm * jws_stride_ : 1, &bytes_);
+    d_jV64 = dalloc<double>((size_t)nm * jws_stride_, &bytes_);
+  }
+}
+
+Batch::~Batch() {
+  free_jobs();
+  for (int* p : d_bucket_lists_) cudaFree(p);
+  void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
+                  d_hist_dens, d_hist_err, d_G32, d_T32, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
+                  d_state, d_trace, d_charges, d_sweeps, d_count};
+  for (void* p : ptrs) if (p) cudaFree(p);
+  for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
+}
+
+void Batch::free_jobs() {
+  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_};
+  for (JobSet* j : all) { if (j->d) cudaFree(j->d); j->d = nullptr; j->n = 0; j->tiles = 0; }
+}
+
+void Batch::make_jobset(JobSet* js, const std::vector<GemmJob>& jobs_in) {
+  std::vector<GemmJob> jobs = jobs_in;
+  int tiles = 0;
+  for (GemmJob& j : jobs) {
+    j.tile0 = tiles;
+    j.tiles_n = gemm_tiles_n(j.N);
+    tiles += (j.M > 0 && j.N > 0) ? gemm_tiles(j.M, j.N) : 0;
+  }
+  js->n = (int)jobs.size();
+  js->tiles = tiles;
+  if (jobs.empty()) return;
+  cuda_check(cudaMalloc(&js->d, jobs.size() * sizeof(GemmJob)), "cudaMalloc jobs");
+  cuda_check(cudaMemcpyAsync(js->d, jobs.data(), jobs.size() * sizeof(GemmJob), cudaMemcpyHostToDevice, stream_), "upload jobs");
+}
+
+static GemmJob job(long long a, long long b, long long c, int M, int N, int K, int lda, int ldb, int ldc, int mol,
+                   double alpha = 1.0, double beta = 0.0) {
+  GemmJob j;
+  std::memset(&j, 0, sizeof(j));
+  j.a_off = a; j.b_off = b; j.c_off = c; j.M = M; j.N = N; j.K = K; j.lda = lda; j.ldb = ldb; j.ldc = ldc;
+  j.mol = mol; j.alpha = alpha; j.beta = beta;
+  return j;
+}
+
+void Batch::build_jobs(const std::vector<int>& which) {
+  free_jobs();
+  std::vector<GemmJob> t1, t2, dn, w, kt, yt, mm, d2, z, pp;
+  for (int m : which) {
+    const DevMol& d = h_mols[m];
+    const int n = d.nao, o = d.nocc, v = n - o;
+    const long long b = d.mat0;
+    t1.push_back(job(b, b, b, n, n, n, n, n, n, m));            // T = F C^T          (B transposed)
+    t2.push_back(job(b, b, b, n, n, n, n, n, n, m));            // G = C T
+    dn.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0));       // P = 2 C_o^T C_o    (A transposed)
+    if (o > 0 && v > 0) {
+      w.push_back(job(b, b, b, n, o, n, n, n, o, m));                       // W = F C_o^T   (B transposed)
+      kt.push_back(job(b + (long long)o * n, b, b, v, o, n, n, o, o, m));   // Kt = C_v W
+      yt.push_back(job(b, b + (long long)o * n, b, o, n, v, o, n, n, m, 1.0, 1.0));  // Yt = C_o + K^T C_v (A transposed)
+      mm.push_back(job(b, b, b, o, o, n, n, n, o, m));                      // M = Yt Yt^T   (B transposed)
+      d2.push_back(job(b, b, b, o, o, o, o, o, o, m));                      // D2 = D D
+      z.push_back(job(b, b, b, o, n, o, o, n, n, m));                       // Z = Minv Yt
+      pp.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0));                 // P = 2 Yt^T Z  (A transposed)
+    }
+  }
+  make_jobset(&j_trans1_, t1); make_jobset(&j_trans2_, t2); make_jobset(&j_dens_, dn);
+  make_jobset(&j_w_, w); make_jobset(&j_kt_, kt); make_jobset(&j_yt_, yt); make_jobset(&j_m_, mm);
+  make_jobset(&j_d2_, d2); make_jobset(&j_z_, z); make_jobset(&j_p_, pp);
+}
+
+void Batch::upload_list(const std::vector<int>& which) {
+  if (which == cur_list_ && !buckets_.empty()) return;
+  cur_list_ = which;
+  cuda_check(cudaMemcpyAsync(d_list, which.data(), which.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload list");
+  build_jobs(which);
+  // Jacobi size buckets: smaller molecules get a smaller shared-memory footprint
+  for (int* p : d_bucket_lists_) cudaFree(p);
+  d_bucket_lists_.clear();
+  buckets_.clear();
+  bucket_max_n_.clear();
+  const int edges[] = {64, 96, 128, 160, 194, 256, 338, 1 << 30};
+  int lo = 0;
+  for (int hi : edges) {
+    std::vector<int> b;
+    int mx = 0;
+    for (int m : which) {
+      const int n = h_mols[m].nao;
+      if (n > lo && n <= hi) { b.push_back(m); mx = std::max(mx, n); }
+    }
+    lo = hi;
+    if (b.empty()) continue;
+    int* d = nullptr;
+    cuda_check(cudaMalloc(&d, b.size() * sizeof(int)), "cudaMalloc bucket");
+    cuda_check(cudaMemcpyAsync(d, b.data(), b.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload bucket");
+    d_bucket_lists_.push_back(d);
+    buckets_.push_back(b);
+    bucket_max_n_.push_back(mx);
+  }
+}
+
+void Batch::integrals() {
+  std::vector<int> all(h_mols.size());
+  for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+  upload_list(all);
+  launch_pair_kernel(d_atoms, d_pairs, (long long)h_pairs.size(), d_mols, eng_->eri(), eng_->ovt(), d_blocks, d_H,
+                     d_ecore_pair, stream_);
+  cuda_check(cudaGetLastError(), "pair_kernel");
+  launch_hcore_kernel(d_atoms, d_pairs, d_mols, d_list, (int)all.size(), d_blocks, d_ecore_pair, d_H, d_state, stream_);
+  cuda_check(cudaGetLastError(), "hcore_kernel");
+}
+
+static ScfParamsDev to_dev(const ScfSettings& s) {
+  ScfParamsDev p;
+  std::memset(&p, 0, sizeof(p));
+  p.max_iter = s.max_iter;
+  p.diis_m = s.diis_num_error_vect;
+  p.rms_density = s.rms_density;
+  p.damping_thresh = s.damping_thresh;
+  p.damping_weight = s.damping_weight;
+  p.diis_start = s.diis_start_error;
+  p.diis_end = s.diis_end_error;
+  p.switch_error = s.switch_error;
+  p.precision = s.precision;
+  return p;
+}
+
+void Batch::begin(const ScfSettings& s, const std::vector<int>& which, bool requires_guess) {
+  if (s.diis_num_error_vect != diis_m_) throw std::invalid_argument("DIIS window differs from the batch allocation");
+  if (s.keep_trace && s.max_iter > max_iter_alloc_) {
+    if (d_trace) cudaFree(d_trace);
+    cuda_check(cudaMalloc(&d_trace, (size_t)h_mols.size() * s.max_iter * sizeof(TraceEntry)), "cudaMalloc trace");
+    max_iter_alloc_ = s.max_iter;
+  }
+  upload_list(which);
+  init_state_kernel<<<(unsigned)which.size(), 256, 0, stream_>>>(d_mols, d_list, (int)which.size(), d_state, d_C,
+                                                                 d_P, requires_guess ? 1 : 0, requires_guess ? 1 : 0);
+  cuda_check(cudaGetLastError(), "init_state");
+}
+
+void Batch::eigen_step(const ScfSettings& s) {
+  const int nl = (int)cur_list_.size();
+  (void)nl;
+  if (s.precision == 0) {
+    launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, d_C, d_T64, false, true, 0.0, d_state, 1, -1, stream_);
+    launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, d_C, d_T64, d_G64, false, false, 0.0, d_state, 1, -1, stream_);
+    for (size_t b = 0; b < buckets_.size(); ++b)
+      launch_jacobi_f64(d_mols, d_bucket_lists_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_G64, d_C,
+                        1, d_C, d_eps, d_jA64, d_jV64, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+  } else {
+    launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, d_C, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
+    launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, d_C, d_T32, d_G32, false, false, 0.0f, d_state, 1, -1, stream_);
+    for (size_t b = 0; b < buckets_.size(); ++b)
+      launch_jacobi_f32(d_mols, d_bucket_lists_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_G32, d_C,
+                        1, d_C, d_eps, d_jA32, d_jV32, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+  }
+  cuda_check(cudaGetLastError(), "eigen step");
+}
+
+void Batch::density_step(const ScfSettings& s) {
+  if (s.precision == 0) {
+    launch_gemm(j_dens_.d, j_dens_.n, j_dens_.tiles, d_C, d_C, d_P, true, false, 0.0, d_state, 1, -1, stream_);
+  } else {
+    // FP32 phase: density from the FP32 eigenvectors
+    launch_gemm(j_dens_.d, j_dens_.n, j_dens_.tiles, d_C, d_C, d_P, true, false, 0.0f, d_state, 1, 0, stream_);
+    // FP64 phase: one Newton step on the occupied subspace, then P = 2 Y (Y^T Y)^-1 Y^T
+    const int nl = (int)cur_list_.size();
+    double *W = d_S[0], *K = d_S[1], *Yt = d_S[2], *Mm = d_S[3], *D2 = d_S[4], *Z = d_S[5];
+    launch_gemm(j_w_.d, j_w_.n, j_w_.tiles, d_F, d_C, W, false, true, 0.0, d_state, 1, 1, stream_);
+    launch_gemm(j_kt_.d, j_kt_.n, j_kt_.tiles, d_C, W, K, false, false, 0.0, d_state, 1, 1, stream_);
+    launch_newton_scale(d_mols, d_list, nl, d_state, 1, K, d_eps, stream_);
+    launch_copy_occ_rows(d_mols, d_list, nl, d_state, 1, d_C, Yt, stream_);
+    launch_gemm(j_yt_.d, j_yt_.n, j_yt_.tiles, K, d_C, Yt, true, false, 0.0, d_state, 1, 1, stream_);
+    launch_gemm(j_m_.d, j_m_.n, j_m_.tiles, Yt, Yt, Mm, false, true, 0.0, d_state, 1, 1, stream_);
+    launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, D2, 0, stream_);
+    launch_gemm(j_d2_.d, j_d2_.n, j_d2_.tiles, Mm, Mm, D2, false, false, 0.0, d_state, 1, 1, stream_);
+    launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, D2, 1, stream_);
+    launch_gemm(j_z_.d, j_z_.n, j_z_.tiles, Mm, Yt, Z, false, false, 0.0, d_state, 1, 1, stream_);
+    launch_gemm(j_p_.d, j_p_.n, j_p_.tiles, Yt, Z, d_P, true, false, 0.0, d_state, 1, 1, stream_);
+  }
+  cuda_check(cudaGetLastError(), "density step");
+}
+
+void Batch::iterate(const ScfSettings& s, const std::vector<int>& which) {
+  upload_list(which);
+  const int nl = (int)which.size();
+  launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, d_blocks, d_H, d_P, d_F, d_Pold, d_state, -1, 1, 1, stream_);
+  cuda_check(cudaGetLastError(), "fock_kernel");
+  eigen_step(s);
+  density_step(s);
+  launch_diis(d_mols, d_list, nl, d_state, to_dev(s), d_P, d_Pold, d_hist_dens, d_hist_err, mat_total_,
+              s.keep_trace ? d_trace : nullptr, max_iter_alloc_, stream_);
+  cuda_check(cudaGetLastError(), "diis_kernel");
+}
+
+int Batch::count_active(const std::vector<int>& which) {
+  upload_list(which);
+  count_active_kernel<<<1, 256, 0, stream_>>>(d_list, (int)which.size(), d_state, d_count);
+  int h = 0;
+  cuda_check(cudaMemcpyAsync(&h, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream_), "count copy");
+  cuda_check(cudaStreamSynchronize(stream_), "count sync");
+  return h;
+}
+
+void Batch::finish(const ScfSettings& s, const std::vector<int>& which) {
+  (void)s;
+  upload_list(which);
+  const int nl = (int)which.size();
+  launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0, 0, 0, stream_);
+  launch_energy_kernel(d_atoms, d_mols, d_list, nl, d_P, d_F, d_H, d_state, d_charges, stream_);
+  cuda_check(cudaGetLastError(), "finish");
+}
+
+void Batch::scf(const ScfSettings& s, bool requires_guess) {
+  std::vector<int> all(h_mols.size());
+  for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+  begin(s, all, requires_guess);
+  for (int it = 0; it < s.max_iter; ++it) {
+    iterate(s, all);
+    if (count_active(all) == 0) break;
+  }
+  finish(s, all);
+  cuda_check(cudaStreamSynchronize(stream_), "scf");
+}
+
+void Batch::results(std::vector<MolResult>* out) {
+  std::vector<MolState> st(h_mols.size());
+  cuda_check(cudaMemcpyAsync(st.data(), d_state, st.size() * sizeof(MolState), cudaMemcpyDeviceToHost, stream_), "state copy");
+  cuda_check(cudaStreamSynchronize(stream_), "results");
+  out->resize(st.size());
+  for (size_t m = 0; m < st.size(); ++m) {
+    MolResult& r = (*out)[m];
+    r.status = st[m].status;
+    r.iterations = st[m].status == kConverged ? st[m].iter + 1 : st[m].iter;
+    r.energy = st[m].energy;
+    r.core_repulsion = st[m].ecore;
+    r.heat_of_formation = st[m].heat_of_formation;
+    r.final_rms = st[m].rms;
+    r.final_diis_error = st[m].diis_err;
+  }
+}
+
+void Batch::copy_matrix(int which, int m, double* host) const {
+  const double* src = which == 0 ? d_H : which == 1 ? d_F : which == 2 ? d_P : d_C;
+  const DevMol& d = h_mols[m];
+  cuda_check(cudaMemcpyAsync(host, src + d.mat0, (size_t)d.nao * d.nao * sizeof(double), cudaMemcpyDeviceToHost, stream_), "copy matrix");
+  cuda_check(cudaStreamSynchronize(stream_), "copy matrix");
+}
+
+void Batch::copy_eps(int m, double* host) const {
+  const DevMol& d = h_mols[m];
+  cuda_check(cudaMemcpyAsync(host, d_eps + d.vec0, d.nao * sizeof(double), cudaMemcpyDeviceToHost, stream_), "copy eps");
+  cuda_check(cudaStreamSynchronize(stream_), "copy eps");
+}
+
+void Batch::copy_charges(int m, double* host) const {
+  const DevMol& d = h_mols[m];
+  cuda_check(cudaMemcpyAsync(host, d_charges + d.atom0, d.natoms * sizeof(double), cudaMemcpyDeviceToHost, stream_), "copy charges");
+  cuda_check(cudaStreamSynchronize(stream_), "copy charges");
+}
+
+void Batch::copy_blocks(int m, double* host, size_t* count) const {
+  const DevMol& d = h_mols[m];
+  long long first = d.npairs ? h_pairs[d.pair0].blk : 0;
+  long long last = first;
+  if (d.npairs) {
+    const DevPair& p = h_pairs[d.pair0 + d.npairs - 1];
+    last = p.blk + (long long)(h_atoms[p.a].nao == 4 ? 10 : 1) * (h_atoms[p.b].nao == 4 ? 10 : 1);
+  }
+  *count = (size_t)(last - first);
+  if (host && *count)
+    cuda_check(cudaMemcpyAsync(host, d_blocks + first, *count * sizeof(double), cudaMemcpyDeviceToHost, stream_), "copy blocks");
+  cuda_check(cudaStreamSynchronize(stream_), "copy blocks");
+}
+
+void Batch::copy_trace(int m, std::vector<TraceEntry>* out) const {
+  out->assign(max_iter_alloc_, TraceEntry{});
+  if (!d_trace || max_iter_alloc_ == 0) return;
+  cuda_check(cudaMemcpyAsync(out->data(), d_trace + (size_t)m * max_iter_alloc_, max_iter_alloc_ * sizeof(TraceEntry),
+                             cudaMemcpyDeviceToHost, stream_), "copy trace");
+  cuda_check(cudaStreamSynchronize(stream_), "copy trace");
+}
+
+void Batch::set_density(int m, const double* host) {
+  const DevMol& d = h_mols[m];
+  cuda_check(cudaMemcpyAsync(d_P + d.mat0, host, (size_t)d.nao * d.nao * sizeof(double), cudaMemcpyHostToDevice, stream_), "set density");
+  cuda_check(cudaStreamSynchronize(stream_), "set density");
+}
+
+}  // namespace nddo

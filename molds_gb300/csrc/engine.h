@@ -1,0 +1,148 @@
+// Host engine: owns one device, one stream and any number of device-resident
+// molecule batches, and drives the batched SCF state machine.
+#pragma once
+#include <cuda_runtime.h>
+#include <memory>
+#include <string>
+#include <vector>
+#include "kernels.h"
+
+namespace nddo {
+
+struct MoleculeInput {
+  int theory = NDDO_PM3;
+  std::vector<int> Z;
+  std::vector<double> xyz;   // bohr, 3 per atom
+};
+
+struct ScfSettings {
+  int max_iter = 100;
+  double rms_density = 1e-8;
+  double damping_thresh = 1.0;
+  double damping_weight = 0.8;
+  int diis_num_error_vect = 5;
+  double diis_start_error = 1e-2;
+  double diis_end_error = 1e-8;
+  int precision = 0;            // 0 FP64 throughout, 1 mixed (FP32 eigen phase + FP64 refinement)
+  double switch_error = 1e-4;   // mixed: FP64 phase once the DIIS error is below this
+  int max_sweeps = 30;
+  int keep_trace = 1;
+};
+
+struct MolResult {
+  int status = 0;               // MolStatus
+  int iterations = 0;
+  double energy = 0, core_repulsion = 0, heat_of_formation = 0, final_rms = 0, final_diis_error = 0;
+};
+
+class Engine;
+
+// A set of molecules resident on the device with every buffer the SCF needs.
+class Batch {
+ public:
+  Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m);
+  ~Batch();
+  Batch(const Batch&) = delete;
+  Batch& operator=(const Batch&) = delete;
+
+  int size() const { return (int)h_mols.size(); }
+  int nao(int m) const { return h_mols[m].nao; }
+  int natoms(int m) const { return h_mols[m].natoms; }
+  int nocc(int m) const { return h_mols[m].nocc; }
+  size_t device_bytes() const { return bytes_; }
+
+  // One-time work: pair integrals, H, core-core energy.
+  void integrals();
+  // Full SCF for every molecule; requires_guess as in MolDS DoSCF(requiresGuess).
+  void scf(const ScfSettings& s, bool requires_guess);
+  // Initialise the SCF state of the listed molecules (serving: admission).
+  void begin(const ScfSettings& s, const std::vector<int>& which, bool requires_guess);
+  // One SCF iteration over the listed (active) molecules.
+  void iterate(const ScfSettings& s, const std::vector<int>& which);
+  // Energies / charges of the listed molecules after convergence.
+  void finish(const ScfSettings& s, const std::vector<int>& which);
+  // Number of still-active molecules among `which` (synchronises).
+  int count_active(const std::vector<int>& which);
+
+  // results (synchronise and copy out)
+  void results(std::vector<MolResult>* out);
+  void copy_matrix(int which_matrix, int m, double* host) const;   // 0 H, 1 F, 2 P, 3 C
+  void copy_eps(int m, double* host) const;
+  void copy_charges(int m, double* host) const;
+  void copy_blocks(int m, double* host, size_t* count) const;
+  void copy_trace(int m, std::vector<TraceEntry>* out) const;
+  void set_density(int m, const double* host);
+
+  const std::vector<DevMol>& mol_table() const { return h_mols; }
+  double* dev_H() const { return d_H; }
+  double* dev_P() const { return d_P; }
+
+ private:
+  void build_jobs(const std::vector<int>& which);
+  void upload_list(const std::vector<int>& which);
+  void eigen_step(const ScfSettings& s);
+  void density_step(const ScfSettings& s);
+
+  Engine* eng_;
+  cudaStream_t stream_;
+  int diis_m_;
+  size_t bytes_ = 0;
+  long long mat_total_ = 0, vec_total_ = 0;
+  int max_n_ = 0, max_iter_alloc_ = 0;
+
+  std::vector<DevAtom> h_atoms;
+  std::vector<DevPair> h_pairs;
+  std::vector<DevMol> h_mols;
+  long long blk_total_ = 0;
+
+  DevAtom* d_atoms = nullptr;
+  DevPair* d_pairs = nullptr;
+  DevMol* d_mols = nullptr;
+  int* d_list = nullptr;
+  double* d_blocks = nullptr;
+  double* d_ecore_pair = nullptr;
+  double *d_H = nullptr, *d_F = nullptr, *d_P = nullptr, *d_Pold = nullptr, *d_C = nullptr, *d_eps = nullptr;
+  double *d_hist_dens = nullptr, *d_hist_err = nullptr;
+  float *d_G32 = nullptr, *d_T32 = nullptr;
+  double *d_G64 = nullptr, *d_T64 = nullptr;
+  double* d_S[6] = {};
+  float *d_jA32 = nullptr, *d_jV32 = nullptr;
+  double *d_jA64 = nullptr, *d_jV64 = nullptr;
+  long long jws_stride_ = 0;
+  MolState* d_state = nullptr;
+  TraceEntry* d_trace = nullptr;
+  double* d_charges = nullptr;
+  int* d_sweeps = nullptr;
+  int* d_count = nullptr;
+
+  // current molecule list and its GEMM job tables
+  std::vector<int> cur_list_;
+  std::vector<std::vector<int>> buckets_;      // jacobi size buckets (indices into cur_list_)
+  std::vector<int*> d_bucket_lists_;
+  std::vector<int> bucket_max_n_;
+  struct JobSet { GemmJob* d = nullptr; int n = 0; int tiles = 0; };
+  JobSet j_trans1_, j_trans2_, j_dens_, j_w_, j_kt_, j_yt_, j_m_, j_d2_, j_z_, j_p_;
+  void free_jobs();
+  void make_jobset(JobSet* js, const std::vector<GemmJob>& jobs);
+};
+
+class Engine {
+ public:
+  explicit Engine(int device);
+  ~Engine();
+  cudaStream_t stream() const { return stream_; }
+  int device() const { return device_; }
+  const EriTable* eri() const { return d_eri_; }
+  const OverlapTable* ovt() const { return d_ovt_; }
+
+ private:
+  int device_;
+  cudaStream_t stream_ = nullptr;
+  EriTable* d_eri_ = nullptr;
+  OverlapTable* d_ovt_ = nullptr;
+};
+
+// throws std::runtime_error with the CUDA error text
+void cuda_check(cudaError_t e, const char* what);
+
+}  // namespace nddo

@@ -1,0 +1,284 @@
+// Kernel (d): batched two-sided cyclic Jacobi eigensolver, one CTA per molecule.
+//
+// Replaces MolDS's Lapack::Dsyevd on the SCF path (src/wrappers/Lapack.cpp:102-160,
+// called at src/cndo/Cndo2.cpp:652-655).  Output convention is the reference's:
+// eigenvalues ascending, eigenvectors as ROWS of C, each row's component sum
+// made >= 0.
+//
+// Layout: the symmetric working matrix is stored as its packed upper triangle
+// and the accumulated rotations V as a full N'xN' matrix, both in shared memory
+// when they fit (N' <= 194 in FP32, <= 138 in FP64); otherwise the kernel runs
+// on a per-molecule workspace in global memory (L2-resident for these sizes).
+// N' = N rounded up to even; an odd N gets a decoupled dummy index.
+//
+// Parallel ordering: round-robin tournament.  In round r the N'/2 disjoint
+// pairs (p, q) are rotated at once; every 2x2 block of the matrix is then
+// updated exactly once per round as J_I^T B J_K, and V as V J.
+//
+// Warm start: V starts from the previous iteration's eigenvectors and the
+// matrix from C_prev F C_prev^T (computed by the transform GEMMs), so late SCF
+// iterations converge in one or two sweeps.
+#include <cuda_runtime.h>
+#include "nddo_batch.cuh"
+#include "kernels.h"
+
+namespace nddo {
+
+constexpr int kJacobiThreads = 512;
+
+__host__ __device__ inline long long jac_pk(int i, int j, int n) {   // packed upper, i <= j
+  return (long long)i * (2 * n - i + 1) / 2 + (j - i);
+}
+
+template <typename T> struct JacTol;
+template <> struct JacTol<float> { static constexpr float rel = 2e-6f; };
+template <> struct JacTol<double> { static constexpr double rel = 2e-14; };
+
+size_t jacobi_smem_bytes(int n, int elem, bool v_in_smem, bool a_in_smem) {
+  const long long np = (n + 1) & ~1;
+  long long b = 0;
+  if (a_in_smem) b += np * (np + 1) / 2 * elem;
+  if (v_in_smem) b += np * np * elem;
+  b += (np / 2) * 2 * elem;        // c, s
+  b += (np / 2) * 2 * 4;           // p, q
+  b += np * 4 + np * elem;         // column order + sign
+  b += 64 * 8 + 16;                // reduction scratch (+ alignment slack)
+  return (size_t)((b + 15) & ~15LL);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kJacobiThreads)
+jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list, const MolState* __restrict__ st,
+              int require_active, const T* __restrict__ G, const double* __restrict__ Cin, int use_basis,
+              double* __restrict__ Cout, double* __restrict__ eps_out, T* __restrict__ Aws, T* __restrict__ Vws,
+              long long ws_stride, int a_in_smem, int v_in_smem, int max_sweeps, int* __restrict__ sweeps_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int m = mol_list[blockIdx.x];
+  if (require_active && st[m].status != kActive) return;
+  const DevMol mol = mols[m];
+  const int n = mol.nao;
+  const int np = (n + 1) & ~1;
+  const int half = np / 2;
+  const long long npk = (long long)np * (np + 1) / 2;
+
+  unsigned char* ptr = smem_raw;
+  T* A;
+  T* V;
+  if (a_in_smem) { A = reinterpret_cast<T*>(ptr); ptr += npk * sizeof(T); }
+  else A = Aws + (long long)blockIdx.x * ws_stride;
+  if (v_in_smem) { V = reinterpret_cast<T*>(ptr); ptr += (long long)np * np * sizeof(T); }
+  else V = Vws + (long long)blockIdx.x * ws_stride;
+  T* cs = reinterpret_cast<T*>(ptr); ptr += 2 * half * sizeof(T);
+  int* pq = reinterpret_cast<int*>(ptr); ptr += 2 * half * sizeof(int);
+  int* order = reinterpret_cast<int*>(ptr); ptr += np * sizeof(int);
+  T* sgn = reinterpret_cast<T*>(ptr); ptr += np * sizeof(T);
+  T* red = reinterpret_cast<T*>(((uintptr_t)ptr + 7) & ~(uintptr_t)7);
+
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const T* Gm = G + mol.mat0;
+  const double* Cm = Cin + mol.mat0;
+
+  // ---- load ------------------------------------------------------------------
+  for (long long e = tid; e < npk; e += nth) {
+    // decode packed index -> (i, j): row i holds np - i entries
+    int i = 0;
+    long long rem = e;
+    // rows are long; a short scan per element is acceptable for a one-time load
+    {
+      // solve i from e using the closed form, then fix rounding
+      double b = 2.0 * np + 1.0;
+      double disc = b * b - 8.0 * (double)e;
+      i = (int)((b - sqrt(disc)) * 0.5);
+      if (i < 0) i = 0;
+      while (i > 0 && jac_pk(i, i, np) > e) --i;
+      while (i + 1 < np && jac_pk(i + 1, i + 1, np) <= e) ++i;
+      rem = e - jac_pk(i, i, np);
+    }
+    const int j = i + (int)rem;
+    T v = 0;
+    if (i < n && j < n) v = Gm[(long long)i * n + j];
+    A[e] = v;
+  }
+  for (long long e = tid; e < (long long)np * np; e += nth) {
+    const int mu = (int)(e / np), i = (int)(e % np);     // V[mu][i] = C_prev[i][mu]
+    T v;
+    if (mu < n && i < n) v = use_basis ? (T)Cm[(long long)i * n + mu] : (T)(mu == i ? 1 : 0);
+    else v = (T)(mu == i ? 1 : 0);
+    V[e] = v;
+  }
+  __syncthreads();
+
+  // matrix scale for the stopping test
+  T scale = 0;
+  for (int i = tid; i < n; i += nth) { T d = fabs(A[jac_pk(i, i, np)]); scale = d > scale ? d : scale; }
+  for (int o = 16; o > 0; o >>= 1) { T t = __shfl_xor_sync(0xffffffffu, scale, o); scale = t > scale ? t : scale; }
+  if ((tid & 31) == 0) red[tid >> 5] = scale;
+  __syncthreads();
+  if (tid == 0) {
+    T s = 0;
+    for (int w = 0; w < (nth >> 5); ++w) s = red[w] > s ? red[w] : s;
+    red[32] = s > (T)1e-30 ? s : (T)1;
+  }
+  __syncthreads();
+  const T thresh = JacTol<T>::rel * red[32];
+  __syncthreads();
+
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    T offmax = 0;
+    for (int r = 0; r < np - 1; ++r) {
+      // pairs and rotations of this round
+      for (int k = tid; k < half; k += nth) {
+        const int i1 = k, i2 = np - 1 - k;
+        const int p1 = (i1 == 0) ? 0 : ((i1 - 1 + r) % (np - 1)) + 1;
+        const int p2 = (i2 == 0) ? 0 : ((i2 - 1 + r) % (np - 1)) + 1;
+        const int p = p1 < p2 ? p1 : p2, q = p1 < p2 ? p2 : p1;
+        const T apq = A[jac_pk(p, q, np)];
+        T c = 1, s = 0;
+        const T aa = fabs(apq);
+        offmax = aa > offmax ? aa : offmax;
+        if (apq != (T)0) {
+          const T app = A[jac_pk(p, p, np)], aqq = A[jac_pk(q, q, np)];
+          const T theta = (aqq - app) / (2 * apq);
+          T t;
+          if (fabs(theta) > (T)1e15) t = (T)0.5 / theta;
+          else t = (theta >= 0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt(theta * theta + (T)1));
+          c = (T)1 / sqrt(t * t + (T)1);
+          s = t * c;
+        }
+        cs[2 * k] = c; cs[2 * k + 1] = s;
+        pq[2 * k] = p; pq[2 * k + 1] = q;
+      }
+      __syncthreads();
+      // A <- J^T A J, one 2x2 block per (I <= K)
+      for (int e = tid; e < half * half; e += nth) {
+        const int I = e / half, K = e % half;
+        if (I > K) continue;
+        const int p = pq[2 * I], q = pq[2 * I + 1];
+        const T c = cs[2 * I], s = cs[2 * I + 1];
+        if (I == K) {
+          const long long ipq = jac_pk(p, q, np);
+          const T apq = A[ipq];
+          if (apq != (T)0) {
+            const T t = s / c;
+            A[jac_pk(p, p, np)] -= t * apq;
+            A[jac_pk(q, q, np)] += t * apq;
+            A[ipq] = 0;
+          }
+          continue;
+        }
+        const int r2 = pq[2 * K], s2 = pq[2 * K + 1];
+        const T c2 = cs[2 * K], s2n = cs[2 * K + 1];
+        const long long i_pr = p < r2 ? jac_pk(p, r2, np) : jac_pk(r2, p, np);
+        const long long i_ps = p < s2 ? jac_pk(p, s2, np) : jac_pk(s2, p, np);
+        const long long i_qr = q < r2 ? jac_pk(q, r2, np) : jac_pk(r2, q, np);
+        const long long i_qs = q < s2 ? jac_pk(q, s2, np) : jac_pk(s2, q, np);
+        const T b00 = A[i_pr], b01 = A[i_ps], b10 = A[i_qr], b11 = A[i_qs];
+        // Y = J_I^T B
+        const T y00 = c * b00 - s * b10, y01 = c * b01 - s * b11;
+        const T y10 = s * b00 + c * b10, y11 = s * b01 + c * b11;
+        // X = Y J_K
+        A[i_pr] = y00 * c2 - y01 * s2n;
+        A[i_ps] = y00 * s2n + y01 * c2;
+        A[i_qr] = y10 * c2 - y11 * s2n;
+        A[i_qs] = y10 * s2n + y11 * c2;
+      }
+      // V <- V J
+      for (int e = tid; e < np * half; e += nth) {
+        const int row = e / half, k = e % half;
+        const int p = pq[2 * k], q = pq[2 * k + 1];
+        const T c = cs[2 * k], s = cs[2 * k + 1];
+        T* vr = V + (long long)row * np;
+        const T vp = vr[p], vq = vr[q];
+        vr[p] = c * vp - s * vq;
+        vr[q] = s * vp + c * vq;
+      }
+      __syncthreads();
+    }
+    // sweep converged when every rotation it applied was at round-off level
+    for (int o = 16; o > 0; o >>= 1) { T t = __shfl_xor_sync(0xffffffffu, offmax, o); offmax = t > offmax ? t : offmax; }
+    if ((tid & 31) == 0) red[tid >> 5] = offmax;
+    __syncthreads();
+    if (tid == 0) {
+      T mx = 0;
+      for (int w = 0; w < (nth >> 5); ++w) mx = red[w] > mx ? red[w] : mx;
+      red[33] = mx;
+    }
+    __syncthreads();
+    const bool done = red[33] <= thresh;
+    __syncthreads();
+    if (done) { ++sweep; break; }
+  }
+
+  // ---- sort ascending, sign fix, write rows ------------------------------------
+  for (int i = tid; i < np; i += nth) {
+    if (i >= n) continue;
+    const T li = A[jac_pk(i, i, np)];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const T lj = A[jac_pk(j, j, np)];
+      rank += (lj < li) || (lj == li && j < i);
+    }
+    order[rank] = i;
+    T sum = 0;
+    for (int mu = 0; mu < n; ++mu) sum += V[(long long)mu * np + i];
+    sgn[i] = sum < (T)0 ? (T)-1 : (T)1;
+    eps_out[mol.vec0 + rank] = (double)li;
+  }
+  __syncthreads();
+  double* Co = Cout + mol.mat0;
+  for (long long e = tid; e < (long long)n * n; e += nth) {
+    const int r = (int)(e / n), mu = (int)(e % n);
+    const int col = order[r];
+    Co[e] = (double)(sgn[col] * V[(long long)mu * np + col]);
+  }
+  if (tid == 0 && sweeps_out) sweeps_out[m] = sweep;
+}
+
+template <typename T>
+void launch_jacobi_impl(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                        int require_active, const T* G, const double* Cin, int use_basis, double* Cout,
+                        double* eps, T* Aws, T* Vws, long long ws_stride, int max_sweeps, int* sweeps_out,
+                        cudaStream_t s) {
+  if (nlist <= 0) return;
+  const int elem = sizeof(T);
+  const size_t limit = 232448;
+  bool a_sm = true, v_sm = true;
+  if (jacobi_smem_bytes(max_n, elem, true, true) > limit) {
+    v_sm = false;
+    if (jacobi_smem_bytes(max_n, elem, false, true) > limit) a_sm = false;
+  }
+  const size_t bytes = jacobi_smem_bytes(max_n, elem, v_sm, a_sm);
+  cudaFuncSetAttribute(jacobi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  jacobi_kernel<T><<<nlist, kJacobiThreads, bytes, s>>>(mols, mol_list, st, require_active, G, Cin, use_basis,
+                                                        Cout, eps, Aws, Vws, ws_stride, a_sm ? 1 : 0,
+                                                        v_sm ? 1 : 0, max_sweeps, sweeps_out);
+}
+
+void launch_jacobi_f32(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                       int require_active, const float* G, const double* Cin, int use_basis, double* Cout,
+                       double* eps, float* Aws, float* Vws, long long ws_stride, int max_sweeps,
+                       int* sweeps_out, cudaStream_t s) {
+  launch_jacobi_impl<float>(mols, mol_list, nlist, max_n, st, require_active, G, Cin, use_basis, Cout, eps, Aws,
+                            Vws, ws_stride, max_sweeps, sweeps_out, s);
+}
+
+void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                       int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
+                       double* eps, double* Aws, double* Vws, long long ws_stride, int max_sweeps,
+                       int* sweeps_out, cudaStream_t s) {
+  launch_jacobi_impl<double>(mols, mol_list, nlist, max_n, st, require_active, G, Cin, use_basis, Cout, eps, Aws,
+                             Vws, ws_stride, max_sweeps, sweeps_out, s);
+}
+
+bool jacobi_needs_workspace(int max_n, int elem, bool* a_global, bool* v_global) {
+  const size_t limit = 232448;
+  *a_global = false; *v_global = false;
+  if (jacobi_smem_bytes(max_n, elem, true, true) > limit) {
+    *v_global = true;
+    if (jacobi_smem_bytes(max_n, elem, false, true) > limit) *a_global = true;
+  }
+  return *a_global || *v_global;
+}
+
+}  // namespace nddo

@@ -1,0 +1,77 @@
+// Host-visible launchers of the NDDO kernels (implemented in the .cu files).
+#pragma once
+#include <cuda_runtime.h>
+#include "nddo_batch.cuh"
+
+namespace nddo {
+
+// one matrix product of a batched GEMM launch: C = alpha op(A) op(B) + beta C
+struct GemmJob {
+  long long a_off, b_off, c_off;
+  int M, N, K;
+  int lda, ldb, ldc;
+  int mol;
+  int tiles_n;
+  int tile0;
+  double alpha, beta;
+};
+
+int gemm_tiles(int M, int N);
+int gemm_tiles_n(int N);
+
+// pair_fock.cu
+void upload_params(const nddo_atom_params* p, cudaStream_t s);
+void launch_pair_kernel(const DevAtom* atoms, const DevPair* pairs, long long npairs, const DevMol* mols,
+                        const EriTable* eri, const OverlapTable* ovt, double* blocks, double* H,
+                        double* ecore_pair, cudaStream_t s);
+void launch_hcore_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
+                         int nlist, const double* blocks, const double* ecore_pair, double* H, MolState* st,
+                         cudaStream_t s);
+void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
+                        int nlist, const double* blocks, const double* H, const double* P, double* F,
+                        double* Pold, const MolState* st, int mode_override, int copy_old, int require_active,
+                        cudaStream_t s);
+void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* mol_list, int nlist,
+                          const double* P, const double* F, const double* H, MolState* st, double* charges,
+                          cudaStream_t s);
+
+// jacobi.cu
+bool jacobi_needs_workspace(int max_n, int elem, bool* a_global, bool* v_global);
+void launch_jacobi_f32(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                       int require_active, const float* G, const double* Cin, int use_basis, double* Cout,
+                       double* eps, float* Aws, float* Vws, long long ws_stride, int max_sweeps,
+                       int* sweeps_out, cudaStream_t s);
+void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                       int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
+                       double* eps, double* Aws, double* Vws, long long ws_stride, int max_sweeps,
+                       int* sweeps_out, cudaStream_t s);
+
+// scf_kernels.cu
+void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C,
+                 bool ta, bool tb, double acc_tag, const MolState* st, int require_active, int require_phase,
+                 cudaStream_t s);
+void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C,
+                 bool ta, bool tb, float acc_tag, const MolState* st, int require_active, int require_phase,
+                 cudaStream_t s);
+void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, float* C,
+                 bool ta, bool tb, float acc_tag, const MolState* st, int require_active, int require_phase,
+                 cudaStream_t s);
+void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, const double* B, float* C,
+                 bool ta, bool tb, float acc_tag, const MolState* st, int require_active, int require_phase,
+                 cudaStream_t s);
+void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const float* B, float* C,
+                 bool ta, bool tb, float acc_tag, const MolState* st, int require_active, int require_phase,
+                 cudaStream_t s);
+void launch_diis(const DevMol* mols, const int* mol_list, int nlist, MolState* st, const ScfParamsDev& prm,
+                 double* P, const double* Pold, double* hist_dens, double* hist_err, long long hist_stride,
+                 TraceEntry* trace, int trace_len, cudaStream_t s);
+void launch_convert_f64_f32(const DevMol* mols, const int* mol_list, int nlist, const MolState* st,
+                            int require_active, const double* src, float* dst, cudaStream_t s);
+void launch_newton_scale(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
+                         double* K, const double* eps, cudaStream_t s);
+void launch_neumann(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
+                    double* M, const double* D2, int mode, cudaStream_t s);
+void launch_copy_occ_rows(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
+                          const double* src, double* dst, cudaStream_t s);
+
+}  // namespace nddo

@@ -1,0 +1,503 @@
+// Kernels (a) and (b): one-time pair integrals and the NDDO Fock build.
+//
+// (a) pair_kernel -- one warp per atom pair of every molecule in the batch.
+//     Evaluates the distinct diatomic-frame two-centre integrals from the term
+//     table (lane = local integral), rotates the packed 10x10 block to the
+//     molecular frame as T2 L T2^T (T2 = symmetrised product rotation), and
+//     stores it with coalesced lane-strided stores.  The same warp computes the
+//     Slater overlap of the pair (diatomic frame, then rotated), the resonance
+//     block 1/2 (beta_mu + beta_nu) S_mu,nu of the core Hamiltonian, and the
+//     core-core repulsion E_AB.
+//     MolDS: Mndo::CalcTwoElecsTwoAtomCores (src/mndo/Mndo.cpp:3703-3820),
+//     CalcDiatomicTwoElecsTwoCores (:3948-4025), RotateDiatomicTwoElecsTwoCores
+//     ToSpaceFrame (:4223-4293), Cndo2::CalcOverlapAOs (src/cndo/Cndo2.cpp:
+//     4030-4146), Mndo::GetDiatomCoreRepulsionEnergy (:319-327, :223-240) and
+//     Am1::GetDiatomCoreRepulsionEnergy (src/am1/Am1.cpp:145-170).
+//
+// (b) hcore_kernel / fock_kernel -- one CTA per molecule, one warp per atom.
+//     Coulomb terms of the diagonal block of atom A are gathered from all
+//     partner blocks by the lanes and reduced with a fixed shuffle tree, so the
+//     result does not depend on scheduling (bitwise reproducible, alone or in a
+//     batch).  Exchange blocks are written by the lane that owns the pair.
+//     MolDS: Cndo2::CalcFockMatrix (src/cndo/Cndo2.cpp:1526-1636) with
+//     Mndo::GetFockDiagElement (src/mndo/Mndo.cpp:422-488), GetFockOffDiagElement
+//     (:490-580), GetCoulombInt/GetExchangeInt (:583-639), GetElectronCoreAttraction
+//     (:643-650).
+#include <cuda_runtime.h>
+#include "nddo_batch.cuh"
+#include "kernels.h"
+
+namespace nddo {
+
+__constant__ nddo_atom_params c_params[kNumParamSlots];
+
+void upload_params(const nddo_atom_params* p, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_params, p, sizeof(nddo_atom_params) * kNumParamSlots, 0,
+                          cudaMemcpyHostToDevice, s);
+}
+
+__device__ __forceinline__ double sel3(int i, double a, double b, double c) {
+  return i == 0 ? a : (i == 1 ? b : c);
+}
+
+constexpr int kPairWarps = 4;
+
+__global__ void __launch_bounds__(kPairWarps * 32)
+pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs, long long npairs,
+            const DevMol* __restrict__ mols, const EriTable* __restrict__ eri,
+            const OverlapTable* __restrict__ ovt, double* __restrict__ blocks,
+            double* __restrict__ H, double* __restrict__ ecore_pair) {
+  __shared__ double s_val[kPairWarps][24];
+  __shared__ double s_T2[kPairWarps][100];
+  __shared__ double s_L[kPairWarps][100];
+  __shared__ double s_M[kPairWarps][100];
+  __shared__ double s_ab[kPairWarps][4][24];
+  __shared__ double s_ov[kPairWarps][8];
+  __shared__ double s_R[kPairWarps][16];
+  const unsigned full = 0xffffffffu;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long p = (long long)blockIdx.x * kPairWarps + warp;
+  if (p >= npairs) return;
+
+  const DevPair pr = pairs[p];
+  const DevAtom A = atoms[pr.a], B = atoms[pr.b];
+  const DevMol mol = mols[pr.mol];
+  const nddo_atom_params& pa = c_params[A.pidx];
+  const nddo_atom_params& pb = c_params[B.pidx];
+  const double dx = B.x - A.x, dy = B.y - A.y, dz = B.z - A.z;
+  const double R = sqrt(dx * dx + dy * dy + dz * dz);
+  const int nA = A.nao, nB = B.nao;
+  const int dA = nA == 4 ? 10 : 1, dB = nB == 4 ? 10 : 1;
+
+  // ---- rotation matrix (lane 0) ------------------------------------------
+  if (lane == 0) {
+    double Rm[4][4];
+    rotation_matrix(dx, dy, dz, Rm);
+    for (int i = 0; i < 16; ++i) s_R[warp][i] = Rm[i >> 2][i & 3];
+  }
+
+  // ---- local two-centre integrals: lane = slot ----------------------------
+  double val = 0.0;
+  if (lane < 21) {
+    bool need;
+    if (nA == 4 && nB == 4) need = true;
+    else if (nA == 4) need = (lane == 0 || lane == 3 || lane == 4 || lane == 10);
+    else if (nB == 4) need = (lane == 0 || lane == 1 || lane == 2 || lane == 13);
+    else need = (lane == 0);
+    if (need) {
+      const int nt = eri->nterms[lane];
+      for (int t = 0; t < nt; ++t) {
+        const EriTerm e = eri->terms[lane][t];
+        const double da = sel3(e.la, pa.d[0], pa.d[1], pa.d[2]);
+        const double db = sel3(e.lb, pb.d[0], pb.d[1], pb.d[2]);
+        const double ra = sel3(e.la, pa.rho[0], pa.rho[1], pa.rho[2]);
+        const double rb = sel3(e.lb, pb.rho[0], pb.rho[1], pb.rho[2]);
+        const double l = R + (double)e.c1 * da + (double)e.c2 * db;
+        const double u = (double)e.c3 * da + (double)e.c4 * db;
+        const double v = (double)e.c5 * da + (double)e.c6 * db;
+        const double a = ra + rb;
+        const double arg = l * l + u * u + v * v + a * a;
+        val += e.coef * (1.0 / sqrt(arg));
+      }
+    }
+  }
+  const double s5 = __shfl_sync(full, val, 5), s6 = __shfl_sync(full, val, 6);
+  if (lane == 21) val = (nA == 4 && nB == 4) ? 0.5 * (s5 - s6) : 0.0;
+  if (lane < 22) s_val[warp][lane] = val;
+
+  // ---- overlap auxiliary integrals: 4 zeta combinations x (12 A_k, 12 B_k) --
+  const int na = pa.principal_n, nb = pb.principal_n;
+  for (int vv = lane; vv < 96; vv += 32) {
+    const int zc = vv / 24, k = vv % 24;
+    const bool need = (zc == 0) || (zc == 1 && nB == 4) || (zc == 2 && nA == 4) || (zc == 3 && nA == 4 && nB == 4);
+    double r = 0.0;
+    if (need) {
+      const double za = (zc >= 2) ? pa.zeta[1] : pa.zeta[0];
+      const double zb = (zc & 1) ? pb.zeta[1] : pb.zeta[0];
+      r = (k < 12) ? aux_a(k, 0.5 * R * (za + zb)) : aux_b(k - 12, 0.5 * R * (za - zb));
+    }
+    s_ab[warp][zc][k] = r;
+  }
+  __syncwarp();
+
+  // ---- T2 (pair rotation) and local block L ---------------------------------
+  for (int e = lane; e < 100; e += 32) {
+    const int P = e / 10, Q = e % 10;
+    int m, n, i, j;
+    unpack_index(P, &m, &n);
+    unpack_index(Q, &i, &j);
+    const double* Rm = s_R[warp];
+    s_T2[warp][e] = (i == j) ? Rm[m * 4 + i] * Rm[n * 4 + i]
+                             : Rm[m * 4 + i] * Rm[n * 4 + j] + Rm[m * 4 + j] * Rm[n * 4 + i];
+    double l = 0.0;
+    if (P < dA && Q < dB) {
+      const int sl = eri->slot_of[P][Q];
+      if (sl >= 0) l = s_val[warp][sl];
+    }
+    s_L[warp][e] = l;
+  }
+  // overlap sums, lane = combination (ss, s-sigma, sigma-s, sigma-sigma, pi-pi)
+  if (lane < 5) {
+    const int c = lane;
+    const bool need = (c == 0) || (c == 1 && nB == 4) || (c == 2 && nA == 4) || (c >= 3 && nA == 4 && nB == 4);
+    double s = 0.0;
+    if (need) {
+      const int zc = (c == 4) ? 3 : c;
+      const double* coef = &ovt->coef[na - 1][nb - 1][c][0][0];
+      for (int i = 0; i < kOvDeg; ++i) {
+        double row = 0.0;
+        for (int j = 0; j < kOvDeg; ++j) row += coef[i * kOvDeg + j] * s_ab[warp][zc][12 + j];
+        s += row * s_ab[warp][zc][i];
+      }
+      const double za = (c >= 2) ? pa.zeta[1] : pa.zeta[0];
+      const double zb = (c == 1 || c >= 3) ? pb.zeta[1] : pb.zeta[0];
+      double fa = 1.0, fb = 1.0;
+      for (int i = 2; i <= 2 * na; ++i) fa *= i;
+      for (int i = 2; i <= 2 * nb; ++i) fb *= i;
+      const double norm = pow(2.0 * za, na + 0.5) * pow(2.0 * zb, nb + 0.5) / sqrt(fa * fb);
+      s *= norm * ovt->ang[c] * pow(0.5 * R, na + nb + 1);
+    }
+    s_ov[warp][c] = s;
+  }
+  __syncwarp();
+
+  // ---- M = L T2^T,  W = T2 M ----------------------------------------------
+  for (int e = lane; e < dA * 10; e += 32) {
+    const int P = e / 10, Qp = e % 10;
+    double s = 0.0;
+    if (Qp < dB)
+      for (int Q = 0; Q < dB; ++Q) s += s_L[warp][P * 10 + Q] * s_T2[warp][Qp * 10 + Q];
+    s_M[warp][e] = s;
+  }
+  __syncwarp();
+  double* out = blocks + pr.blk;
+  for (int e = lane; e < dA * dB; e += 32) {
+    const int Pp = e / dB, Qp = e % dB;
+    double s = 0.0;
+    for (int P = 0; P < dA; ++P) s += s_T2[warp][Pp * 10 + P] * s_M[warp][P * 10 + Qp];
+    out[e] = s;
+  }
+
+  // ---- resonance block of H:  1/2 (beta_mu + beta_nu) S_mu,nu --------------
+  if (lane < 16) {
+    const int mu = lane >> 2, nu = lane & 3;
+    if (mu < nA && nu < nB) {
+      double Ls[4][4] = {};
+      Ls[0][0] = s_ov[warp][0];
+      Ls[0][2] = s_ov[warp][1];
+      Ls[2][0] = s_ov[warp][2];
+      Ls[2][2] = s_ov[warp][3];
+      Ls[1][1] = s_ov[warp][4];
+      Ls[3][3] = s_ov[warp][4];
+      const double* Rm = s_R[warp];
+      double s = 0.0;
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) s += Rm[mu * 4 + i] * Ls[i][j] * Rm[nu * 4 + j];
+      const double h = 0.5 * (pa.beta[mu == 0 ? 0 : 1] + pb.beta[nu == 0 ? 0 : 1]) * s;
+      const long long ld = mol.nao;
+      const long long r0 = A.ao0 + mu, c0 = B.ao0 + nu;
+      H[mol.mat0 + r0 * ld + c0] = h;
+      H[mol.mat0 + c0 * ld + r0] = h;
+    }
+  }
+
+  // ---- core-core repulsion --------------------------------------------------
+  if (lane == 0) {
+    const double ssss = s_val[warp][0];
+    double f;
+    const bool a_no = (pa.atomic_number == 7 || pa.atomic_number == 8);
+    const bool b_no = (pb.atomic_number == 7 || pb.atomic_number == 8);
+    if (pa.atomic_number == 1 && b_no)
+      f = 1.0 + (R / NDDO_ANG2AU) * exp(-pb.alpha * R) + exp(-pa.alpha * R);
+    else if (pb.atomic_number == 1 && a_no)
+      f = 1.0 + (R / NDDO_ANG2AU) * exp(-pa.alpha * R) + exp(-pb.alpha * R);
+    else
+      f = 1.0 + exp(-pa.alpha * R) + exp(-pb.alpha * R);
+    double e = pa.core_charge * pb.core_charge * ssss * f;
+    if (mol.theory != NDDO_MNDO) {
+      double t = 0.0;
+      for (int i = 0; i < 4; ++i) {
+        t += pa.gk[i] * exp(-pa.gl[i] * pow(R - pa.gm[i], 2.0));
+        t += pb.gk[i] * exp(-pb.gl[i] * pow(R - pb.gm[i], 2.0));
+      }
+      e += pa.core_charge * pb.core_charge * t * NDDO_ANG2AU / R;
+    }
+    ecore_pair[p] = e;
+  }
+}
+
+// warp-wide sum with a fixed tree (bitwise reproducible)
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block (a,b) of the molecule, with a flag telling whether atom `self` owns the rows
+__device__ __forceinline__ const double* partner_block(const DevPair* __restrict__ pairs, const double* blocks,
+                                                       const DevMol& mol, int self, int other, bool* self_rows) {
+  const int a = self < other ? self : other, b = self < other ? other : self;
+  *self_rows = self < other;
+  return blocks + pairs[mol.pair0 + pair_index(a, b, mol.natoms)].blk;
+}
+
+constexpr int kFockThreads = 256;
+
+// One-centre block of H (U on the diagonal plus the attraction of every other
+// core, -Z_B (mu nu|s_B s_B)) and the molecule's core-core energy.
+__global__ void __launch_bounds__(kFockThreads)
+hcore_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs, const DevMol* __restrict__ mols,
+             const int* __restrict__ mol_list, const double* __restrict__ blocks,
+             const double* __restrict__ ecore_pair, double* __restrict__ H, MolState* __restrict__ st) {
+  const int m = mol_list[blockIdx.x];
+  const DevMol mol = mols[m];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const long long ld = mol.nao;
+  for (int ia = warp; ia < mol.natoms; ia += nwarps) {
+    const DevAtom A = atoms[mol.atom0 + ia];
+    const int dA = A.nao == 4 ? 10 : 1;
+    double acc[10];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) acc[k] = 0.0;
+    for (int ib = lane; ib < mol.natoms; ib += 32) {
+      if (ib == ia) continue;
+      const DevAtom Bt = atoms[mol.atom0 + ib];
+      const double zb = c_params[Bt.pidx].core_charge;
+      bool rows;
+      const double* blk = partner_block(pairs, blocks, mol, ia, ib, &rows);
+      const int dB = Bt.nao == 4 ? 10 : 1;
+#pragma unroll
+      for (int k = 0; k < 10; ++k)
+        if (k < dA) acc[k] -= zb * (rows ? blk[k * dB] : blk[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 10; ++k) acc[k] = warp_sum(acc[k]);
+    if (lane < dA) {
+      int mu, nu;
+      unpack_index(lane, &mu, &nu);
+      double v = 0.0;
+#pragma unroll
+      for (int k = 0; k < 10; ++k) if (k == lane) v = acc[k];
+      if (mu == nu) v += c_params[A.pidx].u[mu == 0 ? 0 : 1];
+      const long long r = A.ao0 + mu, c = A.ao0 + nu;
+      H[mol.mat0 + r * ld + c] = v;
+      H[mol.mat0 + c * ld + r] = v;
+    }
+  }
+  if (warp == 0) {
+    double s = 0.0;
+    for (int k = lane; k < mol.npairs; k += 32) s += ecore_pair[mol.pair0 + k];
+    s = warp_sum(s);
+    if (lane == 0) st[m].ecore = s;
+  }
+}
+
+__device__ __forceinline__ double g_one(const nddo_atom_params& p, int m, int n) {   // coulomb
+  if (m == 0 && n == 0) return p.gss;
+  if (m == 0 || n == 0) return p.gsp;
+  return m == n ? p.gpp : p.gp2;
+}
+__device__ __forceinline__ double h_one(const nddo_atom_params& p, int m, int n) {   // exchange
+  if (m == n) return g_one(p, m, n);
+  if (m == 0 || n == 0) return p.hsp;
+  return p.hpp;
+}
+
+// F = H + G(P) (mode 0), the MolDS guess Fock (mode 1: U on the diagonal,
+// zero one-centre off-diagonal, resonance blocks between atoms), or H itself
+// (mode 2).  P_old <- P is copied on the way when copy_old is set.
+__global__ void __launch_bounds__(kFockThreads)
+fock_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs, const DevMol* __restrict__ mols,
+            const int* __restrict__ mol_list, const double* __restrict__ blocks, const double* __restrict__ H,
+            const double* __restrict__ P, double* __restrict__ F, double* __restrict__ Pold,
+            const MolState* __restrict__ st, int mode_override, int copy_old, int require_active) {
+  const int m = mol_list[blockIdx.x];
+  const DevMol mol = mols[m];
+  const MolState s = st[m];
+  if (require_active && s.status != kActive) return;
+  int mode = mode_override;
+  if (mode < 0) mode = (s.iter == 0 && s.requires_guess) ? 1 : 0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const long long ld = mol.nao;
+  const double* Pm = P + mol.mat0;
+  const double* Hm = H + mol.mat0;
+  double* Fm = F + mol.mat0;
+  const long long n2 = ld * ld;
+  if (copy_old) {
+    double* Po = Pold + mol.mat0;
+    for (long long i = threadIdx.x; i < n2; i += blockDim.x) Po[i] = Pm[i];
+  }
+  if (mode == 2) {
+    for (long long i = threadIdx.x; i < n2; i += blockDim.x) Fm[i] = Hm[i];
+    return;
+  }
+  for (int ia = warp; ia < mol.natoms; ia += nwarps) {
+    const DevAtom A = atoms[mol.atom0 + ia];
+    const nddo_atom_params& pa = c_params[A.pidx];
+    const int nA = A.nao, dA = nA == 4 ? 10 : 1;
+    const int fa = A.ao0;
+    double acc[10];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) acc[k] = 0.0;
+    if (mode == 0) {
+      // Coulomb: sum_B sum_{la si in B} P_la,si (mu nu|la si)
+      for (int ib = lane; ib < mol.natoms; ib += 32) {
+        if (ib == ia) continue;
+        const DevAtom Bt = atoms[mol.atom0 + ib];
+        const int nB = Bt.nao, dB = nB == 4 ? 10 : 1, fb = Bt.ao0;
+        double pB[10];
+#pragma unroll
+        for (int q = 0; q < 10; ++q) {
+          pB[q] = 0.0;
+          if (q < dB) {
+            int l, sg;
+            unpack_index(q, &l, &sg);
+            pB[q] = Pm[(fb + l) * ld + fb + sg] * (l == sg ? 1.0 : 2.0);
+          }
+        }
+        bool rows;
+        const double* blk = partner_block(pairs, blocks, mol, ia, ib, &rows);
+        if (rows) {
+#pragma unroll
+          for (int k = 0; k < 10; ++k) {
+            if (k >= dA) break;
+            double t = 0.0;
+#pragma unroll
+            for (int q = 0; q < 10; ++q) if (q < dB) t += blk[k * dB + q] * pB[q];
+            acc[k] += t;
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 10; ++k) {
+            if (k >= dA) break;
+            double t = 0.0;
+#pragma unroll
+            for (int q = 0; q < 10; ++q) if (q < dB) t += blk[q * dA + k] * pB[q];
+            acc[k] += t;
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 10; ++k) acc[k] = warp_sum(acc[k]);
+    }
+    // one-centre block
+    if (lane < dA) {
+      int mu, nu;
+      unpack_index(lane, &mu, &nu);
+      double v;
+      if (mode == 1) {
+        v = (mu == nu) ? pa.u[mu == 0 ? 0 : 1] : 0.0;
+      } else {
+        double j = 0.0;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) if (k == lane) j = acc[k];
+        v = Hm[(fa + mu) * ld + fa + nu];
+        if (mu == nu) {
+          double t = 0.0;
+          for (int n = 0; n < nA; ++n) t += Pm[(fa + n) * ld + fa + n] * (g_one(pa, mu, n) - 0.5 * h_one(pa, mu, n));
+          v += t;
+        } else {
+          v += (1.5 * h_one(pa, mu, nu) - 0.5 * g_one(pa, mu, nu)) * Pm[(fa + mu) * ld + fa + nu];
+        }
+        v += j;
+      }
+      Fm[(fa + mu) * ld + fa + nu] = v;
+      Fm[(fa + nu) * ld + fa + mu] = v;
+    }
+    // two-centre blocks (A, B > A): resonance + exchange -1/2 sum P_nu,si (mu nu|la si)
+    for (int ib = ia + 1 + lane; ib < mol.natoms; ib += 32) {
+      const DevAtom Bt = atoms[mol.atom0 + ib];
+      const int nB = Bt.nao, dB = nB == 4 ? 10 : 1, fb = Bt.ao0;
+      const double* blk = blocks + pairs[mol.pair0 + pair_index(ia, ib, mol.natoms)].blk;
+      double pab[4][4];
+      if (mode == 0) {
+        for (int n = 0; n < nA; ++n)
+          for (int sg = 0; sg < nB; ++sg) pab[n][sg] = Pm[(fa + n) * ld + fb + sg];
+      }
+      for (int mu = 0; mu < nA; ++mu)
+        for (int la = 0; la < nB; ++la) {
+          double v = Hm[(fa + mu) * ld + fb + la];
+          if (mode == 0) {
+            double k = 0.0;
+            for (int n = 0; n < nA; ++n)
+              for (int sg = 0; sg < nB; ++sg) k += pab[n][sg] * blk[pack_index(mu, n) * dB + pack_index(la, sg)];
+            v -= 0.5 * k;
+          }
+          Fm[(fa + mu) * ld + fb + la] = v;
+          Fm[(fb + la) * ld + fa + mu] = v;
+        }
+    }
+  }
+}
+
+void launch_pair_kernel(const DevAtom* atoms, const DevPair* pairs, long long npairs, const DevMol* mols,
+                        const EriTable* eri, const OverlapTable* ovt, double* blocks, double* H,
+                        double* ecore_pair, cudaStream_t s) {
+  if (npairs <= 0) return;
+  const long long grid = (npairs + kPairWarps - 1) / kPairWarps;
+  pair_kernel<<<(unsigned)grid, kPairWarps * 32, 0, s>>>(atoms, pairs, npairs, mols, eri, ovt, blocks, H, ecore_pair);
+}
+
+void launch_hcore_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
+                         int nlist, const double* blocks, const double* ecore_pair, double* H, MolState* st,
+                         cudaStream_t s) {
+  if (nlist <= 0) return;
+  hcore_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, pairs, mols, mol_list, blocks, ecore_pair, H, st);
+}
+
+void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
+                        int nlist, const double* blocks, const double* H, const double* P, double* F,
+                        double* Pold, const MolState* st, int mode_override, int copy_old, int require_active,
+                        cudaStream_t s) {
+  if (nlist <= 0) return;
+  fock_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, pairs, mols, mol_list, blocks, H, P, F, Pold, st,
+                                             mode_override, copy_old, require_active);
+}
+
+// E = 1/2 sum P (F + H) + E_core (Cndo2::CalcElecSCFEnergy, src/cndo/Cndo2.cpp:1324-1416),
+// Mulliken charges q_A = Z_A - sum_{mu in A} P_mu,mu (Cndo2.cpp:1187-1199, 1733-1747)
+// and, for MNDO, the heat of formation (Mndo::CalcHeatsFormation, src/mndo/Mndo.cpp:395-404).
+__global__ void __launch_bounds__(kFockThreads)
+energy_kernel(const DevAtom* __restrict__ atoms, const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+              const double* __restrict__ P, const double* __restrict__ F, const double* __restrict__ H,
+              MolState* __restrict__ st, double* __restrict__ charges) {
+  __shared__ double red[32];
+  const int m = mol_list[blockIdx.x];
+  const DevMol mol = mols[m];
+  const long long n2 = (long long)mol.nao * mol.nao;
+  double acc = 0.0;
+  for (long long i = threadIdx.x; i < n2; i += blockDim.x)
+    acc += P[mol.mat0 + i] * (F[mol.mat0 + i] + H[mol.mat0 + i]);
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  for (int a = threadIdx.x; a < mol.natoms; a += blockDim.x) {
+    const DevAtom A = atoms[mol.atom0 + a];
+    double pop = 0.0;
+    for (int k = 0; k < A.nao; ++k) pop += P[mol.mat0 + (long long)(A.ao0 + k) * mol.nao + A.ao0 + k];
+    charges[mol.atom0 + a] = c_params[A.pidx].core_charge - pop;
+  }
+  if (threadIdx.x == 0) {
+    double e = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) e += red[w];
+    e *= 0.5;
+    MolState* s = st + m;
+    s->energy_electronic = e;
+    s->energy = e + s->ecore;
+    double hof = s->energy;
+    for (int a = 0; a < mol.natoms; ++a) {
+      const nddo_atom_params& pa = c_params[atoms[mol.atom0 + a].pidx];
+      hof -= pa.e_atom;
+      hof += pa.dhf_atom;
+    }
+    s->heat_of_formation = hof;
+  }
+}
+
+void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* mol_list, int nlist,
+                          const double* P, const double* F, const double* H, MolState* st, double* charges,
+                          cudaStream_t s) {
+  if (nlist <= 0) return;
+  energy_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, mols, mol_list, P, F, H, st, charges);
+}
+
+}  // namespace nddo

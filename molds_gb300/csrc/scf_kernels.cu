@@ -1,0 +1,395 @@
+// Kernels (c) and (e): batched dense contractions and the density-DIIS step.
+//
+// (c) gemm_kernel -- one launch multiplies a list of per-molecule matrices of
+//     different shapes ("jobs"); each CTA computes one 64x64 tile of one job.
+//     Used for the warm-start transform G = C_prev F C_prev^T, the density
+//     P = 2 C_occ^T C_occ (MolDS Cndo2::CalcOrbitalElectronPopulation,
+//     src/cndo/Cndo2.cpp:1702-1719 via Blas::Dsyrk) and the FP64 subspace
+//     refinement of the mixed-precision path.  The arithmetic type is a template
+//     parameter: FP32 in the early iterations, FP64 after the switch and on the
+//     plain FP64 path.
+//
+// (e) diis_kernel -- one CTA per molecule: RMS density change and convergence
+//     test (Cndo2::SatisfyConvergenceCriterion, src/cndo/Cndo2.cpp:1472-1517),
+//     density DIIS with MolDS's exact window/acceptance rules (Cndo2::DoDIIS,
+//     :920-1028) and damping (Cndo2::DoDamp, :1030-1061).  The DIIS history is
+//     a ring buffer instead of MolDS's memmove shift; the linear system is
+//     assembled in chronological order so it is the same system.  All
+//     reductions use fixed-order trees.
+#include <cuda_runtime.h>
+#include "nddo_batch.cuh"
+#include "kernels.h"
+
+namespace nddo {
+
+constexpr int kTile = 64, kTileK = 16, kGemmThreads = 256;
+
+template <typename TA, typename TB, typename TC, typename TAcc, bool TA_, bool TB_>
+__global__ void __launch_bounds__(kGemmThreads)
+gemm_kernel(const GemmJob* __restrict__ jobs, int njobs, const TA* __restrict__ A, const TB* __restrict__ B,
+            TC* __restrict__ C, const MolState* __restrict__ st, int require_active, int require_phase) {
+  __shared__ TAcc As[kTileK][kTile + 1];
+  __shared__ TAcc Bs[kTileK][kTile + 1];
+  // job of this tile (jobs sorted by tile0)
+  int lo = 0, hi = njobs - 1;
+  const int t = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].tile0 <= t) lo = mid; else hi = mid - 1;
+  }
+  const GemmJob job = jobs[lo];
+  if (require_active && st[job.mol].status != kActive) return;
+  if (require_phase >= 0 && st[job.mol].phase != require_phase) return;
+  const int local = t - job.tile0;
+  const int row0 = (local / job.tiles_n) * kTile, col0 = (local % job.tiles_n) * kTile;
+  const TA* Aj = A + job.a_off;
+  const TB* Bj = B + job.b_off;
+  TC* Cj = C + job.c_off;
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  TAcc acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0;
+
+  for (int k0 = 0; k0 < job.K; k0 += kTileK) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int e = tid + r * kGemmThreads;
+      int ii, kk;
+      if (TA_) { kk = e >> 6; ii = e & 63; } else { ii = e >> 4; kk = e & 15; }
+      const int gi = row0 + ii, gk = k0 + kk;
+      TAcc v = 0;
+      if (gi < job.M && gk < job.K) v = (TAcc)(TA_ ? Aj[(long long)gk * job.lda + gi] : Aj[(long long)gi * job.lda + gk]);
+      As[kk][ii] = v;
+      int jj, kb;
+      if (TB_) { jj = e >> 4; kb = e & 15; } else { kb = e >> 6; jj = e & 63; }
+      const int gj = col0 + jj, gkb = k0 + kb;
+      TAcc w = 0;
+      if (gj < job.N && gkb < job.K) w = (TAcc)(TB_ ? Bj[(long long)gj * job.ldb + gkb] : Bj[(long long)gkb * job.ldb + gj]);
+      Bs[kb][jj] = w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kTileK; ++kk) {
+      TAcc a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gi = row0 + ty * 4 + i;
+    if (gi >= job.M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gj = col0 + tx * 4 + j;
+      if (gj >= job.N) continue;
+      TC* c = Cj + (long long)gi * job.ldc + gj;
+      const double v = job.alpha * (double)acc[i][j];
+      *c = (TC)(job.beta != 0.0 ? v + job.beta * (double)(*c) : v);
+    }
+  }
+}
+
+int gemm_tiles(int M, int N) { return ((M + kTile - 1) / kTile) * ((N + kTile - 1) / kTile); }
+int gemm_tiles_n(int N) { return (N + kTile - 1) / kTile; }
+
+#define GEMM_LAUNCH(TA, TB, TC, TACC)                                                                        \
+  void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const TA* A, const TB* B, TC* C, bool ta,      \
+                   bool tb, TACC /*acc tag*/, const MolState* st, int require_active, int require_phase,        \
+                   cudaStream_t s) {                                                                         \
+    if (ntiles <= 0 || njobs <= 0) return;                                                                   \
+    if (!ta && !tb) gemm_kernel<TA, TB, TC, TACC, false, false><<<ntiles, kGemmThreads, 0, s>>>(jobs, njobs, A, B, C, st, require_active, require_phase); \
+    else if (ta && !tb) gemm_kernel<TA, TB, TC, TACC, true, false><<<ntiles, kGemmThreads, 0, s>>>(jobs, njobs, A, B, C, st, require_active, require_phase); \
+    else if (!ta && tb) gemm_kernel<TA, TB, TC, TACC, false, true><<<ntiles, kGemmThreads, 0, s>>>(jobs, njobs, A, B, C, st, require_active, require_phase); \
+    else gemm_kernel<TA, TB, TC, TACC, true, true><<<ntiles, kGemmThreads, 0, s>>>(jobs, njobs, A, B, C, st, require_active, require_phase); \
+  }
+GEMM_LAUNCH(double, double, double, double)
+GEMM_LAUNCH(double, double, double, float)
+GEMM_LAUNCH(double, double, float, float)
+GEMM_LAUNCH(float, double, float, float)
+GEMM_LAUNCH(double, float, float, float)
+#undef GEMM_LAUNCH
+
+// ---------------------------------------------------------------------------
+// deterministic block reduction helpers (blockDim = 256)
+// ---------------------------------------------------------------------------
+constexpr int kDiisThreads = 256;
+
+__device__ __forceinline__ double block_sum(double v, double* scratch) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) scratch[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += scratch[i];
+    scratch[32] = r;
+  }
+  __syncthreads();
+  r = scratch[32];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v, double* scratch) {
+  for (int o = 16; o > 0; o >>= 1) { double t = __shfl_xor_sync(0xffffffffu, v, o); v = t > v ? t : v; }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) scratch[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = scratch[i] > r ? scratch[i] : r;
+    scratch[32] = r;
+  }
+  __syncthreads();
+  const double r = scratch[32];
+  __syncthreads();
+  return r;
+}
+
+// One SCF bookkeeping step per molecule, after the new density P is formed.
+__global__ void __launch_bounds__(kDiisThreads)
+diis_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list, MolState* __restrict__ st,
+            ScfParamsDev prm, double* __restrict__ P, const double* __restrict__ Pold,
+            double* __restrict__ hist_dens, double* __restrict__ hist_err, long long hist_stride,
+            TraceEntry* __restrict__ trace, int trace_len) {
+  __shared__ double scratch[40];
+  __shared__ double coef[kMaxDiis + 1];
+  __shared__ int flags[3];
+  const int m = mol_list[blockIdx.x];
+  MolState* s = st + m;
+  if (s->status != kActive) return;
+  const DevMol mol = mols[m];
+  const long long n2 = (long long)mol.nao * mol.nao;
+  double* Pm = P + mol.mat0;
+  const double* Po = Pold + mol.mat0;
+  const int iter = s->iter;
+  const bool is_guess = (iter == 0 && s->requires_guess);
+  const int M = prm.diis_m;
+  const bool do_diis = !is_guess && M > 0;
+  const int slot = do_diis ? (s->diis_count % M) : 0;
+  const int count = do_diis ? min(s->diis_count + 1, M) : 0;
+
+  // one pass: e = P - P_old, sum e^2, max |e|, push history, dot products
+  double sq = 0.0, mx = 0.0;
+  double dots[kMaxDiis];
+#pragma unroll
+  for (int k = 0; k < kMaxDiis; ++k) dots[k] = 0.0;
+  double* dslot = hist_dens + slot * hist_stride + mol.mat0;
+  double* eslot = hist_err + slot * hist_stride + mol.mat0;
+  for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
+    const double p = Pm[i];
+    const double e = p - Po[i];
+    sq += e * e;
+    const double ae = fabs(e);
+    mx = ae > mx ? ae : mx;
+    if (do_diis) {
+      dslot[i] = p;
+      eslot[i] = e;
+#pragma unroll
+      for (int k = 0; k < kMaxDiis; ++k)
+        if (k < count) dots[k] += (k == slot ? e : hist_err[k * hist_stride + mol.mat0 + i]) * e;
+    }
+  }
+  const double sumsq = block_sum(sq, scratch);
+  const double maxe = block_max(mx, scratch);
+  const double rms = sqrt(sumsq / (double)n2);
+  double dsum[kMaxDiis];
+#pragma unroll
+  for (int k = 0; k < kMaxDiis; ++k) dsum[k] = (k < count) ? block_sum(dots[k], scratch) : 0.0;
+
+  if (threadIdx.x == 0) {
+    if (trace && iter < trace_len) {
+      TraceEntry te;
+      te.rms = rms; te.diis_err = s->diis_err; te.diis_on = s->diis_on; te.damp_on = s->damp_on;
+      trace[(long long)m * trace_len + iter] = te;
+    }
+    s->rms = rms;
+    flags[0] = 0; flags[1] = 0; flags[2] = 0;
+    if (rms < prm.rms_density) {
+      s->status = kConverged;
+      flags[0] = 1;
+    } else if (!is_guess) {
+      if (do_diis) {
+        for (int k = 0; k < count; ++k) { s->B[k * kMaxDiis + slot] = dsum[k]; s->B[slot * kMaxDiis + k] = dsum[k]; }
+        s->diis_count += 1;
+        s->diis_head = slot;
+        s->diis_err = maxe;
+        bool apply = (M <= iter) && (prm.diis_end < maxe) && (maxe < prm.diis_start) && (count == M);
+        if (apply) {
+          // chronological order: oldest ... newest
+          int chron[kMaxDiis];
+          for (int k = 0; k < M; ++k) chron[k] = (slot + 1 + k) % M;
+          double a[(kMaxDiis + 1) * (kMaxDiis + 1)], b[kMaxDiis + 1];
+          const int n = M + 1;
+          for (int i = 0; i < M; ++i)
+            for (int j = 0; j < M; ++j) a[i * n + j] = s->B[chron[i] * kMaxDiis + chron[j]];
+          for (int i = 0; i < M; ++i) { a[i * n + M] = -1.0; a[M * n + i] = -1.0; b[i] = 0.0; }
+          a[M * n + M] = 0.0;
+          b[M] = -1.0;
+          // Gaussian elimination with partial pivoting; an exactly zero pivot
+          // means a singular system, which MolDS answers by skipping the step
+          bool singular = false;
+          for (int c = 0; c < n && !singular; ++c) {
+            int piv = c;
+            for (int r = c + 1; r < n; ++r) if (fabs(a[r * n + c]) > fabs(a[piv * n + c])) piv = r;
+            if (a[piv * n + c] == 0.0) { singular = true; break; }
+            if (piv != c) {
+              for (int j = 0; j < n; ++j) { double t = a[c * n + j]; a[c * n + j] = a[piv * n + j]; a[piv * n + j] = t; }
+              double t = b[c]; b[c] = b[piv]; b[piv] = t;
+            }
+            for (int r = c + 1; r < n; ++r) {
+              const double f = a[r * n + c] / a[c * n + c];
+              for (int j = c; j < n; ++j) a[r * n + j] -= f * a[c * n + j];
+              b[r] -= f * b[c];
+            }
+          }
+          if (!singular) {
+            for (int c = n - 1; c >= 0; --c) {
+              double v = b[c];
+              for (int j = c + 1; j < n; ++j) v -= a[c * n + j] * b[j];
+              b[c] = v / a[c * n + c];
+            }
+            for (int k = 0; k < M; ++k) coef[k] = b[k];
+            flags[1] = 1;
+          }
+        }
+        s->diis_on = flags[1];
+      }
+      flags[2] = (prm.damping_weight > 0.0 && prm.damping_thresh < rms) ? 1 : 0;
+      s->damp_on = flags[2];
+      if (prm.precision == 1 && s->phase == 0 && do_diis && maxe < prm.switch_error) s->phase = 1;
+    }
+  }
+  __syncthreads();
+  if (flags[0]) return;
+  if (flags[1]) {
+    // P = sum_k c_k P_k in chronological order (MolDS sums the stored
+    // densities in slot order through Dgemv)
+    const int newest = slot;
+    for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
+      double v = 0.0;
+      for (int k = 0; k < M; ++k) {
+        const int rs = (newest + 1 + k) % M;
+        v += coef[k] * hist_dens[rs * hist_stride + mol.mat0 + i];
+      }
+      Pm[i] = v;
+    }
+  }
+  if (flags[2]) {
+    const double w = prm.damping_weight;
+    __syncthreads();
+    for (long long i = threadIdx.x; i < n2; i += blockDim.x) Pm[i] = Pm[i] * (1.0 - w) + w * Po[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s->iter = iter + 1;
+    if (s->iter >= prm.max_iter) s->status = kNotConverged;
+  }
+}
+
+void launch_diis(const DevMol* mols, const int* mol_list, int nlist, MolState* st, const ScfParamsDev& prm,
+                 double* P, const double* Pold, double* hist_dens, double* hist_err, long long hist_stride,
+                 TraceEntry* trace, int trace_len, cudaStream_t s) {
+  if (nlist <= 0) return;
+  diis_kernel<<<nlist, kDiisThreads, 0, s>>>(mols, mol_list, st, prm, P, Pold, hist_dens, hist_err, hist_stride,
+                                             trace, trace_len);
+}
+
+// ---------------------------------------------------------------------------
+// small elementwise helpers
+// ---------------------------------------------------------------------------
+__global__ void convert_f64_to_f32_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+                                          const MolState* __restrict__ st, int require_active,
+                                          const double* __restrict__ src, float* __restrict__ dst) {
+  const int m = mol_list[blockIdx.y];
+  if (require_active && st[m].status != kActive) return;
+  const DevMol mol = mols[m];
+  const long long n2 = (long long)mol.nao * mol.nao;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x)
+    dst[mol.mat0 + i] = (float)src[mol.mat0 + i];
+}
+
+void launch_convert_f64_f32(const DevMol* mols, const int* mol_list, int nlist, const MolState* st,
+                            int require_active, const double* src, float* dst, cudaStream_t s) {
+  if (nlist <= 0) return;
+  dim3 grid(8, nlist);
+  convert_f64_to_f32_kernel<<<grid, 256, 0, s>>>(mols, mol_list, st, require_active, src, dst);
+}
+
+// FP64 refinement helper: K_ai = -Kt_ai / (eps_a - eps_i), a virtual, i occupied
+__global__ void newton_scale_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+                                    const MolState* __restrict__ st, int require_phase, double* __restrict__ K,
+                                    const double* __restrict__ eps) {
+  const int m = mol_list[blockIdx.y];
+  if (st[m].status != kActive || (require_phase >= 0 && st[m].phase != require_phase)) return;
+  const DevMol mol = mols[m];
+  const int n = mol.nao, o = mol.nocc, v = n - o;
+  const long long cnt = (long long)v * o;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x) {
+    const int a = (int)(e / o), i = (int)(e % o);
+    const double gap = eps[mol.vec0 + o + a] - eps[mol.vec0 + i];
+    K[mol.mat0 + e] = -K[mol.mat0 + e] / gap;
+  }
+}
+
+void launch_newton_scale(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
+                         double* K, const double* eps, cudaStream_t s) {
+  if (nlist <= 0) return;
+  newton_scale_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, K, eps);
+}
+
+// Minv = I - D + D2 with D = M - I (o x o); D2 computed separately as D*D.
+// mode 0: M <- M - I (so M holds D); mode 1: M <- I - M + D2
+__global__ void neumann_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+                               const MolState* __restrict__ st, int require_phase, double* __restrict__ Mm,
+                               const double* __restrict__ D2, int mode) {
+  const int m = mol_list[blockIdx.y];
+  if (st[m].status != kActive || (require_phase >= 0 && st[m].phase != require_phase)) return;
+  const DevMol mol = mols[m];
+  const int o = mol.nocc;
+  const long long cnt = (long long)o * o;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / o), j = (int)(e % o);
+    double* x = Mm + mol.mat0 + e;
+    if (mode == 0) *x = *x - (i == j ? 1.0 : 0.0);
+    else *x = (i == j ? 1.0 : 0.0) - *x + D2[mol.mat0 + e];
+  }
+}
+
+void launch_neumann(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
+                    double* M, const double* D2, int mode, cudaStream_t s) {
+  if (nlist <= 0) return;
+  neumann_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, M, D2, mode);
+}
+
+// copy the first `rows` rows of C (n x n, row-major) into dst (rows x n)
+__global__ void copy_rows_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+                                 const MolState* __restrict__ st, int require_phase, const double* __restrict__ src,
+                                 double* __restrict__ dst) {
+  const int m = mol_list[blockIdx.y];
+  if (st[m].status != kActive || (require_phase >= 0 && st[m].phase != require_phase)) return;
+  const DevMol mol = mols[m];
+  const long long cnt = (long long)mol.nocc * mol.nao;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x)
+    dst[mol.mat0 + e] = src[mol.mat0 + e];
+}
+
+void launch_copy_occ_rows(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
+                          const double* src, double* dst, cudaStream_t s) {
+  if (nlist <= 0) return;
+  copy_rows_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, src, dst);
+}
+
+}  // namespace nddo

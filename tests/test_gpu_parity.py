@@ -1,0 +1,208 @@
+"""Parity of the CUDA path with the oracle, through the C ABI.
+
+Bars (from the reference's own correctness targets):
+  * plain FP64 path: total energy within 1e-8 Eh, Mulliken charges within 1e-6
+  * mixed precision: total energy within 1e-6 Eh
+  * one-time integrals (pair blocks, core Hamiltonian): 1e-11 absolute
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import molds_gb300 as M
+from molds_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIX = json.load(open(os.path.join(HERE, "golden", "reference_fixtures.json")))["cases"]
+E_TOL_FP64 = 1e-8
+Q_TOL = 1e-6
+E_TOL_MIXED = 1e-6
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from molds_gb300 import build
+    build.build()
+    return M.Context(0)
+
+
+def oracle_params(p: M.SCFParams):
+    return O.SCFParams(max_iter=p.max_iter, rms_density=p.rms_density, damping_thresh=p.damping_thresh,
+                       damping_weight=p.damping_weight, diis_num_error_vect=p.diis_num_error_vect,
+                       diis_start_error=p.diis_start_error, diis_end_error=p.diis_end_error)
+
+
+BENCH_SCF = M.SCFParams(max_iter=500, rms_density=1e-8, damping_thresh=1.0, damping_weight=0.0,
+                        diis_num_error_vect=5, diis_start_error=0.1, diis_end_error=0.0)
+
+
+def packed_from_oracle(mol, eri):
+    """Oracle 4-index pair blocks -> the library's packed layout."""
+    info = O.atom_info(mol)
+    nao = info[:, 1].astype(int)
+    out = []
+    pidx = 0
+    idx = [(0, 0), (0, 1), (0, 2), (0, 3), (1, 1), (1, 2), (1, 3), (2, 2), (2, 3), (3, 3)]
+    A = mol.natoms
+    for a in range(A):
+        for b in range(a + 1, A):
+            da = 10 if nao[a] == 4 else 1
+            db = 10 if nao[b] == 4 else 1
+            W4 = eri[pidx]
+            blk = np.zeros((da, db))
+            for P in range(da):
+                for Q in range(db):
+                    m, n = idx[P]
+                    l, s = idx[Q]
+                    blk[P, Q] = W4[m, n, l, s]
+            out.append(blk.ravel())
+            pidx += 1
+    return np.concatenate(out) if out else np.zeros(0)
+
+
+MOLS = {
+    "ch3cl_pm3": lambda: O.parse_input([c for c in FIX if c["name"] == "ch3cl_pm3"][0]["input"])[0],
+    "ch3f_mndo": lambda: O.parse_input([c for c in FIX if c["name"] == "ch3f_mndo"][0]["input"])[0],
+    "water2_am1": lambda: O.make_molecule("am1", *_w2()),
+    "nh3_h2s_mndo": lambda: O.make_molecule("mndo", np.array([7, 1, 1, 1, 16, 1, 1], dtype=np.int32),
+                                            np.array([[0, 0, 0], [1.9, 0, 0], [-0.6, 1.8, 0], [-0.6, -0.9, 1.6],
+                                                      [5.0, 1.0, 0.5], [6.0, 2.2, 0.5], [5.5, -0.3, 1.7]])),
+}
+
+
+def _w2():
+    m = W.water_cluster(shape=(2, 1, 1), seed=7)
+    return m.Z, m.xyz
+
+
+@pytest.mark.parametrize("name", sorted(MOLS))
+def test_pair_blocks_and_core_hamiltonian(ctx, name):
+    mol = MOLS[name]()
+    S, eri, ecore = O.integrals(mol)
+    es = M.ElectronicStructure(mol.theory, context=ctx)
+    es.SetMolecule(M.Molecule(mol.Z, mol.xyz))
+    blocks = es.GetPairBlocks()
+    ref = packed_from_oracle(mol, eri)
+    assert blocks.shape == ref.shape
+    assert np.max(np.abs(blocks - ref)) < 1e-11
+    H = es.GetCoreHamiltonian()
+    H_ref = O.fock(mol, S, eri, np.zeros_like(S), guess=False)
+    assert np.max(np.abs(H - H_ref)) < 1e-11
+
+
+@pytest.mark.parametrize("case", FIX, ids=[c["name"] for c in FIX])
+def test_reference_fixtures_fp64(ctx, case):
+    mol, p = O.parse_input(case["input"])
+    ref = O.scf(mol, p)
+    params = M.SCFParams(max_iter=p.max_iter, rms_density=p.rms_density, damping_thresh=p.damping_thresh,
+                         damping_weight=p.damping_weight, diis_num_error_vect=p.diis_num_error_vect,
+                         diis_start_error=p.diis_start_error, diis_end_error=p.diis_end_error)
+    es = M.ElectronicStructure(mol.theory, params, context=ctx)
+    es.SetMolecule(M.Molecule(mol.Z, mol.xyz))
+    es.DoSCF(True)
+    assert abs(es.GetElectronicEnergy(0) - ref.energy) < E_TOL_FP64
+    assert abs(es.GetCoreRepulsionEnergy() - ref.core_repulsion) < 1e-10
+    assert np.max(np.abs(es.GetMullikenCharges() - ref.charges)) < Q_TOL
+    assert np.max(np.abs(es.GetEnergiesMO() - ref.eps)) < 1e-7
+    # the printed values of the reference itself (7 significant digits)
+    assert abs(es.GetElectronicEnergy(0) - case["energy"]) <= 1e-6 * abs(case["energy"])
+    if p.rms_density >= 1e-12:
+        assert es.GetIterations() == ref.iterations
+        tr = es.GetTrace()
+        for (i, rms, derr, on, _), (_, rrms, rderr, ron, _) in zip(tr, ref.trace):
+            assert abs(rms - rrms) <= 1e-6 * rrms + 1e-12, (i, rms, rrms)
+            assert on == ron
+    if mol.theory == 0:
+        assert abs(es.GetHeatsFormation() - ref.heat_of_formation) < E_TOL_FP64
+
+
+def test_density_and_eigenvectors_fp64(ctx):
+    case = [c for c in FIX if c["name"] == "c2h6_am1"][0]
+    mol, p = O.parse_input(case["input"])
+    ref = O.scf(mol, p)
+    es = M.ElectronicStructure(mol.theory, M.SCFParams(**{k: getattr(p, k) for k in vars(p)}), context=ctx)
+    es.SetMolecule(M.Molecule(mol.Z, mol.xyz))
+    es.DoSCF(True)
+    P = es.GetOrbitalElectronPopulation()
+    assert np.max(np.abs(P - ref.P)) < 1e-8
+    C = es.GetFockMatrix()
+    eps = es.GetEnergiesMO()
+    # rows are orthonormal eigenvectors with component sum >= 0 (Lapack.cpp:141-150)
+    assert np.max(np.abs(C @ C.T - np.eye(len(eps)))) < 1e-10
+    assert np.all(C.sum(axis=1) >= 0)
+
+
+def test_octane_pm3_fp64(ctx):
+    mol = W.octane()
+    ref = O.scf(O.make_molecule("pm3", mol.Z, mol.xyz), oracle_params(BENCH_SCF))
+    es = M.ElectronicStructure("pm3", BENCH_SCF, context=ctx)
+    es.SetMolecule(mol)
+    es.DoSCF(True)
+    assert abs(es.GetElectronicEnergy(0) - ref.energy) < E_TOL_FP64
+    assert np.max(np.abs(es.GetMullikenCharges() - ref.charges)) < Q_TOL
+    assert es.GetIterations() == ref.iterations
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_water_cluster_am1(ctx, precision):
+    mol = W.water_cluster(shape=(2, 2, 2), seed=2)          # (H2O)8, 48 basis functions
+    ref = O.scf(O.make_molecule("am1", mol.Z, mol.xyz), oracle_params(BENCH_SCF))
+    p = M.SCFParams(**{**vars(BENCH_SCF), "precision": precision})
+    es = M.ElectronicStructure("am1", p, context=ctx)
+    es.SetMolecule(mol)
+    es.DoSCF(True)
+    tol = E_TOL_FP64 if precision == "fp64" else E_TOL_MIXED
+    assert abs(es.GetElectronicEnergy(0) - ref.energy) < tol
+    assert np.max(np.abs(es.GetMullikenCharges() - ref.charges)) < Q_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_matches_oracle_and_is_invariant(ctx, precision):
+    base = W.water_cluster(shape=(2, 2, 1), seed=2)          # (H2O)4
+    mols = W.water_replicas(base, 6)
+    p = M.SCFParams(**{**vars(BENCH_SCF), "precision": precision})
+    res, charges = M.batch_scf("am1", mols, p, context=ctx)
+    tol = E_TOL_FP64 if precision == "fp64" else E_TOL_MIXED
+    for m, r, q in zip(mols, res, charges):
+        ref = O.scf(O.make_molecule("am1", m.Z, m.xyz), oracle_params(BENCH_SCF))
+        assert r["status"] == M.STATUS_CONVERGED
+        assert abs(r["energy"] - ref.energy) < tol
+        assert np.max(np.abs(q - ref.charges)) < Q_TOL
+    # each molecule's result is the same alone and in the batch (bitwise)
+    alone, qa = M.batch_scf("am1", [mols[3]], p, context=ctx)
+    assert alone[0]["energy"] == res[3]["energy"]
+    assert np.array_equal(qa[0], charges[3])
+
+
+def test_uneven_batch(ctx):
+    mols = [W.random_alkane(3000000 + j, n=n) for j, n in enumerate([3, 7, 12, 5])]
+    mols.append(W.octane())
+    res, charges = M.batch_scf("pm3", mols, BENCH_SCF, context=ctx)
+    for m, r, q in zip(mols, res, charges):
+        ref = O.scf(O.make_molecule("pm3", m.Z, m.xyz), oracle_params(BENCH_SCF))
+        assert abs(r["energy"] - ref.energy) < E_TOL_FP64
+        assert np.max(np.abs(q - ref.charges)) < Q_TOL
+        assert r["iterations"] == ref.iterations
+
+
+def test_errors(ctx):
+    es = M.ElectronicStructure("pm3", context=ctx)
+    with pytest.raises(M.NddoError):          # odd electron count (Cndo2.cpp:351-357)
+        es.SetMolecule(M.Molecule(np.array([1], dtype=np.int32), np.zeros((1, 3))))
+    with pytest.raises(M.NddoError):          # no parameters for the element
+        es.SetMolecule(M.Molecule(np.array([54, 54], dtype=np.int32), np.array([[0, 0, 0], [3.0, 0, 0]])))
+    with pytest.raises(M.NddoError):          # coincident atoms (EularAngle.cpp:42-46)
+        es.SetMolecule(M.Molecule(np.array([1, 1], dtype=np.int32), np.zeros((2, 3))))
+    with pytest.raises(M.NddoError):          # non-finite coordinate
+        es.SetMolecule(M.Molecule(np.array([1, 1], dtype=np.int32), np.array([[0, 0, 0], [np.nan, 0, 0]])))
+    es.SetMolecule(W.octane())
+    with pytest.raises(M.SCFNotConverged):    # Cndo2.cpp:700-704
+        es.DoSCF(True, M.SCFParams(max_iter=3))
+    tiny = M.Context(0, hbm_budget_bytes=1024)
+    with pytest.raises(M.BudgetExceeded):
+        M.ElectronicStructure("pm3", context=tiny).SetMolecule(W.octane())
