@@ -107,6 +107,39 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
                    const double* xyz_bohr, const nddo_scf_params* params, nddo_scf_result* results,
                    double* charges);
 
+/* A device-resident batch: the molecules' geometry, integrals, densities and
+ * DIIS history stay on the GPU between calls, so repeated SCFs of the same
+ * molecules (MD / MC / optimiser steps that call DoSCF again, src/md/MD.cpp:108,
+ * src/mc/MC.cpp:124) pay no allocation and no re-upload. */
+typedef struct nddo_batch nddo_batch;
+int nddo_batch_create(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, const int* atomic_numbers,
+                      const double* xyz_bohr, int diis_num_error_vect, nddo_batch** out);
+/* Integrals + SCF + energies of every molecule, on the device only. */
+int nddo_batch_run(nddo_batch* b, const nddo_scf_params* params);
+/* New coordinates for all atoms (same atoms, batch order), bohr. */
+int nddo_batch_set_coordinates(nddo_batch* b, const double* xyz_bohr);
+int nddo_batch_results(nddo_batch* b, nddo_scf_result* results, double* charges);
+size_t nddo_batch_device_bytes(const nddo_batch* b);
+void nddo_batch_destroy(nddo_batch* b);
+/* Per-kernel-class CUDA-event timing on the launching stream: after enabling,
+ * nddo_batch_kernel_times returns, per class, the accumulated milliseconds,
+ * the number of timed launches and the algorithmic work of those launches
+ * (FLOPs for contractions and the eigensolver, bytes for memory-bound steps).
+ * Returns the number of classes. */
+int nddo_batch_profile(nddo_batch* b, int enable);
+int nddo_batch_kernel_times(nddo_batch* b, int max_classes, double* ms, long long* launches, double* work);
+const char* nddo_kernel_class_name(int k);
+/* CUDA events on the batch's stream: op 0 records the start, op 1 the stop,
+ * op 2 synchronises and writes the elapsed milliseconds to *ms. */
+int nddo_batch_timer(nddo_batch* b, int op, double* ms);
+/* Number of CUDA kernels this batch has launched so far. */
+long long nddo_batch_launch_count(const nddo_batch* b);
+
+/* Measured arithmetic peak of this GPU's CUDA cores (not the tensor cores):
+ * a dependent-FMA loop over every SM, FP32 (precision 0) or FP64 (1), in
+ * TFLOP/s.  The denominator of the eigensolver's roofline. */
+int nddo_measure_fma_peak(nddo_ctx* ctx, int precision, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,20 @@ SIGNATURES = {
     "nddo_get_pair_blocks": (ctypes.c_int, [_CTX, _DP, ctypes.POINTER(ctypes.c_size_t)]),
     "nddo_batch_scf": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, ctypes.POINTER(ScfParamsC),
                                       ctypes.POINTER(ScfResultC), _DP]),
+    "nddo_batch_create": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "nddo_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScfParamsC)]),
+    "nddo_batch_set_coordinates": (ctypes.c_int, [ctypes.c_void_p, _DP]),
+    "nddo_batch_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScfResultC), _DP]),
+    "nddo_batch_device_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "nddo_batch_destroy": (None, [ctypes.c_void_p]),
+    "nddo_batch_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "nddo_batch_kernel_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _DP,
+                                               ctypes.POINTER(ctypes.c_longlong), _DP]),
+    "nddo_kernel_class_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "nddo_batch_timer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _DP]),
+    "nddo_measure_fma_peak": (ctypes.c_int, [_CTX, ctypes.c_int, _DP]),
+    "nddo_batch_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
 }
 
 _lib = None
@@ -150,6 +164,11 @@ class Context:
         if getattr(self, "h", None):
             self.lib.nddo_destroy(self.h)
             self.h = None
+
+    def fma_peak_tflops(self, precision="fp32") -> float:
+        v = ctypes.c_double()
+        self.check(self.lib.nddo_measure_fma_peak(self.h, 0 if precision == "fp32" else 1, ctypes.byref(v)))
+        return v.value
 
     def __del__(self):
         try:
@@ -277,3 +296,74 @@ def batch_scf(theory, molecules, params: SCFParams | None = None, context: Conte
                 final_diis_error=r.final_diis_error) for r in res]
     offs = np.concatenate([[0], np.cumsum(nat)])
     return out, [ch[offs[i]:offs[i + 1]] for i in range(len(molecules))]
+
+
+class ResidentBatch:
+    """A batch of molecules kept on the device (nddo_batch_*): run() repeats
+    integrals + SCF + energies with no host traffic besides the per-iteration
+    convergence count."""
+
+    def __init__(self, theory, molecules, diis_num_error_vect=5, context: Context | None = None):
+        self.ctx = context or Context()
+        th = THEORIES[theory.lower()] if isinstance(theory, str) else int(theory)
+        self.nat = np.array([m.natoms for m in molecules], dtype=np.int32)
+        Z = np.ascontiguousarray(np.concatenate([m.Z for m in molecules]), dtype=np.int32)
+        xyz = np.ascontiguousarray(np.concatenate([np.asarray(m.xyz).reshape(-1, 3) for m in molecules]))
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.nddo_batch_create(self.ctx.h, th, len(molecules), _ip(self.nat), _ip(Z), _dp(xyz),
+                                                      diis_num_error_vect, ctypes.byref(h)))
+        self.h = h
+        self.n = len(molecules)
+
+    def run(self, params: SCFParams):
+        p = to_c_params(params)
+        self.ctx.check(self.ctx.lib.nddo_batch_run(self.h, ctypes.byref(p)))
+
+    def set_coordinates(self, xyz):
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        self.ctx.check(self.ctx.lib.nddo_batch_set_coordinates(self.h, _dp(x)))
+
+    def results(self):
+        res = (ScfResultC * self.n)()
+        ch = np.zeros(int(self.nat.sum()))
+        rc = self.ctx.lib.nddo_batch_results(self.h, res, _dp(ch))
+        if rc < 0:
+            self.ctx.check(rc)
+        offs = np.concatenate([[0], np.cumsum(self.nat)])
+        out = [dict(status=r.status, iterations=r.iterations, energy=r.energy, core_repulsion=r.core_repulsion,
+                    heat_of_formation=r.heat_of_formation, final_rms=r.final_rms,
+                    final_diis_error=r.final_diis_error) for r in res]
+        return out, [ch[offs[i]:offs[i + 1]] for i in range(self.n)]
+
+    def device_bytes(self) -> int:
+        return int(self.ctx.lib.nddo_batch_device_bytes(self.h))
+
+    def launch_count(self) -> int:
+        return int(self.ctx.lib.nddo_batch_launch_count(self.h))
+
+    def timer(self, op):
+        ms = ctypes.c_double()
+        self.ctx.check(self.ctx.lib.nddo_batch_timer(self.h, op, ctypes.byref(ms)))
+        return ms.value
+
+    def profile(self, enable=True):
+        self.ctx.check(self.ctx.lib.nddo_batch_profile(self.h, 1 if enable else 0))
+
+    def kernel_times(self):
+        k = 16
+        ms, w = np.zeros(k), np.zeros(k)
+        ln = (ctypes.c_longlong * k)()
+        n = self.ctx.check(self.ctx.lib.nddo_batch_kernel_times(self.h, k, _dp(ms), ln, _dp(w)))
+        return {self.ctx.lib.nddo_kernel_class_name(i).decode(): dict(ms=float(ms[i]), launches=int(ln[i]),
+                                                                      work=float(w[i])) for i in range(n)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.nddo_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -10,6 +10,60 @@
 
 #include "engine.h"
 
+struct nddo_batch {
+  nddo_ctx* ctx;
+  std::unique_ptr<nddo::Batch> b;
+  std::vector<int> n_atoms;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  ~nddo_batch() {
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+  }
+};
+
+namespace {
+// Calibration kernel: eight independent FMA chains per thread.
+template <typename T>
+__global__ void fma_peak_kernel(T* out, int iters, T a, T b) {
+  T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+    x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <typename T>
+double fma_peak(cudaStream_t s, int iters) {
+  int dev = 0, sms = 0;
+  nddo::cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  nddo::cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+  const int blocks = sms * 4, threads = 256;
+  T* out = nullptr;
+  nddo::cuda_check(cudaMalloc(&out, sizeof(T) * blocks * threads), "cudaMalloc");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fma_peak_kernel<T><<<blocks, threads, 0, s>>>(out, 16, (T)0.999, (T)0.001);
+  double best = 0.0;
+  for (int r = 0; r < 3; ++r) {
+    cudaEventRecord(e0, s);
+    fma_peak_kernel<T><<<blocks, threads, 0, s>>>(out, iters, (T)0.999, (T)0.001);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double tf = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    best = tf > best ? tf : best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  nddo::cuda_check(cudaGetLastError(), "fma_peak_kernel");
+  return best;
+}
+}  // namespace
+
 struct nddo_ctx {
   std::unique_ptr<nddo::Engine> engine;
   std::unique_ptr<nddo::Batch> mol;      // current molecule (SetMolecule / DoSCF API)
@@ -254,6 +308,144 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
     }
     if (rc != NDDO_OK) ctx->err = "SCF did not met convergence criterion for at least one molecule";
     return rc;
+  });
+}
+
+int nddo_batch_create(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, const int* Z, const double* xyz,
+                      int diis_m, nddo_batch** out) {
+  return guarded(ctx, [&]() {
+    if (!out) return fail(ctx, NDDO_ERR_ARGUMENT, "null output handle");
+    *out = nullptr;
+    if (!ctx->engine) return fail(ctx, NDDO_ERR_STATE, "engine not initialised");
+    if (n_mol < 1 || !n_atoms || !Z || !xyz) return fail(ctx, NDDO_ERR_ARGUMENT, "bad batch arguments");
+    if (diis_m < 0 || diis_m > nddo::kMaxDiis) return fail(ctx, NDDO_ERR_ARGUMENT, "diis_num_error_vect must be in 0..8");
+    std::vector<nddo::MoleculeInput> mols(n_mol);
+    size_t off = 0;
+    for (int i = 0; i < n_mol; ++i) {
+      if (n_atoms[i] < 1) return fail(ctx, NDDO_ERR_ARGUMENT, "molecule without atoms");
+      mols[i].theory = theory;
+      mols[i].Z.assign(Z + off, Z + off + n_atoms[i]);
+      mols[i].xyz.assign(xyz + 3 * off, xyz + 3 * (off + n_atoms[i]));
+      off += n_atoms[i];
+    }
+    std::unique_ptr<nddo::Batch> b(new nddo::Batch(ctx->engine.get(), mols, diis_m));
+    if (ctx->budget && b->device_bytes() > ctx->budget)
+      return fail(ctx, NDDO_ERR_BUDGET, "batch needs " + std::to_string(b->device_bytes()) + " bytes of HBM, budget is " + std::to_string(ctx->budget));
+    nddo_batch* h = new nddo_batch();
+    h->ctx = ctx;
+    h->b = std::move(b);
+    h->n_atoms.assign(n_atoms, n_atoms + n_mol);
+    *out = h;
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_batch_run(nddo_batch* h, const nddo_scf_params* params) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() {
+    std::string why;
+    if (!valid_params(params, &why)) return fail(h->ctx, NDDO_ERR_ARGUMENT, why);
+    nddo::ScfSettings s = to_settings(params);
+    s.keep_trace = 0;
+    h->b->integrals();
+    h->b->scf(s, true);
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_batch_set_coordinates(nddo_batch* h, const double* xyz) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() {
+    if (!xyz) return fail(h->ctx, NDDO_ERR_ARGUMENT, "null coordinates");
+    h->b->set_coordinates(xyz);
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_batch_results(nddo_batch* h, nddo_scf_result* results, double* charges) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() {
+    if (!results) return fail(h->ctx, NDDO_ERR_ARGUMENT, "null results");
+    std::vector<nddo::MolResult> r;
+    h->b->results(&r);
+    int rc = NDDO_OK;
+    size_t off = 0;
+    for (size_t i = 0; i < r.size(); ++i) {
+      results[i].status = r[i].status;
+      results[i].iterations = r[i].iterations;
+      results[i].energy = r[i].energy;
+      results[i].core_repulsion = r[i].core_repulsion;
+      results[i].heat_of_formation = r[i].heat_of_formation;
+      results[i].final_rms = r[i].final_rms;
+      results[i].final_diis_error = r[i].final_diis_error;
+      if (r[i].status != nddo::kConverged) rc = NDDO_NOT_CONVERGED;
+      if (charges) h->b->copy_charges((int)i, charges + off);
+      off += h->n_atoms[i];
+    }
+    if (rc != NDDO_OK) h->ctx->err = "SCF did not met convergence criterion for at least one molecule";
+    return rc;
+  });
+}
+
+size_t nddo_batch_device_bytes(const nddo_batch* h) { return h ? h->b->device_bytes() : 0; }
+
+long long nddo_batch_launch_count(const nddo_batch* h) { return h ? h->b->launches() : -1; }
+
+void nddo_batch_destroy(nddo_batch* h) { delete h; }
+
+int nddo_batch_profile(nddo_batch* h, int enable) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() {
+    h->b->profile_reset();
+    h->b->set_profiling(enable != 0);
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_batch_kernel_times(nddo_batch* h, int max_classes, double* ms, long long* launches, double* work) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() {
+    double a[nddo::kKNumClasses], w[nddo::kKNumClasses];
+    long long l[nddo::kKNumClasses];
+    h->b->profile_collect(a, l, w);
+    const int n = std::min<int>(max_classes, nddo::kKNumClasses);
+    for (int k = 0; k < n; ++k) {
+      if (ms) ms[k] = a[k];
+      if (launches) launches[k] = l[k];
+      if (work) work[k] = w[k];
+    }
+    return (int)nddo::kKNumClasses;
+  });
+}
+
+const char* nddo_kernel_class_name(int k) { return nddo::kernel_class_name(k); }
+
+int nddo_batch_timer(nddo_batch* h, int op, double* ms) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() {
+    cudaStream_t s = h->ctx->engine->stream();
+    if (!h->t0) {
+      nddo::cuda_check(cudaEventCreate(&h->t0), "cudaEventCreate");
+      nddo::cuda_check(cudaEventCreate(&h->t1), "cudaEventCreate");
+    }
+    if (op == 0) nddo::cuda_check(cudaEventRecord(h->t0, s), "cudaEventRecord");
+    else if (op == 1) nddo::cuda_check(cudaEventRecord(h->t1, s), "cudaEventRecord");
+    else {
+      nddo::cuda_check(cudaEventSynchronize(h->t1), "cudaEventSynchronize");
+      float t = 0.f;
+      nddo::cuda_check(cudaEventElapsedTime(&t, h->t0, h->t1), "cudaEventElapsedTime");
+      if (ms) *ms = t;
+    }
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_measure_fma_peak(nddo_ctx* ctx, int precision, double* tflops) {
+  return guarded(ctx, [&]() {
+    if (!ctx->engine || !tflops) return fail(ctx, NDDO_ERR_ARGUMENT, "bad arguments");
+    cudaStream_t s = ctx->engine->stream();
+    *tflops = precision == 0 ? fma_peak<float>(s, 200000) : fma_peak<double>(s, 20000);
+    return (int)NDDO_OK;
   });
 }
 

@@ -54,12 +54,16 @@ __global__ void init_state_kernel(const DevMol* __restrict__ mols, const int* __
 }
 
 __global__ void count_active_kernel(const int* __restrict__ list, int n, const MolState* __restrict__ st,
-                                    int* __restrict__ out) {
+                                    int* __restrict__ out, char* __restrict__ active) {
   __shared__ int cnt;
   if (threadIdx.x == 0) cnt = 0;
   __syncthreads();
   int c = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) c += (st[list[i]].status == kActive);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int a = (st[list[i]].status == kActive);
+    active[list[i]] = (char)a;
+    c += a;
+  }
   atomicAdd(&cnt, c);
   __syncthreads();
   if (threadIdx.x == 0) *out = cnt;
@@ -175,6 +179,7 @@ Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
   d_charges = dalloc<double>(h_atoms.size(), &bytes_);
   d_sweeps = dalloc<int>(nm, &bytes_);
   d_count = dalloc<int>(1, &bytes_);
+  d_active = dalloc<char>(nm, &bytes_);
   cuda_check(cudaMemcpyAsync(d_atoms, h_atoms.data(), h_atoms.size() * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_), "upload atoms");
   if (!h_pairs.empty())
     cuda_check(cudaMemcpyAsync(d_pairs, h_pairs.data(), h_pairs.size() * sizeof(DevPair), cudaMemcpyHostToDevice, stream_), "upload pairs");
@@ -200,16 +205,17 @@ Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
 
 Batch::~Batch() {
   free_jobs();
+  for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   for (int* p : d_bucket_lists_) cudaFree(p);
   void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
                   d_hist_dens, d_hist_err, d_G32, d_T32, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
-                  d_state, d_trace, d_charges, d_sweeps, d_count};
+                  d_state, d_trace, d_charges, d_sweeps, d_count, d_active};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
 }
 
 void Batch::free_jobs() {
-  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_};
+  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_};
   for (JobSet* j : all) { if (j->d) cudaFree(j->d); j->d = nullptr; j->n = 0; j->tiles = 0; }
 }
 
@@ -239,17 +245,20 @@ static GemmJob job(long long a, long long b, long long c, int M, int N, int K, i
 
 void Batch::build_jobs(const std::vector<int>& which) {
   free_jobs();
-  std::vector<GemmJob> t1, t2, dn, w, kt, yt, mm, d2, z, pp;
+  std::vector<GemmJob> t1, t2, dn, w, kt, yt, mm, d2, z, pp, ns1, ns2, ov;
   for (int m : which) {
     const DevMol& d = h_mols[m];
     const int n = d.nao, o = d.nocc, v = n - o;
     const long long b = d.mat0;
+    ns1.push_back(job(b, b, b, n, n, n, n, n, n, m));           // M = C C^T          (B transposed)
+    ns2.push_back(job(b, b, b, n, n, n, n, n, n, m, -0.5, 1.5)); // C' = 1.5 C - 0.5 M C
     t1.push_back(job(b, b, b, n, n, n, n, n, n, m));            // T = F C^T          (B transposed)
     t2.push_back(job(b, b, b, n, n, n, n, n, n, m));            // G = C T
     dn.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0));       // P = 2 C_o^T C_o    (A transposed)
     if (o > 0 && v > 0) {
       w.push_back(job(b, b, b, n, o, n, n, n, o, m));                       // W = F C_o^T   (B transposed)
       kt.push_back(job(b + (long long)o * n, b, b, v, o, n, n, o, o, m));   // Kt = C_v W
+      ov.push_back(job(b + (long long)o * n, b, b, v, o, n, n, n, o, m));   // O = C_v C_o^T (B transposed)
       yt.push_back(job(b, b + (long long)o * n, b, o, n, v, o, n, n, m, 1.0, 1.0));  // Yt = C_o + K^T C_v (A transposed)
       mm.push_back(job(b, b, b, o, o, n, n, n, o, m));                      // M = Yt Yt^T   (B transposed)
       d2.push_back(job(b, b, b, o, o, o, o, o, o, m));                      // D2 = D D
@@ -260,6 +269,7 @@ void Batch::build_jobs(const std::vector<int>& which) {
   make_jobset(&j_trans1_, t1); make_jobset(&j_trans2_, t2); make_jobset(&j_dens_, dn);
   make_jobset(&j_w_, w); make_jobset(&j_kt_, kt); make_jobset(&j_yt_, yt); make_jobset(&j_m_, mm);
   make_jobset(&j_d2_, d2); make_jobset(&j_z_, z); make_jobset(&j_p_, pp);
+  make_jobset(&j_ns1_, ns1); make_jobset(&j_ns2_, ns2); make_jobset(&j_ov_, ov);
 }
 
 void Batch::upload_list(const std::vector<int>& which) {
@@ -292,14 +302,124 @@ void Batch::upload_list(const std::vector<int>& which) {
   }
 }
 
+const char* kernel_class_name(int k) {
+  static const char* names[kKNumClasses] = {"pair_integrals", "core_hamiltonian", "fock_build", "basis_orthonormalise",
+                                            "warm_start_transform", "jacobi_eigensolver", "density", "fp64_refinement",
+                                            "diis", "energy"};
+  return (k >= 0 && k < kKNumClasses) ? names[k] : "?";
+}
+
+cudaEvent_t Batch::next_event() {
+  if (ev_used_ == ev_pool_.size()) {
+    cudaEvent_t e;
+    cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    ev_pool_.push_back(e);
+  }
+  return ev_pool_[ev_used_++];
+}
+
+int Batch::prof_begin(int cls, double work) {
+  if (!prof_on_) return -1;
+  Rec r;
+  r.a = next_event();
+  r.b = next_event();
+  r.cls = cls;
+  r.work = work;
+  cuda_check(cudaEventRecord(r.a, stream_), "cudaEventRecord");
+  recs_.push_back(r);
+  return (int)recs_.size() - 1;
+}
+
+void Batch::prof_end(int h) {
+  if (h < 0) return;
+  cuda_check(cudaEventRecord(recs_[h].b, stream_), "cudaEventRecord");
+}
+
+void Batch::profile_collect(double* ms, long long* launches, double* work) {
+  cuda_check(cudaStreamSynchronize(stream_), "profile sync");
+  for (const Rec& r : recs_) {
+    float t = 0.f;
+    cuda_check(cudaEventElapsedTime(&t, r.a, r.b), "cudaEventElapsedTime");
+    prof_ms_[r.cls] += t;
+    prof_launches_[r.cls] += 1;
+    prof_work_[r.cls] += r.work;
+  }
+  recs_.clear();
+  ev_used_ = 0;
+  for (int k = 0; k < kKNumClasses; ++k) {
+    if (ms) ms[k] = prof_ms_[k];
+    if (launches) launches[k] = prof_launches_[k];
+    if (work) work[k] = prof_work_[k];
+  }
+}
+
+void Batch::profile_reset() {
+  cuda_check(cudaStreamSynchronize(stream_), "profile sync");
+  recs_.clear();
+  ev_used_ = 0;
+  for (int k = 0; k < kKNumClasses; ++k) { prof_ms_[k] = 0; prof_launches_[k] = 0; prof_work_[k] = 0; }
+}
+
+// Algorithmic work of one launch over the molecules that are still active:
+// FLOPs for the contractions and the eigensolver (eigensolve counted as
+// 10/3 N^3 whatever the method), bytes for the memory-bound steps.
+double Batch::active_work_estimate(int cls) const {
+  double w = 0.0;
+  for (int m : cur_list_) {
+    if (!active_host_.empty() && !active_host_[m]) continue;
+    const DevMol& d = h_mols[m];
+    const double n = d.nao, o = d.nocc, v = n - o;
+    switch (cls) {
+      case kKJacobi: w += 10.0 / 3.0 * n * n * n; break;
+      case kKTransform: w += 4.0 * n * n * n; break;
+      case kKOrtho: w += 4.0 * n * n * n; break;
+      case kKDensity: w += 2.0 * n * n * o; break;
+      case kKRefine: w += 2 * n * n * o + 6 * n * v * o + 2 * n * o * o + 2 * o * o * o + 2 * o * o * n + 2 * n * n * o; break;
+      case kKDiis: w += 8.0 * n * n * (2.0 * diis_m_ + 3.0); break;
+      case kKFock: {
+        double blk = 0.0;
+        for (int k = 0; k < d.npairs; ++k) {
+          const DevPair& p = h_pairs[d.pair0 + k];
+          blk += (h_atoms[p.a].nao == 4 ? 10 : 1) * (h_atoms[p.b].nao == 4 ? 10 : 1);
+        }
+        w += 8.0 * blk + 16.0 * n * n;
+        break;
+      }
+      default: break;
+    }
+  }
+  return w;
+}
+
+void Batch::set_coordinates(const double* xyz) {
+  for (size_t a = 0; a < h_atoms.size(); ++a) {
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(xyz[3 * a + k])) throw std::invalid_argument("non-finite coordinate");
+    h_atoms[a].x = xyz[3 * a]; h_atoms[a].y = xyz[3 * a + 1]; h_atoms[a].z = xyz[3 * a + 2];
+  }
+  for (const DevPair& p : h_pairs) {
+    const DevAtom& A = h_atoms[p.a];
+    const DevAtom& B = h_atoms[p.b];
+    if (A.x == B.x && A.y == B.y && A.z == B.z) throw std::invalid_argument("two atoms at the same position");
+  }
+  cuda_check(cudaMemcpyAsync(d_atoms, h_atoms.data(), h_atoms.size() * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_),
+             "upload atoms");
+}
+
 void Batch::integrals() {
   std::vector<int> all(h_mols.size());
   for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
   upload_list(all);
+  int h = prof_begin(kKPair, 8.0 * (double)blk_total_);
+  launches_ += 1;
   launch_pair_kernel(d_atoms, d_pairs, (long long)h_pairs.size(), d_mols, eng_->eri(), eng_->ovt(), d_blocks, d_H,
                      d_ecore_pair, stream_);
+  prof_end(h);
   cuda_check(cudaGetLastError(), "pair_kernel");
+  h = prof_begin(kKHcore, 0.0);
+  launches_ += 1;
   launch_hcore_kernel(d_atoms, d_pairs, d_mols, d_list, (int)all.size(), d_blocks, d_ecore_pair, d_H, d_state, stream_);
+  prof_end(h);
   cuda_check(cudaGetLastError(), "hcore_kernel");
 }
 
@@ -326,42 +446,70 @@ void Batch::begin(const ScfSettings& s, const std::vector<int>& which, bool requ
     max_iter_alloc_ = s.max_iter;
   }
   upload_list(which);
+  active_host_.resize(h_mols.size(), 0);
+  for (int m : which) active_host_[m] = 1;
+  launches_ += 1;
   init_state_kernel<<<(unsigned)which.size(), 256, 0, stream_>>>(d_mols, d_list, (int)which.size(), d_state, d_C,
                                                                  d_P, requires_guess ? 1 : 0, requires_guess ? 1 : 0);
   cuda_check(cudaGetLastError(), "init_state");
 }
 
 void Batch::eigen_step(const ScfSettings& s) {
-  const int nl = (int)cur_list_.size();
-  (void)nl;
   if (s.precision == 0) {
+    int h = prof_begin(kKTransform, active_work_estimate(kKTransform));
+    launches_ += 2 + (long long)buckets_.size();
     launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, d_C, d_T64, false, true, 0.0, d_state, 1, -1, stream_);
     launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, d_C, d_T64, d_G64, false, false, 0.0, d_state, 1, -1, stream_);
+    prof_end(h);
+    h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
     for (size_t b = 0; b < buckets_.size(); ++b)
       launch_jacobi_f64(d_mols, d_bucket_lists_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_G64, d_C,
                         1, d_C, d_eps, d_jA64, d_jV64, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+    prof_end(h);
   } else {
-    launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, d_C, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
-    launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, d_C, d_T32, d_G32, false, false, 0.0f, d_state, 1, -1, stream_);
+    // The FP32 rotations of each iteration erode the orthonormality of the
+    // warm-start basis; one Newton-Schulz step C <- 1.5 C - 0.5 (C C^T) C
+    // (FP32 accumulation) restores it to FP32 round-off before it is reused.
+    double* Cn = d_T64;
+    launches_ += 4 + (long long)buckets_.size();
+    int h = prof_begin(kKOrtho, active_work_estimate(kKOrtho));
+    cuda_check(cudaMemcpyAsync(Cn, d_C, mat_total_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy basis");
+    launch_gemm(j_ns1_.d, j_ns1_.n, j_ns1_.tiles, d_C, d_C, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
+    launch_gemm(j_ns2_.d, j_ns2_.n, j_ns2_.tiles, d_T32, d_C, Cn, false, false, 0.0f, d_state, 1, -1, stream_);
+    prof_end(h);
+    h = prof_begin(kKTransform, active_work_estimate(kKTransform));
+    launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, Cn, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
+    launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, Cn, d_T32, d_G32, false, false, 0.0f, d_state, 1, -1, stream_);
+    prof_end(h);
+    h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
     for (size_t b = 0; b < buckets_.size(); ++b)
-      launch_jacobi_f32(d_mols, d_bucket_lists_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_G32, d_C,
+      launch_jacobi_f32(d_mols, d_bucket_lists_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_G32, Cn,
                         1, d_C, d_eps, d_jA32, d_jV32, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+    prof_end(h);
   }
   cuda_check(cudaGetLastError(), "eigen step");
 }
 
 void Batch::density_step(const ScfSettings& s) {
   if (s.precision == 0) {
+    launches_ += 1;
+    int h = prof_begin(kKDensity, active_work_estimate(kKDensity));
     launch_gemm(j_dens_.d, j_dens_.n, j_dens_.tiles, d_C, d_C, d_P, true, false, 0.0, d_state, 1, -1, stream_);
+    prof_end(h);
   } else {
     // FP32 phase: density from the FP32 eigenvectors
+    launches_ += 13;
+    int h = prof_begin(kKDensity, active_work_estimate(kKDensity));
     launch_gemm(j_dens_.d, j_dens_.n, j_dens_.tiles, d_C, d_C, d_P, true, false, 0.0f, d_state, 1, 0, stream_);
+    prof_end(h);
+    h = prof_begin(kKRefine, active_work_estimate(kKRefine));
     // FP64 phase: one Newton step on the occupied subspace, then P = 2 Y (Y^T Y)^-1 Y^T
     const int nl = (int)cur_list_.size();
     double *W = d_S[0], *K = d_S[1], *Yt = d_S[2], *Mm = d_S[3], *D2 = d_S[4], *Z = d_S[5];
     launch_gemm(j_w_.d, j_w_.n, j_w_.tiles, d_F, d_C, W, false, true, 0.0, d_state, 1, 1, stream_);
     launch_gemm(j_kt_.d, j_kt_.n, j_kt_.tiles, d_C, W, K, false, false, 0.0, d_state, 1, 1, stream_);
-    launch_newton_scale(d_mols, d_list, nl, d_state, 1, K, d_eps, stream_);
+    launch_gemm(j_ov_.d, j_ov_.n, j_ov_.tiles, d_C, d_C, D2, false, true, 0.0, d_state, 1, 1, stream_);
+    launch_newton_scale(d_mols, d_list, nl, d_state, 1, K, D2, d_eps, stream_);
     launch_copy_occ_rows(d_mols, d_list, nl, d_state, 1, d_C, Yt, stream_);
     launch_gemm(j_yt_.d, j_yt_.n, j_yt_.tiles, K, d_C, Yt, true, false, 0.0, d_state, 1, 1, stream_);
     launch_gemm(j_m_.d, j_m_.n, j_m_.tiles, Yt, Yt, Mm, false, true, 0.0, d_state, 1, 1, stream_);
@@ -370,6 +518,7 @@ void Batch::density_step(const ScfSettings& s) {
     launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, D2, 1, stream_);
     launch_gemm(j_z_.d, j_z_.n, j_z_.tiles, Mm, Yt, Z, false, false, 0.0, d_state, 1, 1, stream_);
     launch_gemm(j_p_.d, j_p_.n, j_p_.tiles, Yt, Z, d_P, true, false, 0.0, d_state, 1, 1, stream_);
+    prof_end(h);
   }
   cuda_check(cudaGetLastError(), "density step");
 }
@@ -377,20 +526,31 @@ void Batch::density_step(const ScfSettings& s) {
 void Batch::iterate(const ScfSettings& s, const std::vector<int>& which) {
   upload_list(which);
   const int nl = (int)which.size();
+  launches_ += 2;   // fock + diis
+  int h = prof_begin(kKFock, active_work_estimate(kKFock));
   launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, d_blocks, d_H, d_P, d_F, d_Pold, d_state, -1, 1, 1, stream_);
+  prof_end(h);
   cuda_check(cudaGetLastError(), "fock_kernel");
   eigen_step(s);
   density_step(s);
+  h = prof_begin(kKDiis, active_work_estimate(kKDiis));
   launch_diis(d_mols, d_list, nl, d_state, to_dev(s), d_P, d_Pold, d_hist_dens, d_hist_err, mat_total_,
               s.keep_trace ? d_trace : nullptr, max_iter_alloc_, stream_);
+  prof_end(h);
   cuda_check(cudaGetLastError(), "diis_kernel");
 }
 
 int Batch::count_active(const std::vector<int>& which) {
   upload_list(which);
-  count_active_kernel<<<1, 256, 0, stream_>>>(d_list, (int)which.size(), d_state, d_count);
+  launches_ += 1;
+  count_active_kernel<<<1, 256, 0, stream_>>>(d_list, (int)which.size(), d_state, d_count, d_active);
   int h = 0;
   cuda_check(cudaMemcpyAsync(&h, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream_), "count copy");
+  if (prof_on_) {
+    active_host_.resize(h_mols.size());
+    cuda_check(cudaMemcpyAsync(active_host_.data(), d_active, h_mols.size(), cudaMemcpyDeviceToHost, stream_),
+               "active copy");
+  }
   cuda_check(cudaStreamSynchronize(stream_), "count sync");
   return h;
 }
@@ -399,8 +559,11 @@ void Batch::finish(const ScfSettings& s, const std::vector<int>& which) {
   (void)s;
   upload_list(which);
   const int nl = (int)which.size();
+  launches_ += 2;
+  int h = prof_begin(kKEnergy, 0.0);
   launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0, 0, 0, stream_);
   launch_energy_kernel(d_atoms, d_mols, d_list, nl, d_P, d_F, d_H, d_state, d_charges, stream_);
+  prof_end(h);
   cuda_check(cudaGetLastError(), "finish");
 }
 

@@ -29,6 +29,12 @@ struct ScfSettings {
   int keep_trace = 1;
 };
 
+// kernel classes timed by the optional per-launch CUDA-event profiler
+enum KernelClass {
+  kKPair = 0, kKHcore, kKFock, kKOrtho, kKTransform, kKJacobi, kKDensity, kKRefine, kKDiis, kKEnergy, kKNumClasses
+};
+const char* kernel_class_name(int k);
+
 struct MolResult {
   int status = 0;               // MolStatus
   int iterations = 0;
@@ -74,6 +80,12 @@ class Batch {
   void set_density(int m, const double* host);
 
   const std::vector<DevMol>& mol_table() const { return h_mols; }
+  void set_coordinates(const double* xyz);          // bohr, 3 per atom, batch order
+  // per-kernel-class timing with CUDA events on the launching stream
+  void set_profiling(bool on) { prof_on_ = on; }
+  void profile_collect(double* ms, long long* launches, double* work);  // accumulates since last reset
+  void profile_reset();
+  long long launches() const { return launches_; }
   double* dev_H() const { return d_H; }
   double* dev_P() const { return d_P; }
 
@@ -114,6 +126,7 @@ class Batch {
   double* d_charges = nullptr;
   int* d_sweeps = nullptr;
   int* d_count = nullptr;
+  char* d_active = nullptr;
 
   // current molecule list and its GEMM job tables
   std::vector<int> cur_list_;
@@ -121,9 +134,26 @@ class Batch {
   std::vector<int*> d_bucket_lists_;
   std::vector<int> bucket_max_n_;
   struct JobSet { GemmJob* d = nullptr; int n = 0; int tiles = 0; };
-  JobSet j_trans1_, j_trans2_, j_dens_, j_w_, j_kt_, j_yt_, j_m_, j_d2_, j_z_, j_p_;
+  JobSet j_trans1_, j_trans2_, j_dens_, j_w_, j_kt_, j_yt_, j_m_, j_d2_, j_z_, j_p_, j_ns1_, j_ns2_, j_ov_;
   void free_jobs();
   void make_jobset(JobSet* js, const std::vector<GemmJob>& jobs);
+
+  // profiler
+  long long launches_ = 0;   // kernels launched by this batch so far
+  bool prof_on_ = false;
+  struct Rec { cudaEvent_t a, b; int cls; double work; };
+  std::vector<cudaEvent_t> ev_pool_;
+  size_t ev_used_ = 0;
+  std::vector<Rec> recs_;
+  double prof_ms_[kKNumClasses] = {};
+  long long prof_launches_[kKNumClasses] = {};
+  double prof_work_[kKNumClasses] = {};
+  cudaEvent_t next_event();
+  int prof_begin(int cls, double work);
+  void prof_end(int handle);
+  // algorithmic work of the molecules still active (flop counts, see engine.cu)
+  double active_work_estimate(int cls) const;
+  std::vector<char> active_host_;
 };
 
 class Engine {

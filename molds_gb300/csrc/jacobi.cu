@@ -31,7 +31,7 @@ __host__ __device__ inline long long jac_pk(int i, int j, int n) {   // packed u
 }
 
 template <typename T> struct JacTol;
-template <> struct JacTol<float> { static constexpr float rel = 2e-6f; };
+template <> struct JacTol<float> { static constexpr float rel = 3e-7f; };
 template <> struct JacTol<double> { static constexpr double rel = 2e-14; };
 
 size_t jacobi_smem_bytes(int n, int elem, bool v_in_smem, bool a_in_smem) {

@@ -62,13 +62,16 @@ void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, con
 void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const float* B, float* C,
                  bool ta, bool tb, float acc_tag, const MolState* st, int require_active, int require_phase,
                  cudaStream_t s);
+void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, const double* B, double* C,
+                 bool ta, bool tb, float acc_tag, const MolState* st, int require_active, int require_phase,
+                 cudaStream_t s);
 void launch_diis(const DevMol* mols, const int* mol_list, int nlist, MolState* st, const ScfParamsDev& prm,
                  double* P, const double* Pold, double* hist_dens, double* hist_err, long long hist_stride,
                  TraceEntry* trace, int trace_len, cudaStream_t s);
 void launch_convert_f64_f32(const DevMol* mols, const int* mol_list, int nlist, const MolState* st,
                             int require_active, const double* src, float* dst, cudaStream_t s);
 void launch_newton_scale(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
-                         double* K, const double* eps, cudaStream_t s);
+                         double* K, const double* O, const double* eps, cudaStream_t s);
 void launch_neumann(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
                     double* M, const double* D2, int mode, cudaStream_t s);
 void launch_copy_occ_rows(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,

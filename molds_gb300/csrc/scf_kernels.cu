@@ -117,6 +117,7 @@ GEMM_LAUNCH(double, double, double, float)
 GEMM_LAUNCH(double, double, float, float)
 GEMM_LAUNCH(float, double, float, float)
 GEMM_LAUNCH(double, float, float, float)
+GEMM_LAUNCH(float, double, double, float)
 #undef GEMM_LAUNCH
 
 // ---------------------------------------------------------------------------
@@ -328,10 +329,14 @@ void launch_convert_f64_f32(const DevMol* mols, const int* mol_list, int nlist, 
   convert_f64_to_f32_kernel<<<grid, 256, 0, s>>>(mols, mol_list, st, require_active, src, dst);
 }
 
-// FP64 refinement helper: K_ai = -Kt_ai / (eps_a - eps_i), a virtual, i occupied
+// FP64 refinement (one Newton step of Ogita & Aishima's eigenvector refinement,
+// restricted to the occupied columns): with approximate eigenvectors x and
+// eigenvalues lam, K_ai = -(x_a^T F x_i - lam_i x_a^T x_i) / (lam_a - lam_i),
+// a virtual, i occupied.  The overlap term removes the first-order error left
+// by the non-orthogonality of FP32 eigenvectors.
 __global__ void newton_scale_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
                                     const MolState* __restrict__ st, int require_phase, double* __restrict__ K,
-                                    const double* __restrict__ eps) {
+                                    const double* __restrict__ O, const double* __restrict__ eps) {
   const int m = mol_list[blockIdx.y];
   if (st[m].status != kActive || (require_phase >= 0 && st[m].phase != require_phase)) return;
   const DevMol mol = mols[m];
@@ -339,15 +344,16 @@ __global__ void newton_scale_kernel(const DevMol* __restrict__ mols, const int* 
   const long long cnt = (long long)v * o;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x) {
     const int a = (int)(e / o), i = (int)(e % o);
-    const double gap = eps[mol.vec0 + o + a] - eps[mol.vec0 + i];
-    K[mol.mat0 + e] = -K[mol.mat0 + e] / gap;
+    const double li = eps[mol.vec0 + i];
+    const double gap = eps[mol.vec0 + o + a] - li;
+    K[mol.mat0 + e] = -(K[mol.mat0 + e] - li * O[mol.mat0 + e]) / gap;
   }
 }
 
 void launch_newton_scale(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
-                         double* K, const double* eps, cudaStream_t s) {
+                         double* K, const double* O, const double* eps, cudaStream_t s) {
   if (nlist <= 0) return;
-  newton_scale_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, K, eps);
+  newton_scale_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, K, O, eps);
 }
 
 // Minv = I - D + D2 with D = M - I (o x o); D2 computed separately as D*D.
