@@ -140,6 +140,27 @@ long long nddo_batch_launch_count(const nddo_batch* b);
  * TFLOP/s.  The denominator of the eigensolver's roofline. */
 int nddo_measure_fma_peak(nddo_ctx* ctx, int precision, double* tflops);
 
+/* Allocation-free pair integrals.  No counterpart in the reference: MolDS
+ * allocates its integral store itself.  For callers that cannot call
+ * cudaMalloc (a host program that owns all device memory through its own
+ * arena, code where a device allocation is forbidden or may not fail), this
+ * computes what nddo_set_molecule computes -- the packed pair blocks (layout of
+ * nddo_get_pair_blocks), the core Hamiltonian H (n_ao x n_ao, row-major) and
+ * the core-core energy -- into the caller's device buffers d_pair_blocks and
+ * d_core_hamiltonian, and allocates nothing: its scratch is one fixed static
+ * device array of about 4.3 MB that every GPU loading the library keeps until
+ * exit.  Inputs (atomic numbers, coordinates in bohr) are host arrays;
+ * core_repulsion is a host output (may be NULL); stream is a cudaStream_t (NULL
+ * = default stream); err/err_len receive the message of a failure.
+ * Limit: n_atoms <= 512; larger molecules are rejected with NDDO_ERR_BUDGET.
+ * The first call on a device sets that device up (resolves the array's address
+ * and uploads constant tables): make it before any stream capture.  Calls
+ * share the one array, so calls that overlap on the GPU race; serialise them. */
+int nddo_pair_integrals_noalloc(int device, int theory, int n_atoms, const int* atomic_numbers,
+                                const double* xyz_bohr, double* d_pair_blocks, size_t pair_block_capacity,
+                                double* d_core_hamiltonian, double* core_repulsion, void* stream,
+                                char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -91,6 +91,9 @@ SIGNATURES = {
     "nddo_batch_timer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _DP]),
     "nddo_measure_fma_peak": (ctypes.c_int, [_CTX, ctypes.c_int, _DP]),
     "nddo_batch_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "nddo_pair_integrals_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _IP, _DP, ctypes.c_void_p,
+                                                   ctypes.c_size_t, ctypes.c_void_p, _DP, ctypes.c_void_p,
+                                                   ctypes.c_char_p, ctypes.c_size_t]),
 }
 
 _lib = None

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnddo_gb300.so")
-SOURCES = ["nddo_tables.cpp", "pair_fock.cu", "jacobi.cu", "scf_kernels.cu", "engine.cu", "capi.cu"]
+SOURCES = ["nddo_tables.cpp", "pair_fock.cu", "jacobi.cu", "scf_kernels.cu", "engine.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
