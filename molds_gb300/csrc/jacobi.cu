@@ -42,6 +42,8 @@ size_t jacobi_smem_bytes(int n, int elem, bool v_in_smem, bool a_in_smem) {
   b += (np / 2) * 2 * elem;        // c, s
   b += (np / 2) * 2 * 4;           // p, q
   b += np * 4 + np * elem;         // column order + sign
+  b += np * 4;                     // packed row offsets
+  b += (np / 2) * 4;               // rotation flags
   b += 64 * 8 + 16;                // reduction scratch (+ alignment slack)
   return (size_t)((b + 15) & ~15LL);
 }
@@ -72,6 +74,8 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
   int* pq = reinterpret_cast<int*>(ptr); ptr += 2 * half * sizeof(int);
   int* order = reinterpret_cast<int*>(ptr); ptr += np * sizeof(int);
   T* sgn = reinterpret_cast<T*>(ptr); ptr += np * sizeof(T);
+  int* rowoff = reinterpret_cast<int*>(ptr); ptr += np * sizeof(int);
+  int* rot = reinterpret_cast<int*>(ptr); ptr += half * sizeof(int);
   T* red = reinterpret_cast<T*>(((uintptr_t)ptr + 7) & ~(uintptr_t)7);
 
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -99,18 +103,20 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
     if (i < n && j < n) v = Gm[(long long)i * n + j];
     A[e] = v;
   }
+  // V is kept transposed: row i of V holds eigenvector i (V[i][mu] = C_prev[i][mu])
   for (long long e = tid; e < (long long)np * np; e += nth) {
-    const int mu = (int)(e / np), i = (int)(e % np);     // V[mu][i] = C_prev[i][mu]
+    const int i = (int)(e / np), mu = (int)(e % np);
     T v;
     if (mu < n && i < n) v = use_basis ? (T)Cm[(long long)i * n + mu] : (T)(mu == i ? 1 : 0);
     else v = (T)(mu == i ? 1 : 0);
     V[e] = v;
   }
+  for (int i = tid; i < np; i += nth) rowoff[i] = (int)jac_pk(i, i, np);
   __syncthreads();
 
   // matrix scale for the stopping test
   T scale = 0;
-  for (int i = tid; i < n; i += nth) { T d = fabs(A[jac_pk(i, i, np)]); scale = d > scale ? d : scale; }
+  for (int i = tid; i < n; i += nth) { T d = fabs(A[rowoff[i]]); scale = d > scale ? d : scale; }
   for (int o = 16; o > 0; o >>= 1) { T t = __shfl_xor_sync(0xffffffffu, scale, o); scale = t > scale ? t : scale; }
   if ((tid & 31) == 0) red[tid >> 5] = scale;
   __syncthreads();
@@ -127,53 +133,56 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
   for (; sweep < max_sweeps; ++sweep) {
     T offmax = 0;
     for (int r = 0; r < np - 1; ++r) {
-      // pairs and rotations of this round
+      // pairs and rotations of this round; rotations below the stopping
+      // threshold are skipped (they could not change the result it certifies)
+      int any = 0;
       for (int k = tid; k < half; k += nth) {
         const int i1 = k, i2 = np - 1 - k;
         const int p1 = (i1 == 0) ? 0 : ((i1 - 1 + r) % (np - 1)) + 1;
         const int p2 = (i2 == 0) ? 0 : ((i2 - 1 + r) % (np - 1)) + 1;
         const int p = p1 < p2 ? p1 : p2, q = p1 < p2 ? p2 : p1;
-        const T apq = A[jac_pk(p, q, np)];
+        const T apq = A[rowoff[p] + (q - p)];
         T c = 1, s = 0;
         const T aa = fabs(apq);
         offmax = aa > offmax ? aa : offmax;
-        if (apq != (T)0) {
-          const T app = A[jac_pk(p, p, np)], aqq = A[jac_pk(q, q, np)];
+        const int doit = aa > thresh;
+        if (doit) {
+          const T app = A[rowoff[p]], aqq = A[rowoff[q]];
           const T theta = (aqq - app) / (2 * apq);
           T t;
           if (fabs(theta) > (T)1e15) t = (T)0.5 / theta;
           else t = (theta >= 0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt(theta * theta + (T)1));
           c = (T)1 / sqrt(t * t + (T)1);
           s = t * c;
+          // diagonal block: exact update, off-diagonal element annihilated
+          A[rowoff[p]] = app - t * apq;
+          A[rowoff[q]] = aqq + t * apq;
+          A[rowoff[p] + (q - p)] = 0;
         }
         cs[2 * k] = c; cs[2 * k + 1] = s;
         pq[2 * k] = p; pq[2 * k + 1] = q;
+        rot[k] = doit;
+        any |= doit;
       }
-      __syncthreads();
-      // A <- J^T A J, one 2x2 block per (I <= K)
+      if (!__syncthreads_or(any)) continue;
+      // A <- J^T A J for the off-diagonal 2x2 blocks (I < K) touching a rotated pair
+      const float inv_half = 1.0f / (float)half, inv_np = 1.0f / (float)np;
       for (int e = tid; e < half * half; e += nth) {
-        const int I = e / half, K = e % half;
-        if (I > K) continue;
+        int I = (int)(((float)e + 0.5f) * inv_half);
+        int K = e - I * half;
+        if (K < 0) { --I; K += half; } else if (K >= half) { ++I; K -= half; }
+        if (I >= K) continue;
+        const int rI = rot[I], rK = rot[K];
+        if (!(rI | rK)) continue;
         const int p = pq[2 * I], q = pq[2 * I + 1];
-        const T c = cs[2 * I], s = cs[2 * I + 1];
-        if (I == K) {
-          const long long ipq = jac_pk(p, q, np);
-          const T apq = A[ipq];
-          if (apq != (T)0) {
-            const T t = s / c;
-            A[jac_pk(p, p, np)] -= t * apq;
-            A[jac_pk(q, q, np)] += t * apq;
-            A[ipq] = 0;
-          }
-          continue;
-        }
         const int r2 = pq[2 * K], s2 = pq[2 * K + 1];
-        const T c2 = cs[2 * K], s2n = cs[2 * K + 1];
-        const long long i_pr = p < r2 ? jac_pk(p, r2, np) : jac_pk(r2, p, np);
-        const long long i_ps = p < s2 ? jac_pk(p, s2, np) : jac_pk(s2, p, np);
-        const long long i_qr = q < r2 ? jac_pk(q, r2, np) : jac_pk(r2, q, np);
-        const long long i_qs = q < s2 ? jac_pk(q, s2, np) : jac_pk(s2, q, np);
+        const int i_pr = p < r2 ? rowoff[p] + (r2 - p) : rowoff[r2] + (p - r2);
+        const int i_ps = p < s2 ? rowoff[p] + (s2 - p) : rowoff[s2] + (p - s2);
+        const int i_qr = q < r2 ? rowoff[q] + (r2 - q) : rowoff[r2] + (q - r2);
+        const int i_qs = q < s2 ? rowoff[q] + (s2 - q) : rowoff[s2] + (q - s2);
         const T b00 = A[i_pr], b01 = A[i_ps], b10 = A[i_qr], b11 = A[i_qs];
+        const T c = cs[2 * I], s = cs[2 * I + 1];
+        const T c2 = cs[2 * K], s2n = cs[2 * K + 1];
         // Y = J_I^T B
         const T y00 = c * b00 - s * b10, y01 = c * b01 - s * b11;
         const T y10 = s * b00 + c * b10, y11 = s * b01 + c * b11;
@@ -183,15 +192,19 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
         A[i_qr] = y10 * c2 - y11 * s2n;
         A[i_qs] = y10 * s2n + y11 * c2;
       }
-      // V <- V J
-      for (int e = tid; e < np * half; e += nth) {
-        const int row = e / half, k = e % half;
+      // V <- V J on the rows of V^T (eigenvector p, q)
+      for (int e = tid; e < half * np; e += nth) {
+        int k = (int)(((float)e + 0.5f) * inv_np);
+        int mu = e - k * np;
+        if (mu < 0) { --k; mu += np; } else if (mu >= np) { ++k; mu -= np; }
+        if (!rot[k]) continue;
         const int p = pq[2 * k], q = pq[2 * k + 1];
         const T c = cs[2 * k], s = cs[2 * k + 1];
-        T* vr = V + (long long)row * np;
-        const T vp = vr[p], vq = vr[q];
-        vr[p] = c * vp - s * vq;
-        vr[q] = s * vp + c * vq;
+        T* vp = V + (long long)p * np + mu;
+        T* vq = V + (long long)q * np + mu;
+        const T a = *vp, b = *vq;
+        *vp = c * a - s * b;
+        *vq = s * a + c * b;
       }
       __syncthreads();
     }
@@ -213,15 +226,15 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
   // ---- sort ascending, sign fix, write rows ------------------------------------
   for (int i = tid; i < np; i += nth) {
     if (i >= n) continue;
-    const T li = A[jac_pk(i, i, np)];
+    const T li = A[rowoff[i]];
     int rank = 0;
     for (int j = 0; j < n; ++j) {
-      const T lj = A[jac_pk(j, j, np)];
+      const T lj = A[rowoff[j]];
       rank += (lj < li) || (lj == li && j < i);
     }
     order[rank] = i;
     T sum = 0;
-    for (int mu = 0; mu < n; ++mu) sum += V[(long long)mu * np + i];
+    for (int mu = 0; mu < n; ++mu) sum += V[(long long)i * np + mu];
     sgn[i] = sum < (T)0 ? (T)-1 : (T)1;
     eps_out[mol.vec0 + rank] = (double)li;
   }
@@ -230,7 +243,7 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
   for (long long e = tid; e < (long long)n * n; e += nth) {
     const int r = (int)(e / n), mu = (int)(e % n);
     const int col = order[r];
-    Co[e] = (double)(sgn[col] * V[(long long)mu * np + col]);
+    Co[e] = (double)(sgn[col] * V[(long long)col * np + mu]);
   }
   if (tid == 0 && sweeps_out) sweeps_out[m] = sweep;
 }

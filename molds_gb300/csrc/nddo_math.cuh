@@ -134,4 +134,39 @@ __host__ __device__ inline T aux_b(int k, T q) {
   return -exp(-q) * s1 + sgn * exp(q) * s2;
 }
 
+// All A_k(p), k = 0..kmax, by the upward recurrence A_k = (e^-p + k A_{k-1}) / p
+// (stable for p > 0: every term is positive).
+template <typename T>
+__host__ __device__ inline void aux_a_all(T p, int kmax, T* a) {
+  const T e = exp(-p), ip = (T)1 / p;
+  T v = e * ip;
+  a[0] = v;
+  for (int k = 1; k <= kmax; ++k) { v = (e + (T)k * v) * ip; a[k] = v; }
+}
+
+// All B_k(q), k = 0..kmax.  For |q| <= 4: B_kmax from its power series, then
+// the downward recurrence B_{k-1} = (q B_k - (-1)^k e^q + e^-q) / k, which
+// damps errors by |q|/k per step.  For |q| > 4: the upward recurrence
+// B_k = (k B_{k-1} + (-1)^k e^q - e^-q) / q from B_0 = (e^q - e^-q) / q, whose
+// error growth k/|q| per step stays below 11!/4^11 overall.
+template <typename T>
+__host__ __device__ inline void aux_b_all(T q, int kmax, T* b) {
+  const T ep = exp(q), em = exp(-q);
+  if (fabs(q) <= (T)4) {
+    T term = 1, sum = 0;
+    for (int m = 0; m < 80; ++m) {
+      if (((kmax + m) & 1) == 0) sum += term * (T)2 / (T)(kmax + m + 1);
+      term *= -q / (T)(m + 1);
+      if (fabs(term) < (T)1e-19) break;
+    }
+    b[kmax] = sum;
+    for (int k = kmax; k > 0; --k) b[k - 1] = (q * b[k] - ((k & 1) ? -ep : ep) + em) / (T)k;
+  } else {
+    const T iq = (T)1 / q;
+    T v = (ep - em) * iq;
+    b[0] = v;
+    for (int k = 1; k <= kmax; ++k) { v = ((T)k * v + ((k & 1) ? -ep : ep) - em) * iq; b[k] = v; }
+  }
+}
+
 }  // namespace nddo

@@ -27,6 +27,7 @@ typedef struct {
   double rho[3];        /* additive terms of monopole/dipole/quadrupole */
   double gk[4], gl[4], gm[4];   /* Gaussian core-core terms (a.u.)     */
   double e_atom, dhf_atom;      /* MNDO heat-of-formation bookkeeping  */
+  double sto_norm[2];   /* Slater normalisation (2 zeta)^(n+1/2) / sqrt((2n)!) of s and p */
   int n_ao;             /* 1 or 4                                      */
   int principal_n;      /* 1, 2 or 3                                   */
   int atomic_number;
@@ -67,6 +68,13 @@ static inline int nddo_fill_atom_params(int theory, int atomic_number, nddo_atom
   }
   out->e_atom = t->e_atom * NDDO_EV2AU;
   out->dhf_atom = t->dhf_atom * NDDO_KCAL2AU;
+  {
+    double f = 1.0;
+    int k;
+    for (k = 2; k <= 2 * el->principal_n; ++k) f *= k;
+    out->sto_norm[0] = pow(2.0 * t->zeta_s, el->principal_n + 0.5) / sqrt(f);
+    out->sto_norm[1] = (t->zeta_p > 0.0) ? pow(2.0 * t->zeta_p, el->principal_n + 0.5) / sqrt(f) : 0.0;
+  }
   out->n_ao = el->n_ao;
   out->principal_n = el->principal_n;
   out->atomic_number = atomic_number;

@@ -97,7 +97,7 @@ pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
         const double v = (double)e.c5 * da + (double)e.c6 * db;
         const double a = ra + rb;
         const double arg = l * l + u * u + v * v + a * a;
-        val += e.coef * (1.0 / sqrt(arg));
+        val += e.coef * rsqrt(arg);
       }
     }
   }
@@ -105,18 +105,24 @@ pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
   if (lane == 21) val = (nA == 4 && nB == 4) ? 0.5 * (s5 - s6) : 0.0;
   if (lane < 22) s_val[warp][lane] = val;
 
-  // ---- overlap auxiliary integrals: 4 zeta combinations x (12 A_k, 12 B_k) --
+  // ---- overlap auxiliary integrals: lane zc computes A_0..11 of zeta combination
+  //      zc, lane 4 + zc its B_0..11 (zc: ss, s-p, p-s, p-p exponents) --------
   const int na = pa.principal_n, nb = pb.principal_n;
-  for (int vv = lane; vv < 96; vv += 32) {
-    const int zc = vv / 24, k = vv % 24;
+  if (lane < 8) {
+    const int zc = lane & 3;
     const bool need = (zc == 0) || (zc == 1 && nB == 4) || (zc == 2 && nA == 4) || (zc == 3 && nA == 4 && nB == 4);
-    double r = 0.0;
+    double v[12];
     if (need) {
       const double za = (zc >= 2) ? pa.zeta[1] : pa.zeta[0];
       const double zb = (zc & 1) ? pb.zeta[1] : pb.zeta[0];
-      r = (k < 12) ? aux_a(k, 0.5 * R * (za + zb)) : aux_b(k - 12, 0.5 * R * (za - zb));
+      if (lane < 4) aux_a_all(0.5 * R * (za + zb), 11, v);
+      else aux_b_all(0.5 * R * (za - zb), 11, v);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) v[k] = 0.0;
     }
-    s_ab[warp][zc][k] = r;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) s_ab[warp][zc][(lane < 4 ? 0 : 12) + k] = v[k];
   }
   __syncwarp();
 
@@ -149,13 +155,10 @@ pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
         for (int j = 0; j < kOvDeg; ++j) row += coef[i * kOvDeg + j] * s_ab[warp][zc][12 + j];
         s += row * s_ab[warp][zc][i];
       }
-      const double za = (c >= 2) ? pa.zeta[1] : pa.zeta[0];
-      const double zb = (c == 1 || c >= 3) ? pb.zeta[1] : pb.zeta[0];
-      double fa = 1.0, fb = 1.0;
-      for (int i = 2; i <= 2 * na; ++i) fa *= i;
-      for (int i = 2; i <= 2 * nb; ++i) fb *= i;
-      const double norm = pow(2.0 * za, na + 0.5) * pow(2.0 * zb, nb + 0.5) / sqrt(fa * fb);
-      s *= norm * ovt->ang[c] * pow(0.5 * R, na + nb + 1);
+      const double norm = pa.sto_norm[c >= 2 ? 1 : 0] * pb.sto_norm[(c == 1 || c >= 3) ? 1 : 0];
+      double rp = 1.0;
+      for (int i = 0; i < na + nb + 1; ++i) rp *= 0.5 * R;
+      s *= norm * ovt->ang[c] * rp;
     }
     s_ov[warp][c] = s;
   }
