@@ -257,7 +257,8 @@ def run_ours(args):
         de = [abs(a["energy"] - b["energy"]) for a, b in zip(res, ref64)]
         dq = [float(np.max(np.abs(a - b))) for a, b in zip(charges, q64)]
         its = [r["iterations"] for r in res]
-        acc = {"max_abs_dE_vs_fp64_gpu_Eh": max(de), "max_abs_dq_vs_fp64_gpu": max(dq),
+        sweeps = batch.jacobi_sweeps()
+        acc = {"jacobi_sweeps_per_diagonalisation": sweeps / max(1, sum(its)),"max_abs_dE_vs_fp64_gpu_Eh": max(de), "max_abs_dq_vs_fp64_gpu": max(dq),
                "all_converged": all(r["status"] == M.STATUS_CONVERGED for r in res),
                "iterations_min_max": [min(its), max(its)],
                "fp64_iterations_min_max": [min(r["iterations"] for r in ref64), max(r["iterations"] for r in ref64)]}

@@ -134,6 +134,8 @@ const char* nddo_kernel_class_name(int k);
 int nddo_batch_timer(nddo_batch* b, int op, double* ms);
 /* Number of CUDA kernels this batch has launched so far. */
 long long nddo_batch_launch_count(const nddo_batch* b);
+/* Jacobi sweeps summed over the molecules of the last run (eigensolver work). */
+long long nddo_batch_jacobi_sweeps(nddo_batch* b);
 
 /* Measured arithmetic peak of this GPU's CUDA cores (not the tensor cores):
  * a dependent-FMA loop over every SM, FP32 (precision 0) or FP64 (1), in

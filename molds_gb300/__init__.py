@@ -91,6 +91,7 @@ SIGNATURES = {
     "nddo_batch_timer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _DP]),
     "nddo_measure_fma_peak": (ctypes.c_int, [_CTX, ctypes.c_int, _DP]),
     "nddo_batch_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "nddo_batch_jacobi_sweeps": (ctypes.c_longlong, [ctypes.c_void_p]),
     "nddo_pair_integrals_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _IP, _DP, ctypes.c_void_p,
                                                    ctypes.c_size_t, ctypes.c_void_p, _DP, ctypes.c_void_p,
                                                    ctypes.c_char_p, ctypes.c_size_t]),
@@ -340,6 +341,9 @@ class ResidentBatch:
 
     def device_bytes(self) -> int:
         return int(self.ctx.lib.nddo_batch_device_bytes(self.h))
+
+    def jacobi_sweeps(self) -> int:
+        return int(self.ctx.lib.nddo_batch_jacobi_sweeps(self.h))
 
     def launch_count(self) -> int:
         return int(self.ctx.lib.nddo_batch_launch_count(self.h))

@@ -391,6 +391,16 @@ size_t nddo_batch_device_bytes(const nddo_batch* h) { return h ? h->b->device_by
 
 long long nddo_batch_launch_count(const nddo_batch* h) { return h ? h->b->launches() : -1; }
 
+long long nddo_batch_jacobi_sweeps(nddo_batch* h) {
+  if (!h) return -1;
+  try {
+    return h->b->jacobi_sweeps();
+  } catch (const std::exception& e) {
+    h->ctx->err = e.what();
+    return -1;
+  }
+}
+
 void nddo_batch_destroy(nddo_batch* h) { delete h; }
 
 int nddo_batch_profile(nddo_batch* h, int enable) {

@@ -162,6 +162,25 @@ Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
   d_list = dalloc<int>(nm, &bytes_);
   d_blocks = dalloc<double>(blk_total_, &bytes_);
   d_ecore_pair = dalloc<double>(h_pairs.size(), &bytes_);
+  {
+    std::vector<int> heavy, xh, hh;
+    for (size_t k = 0; k < h_pairs.size(); ++k) {
+      const int na = h_atoms[h_pairs[k].a].nao, nb = h_atoms[h_pairs[k].b].nao;
+      if (na == 4 && nb == 4) heavy.push_back((int)k);
+      else if (na == 4 || nb == 4) xh.push_back((int)k);
+      else hh.push_back((int)k);
+    }
+    xh.insert(xh.end(), hh.begin(), hh.end());
+    n_heavy_ = (long long)heavy.size();
+    n_light_ = (long long)xh.size();
+    d_heavy_pairs = dalloc<int>(heavy.size(), &bytes_);
+    d_light_pairs = dalloc<int>(xh.size(), &bytes_);
+    if (!heavy.empty())
+      cuda_check(cudaMemcpyAsync(d_heavy_pairs, heavy.data(), heavy.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload heavy pairs");
+    if (!xh.empty())
+      cuda_check(cudaMemcpyAsync(d_light_pairs, xh.data(), xh.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload light pairs");
+    cuda_check(cudaStreamSynchronize(stream_), "upload pair lists");
+  }
   d_H = dalloc<double>(mat, &bytes_);
   d_F = dalloc<double>(mat, &bytes_);
   d_P = dalloc<double>(mat, &bytes_);
@@ -209,7 +228,7 @@ Batch::~Batch() {
   for (int* p : d_bucket_lists_) cudaFree(p);
   void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
                   d_hist_dens, d_hist_err, d_G32, d_T32, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
-                  d_state, d_trace, d_charges, d_sweeps, d_count, d_active};
+                  d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
 }
@@ -391,6 +410,15 @@ double Batch::active_work_estimate(int cls) const {
   return w;
 }
 
+long long Batch::jacobi_sweeps() const {
+  std::vector<int> h(h_mols.size());
+  cuda_check(cudaMemcpyAsync(h.data(), d_sweeps, h.size() * sizeof(int), cudaMemcpyDeviceToHost, stream_), "sweeps");
+  cuda_check(cudaStreamSynchronize(stream_), "sweeps");
+  long long t = 0;
+  for (int v : h) t += v;
+  return t;
+}
+
 void Batch::set_coordinates(const double* xyz) {
   for (size_t a = 0; a < h_atoms.size(); ++a) {
     for (int k = 0; k < 3; ++k)
@@ -411,9 +439,9 @@ void Batch::integrals() {
   for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
   upload_list(all);
   int h = prof_begin(kKPair, 8.0 * (double)blk_total_);
-  launches_ += 1;
-  launch_pair_kernel(d_atoms, d_pairs, (long long)h_pairs.size(), d_mols, eng_->eri(), eng_->ovt(), d_blocks, d_H,
-                     d_ecore_pair, stream_);
+  launches_ += 2;
+  launch_pair_kernels_split(d_atoms, d_pairs, d_heavy_pairs, n_heavy_, d_light_pairs, n_light_, d_mols, eng_->eri(),
+                            eng_->ovt(), d_blocks, d_H, d_ecore_pair, stream_);
   prof_end(h);
   cuda_check(cudaGetLastError(), "pair_kernel");
   h = prof_begin(kKHcore, 0.0);
@@ -448,6 +476,7 @@ void Batch::begin(const ScfSettings& s, const std::vector<int>& which, bool requ
   upload_list(which);
   active_host_.resize(h_mols.size(), 0);
   for (int m : which) active_host_[m] = 1;
+  cuda_check(cudaMemsetAsync(d_sweeps, 0, h_mols.size() * sizeof(int), stream_), "memset sweeps");
   launches_ += 1;
   init_state_kernel<<<(unsigned)which.size(), 256, 0, stream_>>>(d_mols, d_list, (int)which.size(), d_state, d_C,
                                                                  d_P, requires_guess ? 1 : 0, requires_guess ? 1 : 0);

@@ -86,6 +86,7 @@ class Batch {
   void profile_collect(double* ms, long long* launches, double* work);  // accumulates since last reset
   void profile_reset();
   long long launches() const { return launches_; }
+  long long jacobi_sweeps() const;   // Jacobi sweeps summed over molecules since the last begin()
   double* dev_H() const { return d_H; }
   double* dev_P() const { return d_P; }
 
@@ -113,6 +114,9 @@ class Batch {
   int* d_list = nullptr;
   double* d_blocks = nullptr;
   double* d_ecore_pair = nullptr;
+  int* d_heavy_pairs = nullptr;   // indices of sp-sp pairs
+  int* d_light_pairs = nullptr;   // indices of pairs with a hydrogen (X-H first, then H-H)
+  long long n_heavy_ = 0, n_light_ = 0;
   double *d_H = nullptr, *d_F = nullptr, *d_P = nullptr, *d_Pold = nullptr, *d_C = nullptr, *d_eps = nullptr;
   double *d_hist_dens = nullptr, *d_hist_err = nullptr;
   float *d_G32 = nullptr, *d_T32 = nullptr;

@@ -245,7 +245,7 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
     const int col = order[r];
     Co[e] = (double)(sgn[col] * V[(long long)col * np + mu]);
   }
-  if (tid == 0 && sweeps_out) sweeps_out[m] = sweep;
+  if (tid == 0 && sweeps_out) sweeps_out[m] += sweep;   // cumulative over the SCF
 }
 
 template <typename T>

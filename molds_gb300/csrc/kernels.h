@@ -24,6 +24,12 @@ void upload_params(const nddo_atom_params* p, cudaStream_t s);
 void launch_pair_kernel(const DevAtom* atoms, const DevPair* pairs, long long npairs, const DevMol* mols,
                         const EriTable* eri, const OverlapTable* ovt, double* blocks, double* H,
                         double* ecore_pair, cudaStream_t s);
+// pair integrals with the pair list split by type: sp-sp pairs one warp each,
+// pairs with a hydrogen one thread each
+void launch_pair_kernels_split(const DevAtom* atoms, const DevPair* pairs, const int* heavy_list, long long n_heavy,
+                               const int* light_list, long long n_light, const DevMol* mols, const EriTable* eri,
+                               const OverlapTable* ovt, double* blocks, double* H, double* ecore_pair,
+                               cudaStream_t s);
 void launch_hcore_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
                          int nlist, const double* blocks, const double* ecore_pair, double* H, MolState* st,
                          cudaStream_t s);

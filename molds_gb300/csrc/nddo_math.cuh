@@ -43,9 +43,17 @@ struct EriTable {
 //   sum_ij coef[i][j] A_i(p) B_j(q), p = R(za+zb)/2, q = R(za-zb)/2.
 constexpr int kOvDeg = 12;
 constexpr int kNumOvCombos = 5;   // ss, s-sigma, sigma-s, sigma-sigma, pi-pi
+constexpr int kOvMaxTerms = 64;
 struct OverlapTable {
   double coef[3][3][kNumOvCombos][kOvDeg][kOvDeg];   // [na-1][nb-1][combo][i][j]
   double ang[kNumOvCombos];
+  // the same polynomials as compact lists of nonzero terms, and the highest
+  // A / B index each needs (thread-per-pair evaluation)
+  int nterms[3][3][kNumOvCombos];
+  int kmax[3][3][kNumOvCombos];
+  unsigned char ti[3][3][kNumOvCombos][kOvMaxTerms];
+  unsigned char tj[3][3][kNumOvCombos][kOvMaxTerms];
+  double tc[3][3][kNumOvCombos][kOvMaxTerms];
 };
 
 // packed (mu<=nu) index for the orbital order s, py, pz, px
@@ -148,19 +156,19 @@ __host__ __device__ inline void aux_a_all(T p, int kmax, T* a) {
 // the downward recurrence B_{k-1} = (q B_k - (-1)^k e^q + e^-q) / k, which
 // damps errors by |q|/k per step.  For |q| > 4: the upward recurrence
 // B_k = (k B_{k-1} + (-1)^k e^q - e^-q) / q from B_0 = (e^q - e^-q) / q, whose
-// error growth k/|q| per step stays below 11!/4^11 overall.
+// error growth k/|q| per step stays below 11!/4^11 overall.  inv[j] = 1/j.
 template <typename T>
-__host__ __device__ inline void aux_b_all(T q, int kmax, T* b) {
+__host__ __device__ inline void aux_b_all(T q, int kmax, T* b, const T* inv) {
   const T ep = exp(q), em = exp(-q);
   if (fabs(q) <= (T)4) {
     T term = 1, sum = 0;
     for (int m = 0; m < 80; ++m) {
-      if (((kmax + m) & 1) == 0) sum += term * (T)2 / (T)(kmax + m + 1);
-      term *= -q / (T)(m + 1);
+      if (((kmax + m) & 1) == 0) sum += (T)2 * term * inv[kmax + m + 1];
+      term *= -q * inv[m + 1];
       if (fabs(term) < (T)1e-19) break;
     }
     b[kmax] = sum;
-    for (int k = kmax; k > 0; --k) b[k - 1] = (q * b[k] - ((k & 1) ? -ep : ep) + em) / (T)k;
+    for (int k = kmax; k > 0; --k) b[k - 1] = (q * b[k] - ((k & 1) ? -ep : ep) + em) * inv[k];
   } else {
     const T iq = (T)1 / q;
     T v = (ep - em) * iq;

@@ -217,6 +217,19 @@ void build_overlap_table(OverlapTable* t) {
         if ((ka != 0 && na < 2) || (kb != 0 && nb < 2)) continue;
         Poly p = overlap_poly(na, ka, nb, kb);
         std::memcpy(t->coef[na - 1][nb - 1][c], p.c, sizeof(p.c));
+        int n = 0, km = 0;
+        for (int i = 0; i < kOvDeg; ++i)
+          for (int j = 0; j < kOvDeg; ++j)
+            if (p.c[i][j] != 0.0 && n < kOvMaxTerms) {
+              t->ti[na - 1][nb - 1][c][n] = (unsigned char)i;
+              t->tj[na - 1][nb - 1][c][n] = (unsigned char)j;
+              t->tc[na - 1][nb - 1][c][n] = p.c[i][j];
+              if (i > km) km = i;
+              if (j > km) km = j;
+              ++n;
+            }
+        t->nterms[na - 1][nb - 1][c] = n;
+        t->kmax[na - 1][nb - 1][c] = km;
       }
 }
 

@@ -30,10 +30,15 @@
 namespace nddo {
 
 __constant__ nddo_atom_params c_params[kNumParamSlots];
+__constant__ double c_inv[128];   // c_inv[j] = 1 / j
 
 void upload_params(const nddo_atom_params* p, cudaStream_t s) {
+  static double inv[128];
+  inv[0] = 0.0;
+  for (int j = 1; j < 128; ++j) inv[j] = 1.0 / (double)j;
   cudaMemcpyToSymbolAsync(c_params, p, sizeof(nddo_atom_params) * kNumParamSlots, 0,
                           cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_inv, inv, sizeof(inv), 0, cudaMemcpyHostToDevice, s);
 }
 
 __device__ __forceinline__ double sel3(int i, double a, double b, double c) {
@@ -42,9 +47,132 @@ __device__ __forceinline__ double sel3(int i, double a, double b, double c) {
 
 constexpr int kPairWarps = 4;
 
+// E_AB of MNDO (Mndo.cpp:223-240, 319-327) plus the AM1/PM3 Gaussians
+// (Am1.cpp:145-170); ssss = (s_A s_A | s_B s_B).
+__device__ __forceinline__ double core_core(const nddo_atom_params& pa, const nddo_atom_params& pb, double R,
+                                            double ssss, int theory) {
+  double f;
+  const bool a_no = (pa.atomic_number == 7 || pa.atomic_number == 8);
+  const bool b_no = (pb.atomic_number == 7 || pb.atomic_number == 8);
+  if (pa.atomic_number == 1 && b_no)
+    f = 1.0 + (R / NDDO_ANG2AU) * exp(-pb.alpha * R) + exp(-pa.alpha * R);
+  else if (pb.atomic_number == 1 && a_no)
+    f = 1.0 + (R / NDDO_ANG2AU) * exp(-pa.alpha * R) + exp(-pb.alpha * R);
+  else
+    f = 1.0 + exp(-pa.alpha * R) + exp(-pb.alpha * R);
+  double e = pa.core_charge * pb.core_charge * ssss * f;
+  if (theory != NDDO_MNDO) {
+    double t = 0.0;
+    for (int i = 0; i < 4; ++i) {
+      if (pa.gk[i] != 0.0) { const double d = R - pa.gm[i]; t += pa.gk[i] * exp(-pa.gl[i] * (d * d)); }
+      if (pb.gk[i] != 0.0) { const double d = R - pb.gm[i]; t += pb.gk[i] * exp(-pb.gl[i] * (d * d)); }
+    }
+    e += pa.core_charge * pb.core_charge * t * NDDO_ANG2AU / R;
+  }
+  return e;
+}
+
+// One overlap combination of the pair in the diatomic frame (thread-level):
+// norm * ang * (R/2)^(na+nb+1) * sum_t c_t A_i(p) B_j(q).
+__device__ __forceinline__ double overlap_combo(const OverlapTable* __restrict__ ovt, int na, int nb, int c,
+                                                double za, double zb, double norm, double R) {
+  const int km = ovt->kmax[na - 1][nb - 1][c];
+  double a[12], b[12];
+  aux_a_all(0.5 * R * (za + zb), km, a);
+  aux_b_all(0.5 * R * (za - zb), km, b, c_inv);
+  double s = 0.0;
+  const int nt = ovt->nterms[na - 1][nb - 1][c];
+  for (int t = 0; t < nt; ++t)
+    s += ovt->tc[na - 1][nb - 1][c][t] * a[ovt->ti[na - 1][nb - 1][c][t]] * b[ovt->tj[na - 1][nb - 1][c][t]];
+  double rp = 1.0;
+  for (int i = 0; i < na + nb + 1; ++i) rp *= 0.5 * R;
+  return norm * ovt->ang[c] * rp * s;
+}
+
+__device__ __forceinline__ double slot_value(const EriTable* __restrict__ eri, int slot, double R,
+                                             const nddo_atom_params& pa, const nddo_atom_params& pb) {
+  double v = 0.0;
+  const int nt = eri->nterms[slot];
+  for (int t = 0; t < nt; ++t) {
+    const EriTerm e = eri->terms[slot][t];
+    const double da = e.la == 0 ? pa.d[0] : (e.la == 1 ? pa.d[1] : pa.d[2]);
+    const double db = e.lb == 0 ? pb.d[0] : (e.lb == 1 ? pb.d[1] : pb.d[2]);
+    const double ra = e.la == 0 ? pa.rho[0] : (e.la == 1 ? pa.rho[1] : pa.rho[2]);
+    const double rb = e.lb == 0 ? pb.rho[0] : (e.lb == 1 ? pb.rho[1] : pb.rho[2]);
+    const double l = R + (double)e.c1 * da + (double)e.c2 * db;
+    const double u = (double)e.c3 * da + (double)e.c4 * db;
+    const double w = (double)e.c5 * da + (double)e.c6 * db;
+    const double a = ra + rb;
+    v += e.coef * rsqrt(l * l + u * u + w * w + a * a);
+  }
+  return v;
+}
+
+// Pairs with at least one hydrogen, one thread per pair.  With X the atom
+// carrying p orbitals (if any) and u the unit vector from X to H, the rotated
+// block (X mu nu | H s s) of the local values s0 = (ss|ss), s3 = (xx|ss),
+// s4 = (zz|ss), s10 = (sz|ss) is
+//   (s s | s s) = s0,   (s p_mu | s s) = s10 u_mu,
+//   (p_mu p_nu | s s) = s3 delta_mu,nu + (s4 - s3) u_mu u_nu,
+// which is T2 L T2^T written out for this sparsity (the local z axis is u).
+// Block layout is the same for both atom orders: 10 or 1 doubles.
+__global__ void __launch_bounds__(128)
+pair_light_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs,
+                  const int* __restrict__ list, long long n, const DevMol* __restrict__ mols,
+                  const EriTable* __restrict__ eri, const OverlapTable* __restrict__ ovt,
+                  double* __restrict__ blocks, double* __restrict__ H, double* __restrict__ ecore_pair) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int p = list[t];
+  const DevPair pr = pairs[p];
+  const DevAtom A = atoms[pr.a], B = atoms[pr.b];
+  const bool swap = (A.nao == 1 && B.nao == 4);
+  const DevAtom X = swap ? B : A, Y = swap ? A : B;       // Y is a hydrogen
+  const nddo_atom_params& px = c_params[X.pidx];
+  const nddo_atom_params& py = c_params[Y.pidx];
+  const DevMol mol = mols[pr.mol];
+  const double dx = Y.x - X.x, dy = Y.y - X.y, dz = Y.z - X.z;
+  const double R = sqrt(dx * dx + dy * dy + dz * dz);
+  const double iR = 1.0 / R;
+  const double u[4] = {0.0, dy * iR, dz * iR, dx * iR};   // orbital order s, py, pz, px
+  const double s0 = slot_value(eri, 0, R, px, py);
+  double* out = blocks + pr.blk;
+  const long long ld = mol.nao;
+  double Sss, Sps = 0.0;
+  Sss = overlap_combo(ovt, px.principal_n, py.principal_n, 0, px.zeta[0], py.zeta[0],
+                      px.sto_norm[0] * py.sto_norm[0], R);
+  if (X.nao == 4) {
+    const double s3 = slot_value(eri, 3, R, px, py);
+    const double s4 = slot_value(eri, 4, R, px, py);
+    const double s10 = slot_value(eri, 10, R, px, py);
+    for (int P = 0; P < 10; ++P) {
+      int m, k;
+      unpack_index(P, &m, &k);
+      double v;
+      if (m == 0 && k == 0) v = s0;
+      else if (m == 0) v = s10 * u[k];
+      else v = (m == k ? s3 : 0.0) + (s4 - s3) * u[m] * u[k];
+      out[P] = v;
+    }
+    Sps = overlap_combo(ovt, px.principal_n, py.principal_n, 2, px.zeta[1], py.zeta[0],
+                        px.sto_norm[1] * py.sto_norm[0], R);
+  } else {
+    out[0] = s0;
+  }
+  // resonance entries 1/2 (beta_mu + beta_H) S_mu,H  (S_p,H = u_mu S_sigma-s)
+  for (int mu = 0; mu < X.nao; ++mu) {
+    const double sv = (mu == 0) ? Sss : u[mu] * Sps;
+    const double h = 0.5 * (px.beta[mu == 0 ? 0 : 1] + py.beta[0]) * sv;
+    const long long r = X.ao0 + mu, c = Y.ao0;
+    H[mol.mat0 + r * ld + c] = h;
+    H[mol.mat0 + c * ld + r] = h;
+  }
+  ecore_pair[p] = core_core(px, py, R, s0, mol.theory);
+}
+
 __global__ void __launch_bounds__(kPairWarps * 32)
-pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs, long long npairs,
-            const DevMol* __restrict__ mols, const EriTable* __restrict__ eri,
+pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs, const int* __restrict__ list,
+            long long npairs, const DevMol* __restrict__ mols, const EriTable* __restrict__ eri,
             const OverlapTable* __restrict__ ovt, double* __restrict__ blocks,
             double* __restrict__ H, double* __restrict__ ecore_pair) {
   __shared__ double s_val[kPairWarps][24];
@@ -56,8 +184,9 @@ pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
   __shared__ double s_R[kPairWarps][16];
   const unsigned full = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long p = (long long)blockIdx.x * kPairWarps + warp;
-  if (p >= npairs) return;
+  const long long pi = (long long)blockIdx.x * kPairWarps + warp;
+  if (pi >= npairs) return;
+  const long long p = list ? list[pi] : pi;
 
   const DevPair pr = pairs[p];
   const DevAtom A = atoms[pr.a], B = atoms[pr.b];
@@ -115,8 +244,8 @@ pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
     if (need) {
       const double za = (zc >= 2) ? pa.zeta[1] : pa.zeta[0];
       const double zb = (zc & 1) ? pb.zeta[1] : pb.zeta[0];
-      if (lane < 4) aux_a_all(0.5 * R * (za + zb), 11, v);
-      else aux_b_all(0.5 * R * (za - zb), 11, v);
+      if (lane < 4) aux_a_all(0.5 * R * (za + zb), 6, v);
+      else aux_b_all(0.5 * R * (za - zb), 6, v, c_inv);
     } else {
 #pragma unroll
       for (int k = 0; k < 12; ++k) v[k] = 0.0;
@@ -149,12 +278,10 @@ pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
     double s = 0.0;
     if (need) {
       const int zc = (c == 4) ? 3 : c;
-      const double* coef = &ovt->coef[na - 1][nb - 1][c][0][0];
-      for (int i = 0; i < kOvDeg; ++i) {
-        double row = 0.0;
-        for (int j = 0; j < kOvDeg; ++j) row += coef[i * kOvDeg + j] * s_ab[warp][zc][12 + j];
-        s += row * s_ab[warp][zc][i];
-      }
+      const int nt = ovt->nterms[na - 1][nb - 1][c];
+      for (int t = 0; t < nt; ++t)
+        s += ovt->tc[na - 1][nb - 1][c][t] * s_ab[warp][zc][ovt->ti[na - 1][nb - 1][c][t]] *
+             s_ab[warp][zc][12 + ovt->tj[na - 1][nb - 1][c][t]];
       const double norm = pa.sto_norm[c >= 2 ? 1 : 0] * pb.sto_norm[(c == 1 || c >= 3) ? 1 : 0];
       double rp = 1.0;
       for (int i = 0; i < na + nb + 1; ++i) rp *= 0.5 * R;
@@ -205,28 +332,7 @@ pair_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
   }
 
   // ---- core-core repulsion --------------------------------------------------
-  if (lane == 0) {
-    const double ssss = s_val[warp][0];
-    double f;
-    const bool a_no = (pa.atomic_number == 7 || pa.atomic_number == 8);
-    const bool b_no = (pb.atomic_number == 7 || pb.atomic_number == 8);
-    if (pa.atomic_number == 1 && b_no)
-      f = 1.0 + (R / NDDO_ANG2AU) * exp(-pb.alpha * R) + exp(-pa.alpha * R);
-    else if (pb.atomic_number == 1 && a_no)
-      f = 1.0 + (R / NDDO_ANG2AU) * exp(-pa.alpha * R) + exp(-pb.alpha * R);
-    else
-      f = 1.0 + exp(-pa.alpha * R) + exp(-pb.alpha * R);
-    double e = pa.core_charge * pb.core_charge * ssss * f;
-    if (mol.theory != NDDO_MNDO) {
-      double t = 0.0;
-      for (int i = 0; i < 4; ++i) {
-        t += pa.gk[i] * exp(-pa.gl[i] * pow(R - pa.gm[i], 2.0));
-        t += pb.gk[i] * exp(-pb.gl[i] * pow(R - pb.gm[i], 2.0));
-      }
-      e += pa.core_charge * pb.core_charge * t * NDDO_ANG2AU / R;
-    }
-    ecore_pair[p] = e;
-  }
+  if (lane == 0) ecore_pair[p] = core_core(pa, pb, R, s_val[warp][0], mol.theory);
 }
 
 // warp-wide sum with a fixed tree (bitwise reproducible)
@@ -437,7 +543,24 @@ void launch_pair_kernel(const DevAtom* atoms, const DevPair* pairs, long long np
                         double* ecore_pair, cudaStream_t s) {
   if (npairs <= 0) return;
   const long long grid = (npairs + kPairWarps - 1) / kPairWarps;
-  pair_kernel<<<(unsigned)grid, kPairWarps * 32, 0, s>>>(atoms, pairs, npairs, mols, eri, ovt, blocks, H, ecore_pair);
+  pair_kernel<<<(unsigned)grid, kPairWarps * 32, 0, s>>>(atoms, pairs, nullptr, npairs, mols, eri, ovt, blocks, H,
+                                                         ecore_pair);
+}
+
+void launch_pair_kernels_split(const DevAtom* atoms, const DevPair* pairs, const int* heavy_list, long long n_heavy,
+                               const int* light_list, long long n_light, const DevMol* mols, const EriTable* eri,
+                               const OverlapTable* ovt, double* blocks, double* H, double* ecore_pair,
+                               cudaStream_t s) {
+  if (n_heavy > 0) {
+    const long long grid = (n_heavy + kPairWarps - 1) / kPairWarps;
+    pair_kernel<<<(unsigned)grid, kPairWarps * 32, 0, s>>>(atoms, pairs, heavy_list, n_heavy, mols, eri, ovt, blocks,
+                                                           H, ecore_pair);
+  }
+  if (n_light > 0) {
+    const long long grid = (n_light + 127) / 128;
+    pair_light_kernel<<<(unsigned)grid, 128, 0, s>>>(atoms, pairs, light_list, n_light, mols, eri, ovt, blocks, H,
+                                                     ecore_pair);
+  }
 }
 
 void launch_hcore_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
