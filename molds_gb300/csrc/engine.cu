@@ -210,7 +210,7 @@ Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
   cuda_check(cudaMemsetAsync(d_hist_err, 0, std::max(diis_m_, 1) * mat * sizeof(double), stream_), "memset hist");
   // Jacobi workspaces for molecules too large for shared memory
   bool ag, vg;
-  const long long np = (max_n_ + 1) & ~1;
+  const long long np = (max_n_ + 3) & ~3;   // the Jacobi working size (see jacobi.cu)
   jws_stride_ = np * np;
   if (jacobi_needs_workspace(max_n_, 4, &ag, &vg)) {
     d_jA32 = dalloc<float>(ag ? (size_t)nm * jws_stride_ : 1, &bytes_);

@@ -30,19 +30,47 @@ __host__ __device__ inline long long jac_pk(int i, int j, int n) {   // packed u
   return (long long)i * (2 * n - i + 1) / 2 + (j - i);
 }
 
+// vector access of V rows: float4 in FP32, double2 in FP64
+template <typename T> struct Vec4;
+template <> struct Vec4<float> {
+  typedef float4 type;
+  static constexpr int width = 4;
+  __device__ static float4 rot1(float4 a, float4 b, float c, float s) {
+    return make_float4(c * a.x - s * b.x, c * a.y - s * b.y, c * a.z - s * b.z, c * a.w - s * b.w);
+  }
+  __device__ static float4 rot2(float4 a, float4 b, float c, float s) {
+    return make_float4(s * a.x + c * b.x, s * a.y + c * b.y, s * a.z + c * b.z, s * a.w + c * b.w);
+  }
+};
+template <> struct Vec4<double> {
+  typedef double2 type;
+  static constexpr int width = 2;
+  __device__ static double2 rot1(double2 a, double2 b, double c, double s) {
+    return make_double2(c * a.x - s * b.x, c * a.y - s * b.y);
+  }
+  __device__ static double2 rot2(double2 a, double2 b, double c, double s) {
+    return make_double2(s * a.x + c * b.x, s * a.y + c * b.y);
+  }
+};
+
 template <typename T> struct JacTol;
 template <> struct JacTol<float> { static constexpr float rel = 3e-7f; };
 template <> struct JacTol<double> { static constexpr double rel = 2e-14; };
 
+// working size: n rounded up to a multiple of 4 (even for the round-robin
+// pairing, and 16-byte rows of V for vector loads); padding indices are
+// decoupled (zero off-diagonal) and never rotated
+__host__ __device__ inline int jac_np(int n) { return (n + 3) & ~3; }
+
 size_t jacobi_smem_bytes(int n, int elem, bool v_in_smem, bool a_in_smem) {
-  const long long np = (n + 1) & ~1;
+  const long long np = jac_np(n);
   long long b = 0;
   if (a_in_smem) b += np * (np + 1) / 2 * elem;
   if (v_in_smem) b += np * np * elem;
   b += (np / 2) * 2 * elem;        // c, s
   b += (np / 2) * 2 * 4;           // p, q
   b += np * 4 + np * elem;         // column order + sign
-  b += np * 4;                     // packed row offsets
+  b += np * 4 + 16;                // packed row offsets (+ alignment of the packed matrix)
   b += (np / 2) * 4;               // rotation flags
   b += 64 * 8 + 16;                // reduction scratch (+ alignment slack)
   return (size_t)((b + 15) & ~15LL);
@@ -59,17 +87,18 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
   if (require_active && st[m].status != kActive) return;
   const DevMol mol = mols[m];
   const int n = mol.nao;
-  const int np = (n + 1) & ~1;
+  const int np = jac_np(n);
   const int half = np / 2;
   const long long npk = (long long)np * (np + 1) / 2;
 
   unsigned char* ptr = smem_raw;
   T* A;
   T* V;
-  if (a_in_smem) { A = reinterpret_cast<T*>(ptr); ptr += npk * sizeof(T); }
-  else A = Aws + (long long)blockIdx.x * ws_stride;
+  // V first: its rows must stay 16-byte aligned for vector access
   if (v_in_smem) { V = reinterpret_cast<T*>(ptr); ptr += (long long)np * np * sizeof(T); }
   else V = Vws + (long long)blockIdx.x * ws_stride;
+  if (a_in_smem) { A = reinterpret_cast<T*>(ptr); ptr += ((npk * sizeof(T) + 15) & ~15LL); }
+  else A = Aws + (long long)blockIdx.x * ws_stride;
   T* cs = reinterpret_cast<T*>(ptr); ptr += 2 * half * sizeof(T);
   int* pq = reinterpret_cast<int*>(ptr); ptr += 2 * half * sizeof(int);
   int* order = reinterpret_cast<int*>(ptr); ptr += np * sizeof(int);
@@ -165,46 +194,53 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
         any |= doit;
       }
       if (!__syncthreads_or(any)) continue;
-      // A <- J^T A J for the off-diagonal 2x2 blocks (I < K) touching a rotated pair
-      const float inv_half = 1.0f / (float)half, inv_np = 1.0f / (float)np;
-      for (int e = tid; e < half * half; e += nth) {
-        int I = (int)(((float)e + 0.5f) * inv_half);
-        int K = e - I * half;
-        if (K < 0) { --I; K += half; } else if (K >= half) { ++I; K -= half; }
-        if (I >= K) continue;
-        const int rI = rot[I], rK = rot[K];
-        if (!(rI | rK)) continue;
-        const int p = pq[2 * I], q = pq[2 * I + 1];
-        const int r2 = pq[2 * K], s2 = pq[2 * K + 1];
-        const int i_pr = p < r2 ? rowoff[p] + (r2 - p) : rowoff[r2] + (p - r2);
-        const int i_ps = p < s2 ? rowoff[p] + (s2 - p) : rowoff[s2] + (p - s2);
-        const int i_qr = q < r2 ? rowoff[q] + (r2 - q) : rowoff[r2] + (q - r2);
-        const int i_qs = q < s2 ? rowoff[q] + (s2 - q) : rowoff[s2] + (q - s2);
-        const T b00 = A[i_pr], b01 = A[i_ps], b10 = A[i_qr], b11 = A[i_qs];
-        const T c = cs[2 * I], s = cs[2 * I + 1];
-        const T c2 = cs[2 * K], s2n = cs[2 * K + 1];
-        // Y = J_I^T B
-        const T y00 = c * b00 - s * b10, y01 = c * b01 - s * b11;
-        const T y10 = s * b00 + c * b10, y11 = s * b01 + c * b11;
-        // X = Y J_K
-        A[i_pr] = y00 * c2 - y01 * s2n;
-        A[i_ps] = y00 * s2n + y01 * c2;
-        A[i_qr] = y10 * c2 - y11 * s2n;
-        A[i_qs] = y10 * s2n + y11 * c2;
+      // A <- J^T A J for the off-diagonal 2x2 blocks (I < K) touching a rotated
+      // pair.  A warp owns the row pairs rp and half-1-rp (balanced lengths);
+      // its lanes walk K.
+      const int warp = tid >> 5, lane = tid & 31, nwarps = nth >> 5;
+      for (int rp = warp; rp < (half + 1) / 2; rp += nwarps) {
+        for (int side = 0; side < 2; ++side) {
+          const int I = side == 0 ? rp : half - 1 - rp;
+          if (side == 1 && I == rp) break;
+          const int rI = rot[I];
+          const int p = pq[2 * I], q = pq[2 * I + 1];
+          const int op = rowoff[p], oq = rowoff[q];
+          const T c = cs[2 * I], s = cs[2 * I + 1];
+          for (int K = I + 1 + lane; K < half; K += 32) {
+            if (!(rI | rot[K])) continue;
+            const int r2 = pq[2 * K], s2 = pq[2 * K + 1];
+            const int i_pr = p < r2 ? op + (r2 - p) : rowoff[r2] + (p - r2);
+            const int i_ps = p < s2 ? op + (s2 - p) : rowoff[s2] + (p - s2);
+            const int i_qr = q < r2 ? oq + (r2 - q) : rowoff[r2] + (q - r2);
+            const int i_qs = q < s2 ? oq + (s2 - q) : rowoff[s2] + (q - s2);
+            const T b00 = A[i_pr], b01 = A[i_ps], b10 = A[i_qr], b11 = A[i_qs];
+            const T c2 = cs[2 * K], s2n = cs[2 * K + 1];
+            // Y = J_I^T B
+            const T y00 = c * b00 - s * b10, y01 = c * b01 - s * b11;
+            const T y10 = s * b00 + c * b10, y11 = s * b01 + c * b11;
+            // X = Y J_K
+            A[i_pr] = y00 * c2 - y01 * s2n;
+            A[i_ps] = y00 * s2n + y01 * c2;
+            A[i_qr] = y10 * c2 - y11 * s2n;
+            A[i_qs] = y10 * s2n + y11 * c2;
+          }
+        }
       }
-      // V <- V J on the rows of V^T (eigenvector p, q)
-      for (int e = tid; e < half * np; e += nth) {
-        int k = (int)(((float)e + 0.5f) * inv_np);
-        int mu = e - k * np;
-        if (mu < 0) { --k; mu += np; } else if (mu >= np) { ++k; mu -= np; }
+      // V <- V J: rows p and q of V (eigenvectors p, q), one warp per pair,
+      // four (two in FP64) consecutive components per lane
+      typedef typename Vec4<T>::type V4;
+      const int nv = np / Vec4<T>::width;
+      for (int k = warp; k < half; k += nwarps) {
         if (!rot[k]) continue;
         const int p = pq[2 * k], q = pq[2 * k + 1];
         const T c = cs[2 * k], s = cs[2 * k + 1];
-        T* vp = V + (long long)p * np + mu;
-        T* vq = V + (long long)q * np + mu;
-        const T a = *vp, b = *vq;
-        *vp = c * a - s * b;
-        *vq = s * a + c * b;
+        V4* vp = reinterpret_cast<V4*>(V + (long long)p * np);
+        V4* vq = reinterpret_cast<V4*>(V + (long long)q * np);
+        for (int m = lane; m < nv; m += 32) {
+          const V4 a = vp[m], b = vq[m];
+          vp[m] = Vec4<T>::rot1(a, b, c, s);
+          vq[m] = Vec4<T>::rot2(a, b, c, s);
+        }
       }
       __syncthreads();
     }
