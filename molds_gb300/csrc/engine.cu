@@ -244,7 +244,7 @@ void Batch::make_jobset(JobSet* js, const std::vector<GemmJob>& jobs_in) {
   for (GemmJob& j : jobs) {
     j.tile0 = tiles;
     j.tiles_n = gemm_tiles_n(j.N);
-    tiles += (j.M > 0 && j.N > 0) ? gemm_tiles(j.M, j.N) : 0;
+    if (j.M > 0 && j.N > 0) tiles += j.sym ? gemm_tiles_sym(j.N) : gemm_tiles(j.M, j.N);
   }
   js->n = (int)jobs.size();
   js->tiles = tiles;
@@ -254,11 +254,11 @@ void Batch::make_jobset(JobSet* js, const std::vector<GemmJob>& jobs_in) {
 }
 
 static GemmJob job(long long a, long long b, long long c, int M, int N, int K, int lda, int ldb, int ldc, int mol,
-                   double alpha = 1.0, double beta = 0.0) {
+                   double alpha = 1.0, double beta = 0.0, int sym = 0) {
   GemmJob j;
   std::memset(&j, 0, sizeof(j));
   j.a_off = a; j.b_off = b; j.c_off = c; j.M = M; j.N = N; j.K = K; j.lda = lda; j.ldb = ldb; j.ldc = ldc;
-  j.mol = mol; j.alpha = alpha; j.beta = beta;
+  j.mol = mol; j.alpha = alpha; j.beta = beta; j.sym = sym;
   return j;
 }
 
@@ -269,20 +269,20 @@ void Batch::build_jobs(const std::vector<int>& which) {
     const DevMol& d = h_mols[m];
     const int n = d.nao, o = d.nocc, v = n - o;
     const long long b = d.mat0;
-    ns1.push_back(job(b, b, b, n, n, n, n, n, n, m));           // M = C C^T          (B transposed)
+    ns1.push_back(job(b, b, b, n, n, n, n, n, n, m, 1.0, 0.0, 1)); // M = C C^T        (B transposed, symmetric)
     ns2.push_back(job(b, b, b, n, n, n, n, n, n, m, -0.5, 1.5)); // C' = 1.5 C - 0.5 M C
     t1.push_back(job(b, b, b, n, n, n, n, n, n, m));            // T = F C^T          (B transposed)
     t2.push_back(job(b, b, b, n, n, n, n, n, n, m));            // G = C T
-    dn.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0));       // P = 2 C_o^T C_o    (A transposed)
+    dn.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0, 0.0, 1)); // P = 2 C_o^T C_o  (A transposed, symmetric)
     if (o > 0 && v > 0) {
       w.push_back(job(b, b, b, n, o, n, n, n, o, m));                       // W = F C_o^T   (B transposed)
       kt.push_back(job(b + (long long)o * n, b, b, v, o, n, n, o, o, m));   // Kt = C_v W
       ov.push_back(job(b + (long long)o * n, b, b, v, o, n, n, n, o, m));   // O = C_v C_o^T (B transposed)
       yt.push_back(job(b, b + (long long)o * n, b, o, n, v, o, n, n, m, 1.0, 1.0));  // Yt = C_o + K^T C_v (A transposed)
-      mm.push_back(job(b, b, b, o, o, n, n, n, o, m));                      // M = Yt Yt^T   (B transposed)
+      mm.push_back(job(b, b, b, o, o, n, n, n, o, m, 1.0, 0.0, 1));         // M = Yt Yt^T   (B transposed, symmetric)
       d2.push_back(job(b, b, b, o, o, o, o, o, o, m));                      // D2 = D D
       z.push_back(job(b, b, b, o, n, o, o, n, n, m));                       // Z = Minv Yt
-      pp.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0));                 // P = 2 Yt^T Z  (A transposed)
+      pp.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0, 0.0, 1));         // P = 2 Yt^T Z  (A transposed, symmetric)
     }
   }
   make_jobset(&j_trans1_, t1); make_jobset(&j_trans2_, t2); make_jobset(&j_dens_, dn);
@@ -393,7 +393,7 @@ double Batch::active_work_estimate(int cls) const {
       case kKTransform: w += 4.0 * n * n * n; break;
       case kKOrtho: w += 4.0 * n * n * n; break;
       case kKDensity: w += 2.0 * n * n * o; break;
-      case kKRefine: w += 2 * n * n * o + 6 * n * v * o + 2 * n * o * o + 2 * o * o * o + 2 * o * o * n + 2 * n * n * o; break;
+      case kKRefine: w += 2 * n * n * o + 6 * n * v * o + 2 * n * o * o + 2 * o * o * n + 2 * n * n * o; break;
       case kKDiis: w += 8.0 * n * n * (2.0 * diis_m_ + 3.0); break;
       case kKFock: {
         double blk = 0.0;
@@ -527,7 +527,7 @@ void Batch::density_step(const ScfSettings& s) {
     prof_end(h);
   } else {
     // FP32 phase: density from the FP32 eigenvectors
-    launches_ += 13;
+    launches_ += 12;
     int h = prof_begin(kKDensity, active_work_estimate(kKDensity));
     launch_gemm(j_dens_.d, j_dens_.n, j_dens_.tiles, d_C, d_C, d_P, true, false, 0.0f, d_state, 1, 0, stream_);
     prof_end(h);
@@ -542,9 +542,10 @@ void Batch::density_step(const ScfSettings& s) {
     launch_copy_occ_rows(d_mols, d_list, nl, d_state, 1, d_C, Yt, stream_);
     launch_gemm(j_yt_.d, j_yt_.n, j_yt_.tiles, K, d_C, Yt, true, false, 0.0, d_state, 1, 1, stream_);
     launch_gemm(j_m_.d, j_m_.n, j_m_.tiles, Yt, Yt, Mm, false, true, 0.0, d_state, 1, 1, stream_);
+    // (Y^T Y)^-1 = I - D + O(D^2) with D = Y^T Y - I: D is at the FP32 round-off
+    // of the orthonormalised basis (~1e-7), so the second-order term is ~1e-14
     launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, D2, 0, stream_);
-    launch_gemm(j_d2_.d, j_d2_.n, j_d2_.tiles, Mm, Mm, D2, false, false, 0.0, d_state, 1, 1, stream_);
-    launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, D2, 1, stream_);
+    launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, nullptr, 1, stream_);
     launch_gemm(j_z_.d, j_z_.n, j_z_.tiles, Mm, Yt, Z, false, false, 0.0, d_state, 1, 1, stream_);
     launch_gemm(j_p_.d, j_p_.n, j_p_.tiles, Yt, Z, d_P, true, false, 0.0, d_state, 1, 1, stream_);
     prof_end(h);

@@ -14,9 +14,12 @@ struct GemmJob {
   int tiles_n;
   int tile0;
   double alpha, beta;
+  int sym;          // 1: C is symmetric; only tiles on/above the diagonal are computed and mirrored
+  int pad;
 };
 
 int gemm_tiles(int M, int N);
+int gemm_tiles_sym(int N);
 int gemm_tiles_n(int N);
 
 // pair_fock.cu

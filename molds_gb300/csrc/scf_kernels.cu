@@ -41,7 +41,19 @@ gemm_kernel(const GemmJob* __restrict__ jobs, int njobs, const TA* __restrict__ 
   if (require_active && st[job.mol].status != kActive) return;
   if (require_phase >= 0 && st[job.mol].phase != require_phase) return;
   const int local = t - job.tile0;
-  const int row0 = (local / job.tiles_n) * kTile, col0 = (local % job.tiles_n) * kTile;
+  int tm, tn;
+  if (job.sym) {
+    // upper-triangle tile order: row tm holds tiles tm..T-1
+    const int T = job.tiles_n;
+    tm = 0;
+    int rem = local;
+    while (rem >= T - tm) { rem -= T - tm; ++tm; }
+    tn = tm + rem;
+  } else {
+    tm = local / job.tiles_n;
+    tn = local % job.tiles_n;
+  }
+  const int row0 = tm * kTile, col0 = tn * kTile;
   const TA* Aj = A + job.a_off;
   const TB* Bj = B + job.b_off;
   TC* Cj = C + job.c_off;
@@ -95,12 +107,17 @@ gemm_kernel(const GemmJob* __restrict__ jobs, int njobs, const TA* __restrict__ 
       TC* c = Cj + (long long)gi * job.ldc + gj;
       const double v = job.alpha * (double)acc[i][j];
       *c = (TC)(job.beta != 0.0 ? v + job.beta * (double)(*c) : v);
+      if (job.sym && tm != tn) {   // mirror (beta is zero for symmetric jobs)
+        TC* cm = Cj + (long long)gj * job.ldc + gi;
+        *cm = (TC)v;
+      }
     }
   }
 }
 
 int gemm_tiles(int M, int N) { return ((M + kTile - 1) / kTile) * ((N + kTile - 1) / kTile); }
 int gemm_tiles_n(int N) { return (N + kTile - 1) / kTile; }
+int gemm_tiles_sym(int N) { const int T = (N + kTile - 1) / kTile; return T * (T + 1) / 2; }
 
 #define GEMM_LAUNCH(TA, TB, TC, TACC)                                                                        \
   void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const TA* A, const TB* B, TC* C, bool ta,      \
@@ -370,7 +387,7 @@ __global__ void neumann_kernel(const DevMol* __restrict__ mols, const int* __res
     const int i = (int)(e / o), j = (int)(e % o);
     double* x = Mm + mol.mat0 + e;
     if (mode == 0) *x = *x - (i == j ? 1.0 : 0.0);
-    else *x = (i == j ? 1.0 : 0.0) - *x + D2[mol.mat0 + e];
+    else *x = (i == j ? 1.0 : 0.0) - *x + (D2 ? D2[mol.mat0 + e] : 0.0);
   }
 }
 
