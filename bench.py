@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--nmol", type=int, default=N_MOL)
     ap.add_argument("--cpu-sample", type=int, default=48, help="molecules in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-sample", type=int, default=16,
+                    help="molecules solved one at a time on the plain FP64 path (0 = skip)")
     return ap.parse_args()
 
 
@@ -81,6 +83,31 @@ def host_cores() -> int:
         return len(os.sched_getaffinity(0))
     except AttributeError:
         return os.cpu_count() or 1
+
+
+def profiled_traffic(kernel_class: str):
+    """DRAM bytes per launch of a kernel class from the committed ncu summaries
+    (a line 'traffic_per_launch <class> <bytes> <workload>' in profiles/*.md)."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None, None
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.endswith(".md"):
+            continue
+        for line in open(os.path.join(pdir, fn)):
+            f = line.strip().strip("`").split()
+            if len(f) >= 3 and f[0] == "traffic_per_launch" and f[1] == kernel_class:
+                return float(f[2]), "profiles/" + fn
+    return None, None
+
+
+def percentile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = (len(xs) - 1) * q / 100.0
+    lo, hi = int(math.floor(k)), int(math.ceil(k))
+    return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
 
 
 # ---------------------------------------------------------------------------
@@ -263,6 +290,24 @@ def run_ours(args):
                "iterations_min_max": [min(its), max(its)],
                "fp64_iterations_min_max": [min(r["iterations"] for r in ref64), max(r["iterations"] for r in ref64)]}
 
+    # ---- plain path: one molecule at a time, FP64, ElectronicStructure ------
+    plain = None
+    if rank == 0 and args.plain_sample > 0:
+        es = M.ElectronicStructure("am1", M.SCFParams(**SCF, precision="fp64"), context=ctx)
+        lat = []
+        for i, m in enumerate(mols[:args.plain_sample] * 2):
+            t0 = time.perf_counter()
+            es.SetMolecule(m)
+            es.DoSCF(True)
+            es.GetMullikenCharges()
+            if i >= args.plain_sample:          # first pass warms up
+                lat.append(time.perf_counter() - t0)
+        tot = sum(lat)
+        plain = {"value": len(lat) / tot, "unit": "solves/s", "p50_ms": 1e3 * percentile(lat, 50),
+                 "p99_ms": 1e3 * percentile(lat, 99), "sample": f"first {len(lat)} replicas, each SetMolecule + "
+                 "DoSCF + Mulliken through ElectronicStructure (nddo_set_molecule / nddo_scf), FP64 throughout, "
+                 "host wall clock"}
+
     # ---- roofline of the dominant kernel -----------------------------------
     dom = max(kt, key=lambda k: kt[k]["ms"])
     d = kt[dom]
@@ -276,8 +321,9 @@ def run_ours(args):
             prec = "fp64" if (dom == "fp64_refinement" or args.precision == "fp64") else "fp32"
             peak = ctx.fma_peak_tflops(prec)
             achieved = per_launch / (avg_ms * 1e-3) / 1e12
+            traffic, tsrc = profiled_traffic(dom)
             roof = {"bound": f"{prec}-cuda-core", "kernel": dom, "achieved": achieved, "peak": peak,
-                    "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                    "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic, "traffic_source": tsrc,
                     "peak_source": f"measured live: dependent-FMA loop on every SM ({prec}); MEASURED_PEAKS.json "
                                    "holds only HBM copy and bf16 tensor peaks",
                     "work_per_launch": per_launch, "avg_launch_ms": avg_ms, "launches": d["launches"]}
@@ -285,8 +331,10 @@ def run_ours(args):
             peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
                 os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
             achieved = per_launch / (avg_ms * 1e-3) / 1e9
+            traffic, tsrc = profiled_traffic(dom)
             roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                    "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                    "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_source": tsrc,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs",
                     "work_per_launch": per_launch, "avg_launch_ms": avg_ms, "launches": d["launches"]}
 
     # ---- CPU baseline: the oracle on the host cores, bounded sample --------
@@ -314,6 +362,11 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "call": "nddo_batch_scf (allocation, upload, SCF, download)"},
                 "gpu_launches": launches,
+                "latency_ms": {"batched_step": per_step_ms,
+                               "note": "every molecule of a step completes within the step"},
+                "plain_fp64_one_at_a_time": plain,
+                "batched_vs_plain": (value / plain["value"]) if plain else None,
+                "e2e_vs_plain": (e2e_value / plain["value"]) if plain else None,
                 "roofline": roof,
                 "kernels_ms": {k: round(v["ms"], 3) for k, v in kt.items()},
                 "cpu_baseline": cpu,
