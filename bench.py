@@ -46,6 +46,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=16,
                     help="molecules solved one at a time on the plain FP64 path (0 = skip)")
+    ap.add_argument("--workload", default="water32", choices=["water32", "serving", "alkanes", "octane"],
+                    help="water32: 256 x (H2O)32 AM1 batched (the headline); serving: Poisson stream of PM3 "
+                         "requests through the continuous-batching server; alkanes: uneven batch of random "
+                         "alkanes with the precision ramp; octane: the plain one-molecule path")
+    ap.add_argument("--rates", default="100,300,1000,3000,10000,20000", help="serving: arrival rates (req/s)")
+    ap.add_argument("--requests", type=int, default=400, help="serving: requests per rate")
+    ap.add_argument("--hbm-gb", type=float, default=96.0, help="serving: HBM budget of the server")
+    ap.add_argument("--max-basis", type=int, default=1024, help="serving: largest basis accepted")
     return ap.parse_args()
 
 
@@ -379,9 +387,103 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# Serving: Poisson stream of PM3 single-point requests (energy + Mulliken)
+# ---------------------------------------------------------------------------
+def run_serving(args):
+    """Open-loop arrivals at each rate through the continuous-batching server.
+    The same request list (sizes log-uniform in 5..500 atoms, half alkanes,
+    half water clusters, seed 5) is replayed at every rate with its arrival
+    times scaled; latency = completion time - scheduled arrival time."""
+    import numpy as np
+    import molds_gb300 as M
+    from molds_gb300 import build, workloads as W
+    build.build()
+    rates = [float(r) for r in args.rates.split(",")]
+    stream = W.serving_stream(1.0, args.requests, seed=5)
+    base_t = np.array([t for t, _ in stream])
+    mols = [m for _, m in stream]
+    nao = [int(sum(4 if z > 1 else 1 for z in m.Z)) for m in mols]
+    ctx = M.Context(0)
+    params = M.SCFParams(**SCF, precision=args.precision)
+    srv = M.Server(params, hbm_budget_bytes=int(args.hbm_gb * (1 << 30)), max_basis=args.max_basis, context=ctx)
+    # warm-up: one small and one large request
+    srv.submit("pm3", W.water_cluster_k(8, 1))
+    srv.submit("pm3", W.water_cluster_k(40, 2))
+    srv.drain()
+    per_rate = []
+    energies = {}
+    clocks = Clocks(0)
+    clocks.start()
+    for rate in rates:
+        arr = base_t / rate
+        t0 = srv.clock()
+        sched, done = {}, {}
+        i = 0
+        n = len(mols)
+        while len(done) < n:
+            now = srv.clock() - t0
+            while i < n and arr[i] <= now:
+                tk = srv.submit("pm3", mols[i])
+                sched[tk] = (i, t0 + arr[i])
+                i += 1
+            wait = 2000 if i >= n else int(max(0.0, min(2000.0, (arr[i] - (srv.clock() - t0)) * 1e6)))
+            for r in srv.poll(wait):
+                done[r["ticket"]] = r
+        lat = sorted(done[t]["t_done"] - sched[t][1] for t in done)
+        t_end = max(done[t]["t_done"] for t in done)
+        its = [done[t]["iterations"] for t in done]
+        for t in done:
+            if done[t]["status"] == M.STATUS_CONVERGED:
+                energies.setdefault(sched[t][0], done[t]["energy"])
+        conv = sum(done[t]["status"] == M.STATUS_CONVERGED for t in done)
+        lanes = {}
+        for t in done:
+            lanes.setdefault(done[t]["lane"], []).append(done[t])
+        lane_stats = {str(k): {"requests": len(v), "converged": sum(r["status"] == M.STATUS_CONVERGED for r in v),
+                               "mean_iterations": float(np.mean([r["iterations"] for r in v])),
+                               "p50_ms": 1e3 * percentile([r["t_done"] - r["t_submit"] for r in v], 50),
+                               "p99_ms": 1e3 * percentile([r["t_done"] - r["t_submit"] for r in v], 99)}
+                      for k, v in sorted(lanes.items())}
+        per_rate.append({"offered_req_s": rate, "requests": n, "converged": conv,
+                         "solves_s": n / (t_end - t0), "converged_solves_s": conv / (t_end - t0),
+                         "p50_ms": 1e3 * percentile(lat, 50), "p99_ms": 1e3 * percentile(lat, 99),
+                         "max_ms": 1e3 * lat[-1], "mean_iterations": float(np.mean(its)), "span_s": t_end - t0,
+                         "lanes": lane_stats})
+        print(json.dumps({"rate": rate, **per_rate[-1]}), file=sys.stderr, flush=True)
+    clk = clocks.stop()
+    srv.close()
+    # accuracy of the served (mixed-precision) energies against the FP64 path
+    acc = None
+    sample = list(range(0, len(mols), max(1, len(mols) // 48)))[:48]
+    sample = [k for k in sample if k in energies]
+    ref, _ = M.batch_scf("pm3", [mols[k] for k in sample], M.SCFParams(**SCF, precision="fp64"), context=ctx)
+    both = [(k, r) for k, r in zip(sample, ref) if r["status"] == M.STATUS_CONVERGED]
+    acc = {"sample": len(sample), "both_converged": len(both),
+           "max_abs_dE_vs_fp64_gpu_Eh": max((abs(energies[k] - r["energy"]) for k, r in both), default=None)}
+    best = max(per_rate, key=lambda r: r["converged_solves_s"])
+    line = {"metric": "serving: p50/p99 latency and converged solves/s of a Poisson stream of PM3 single-point "
+                      "requests",
+            "value": best["converged_solves_s"], "unit": "solves/s", "n_gpus": 1, "steps": len(rates), "warmup": 1,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32+fp64" if args.precision == "mixed" else "f64",
+            "data": "synthetic: seeded serving stream (sizes log-uniform 5..500 atoms; alkanes n <= 60, "
+                    "water clusters)",
+            "config": {"workload": f"{len(mols)} PM3 requests per rate, Poisson arrivals, rates {rates}",
+                       "hbm_budget_gb": args.hbm_gb, "max_basis": args.max_basis,
+                       "basis_min_median_max": [min(nao), int(np.median(nao)), max(nao)],
+                       "frac_basis_above_194": float(np.mean(np.array(nao) > 194)), "scf": SCF},
+            "rates": per_rate, "accuracy": acc, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
-    else:
+    elif a.workload == "serving":
+        run_serving(a)
+    elif a.workload == "water32":
         run_ours(a)
+    else:
+        raise SystemExit(f"workload {a.workload} is not wired into bench.py yet")

@@ -36,7 +36,7 @@ enum {
   NDDO_ERR_BUDGET = -3,
   NDDO_ERR_STATE = -4
 };
-enum { NDDO_STATUS_ACTIVE = 0, NDDO_STATUS_CONVERGED = 1, NDDO_STATUS_NOT_CONVERGED = 2 };
+enum { NDDO_STATUS_ACTIVE = 0, NDDO_STATUS_CONVERGED = 1, NDDO_STATUS_NOT_CONVERGED = 2, NDDO_STATUS_FAILED = 3 };
 
 /* SCF block of the MolDS input (src/base/InputParser.cpp:646-734) plus the
  * precision choice of this implementation. */
@@ -136,6 +136,44 @@ int nddo_batch_timer(nddo_batch* b, int op, double* ms);
 long long nddo_batch_launch_count(const nddo_batch* b);
 /* Jacobi sweeps summed over the molecules of the last run (eigensolver work). */
 long long nddo_batch_jacobi_sweeps(nddo_batch* b);
+
+/* Serving: a request loop over single-point SCFs with continuous batching.
+ * Stands in for the reference's one-molecule-per-process use of DoSCF
+ * (src/base/MolDS.cpp:165-178) when many independent requests arrive over
+ * time.  Requests are queued by nddo_server_submit (host only, returns at
+ * once) and routed by basis size to lanes; each lane admits queued requests
+ * in arrival order as its HBM arenas free up (the budget is split between the
+ * lanes), keeps every admitted molecule's integrals, density and DIIS history
+ * on the device, and runs SCF iterations over all of its molecules at once;
+ * a molecule leaves at the iteration boundary after it converges.
+ * nddo_server_poll drives the lanes without blocking on the GPU (at most
+ * max_wait_us of host time) and returns finished requests: out[k] for
+ * k < *n_out, their Mulliken charges concatenated in charges (up to
+ * charges_capacity doubles; a result that does not fit stays queued for the
+ * next poll).  Times are seconds on the server's clock (nddo_server_clock).
+ * A molecule's result does not depend on which other requests share its
+ * lane: every kernel works per molecule with fixed-order reductions. */
+typedef struct nddo_server nddo_server;
+typedef struct {
+  long long ticket;            /* returned by nddo_server_submit            */
+  int status;                  /* NDDO_STATUS_CONVERGED / NOT_CONVERGED / FAILED */
+  int iterations;
+  int n_atoms;
+  int lane;
+  double energy, core_repulsion, heat_of_formation, final_rms;
+  double t_submit, t_admit, t_done;
+} nddo_serve_result;
+int nddo_server_create(nddo_ctx* ctx, const nddo_scf_params* params, size_t hbm_budget_bytes, int max_basis,
+                       nddo_server** out);
+int nddo_server_submit(nddo_server* s, int theory, int n_atoms, const int* atomic_numbers, const double* xyz_bohr,
+                       long long* ticket);
+int nddo_server_poll(nddo_server* s, int max_wait_us, int max_results, nddo_serve_result* out, double* charges,
+                     size_t charges_capacity, int* n_out);
+/* Requests queued (not yet admitted) and molecules in the SCF. */
+int nddo_server_pending(const nddo_server* s, int* queued, int* in_flight);
+double nddo_server_clock(const nddo_server* s);
+size_t nddo_server_device_bytes(const nddo_server* s);
+void nddo_server_destroy(nddo_server* s);
 
 /* Measured arithmetic peak of this GPU's CUDA cores (not the tensor cores):
  * a dependent-FMA loop over every SM, FP32 (precision 0) or FP64 (1), in

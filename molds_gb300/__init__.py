@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libnddo_gb300.so")
 
 NDDO_OK, NDDO_NOT_CONVERGED = 0, 1
 ERR_ARGUMENT, ERR_CUDA, ERR_BUDGET, ERR_STATE = -1, -2, -3, -4
-STATUS_CONVERGED = 1
+STATUS_CONVERGED, STATUS_NOT_CONVERGED, STATUS_FAILED = 1, 2, 3
 
 
 class NddoError(RuntimeError):
@@ -53,6 +53,14 @@ class ScfResultC(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("energy", ctypes.c_double),
                 ("core_repulsion", ctypes.c_double), ("heat_of_formation", ctypes.c_double),
                 ("final_rms", ctypes.c_double), ("final_diis_error", ctypes.c_double)]
+
+
+class ServeResultC(ctypes.Structure):
+    _fields_ = [("ticket", ctypes.c_longlong), ("status", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("n_atoms", ctypes.c_int), ("lane", ctypes.c_int), ("energy", ctypes.c_double),
+                ("core_repulsion", ctypes.c_double), ("heat_of_formation", ctypes.c_double),
+                ("final_rms", ctypes.c_double), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double),
+                ("t_done", ctypes.c_double)]
 
 
 # every entry point of include/nddo_gpu.h with its argument types
@@ -92,6 +100,16 @@ SIGNATURES = {
     "nddo_measure_fma_peak": (ctypes.c_int, [_CTX, ctypes.c_int, _DP]),
     "nddo_batch_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
     "nddo_batch_jacobi_sweeps": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "nddo_server_create": (ctypes.c_int, [_CTX, ctypes.POINTER(ScfParamsC), ctypes.c_size_t, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "nddo_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _IP, _DP,
+                                          ctypes.POINTER(ctypes.c_longlong)]),
+    "nddo_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ServeResultC), _DP,
+                                        ctypes.c_size_t, _IP]),
+    "nddo_server_pending": (ctypes.c_int, [ctypes.c_void_p, _IP, _IP]),
+    "nddo_server_clock": (ctypes.c_double, [ctypes.c_void_p]),
+    "nddo_server_device_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "nddo_server_destroy": (None, [ctypes.c_void_p]),
     "nddo_pair_integrals_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _IP, _DP, ctypes.c_void_p,
                                                    ctypes.c_size_t, ctypes.c_void_p, _DP, ctypes.c_void_p,
                                                    ctypes.c_char_p, ctypes.c_size_t]),
@@ -367,6 +385,89 @@ class ResidentBatch:
     def close(self):
         if getattr(self, "h", None):
             self.ctx.lib.nddo_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request loop over single-point SCFs (nddo_server_*).
+
+    submit() queues a molecule and returns a ticket at once; poll() drives the
+    device lanes for up to max_wait_us and returns the finished requests as
+    dicts (ticket, status, iterations, energy, core_repulsion,
+    heat_of_formation, charges, lane, t_submit, t_admit, t_done -- seconds on
+    the server clock, see clock()).
+    """
+
+    def __init__(self, params: SCFParams | None = None, hbm_budget_bytes: int = 0, max_basis: int = 1024,
+                 context: Context | None = None, device: int = 0):
+        self.ctx = context or Context(device)
+        self.lib = self.ctx.lib
+        h = ctypes.c_void_p()
+        p = to_c_params(params or SCFParams())
+        self.ctx.check(self.lib.nddo_server_create(self.ctx.h, ctypes.byref(p), int(hbm_budget_bytes), int(max_basis),
+                                                   ctypes.byref(h)))
+        self.h = h
+        self._cap = 1 << 16
+        self._out = (ServeResultC * 512)()
+        self._charges = np.zeros(self._cap)
+
+    def submit(self, theory, molecule: Molecule) -> int:
+        t = THEORIES[theory.lower()] if isinstance(theory, str) else int(theory)
+        Z = np.ascontiguousarray(molecule.Z, dtype=np.int32)
+        xyz = np.ascontiguousarray(molecule.xyz, dtype=np.float64).reshape(-1, 3)
+        ticket = ctypes.c_longlong()
+        self.ctx.check(self.lib.nddo_server_submit(self.h, t, int(Z.shape[0]), _ip(Z), _dp(xyz), ctypes.byref(ticket)))
+        return ticket.value
+
+    def poll(self, max_wait_us: int = 1000, max_results: int = 512):
+        n = ctypes.c_int()
+        max_results = min(max_results, len(self._out))
+        self.ctx.check(self.lib.nddo_server_poll(self.h, int(max_wait_us), max_results, self._out, _dp(self._charges),
+                                                 self._cap, ctypes.byref(n)))
+        res, off = [], 0
+        for k in range(n.value):
+            o = self._out[k]
+            q = self._charges[off:off + o.n_atoms].copy()
+            off += o.n_atoms
+            res.append({"ticket": o.ticket, "status": o.status, "iterations": o.iterations, "energy": o.energy,
+                        "core_repulsion": o.core_repulsion, "heat_of_formation": o.heat_of_formation,
+                        "final_rms": o.final_rms, "lane": o.lane, "t_submit": o.t_submit, "t_admit": o.t_admit,
+                        "t_done": o.t_done, "charges": q})
+        return res
+
+    def pending(self):
+        q, f = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(self.lib.nddo_server_pending(self.h, ctypes.byref(q), ctypes.byref(f)))
+        return q.value, f.value
+
+    def clock(self) -> float:
+        return self.lib.nddo_server_clock(self.h)
+
+    def device_bytes(self) -> int:
+        return self.lib.nddo_server_device_bytes(self.h)
+
+    def drain(self, max_wait_us: int = 2000):
+        """Polls until nothing is queued or in flight; returns every result."""
+        out = []
+        while True:
+            out.extend(self.poll(max_wait_us))
+            q, f = self.pending()
+            if q == 0 and f == 0:
+                while True:
+                    rest = self.poll(0)
+                    if not rest:
+                        return out
+                    out.extend(rest)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nddo_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -16,7 +16,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnddo_gb300.so")
-SOURCES = ["nddo_tables.cpp", "pair_fock.cu", "jacobi.cu", "scf_kernels.cu", "engine.cu", "capi.cu", "noalloc.cu"]
+# host-only helper library: the alkane geometry generator of the workloads
+HOST_LIB = os.path.join(BUILD, "libworkloads.so")
+HOST_SOURCES = ["alkane_gen.c"]
+SOURCES = ["nddo_tables.cpp", "pair_fock.cu", "jacobi.cu", "scf_kernels.cu", "engine.cu", "capi.cu", "noalloc.cu", "server.cu", "block_jacobi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -35,7 +38,7 @@ def _deps():
 
 
 def needs_build() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(HOST_LIB):
         return True
     t = os.path.getmtime(LIB)
     return any(os.path.getmtime(f) > t for f in _deps() + [os.path.abspath(__file__)])
@@ -58,8 +61,20 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(r.stderr, file=sys.stderr)
         return obj
 
-    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+    def compile_host():
+        cc_host = shutil.which("gcc") or "cc"
+        tmp = HOST_LIB + f".tmp{os.getpid()}"
+        cmd = [cc_host, "-O2", "-std=c11", "-D_DEFAULT_SOURCE", "-shared", "-fPIC", "-o", tmp] + \
+              [os.path.join(CSRC, f) for f in HOST_SOURCES] + ["-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"gcc failed for {HOST_SOURCES}:\n{r.stderr}")
+        os.replace(tmp, HOST_LIB)
+
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES) + 1) as ex:
+        host = ex.submit(compile_host)
         objs = list(ex.map(compile_one, SOURCES))
+        host.result()
     tmp = LIB + f".tmp{os.getpid()}"
     cmd = [cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "server.h"
 
 struct nddo_batch {
   nddo_ctx* ctx;
@@ -63,6 +64,13 @@ double fma_peak(cudaStream_t s, int iters) {
   return best;
 }
 }  // namespace
+
+struct nddo_server {
+  nddo_ctx* ctx;
+  std::unique_ptr<nddo::Server> s;
+  nddo::ServeResult held;      // a result that did not fit the caller's charge buffer
+  bool has_held = false;
+};
 
 struct nddo_ctx {
   std::unique_ptr<nddo::Engine> engine;
@@ -458,5 +466,84 @@ int nddo_measure_fma_peak(nddo_ctx* ctx, int precision, double* tflops) {
     return (int)NDDO_OK;
   });
 }
+
+
+int nddo_server_create(nddo_ctx* ctx, const nddo_scf_params* params, size_t hbm_budget_bytes, int max_basis,
+                       nddo_server** out) {
+  return guarded(ctx, [&]() -> int {
+    if (!out) return fail(ctx, NDDO_ERR_ARGUMENT, "null output handle");
+    *out = nullptr;
+    std::string why;
+    if (!valid_params(params, &why)) return fail(ctx, NDDO_ERR_ARGUMENT, why);
+    if (hbm_budget_bytes == 0) hbm_budget_bytes = ctx->budget ? ctx->budget : (size_t)64 << 30;
+    if (ctx->budget && hbm_budget_bytes > ctx->budget)
+      return fail(ctx, NDDO_ERR_BUDGET, "server budget exceeds the context budget");
+    std::unique_ptr<nddo_server> h(new nddo_server());
+    h->ctx = ctx;
+    h->s.reset(new nddo::Server(ctx->engine.get(), to_settings(params), hbm_budget_bytes, max_basis));
+    *out = h.release();
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_server_submit(nddo_server* h, int theory, int n_atoms, const int* Z, const double* xyz, long long* ticket) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() -> int {
+    if (n_atoms < 1 || !Z || !xyz || !ticket) return fail(h->ctx, NDDO_ERR_ARGUMENT, "bad request arguments");
+    nddo::MoleculeInput in;
+    in.theory = theory;
+    in.Z.assign(Z, Z + n_atoms);
+    in.xyz.assign(xyz, xyz + 3 * (size_t)n_atoms);
+    *ticket = h->s->submit(in);
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_server_poll(nddo_server* h, int max_wait_us, int max_results, nddo_serve_result* out, double* charges,
+                     size_t charges_capacity, int* n_out) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() -> int {
+    if (!n_out || (max_results > 0 && !out)) return fail(h->ctx, NDDO_ERR_ARGUMENT, "bad poll arguments");
+    *n_out = 0;
+    if (!h->has_held) h->s->poll(max_wait_us < 0 ? 0 : max_wait_us);
+    size_t used = 0;
+    while (*n_out < max_results) {
+      if (!h->has_held) {
+        if (!h->s->take(&h->held)) break;
+        h->has_held = true;
+      }
+      const nddo::ServeResult& r = h->held;
+      if (charges && used + r.charges.size() > charges_capacity) {
+        if (*n_out == 0 && r.charges.size() > charges_capacity)
+          return fail(h->ctx, NDDO_ERR_ARGUMENT, "charge buffer smaller than one result");
+        break;
+      }
+      nddo_serve_result& o = out[*n_out];
+      o.ticket = r.ticket; o.status = r.status; o.iterations = r.iterations; o.n_atoms = r.natoms; o.lane = r.lane;
+      o.energy = r.energy; o.core_repulsion = r.core_repulsion; o.heat_of_formation = r.heat_of_formation;
+      o.final_rms = r.final_rms; o.t_submit = r.t_submit; o.t_admit = r.t_admit; o.t_done = r.t_done;
+      if (charges) {
+        std::copy(r.charges.begin(), r.charges.end(), charges + used);
+        used += r.charges.size();
+      }
+      h->has_held = false;
+      ++*n_out;
+    }
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_server_pending(const nddo_server* h, int* queued, int* in_flight) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  if (queued) *queued = h->s->queued();
+  if (in_flight) *in_flight = h->s->in_flight();
+  return NDDO_OK;
+}
+
+double nddo_server_clock(const nddo_server* h) { return h ? h->s->now() : 0.0; }
+
+size_t nddo_server_device_bytes(const nddo_server* h) { return h ? h->s->device_bytes() : 0; }
+
+void nddo_server_destroy(nddo_server* h) { delete h; }
 
 }  // extern "C"

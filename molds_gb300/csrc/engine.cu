@@ -34,7 +34,9 @@ static T* dalloc(size_t count, size_t* total) {
 // ---------------------------------------------------------------------------
 __global__ void init_state_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, int n,
                                   MolState* __restrict__ st, double* __restrict__ C, double* __restrict__ P,
-                                  int requires_guess, int reset_density) {
+                                  int requires_guess, int reset_density, double* __restrict__ hist_dens,
+                                  double* __restrict__ hist_err, int diis_m, long long mat_total,
+                                  int* __restrict__ sweeps) {
   const int m = list[blockIdx.x];
   const DevMol mol = mols[m];
   const long long n2 = (long long)mol.nao * mol.nao;
@@ -45,12 +47,19 @@ __global__ void init_state_kernel(const DevMol* __restrict__ mols, const int* __
     s.requires_guess = requires_guess;
     s.ecore = st[m].ecore;   // computed by the integral pass
     st[m] = s;
+    if (sweeps) sweeps[m] = 0;
   }
   for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
     const long long r = i / mol.nao, c = i % mol.nao;
     C[mol.mat0 + i] = (r == c) ? 1.0 : 0.0;
     if (reset_density) P[mol.mat0 + i] = 0.0;
   }
+  // the DIIS window starts zero-filled (as the reference's zero-initialised history)
+  for (int k = 0; k < diis_m; ++k)
+    for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
+      hist_dens[k * mat_total + mol.mat0 + i] = 0.0;
+      hist_err[k * mat_total + mol.mat0 + i] = 0.0;
+    }
 }
 
 __global__ void count_active_kernel(const int* __restrict__ list, int n, const MolState* __restrict__ st,
@@ -97,90 +106,182 @@ Engine::~Engine() {
 }
 
 // ---------------------------------------------------------------------------
+void ArenaAlloc::reset(long long capacity) {
+  free_.clear();
+  if (capacity > 0) free_[0] = capacity;
+}
+
+long long ArenaAlloc::alloc(long long n) {
+  if (n <= 0) return 0;
+  for (auto it = free_.begin(); it != free_.end(); ++it) {
+    if (it->second < n) continue;
+    const long long off = it->first, len = it->second;
+    free_.erase(it);
+    if (len > n) free_[off + n] = len - n;
+    return off;
+  }
+  return -1;
+}
+
+void ArenaAlloc::release(long long off, long long n) {
+  if (n <= 0) return;
+  auto it = free_.emplace(off, n).first;
+  auto nx = std::next(it);
+  if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+  if (it != free_.begin()) {
+    auto pv = std::prev(it);
+    if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); }
+  }
+}
+
+long long ArenaAlloc::free_total() const {
+  long long t = 0;
+  for (const auto& kv : free_) t += kv.second;
+  return t;
+}
+
+namespace {
+// Checks one molecule and lays out its atoms and pairs (indices relative to
+// the molecule); mirrors the checks MolDS makes when it reads a molecule.
+struct MolLayout {
+  std::vector<DevAtom> atoms;
+  std::vector<DevPair> pairs;   // a, b relative; blk relative
+  int nao = 0, nocc = 0;
+  long long blocks = 0;
+};
+
+MolLayout layout_molecule(const MoleculeInput& in) {
+  MolLayout L;
+  const int na = (int)in.Z.size();
+  if (na < 1) throw std::invalid_argument("molecule without atoms");
+  if ((int)in.xyz.size() != 3 * na) throw std::invalid_argument("coordinate count does not match atom count");
+  if (in.theory < 0 || in.theory >= NDDO_NUM_THEORIES) throw std::invalid_argument("unknown theory");
+  int ao = 0, nelec = 0;
+  for (int a = 0; a < na; ++a) {
+    const int e = nddo_element_index(in.Z[a]);
+    if (e < 0) throw std::invalid_argument("element " + std::to_string(in.Z[a]) + " has no NDDO parameters");
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(in.xyz[3 * a + k])) throw std::invalid_argument("non-finite coordinate");
+    DevAtom at;
+    at.x = in.xyz[3 * a]; at.y = in.xyz[3 * a + 1]; at.z = in.xyz[3 * a + 2];
+    at.pidx = in.theory * NDDO_NUM_ELEMENTS + e;
+    at.ao0 = ao;
+    at.nao = nddo_elements[e].n_ao;
+    at.mol = 0;
+    ao += at.nao;
+    nelec += nddo_elements[e].core_charge;
+    L.atoms.push_back(at);
+  }
+  if (nelec % 2) throw std::invalid_argument("Total number of valence electrons is odd. totalNumberValenceElectrons=" + std::to_string(nelec));
+  L.nao = ao;
+  L.nocc = nelec / 2;
+  for (int a = 0; a < na; ++a)
+    for (int b = a + 1; b < na; ++b) {
+      const DevAtom& A = L.atoms[a];
+      const DevAtom& B = L.atoms[b];
+      const double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+      if (dx == 0.0 && dy == 0.0 && dz == 0.0) throw std::invalid_argument("two atoms at the same position");
+      DevPair p;
+      p.a = a; p.b = b; p.mol = 0; p.pad = 0;
+      p.blk = L.blocks;
+      L.blocks += (long long)(A.nao == 4 ? 10 : 1) * (B.nao == 4 ? 10 : 1);
+      L.pairs.push_back(p);
+    }
+  return L;
+}
+
+inline long long round32(long long x) { return (x + 31) / 32 * 32; }
+}  // namespace
+
+size_t Batch::bytes_per_mat_element(int diis_m) {
+  // H F P P_old C G64 T64 + six refinement buffers (FP64), G32 T32 (FP32), DIIS history
+  return 13 * sizeof(double) + 2 * sizeof(float) + 2 * (size_t)std::max(diis_m, 1) * sizeof(double);
+}
+
 Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
     : eng_(eng), stream_(eng->stream()), diis_m_(diis_m) {
   if (diis_m_ < 0 || diis_m_ > kMaxDiis) throw std::invalid_argument("diis_num_error_vect out of range (0..8)");
   if (mols.empty()) throw std::invalid_argument("empty batch");
   long long mat = 0, vec = 0;
   for (size_t m = 0; m < mols.size(); ++m) {
-    const MoleculeInput& in = mols[m];
-    const int na = (int)in.Z.size();
-    if (na < 1) throw std::invalid_argument("molecule without atoms");
-    if ((int)in.xyz.size() != 3 * na) throw std::invalid_argument("coordinate count does not match atom count");
-    if (in.theory < 0 || in.theory >= NDDO_NUM_THEORIES) throw std::invalid_argument("unknown theory");
+    MolLayout L = layout_molecule(mols[m]);
     DevMol dm;
     std::memset(&dm, 0, sizeof(dm));
-    dm.natoms = na;
-    dm.theory = in.theory;
+    dm.natoms = (int)L.atoms.size();
+    dm.theory = mols[m].theory;
     dm.atom0 = (int)h_atoms.size();
     dm.pair0 = (int)h_pairs.size();
-    int ao = 0, nelec = 0;
-    for (int a = 0; a < na; ++a) {
-      const int e = nddo_element_index(in.Z[a]);
-      if (e < 0) throw std::invalid_argument("element " + std::to_string(in.Z[a]) + " has no NDDO parameters");
-      for (int k = 0; k < 3; ++k)
-        if (!std::isfinite(in.xyz[3 * a + k])) throw std::invalid_argument("non-finite coordinate");
-      DevAtom at;
-      at.x = in.xyz[3 * a]; at.y = in.xyz[3 * a + 1]; at.z = in.xyz[3 * a + 2];
-      at.pidx = in.theory * NDDO_NUM_ELEMENTS + e;
-      at.ao0 = ao;
-      at.nao = nddo_elements[e].n_ao;
-      at.mol = (int)m;
-      ao += at.nao;
-      nelec += nddo_elements[e].core_charge;
-      h_atoms.push_back(at);
+    dm.nao = L.nao;
+    dm.nocc = L.nocc;
+    for (DevAtom a : L.atoms) { a.mol = (int)m; h_atoms.push_back(a); }
+    for (DevPair p : L.pairs) {
+      p.a += dm.atom0; p.b += dm.atom0; p.mol = (int)m; p.blk += blk_total_;
+      h_pairs.push_back(p);
     }
-    if (nelec % 2) throw std::invalid_argument("Total number of valence electrons is odd. totalNumberValenceElectrons=" + std::to_string(nelec));
-    dm.nao = ao;
-    dm.nocc = nelec / 2;
-    for (int a = 0; a < na; ++a)
-      for (int b = a + 1; b < na; ++b) {
-        const DevAtom& A = h_atoms[dm.atom0 + a];
-        const DevAtom& B = h_atoms[dm.atom0 + b];
-        const double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
-        if (dx == 0.0 && dy == 0.0 && dz == 0.0) throw std::invalid_argument("two atoms at the same position");
-        DevPair p;
-        p.a = dm.atom0 + a; p.b = dm.atom0 + b; p.mol = (int)m; p.pad = 0;
-        p.blk = blk_total_;
-        blk_total_ += (long long)(A.nao == 4 ? 10 : 1) * (B.nao == 4 ? 10 : 1);
-        h_pairs.push_back(p);
-      }
-    dm.npairs = (int)h_pairs.size() - dm.pair0;
+    blk_total_ += L.blocks;
+    dm.npairs = (int)L.pairs.size();
     dm.mat0 = mat;
     dm.vec0 = vec;
-    mat += ((long long)ao * ao + 31) / 32 * 32;
-    vec += ((long long)ao + 31) / 32 * 32;
-    max_n_ = std::max(max_n_, ao);
+    mat += round32((long long)L.nao * L.nao);
+    vec += round32(L.nao);
+    max_n_ = std::max(max_n_, L.nao);
     h_mols.push_back(dm);
   }
+  BatchCapacity cap;
+  cap.slots = (int)h_mols.size();
+  cap.atoms = (long long)h_atoms.size();
+  cap.pairs = (long long)h_pairs.size();
+  cap.blocks = blk_total_;
+  cap.mat = mat;
+  cap.vec = vec;
+  cap.max_n = max_n_;
+  cap.ws_slots = cap.slots;
+  allocate(cap);
+  const int nm = (int)h_mols.size();
+  cuda_check(cudaMemcpyAsync(d_atoms, h_atoms.data(), h_atoms.size() * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_), "upload atoms");
+  if (!h_pairs.empty())
+    cuda_check(cudaMemcpyAsync(d_pairs, h_pairs.data(), h_pairs.size() * sizeof(DevPair), cudaMemcpyHostToDevice, stream_), "upload pairs");
+  cuda_check(cudaMemcpyAsync(d_mols, h_mols.data(), nm * sizeof(DevMol), cudaMemcpyHostToDevice, stream_), "upload mols");
+  cuda_check(cudaStreamSynchronize(stream_), "upload batch");
+}
+
+Batch::Batch(Engine* eng, const BatchCapacity& cap, int diis_m, cudaStream_t stream)
+    : eng_(eng), stream_(stream ? stream : eng->stream()), diis_m_(diis_m) {
+  if (diis_m_ < 0 || diis_m_ > kMaxDiis) throw std::invalid_argument("diis_num_error_vect out of range (0..8)");
+  if (cap.slots < 1 || cap.mat < 1 || cap.max_n < 1) throw std::invalid_argument("empty pool capacity");
+  pool_ = true;
+  max_n_ = cap.max_n;
+  allocate(cap);
+  h_atoms.assign(cap.atoms, DevAtom{});
+  h_pairs.assign(cap.pairs, DevPair{});
+  DevMol empty;
+  std::memset(&empty, 0, sizeof(empty));
+  h_mols.assign(cap.slots, empty);
+  slot_blocks_.assign(cap.slots, 0);
+  a_atoms_.reset(cap.atoms);
+  a_pairs_.reset(cap.pairs);
+  a_blocks_.reset(cap.blocks);
+  a_mat_.reset(cap.mat);
+  a_vec_.reset(cap.vec);
+  for (int k = cap.slots - 1; k >= 0; --k) free_slots_.push_back(k);
+  cuda_check(cudaMemcpyAsync(d_mols, h_mols.data(), cap.slots * sizeof(DevMol), cudaMemcpyHostToDevice, stream_), "upload mols");
+  cuda_check(cudaStreamSynchronize(stream_), "pool init");
+}
+
+void Batch::allocate(const BatchCapacity& cap) {
+  cap_ = cap;
+  const int nm = cap.slots;
+  const long long mat = cap.mat, vec = cap.vec;
   mat_total_ = mat;
   vec_total_ = vec;
-  const int nm = (int)h_mols.size();
-  d_atoms = dalloc<DevAtom>(h_atoms.size(), &bytes_);
-  d_pairs = dalloc<DevPair>(h_pairs.size(), &bytes_);
+  d_atoms = dalloc<DevAtom>(cap.atoms, &bytes_);
+  d_pairs = dalloc<DevPair>(cap.pairs, &bytes_);
   d_mols = dalloc<DevMol>(nm, &bytes_);
   d_list = dalloc<int>(nm, &bytes_);
-  d_blocks = dalloc<double>(blk_total_, &bytes_);
-  d_ecore_pair = dalloc<double>(h_pairs.size(), &bytes_);
-  {
-    std::vector<int> heavy, xh, hh;
-    for (size_t k = 0; k < h_pairs.size(); ++k) {
-      const int na = h_atoms[h_pairs[k].a].nao, nb = h_atoms[h_pairs[k].b].nao;
-      if (na == 4 && nb == 4) heavy.push_back((int)k);
-      else if (na == 4 || nb == 4) xh.push_back((int)k);
-      else hh.push_back((int)k);
-    }
-    xh.insert(xh.end(), hh.begin(), hh.end());
-    n_heavy_ = (long long)heavy.size();
-    n_light_ = (long long)xh.size();
-    d_heavy_pairs = dalloc<int>(heavy.size(), &bytes_);
-    d_light_pairs = dalloc<int>(xh.size(), &bytes_);
-    if (!heavy.empty())
-      cuda_check(cudaMemcpyAsync(d_heavy_pairs, heavy.data(), heavy.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload heavy pairs");
-    if (!xh.empty())
-      cuda_check(cudaMemcpyAsync(d_light_pairs, xh.data(), xh.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload light pairs");
-    cuda_check(cudaStreamSynchronize(stream_), "upload pair lists");
-  }
+  d_blocks = dalloc<double>(cap.blocks, &bytes_);
+  d_ecore_pair = dalloc<double>(cap.pairs, &bytes_);
+  d_heavy_pairs = dalloc<int>(cap.pairs, &bytes_);
+  d_light_pairs = dalloc<int>(cap.pairs, &bytes_);
   d_H = dalloc<double>(mat, &bytes_);
   d_F = dalloc<double>(mat, &bytes_);
   d_P = dalloc<double>(mat, &bytes_);
@@ -195,37 +296,124 @@ Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
   d_T64 = dalloc<double>(mat, &bytes_);
   for (int i = 0; i < 6; ++i) d_S[i] = dalloc<double>(mat, &bytes_);
   d_state = dalloc<MolState>(nm, &bytes_);
-  d_charges = dalloc<double>(h_atoms.size(), &bytes_);
+  d_charges = dalloc<double>(cap.atoms, &bytes_);
   d_sweeps = dalloc<int>(nm, &bytes_);
   d_count = dalloc<int>(1, &bytes_);
   d_active = dalloc<char>(nm, &bytes_);
-  cuda_check(cudaMemcpyAsync(d_atoms, h_atoms.data(), h_atoms.size() * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_), "upload atoms");
-  if (!h_pairs.empty())
-    cuda_check(cudaMemcpyAsync(d_pairs, h_pairs.data(), h_pairs.size() * sizeof(DevPair), cudaMemcpyHostToDevice, stream_), "upload pairs");
-  cuda_check(cudaMemcpyAsync(d_mols, h_mols.data(), nm * sizeof(DevMol), cudaMemcpyHostToDevice, stream_), "upload mols");
   cuda_check(cudaMemsetAsync(d_state, 0, nm * sizeof(MolState), stream_), "memset state");
+  cuda_check(cudaMemsetAsync(d_sweeps, 0, nm * sizeof(int), stream_), "memset sweeps");
   cuda_check(cudaMemsetAsync(d_H, 0, mat * sizeof(double), stream_), "memset H");
   cuda_check(cudaMemsetAsync(d_P, 0, mat * sizeof(double), stream_), "memset P");
   cuda_check(cudaMemsetAsync(d_hist_dens, 0, std::max(diis_m_, 1) * mat * sizeof(double), stream_), "memset hist");
   cuda_check(cudaMemsetAsync(d_hist_err, 0, std::max(diis_m_, 1) * mat * sizeof(double), stream_), "memset hist");
-  // Jacobi workspaces for molecules too large for shared memory
+  // Jacobi workspaces: the one-CTA kernel spills V (and A) of FP64 bases above
+  // 138 to global memory; bases above kSmallJacobiMaxN use the block Jacobi
   bool ag, vg;
-  const long long np = (max_n_ + 3) & ~3;   // the Jacobi working size (see jacobi.cu)
+  const int small_n = std::min(cap.max_n, kSmallJacobiMaxN);
+  const long long np = (small_n + 3) & ~3;   // the Jacobi working size (see jacobi.cu)
   jws_stride_ = np * np;
-  if (jacobi_needs_workspace(max_n_, 4, &ag, &vg)) {
-    d_jA32 = dalloc<float>(ag ? (size_t)nm * jws_stride_ : 1, &bytes_);
-    d_jV32 = dalloc<float>((size_t)nm * jws_stride_, &bytes_);
+  const int ws = std::max(1, std::min(cap.ws_slots, nm));
+  if (jacobi_needs_workspace(small_n, 4, &ag, &vg)) {
+    d_jA32 = dalloc<float>(ag ? (size_t)ws * jws_stride_ : 1, &bytes_);
+    d_jV32 = dalloc<float>((size_t)ws * jws_stride_, &bytes_);
   }
-  if (jacobi_needs_workspace(max_n_, 8, &ag, &vg)) {
-    d_jA64 = dalloc<double>(ag ? (size_t)nm * jws_stride_ : 1, &bytes_);
-    d_jV64 = dalloc<double>((size_t)nm * jws_stride_, &bytes_);
+  if (jacobi_needs_workspace(small_n, 8, &ag, &vg)) {
+    d_jA64 = dalloc<double>(ag ? (size_t)ws * jws_stride_ : 1, &bytes_);
+    d_jV64 = dalloc<double>((size_t)ws * jws_stride_, &bytes_);
   }
+  if (cap.max_n > kSmallJacobiMaxN) {
+    long long st, qst;
+    const size_t b = block_jacobi_workspace(cap.max_n, ws, (int)sizeof(double), &st, &qst);
+    cuda_check(cudaMalloc(&d_bj_ws, b), "cudaMalloc block-Jacobi workspace");
+    bytes_ += b;
+  }
+  cuda_check(cudaHostAlloc(&h_bj_pending, sizeof(int), cudaHostAllocDefault), "cudaHostAlloc");
+  cap_.ws_slots = ws;
+  // persistent job tables and lists: one job per molecule per GEMM kind
+  job_cap_ = nm;
+  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_};
+  for (JobSet* j : all) { j->d = dalloc<GemmJob>(job_cap_, &bytes_); j->cap = job_cap_; }
+  cuda_check(cudaHostAlloc(&h_jobs_, sizeof(GemmJob) * (size_t)job_cap_ * 13, cudaHostAllocDefault), "cudaHostAlloc jobs");
+  cuda_check(cudaHostAlloc(&h_lists_, sizeof(int) * (size_t)nm * 9, cudaHostAllocDefault), "cudaHostAlloc lists");
+  for (int b = 0; b < 8; ++b) d_bucket_lists_.push_back(dalloc<int>(nm, &bytes_));
+  cuda_check(cudaStreamSynchronize(stream_), "allocate");
+}
+
+int Batch::admit(const MoleculeInput& in) {
+  if (!pool_) throw std::logic_error("admit on a fixed batch");
+  MolLayout L = layout_molecule(in);
+  if (L.nao > cap_.max_n) throw std::invalid_argument("molecule larger than the pool's largest basis");
+  if (free_slots_.empty()) return -1;
+  const long long na = (long long)L.atoms.size(), npr = (long long)L.pairs.size();
+  const long long nmat = round32((long long)L.nao * L.nao), nvec = round32(L.nao);
+  const long long oa = a_atoms_.alloc(na);
+  if (oa < 0) return -1;
+  const long long op = a_pairs_.alloc(npr);
+  if (op < 0) { a_atoms_.release(oa, na); return -1; }
+  const long long ob = a_blocks_.alloc(L.blocks);
+  if (ob < 0) { a_atoms_.release(oa, na); a_pairs_.release(op, npr); return -1; }
+  const long long om = a_mat_.alloc(nmat);
+  if (om < 0) { a_atoms_.release(oa, na); a_pairs_.release(op, npr); a_blocks_.release(ob, L.blocks); return -1; }
+  const long long ov = a_vec_.alloc(nvec);
+  if (ov < 0) {
+    a_atoms_.release(oa, na); a_pairs_.release(op, npr); a_blocks_.release(ob, L.blocks); a_mat_.release(om, nmat);
+    return -1;
+  }
+  const int slot = free_slots_.back();
+  free_slots_.pop_back();
+  DevMol dm;
+  std::memset(&dm, 0, sizeof(dm));
+  dm.natoms = (int)na;
+  dm.nao = L.nao;
+  dm.nocc = L.nocc;
+  dm.theory = in.theory;
+  dm.atom0 = (int)oa;
+  dm.pair0 = (int)op;
+  dm.npairs = (int)npr;
+  dm.mat0 = om;
+  dm.vec0 = ov;
+  for (long long a = 0; a < na; ++a) { DevAtom x = L.atoms[a]; x.mol = slot; h_atoms[oa + a] = x; }
+  for (long long k = 0; k < npr; ++k) {
+    DevPair p = L.pairs[k];
+    p.a += (int)oa; p.b += (int)oa; p.mol = slot; p.blk += ob;
+    h_pairs[op + k] = p;
+  }
+  h_mols[slot] = dm;
+  slot_blocks_[slot] = L.blocks;
+  // a slot number can now stand for a different molecule: the job tables and
+  // size buckets of any cached list are stale
+  cur_list_.clear();
+  buckets_.clear();
+  cuda_check(cudaMemcpyAsync(d_atoms + oa, &h_atoms[oa], na * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_), "upload atoms");
+  if (npr) cuda_check(cudaMemcpyAsync(d_pairs + op, &h_pairs[op], npr * sizeof(DevPair), cudaMemcpyHostToDevice, stream_), "upload pairs");
+  cuda_check(cudaMemcpyAsync(d_mols + slot, &h_mols[slot], sizeof(DevMol), cudaMemcpyHostToDevice, stream_), "upload mol");
+  return slot;
+}
+
+void Batch::release(int slot) {
+  if (!pool_ || slot < 0 || slot >= (int)h_mols.size() || h_mols[slot].natoms == 0) return;
+  DevMol& d = h_mols[slot];
+  const long long n = d.nao;
+  a_atoms_.release(d.atom0, d.natoms);
+  a_pairs_.release(d.pair0, d.npairs);
+  if (d.npairs > 0) a_blocks_.release(h_pairs[d.pair0].blk, slot_blocks_[slot]);
+  a_mat_.release(d.mat0, round32(n * n));
+  a_vec_.release(d.vec0, round32(n));
+  std::memset(&d, 0, sizeof(d));
+  slot_blocks_[slot] = 0;
+  free_slots_.push_back(slot);
+  cur_list_.clear();
+  buckets_.clear();
 }
 
 Batch::~Batch() {
   free_jobs();
   for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   for (int* p : d_bucket_lists_) cudaFree(p);
+  if (h_jobs_) cudaFreeHost(h_jobs_);
+  if (h_lists_) cudaFreeHost(h_lists_);
+  if (h_bj_pending) cudaFreeHost(h_bj_pending);
+  if (d_bj_ws) cudaFree(d_bj_ws);
   void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
                   d_hist_dens, d_hist_err, d_G32, d_T32, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
                   d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs};
@@ -235,22 +423,28 @@ Batch::~Batch() {
 
 void Batch::free_jobs() {
   JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_};
-  for (JobSet* j : all) { if (j->d) cudaFree(j->d); j->d = nullptr; j->n = 0; j->tiles = 0; }
+  for (JobSet* j : all) { if (j->d) cudaFree(j->d); j->d = nullptr; j->n = 0; j->tiles = 0; j->cap = 0; }
 }
 
 void Batch::make_jobset(JobSet* js, const std::vector<GemmJob>& jobs_in) {
-  std::vector<GemmJob> jobs = jobs_in;
+  // staging slot of this job set inside the pinned table
+  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_};
+  int idx = 0;
+  while (all[idx] != js) ++idx;
+  GemmJob* stage = h_jobs_ + (size_t)idx * job_cap_;
+  if ((int)jobs_in.size() > js->cap) throw std::logic_error("GEMM job table overflow");
   int tiles = 0;
-  for (GemmJob& j : jobs) {
+  for (size_t k = 0; k < jobs_in.size(); ++k) {
+    GemmJob j = jobs_in[k];
     j.tile0 = tiles;
     j.tiles_n = gemm_tiles_n(j.N);
     if (j.M > 0 && j.N > 0) tiles += j.sym ? gemm_tiles_sym(j.N) : gemm_tiles(j.M, j.N);
+    stage[k] = j;
   }
-  js->n = (int)jobs.size();
+  js->n = (int)jobs_in.size();
   js->tiles = tiles;
-  if (jobs.empty()) return;
-  cuda_check(cudaMalloc(&js->d, jobs.size() * sizeof(GemmJob)), "cudaMalloc jobs");
-  cuda_check(cudaMemcpyAsync(js->d, jobs.data(), jobs.size() * sizeof(GemmJob), cudaMemcpyHostToDevice, stream_), "upload jobs");
+  if (jobs_in.empty()) return;
+  cuda_check(cudaMemcpyAsync(js->d, stage, jobs_in.size() * sizeof(GemmJob), cudaMemcpyHostToDevice, stream_), "upload jobs");
 }
 
 static GemmJob job(long long a, long long b, long long c, int M, int N, int K, int lda, int ldb, int ldc, int mol,
@@ -263,7 +457,6 @@ static GemmJob job(long long a, long long b, long long c, int M, int N, int K, i
 }
 
 void Batch::build_jobs(const std::vector<int>& which) {
-  free_jobs();
   std::vector<GemmJob> t1, t2, dn, w, kt, yt, mm, d2, z, pp, ns1, ns2, ov;
   for (int m : which) {
     const DevMol& d = h_mols[m];
@@ -293,16 +486,21 @@ void Batch::build_jobs(const std::vector<int>& which) {
 
 void Batch::upload_list(const std::vector<int>& which) {
   if (which == cur_list_ && !buckets_.empty()) return;
+  if ((int)which.size() > cap_.slots) throw std::logic_error("molecule list longer than the slot table");
+  // the pinned staging buffers may still feed copies of the previous list
+  cuda_check(cudaStreamSynchronize(stream_), "list staging");
   cur_list_ = which;
-  cuda_check(cudaMemcpyAsync(d_list, which.data(), which.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload list");
+  const int nm = cap_.slots;
+  std::copy(which.begin(), which.end(), h_lists_);
+  if (!which.empty())
+    cuda_check(cudaMemcpyAsync(d_list, h_lists_, which.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload list");
   build_jobs(which);
   // Jacobi size buckets: smaller molecules get a smaller shared-memory footprint
-  for (int* p : d_bucket_lists_) cudaFree(p);
-  d_bucket_lists_.clear();
   buckets_.clear();
   bucket_max_n_.clear();
+  bucket_dev_.clear();
   const int edges[] = {64, 96, 128, 160, 194, 256, 338, 1 << 30};
-  int lo = 0;
+  int lo = 0, bi = 0;
   for (int hi : edges) {
     std::vector<int> b;
     int mx = 0;
@@ -311,13 +509,15 @@ void Batch::upload_list(const std::vector<int>& which) {
       if (n > lo && n <= hi) { b.push_back(m); mx = std::max(mx, n); }
     }
     lo = hi;
+    const int slot = bi++;
     if (b.empty()) continue;
-    int* d = nullptr;
-    cuda_check(cudaMalloc(&d, b.size() * sizeof(int)), "cudaMalloc bucket");
-    cuda_check(cudaMemcpyAsync(d, b.data(), b.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload bucket");
-    d_bucket_lists_.push_back(d);
+    int* stage = h_lists_ + (size_t)(slot + 1) * nm;
+    std::copy(b.begin(), b.end(), stage);
+    cuda_check(cudaMemcpyAsync(d_bucket_lists_[slot], stage, b.size() * sizeof(int), cudaMemcpyHostToDevice, stream_),
+               "upload bucket");
     buckets_.push_back(b);
     bucket_max_n_.push_back(mx);
+    bucket_dev_.push_back(d_bucket_lists_[slot]);
   }
 }
 
@@ -437,8 +637,35 @@ void Batch::set_coordinates(const double* xyz) {
 void Batch::integrals() {
   std::vector<int> all(h_mols.size());
   for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
-  upload_list(all);
-  int h = prof_begin(kKPair, 8.0 * (double)blk_total_);
+  integrals(all);
+}
+
+void Batch::integrals(const std::vector<int>& which) {
+  if (which.empty()) return;
+  upload_list(which);
+  // pair index lists of the listed molecules: sp-sp pairs for the warp kernel,
+  // X-H then H-H pairs for the thread-per-pair kernel
+  std::vector<int> heavy, xh, hh;
+  double blk = 0.0;
+  for (int m : which) {
+    const DevMol& d = h_mols[m];
+    for (int k = 0; k < d.npairs; ++k) {
+      const int pi = d.pair0 + k;
+      const int na = h_atoms[h_pairs[pi].a].nao, nb = h_atoms[h_pairs[pi].b].nao;
+      blk += (double)((na == 4 ? 10 : 1) * (nb == 4 ? 10 : 1));
+      if (na == 4 && nb == 4) heavy.push_back(pi);
+      else if (na == 4 || nb == 4) xh.push_back(pi);
+      else hh.push_back(pi);
+    }
+  }
+  xh.insert(xh.end(), hh.begin(), hh.end());
+  n_heavy_ = (long long)heavy.size();
+  n_light_ = (long long)xh.size();
+  if (!heavy.empty())
+    cuda_check(cudaMemcpyAsync(d_heavy_pairs, heavy.data(), heavy.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload heavy pairs");
+  if (!xh.empty())
+    cuda_check(cudaMemcpyAsync(d_light_pairs, xh.data(), xh.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload light pairs");
+  int h = prof_begin(kKPair, 8.0 * blk);
   launches_ += 2;
   launch_pair_kernels_split(d_atoms, d_pairs, d_heavy_pairs, n_heavy_, d_light_pairs, n_light_, d_mols, eng_->eri(),
                             eng_->ovt(), d_blocks, d_H, d_ecore_pair, stream_);
@@ -446,9 +673,11 @@ void Batch::integrals() {
   cuda_check(cudaGetLastError(), "pair_kernel");
   h = prof_begin(kKHcore, 0.0);
   launches_ += 1;
-  launch_hcore_kernel(d_atoms, d_pairs, d_mols, d_list, (int)all.size(), d_blocks, d_ecore_pair, d_H, d_state, stream_);
+  launch_hcore_kernel(d_atoms, d_pairs, d_mols, d_list, (int)which.size(), d_blocks, d_ecore_pair, d_H, d_state, stream_);
   prof_end(h);
   cuda_check(cudaGetLastError(), "hcore_kernel");
+  // the pageable index vectors above must outlive their copies
+  cuda_check(cudaStreamSynchronize(stream_), "integrals");
 }
 
 static ScfParamsDev to_dev(const ScfSettings& s) {
@@ -473,36 +702,68 @@ void Batch::begin(const ScfSettings& s, const std::vector<int>& which, bool requ
     cuda_check(cudaMalloc(&d_trace, (size_t)h_mols.size() * s.max_iter * sizeof(TraceEntry)), "cudaMalloc trace");
     max_iter_alloc_ = s.max_iter;
   }
+  if (which.empty()) return;
   upload_list(which);
   active_host_.resize(h_mols.size(), 0);
   for (int m : which) active_host_[m] = 1;
-  cuda_check(cudaMemsetAsync(d_sweeps, 0, h_mols.size() * sizeof(int), stream_), "memset sweeps");
   launches_ += 1;
   init_state_kernel<<<(unsigned)which.size(), 256, 0, stream_>>>(d_mols, d_list, (int)which.size(), d_state, d_C,
-                                                                 d_P, requires_guess ? 1 : 0, requires_guess ? 1 : 0);
+                                                                 d_P, requires_guess ? 1 : 0, requires_guess ? 1 : 0,
+                                                                 d_hist_dens, d_hist_err, diis_m_, mat_total_, d_sweeps);
   cuda_check(cudaGetLastError(), "init_state");
+}
+
+// One Jacobi launch per size bucket; buckets whose molecules need a
+// global-memory workspace are split into launches of at most ws_slots CTAs.
+void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin) {
+  for (size_t b = 0; b < buckets_.size(); ++b) {
+    bool ag, vg;
+    const int nb = (int)buckets_[b].size();
+    if (bucket_max_n_[b] > kSmallJacobiMaxN) {
+      // block Jacobi, many CTAs per molecule, at most ws_slots molecules per call
+      for (int k0 = 0; k0 < nb; k0 += cap_.ws_slots) {
+        const int cnt = std::min(cap_.ws_slots, nb - k0);
+        if (fp32)
+          launches_ += launch_block_jacobi_f32(d_mols, bucket_dev_[b] + k0, cnt, bucket_max_n_[b], d_state, d_G32, Cin,
+                                               d_C, d_eps, d_bj_ws, s.max_sweeps, d_sweeps, h_bj_pending, stream_);
+        else
+          launches_ += launch_block_jacobi_f64(d_mols, bucket_dev_[b] + k0, cnt, bucket_max_n_[b], d_state, d_G64, Cin,
+                                               d_C, d_eps, d_bj_ws, s.max_sweeps, d_sweeps, h_bj_pending, stream_);
+      }
+      continue;
+    }
+    const int chunk = jacobi_needs_workspace(bucket_max_n_[b], fp32 ? 4 : 8, &ag, &vg) ? cap_.ws_slots : nb;
+    for (int k0 = 0; k0 < nb; k0 += chunk) {
+      const int cnt = std::min(chunk, nb - k0);
+      launches_ += 1;
+      if (fp32)
+        launch_jacobi_f32(d_mols, bucket_dev_[b] + k0, cnt, bucket_max_n_[b], d_state, 1, d_G32, Cin, 1, d_C, d_eps,
+                          d_jA32, d_jV32, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+      else
+        launch_jacobi_f64(d_mols, bucket_dev_[b] + k0, cnt, bucket_max_n_[b], d_state, 1, d_G64, Cin, 1, d_C, d_eps,
+                          d_jA64, d_jV64, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+    }
+  }
 }
 
 void Batch::eigen_step(const ScfSettings& s) {
   if (s.precision == 0) {
     int h = prof_begin(kKTransform, active_work_estimate(kKTransform));
-    launches_ += 2 + (long long)buckets_.size();
+    launches_ += 2;
     launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, d_C, d_T64, false, true, 0.0, d_state, 1, -1, stream_);
     launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, d_C, d_T64, d_G64, false, false, 0.0, d_state, 1, -1, stream_);
     prof_end(h);
     h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
-    for (size_t b = 0; b < buckets_.size(); ++b)
-      launch_jacobi_f64(d_mols, d_bucket_lists_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_G64, d_C,
-                        1, d_C, d_eps, d_jA64, d_jV64, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+    run_jacobi(false, s, d_C);
     prof_end(h);
   } else {
     // The FP32 rotations of each iteration erode the orthonormality of the
     // warm-start basis; one Newton-Schulz step C <- 1.5 C - 0.5 (C C^T) C
     // (FP32 accumulation) restores it to FP32 round-off before it is reused.
     double* Cn = d_T64;
-    launches_ += 4 + (long long)buckets_.size();
+    launches_ += 5;
     int h = prof_begin(kKOrtho, active_work_estimate(kKOrtho));
-    cuda_check(cudaMemcpyAsync(Cn, d_C, mat_total_ * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy basis");
+    launch_copy_matrices(d_mols, d_list, (int)cur_list_.size(), d_state, d_C, Cn, stream_);
     launch_gemm(j_ns1_.d, j_ns1_.n, j_ns1_.tiles, d_C, d_C, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
     launch_gemm(j_ns2_.d, j_ns2_.n, j_ns2_.tiles, d_T32, d_C, Cn, false, false, 0.0f, d_state, 1, -1, stream_);
     prof_end(h);
@@ -511,9 +772,7 @@ void Batch::eigen_step(const ScfSettings& s) {
     launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, Cn, d_T32, d_G32, false, false, 0.0f, d_state, 1, -1, stream_);
     prof_end(h);
     h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
-    for (size_t b = 0; b < buckets_.size(); ++b)
-      launch_jacobi_f32(d_mols, d_bucket_lists_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_G32, Cn,
-                        1, d_C, d_eps, d_jA32, d_jV32, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+    run_jacobi(true, s, Cn);
     prof_end(h);
   }
   cuda_check(cudaGetLastError(), "eigen step");
@@ -583,6 +842,24 @@ int Batch::count_active(const std::vector<int>& which) {
   }
   cuda_check(cudaStreamSynchronize(stream_), "count sync");
   return h;
+}
+
+void Batch::count_active_async(const std::vector<int>& which, int* h_count, char* h_active, cudaEvent_t done) {
+  upload_list(which);
+  launches_ += 1;
+  count_active_kernel<<<1, 256, 0, stream_>>>(d_list, (int)which.size(), d_state, d_count, d_active);
+  cuda_check(cudaMemcpyAsync(h_count, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream_), "count copy");
+  cuda_check(cudaMemcpyAsync(h_active, d_active, h_mols.size(), cudaMemcpyDeviceToHost, stream_), "active copy");
+  cuda_check(cudaEventRecord(done, stream_), "count event");
+}
+
+void Batch::copy_states_async(MolState* host) {
+  cuda_check(cudaMemcpyAsync(host, d_state, h_mols.size() * sizeof(MolState), cudaMemcpyDeviceToHost, stream_), "state copy");
+}
+
+void Batch::copy_charges_async(int m, double* host) {
+  const DevMol& d = h_mols[m];
+  cuda_check(cudaMemcpyAsync(host, d_charges + d.atom0, d.natoms * sizeof(double), cudaMemcpyDeviceToHost, stream_), "copy charges");
 }
 
 void Batch::finish(const ScfSettings& s, const std::vector<int>& which) {

@@ -2,6 +2,7 @@
 // molecule batches, and drives the batched SCF state machine.
 #pragma once
 #include <cuda_runtime.h>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -43,15 +44,54 @@ struct MolResult {
 
 class Engine;
 
+// Arena sizes of a molecule pool (elements of each arena).
+struct BatchCapacity {
+  int slots = 0;               // molecules resident at once
+  long long atoms = 0, pairs = 0, blocks = 0, mat = 0, vec = 0;
+  int max_n = 0;               // largest basis admitted
+  int ws_slots = 0;            // molecules per Jacobi launch that need a global-memory workspace
+};
+
+// First-fit allocator of element ranges inside one arena (coalescing frees).
+class ArenaAlloc {
+ public:
+  void reset(long long capacity);
+  long long alloc(long long n);          // offset, or -1 when no free range is large enough
+  void release(long long off, long long n);
+  long long free_total() const;
+ private:
+  std::map<long long, long long> free_;  // offset -> length
+};
+
 // A set of molecules resident on the device with every buffer the SCF needs.
+// Two modes: a fixed batch (every molecule given at construction), or a pool
+// with fixed arena capacities into which molecules are admitted and released
+// one at a time (the serving loop).
 class Batch {
  public:
   Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m);
+  Batch(Engine* eng, const BatchCapacity& cap, int diis_m, cudaStream_t stream);
   ~Batch();
   Batch(const Batch&) = delete;
   Batch& operator=(const Batch&) = delete;
 
   int size() const { return (int)h_mols.size(); }
+  cudaStream_t stream() const { return stream_; }
+
+  // pool mode: place a molecule (slot index, or -1 when an arena or the slot
+  // table is full) and give its space back
+  int admit(const MoleculeInput& in);
+  void release(int slot);
+  // device bytes one element of the per-molecule N x N arena costs (all buffers)
+  static size_t bytes_per_mat_element(int diis_m);
+  // pair integrals, H and core-core energy of the listed molecules
+  void integrals(const std::vector<int>& which);
+  // count_active without a host wait: the count and per-slot active flags land
+  // in pinned host memory, and `done` is recorded after the copies
+  void count_active_async(const std::vector<int>& which, int* h_count, char* h_active, cudaEvent_t done);
+  // asynchronous copies into pinned host memory (complete at the next stream sync)
+  void copy_states_async(MolState* host);
+  void copy_charges_async(int m, double* host);
   int nao(int m) const { return h_mols[m].nao; }
   int natoms(int m) const { return h_mols[m].natoms; }
   int nocc(int m) const { return h_mols[m].nocc; }
@@ -91,6 +131,7 @@ class Batch {
   double* dev_P() const { return d_P; }
 
  private:
+  void allocate(const BatchCapacity& cap);
   void build_jobs(const std::vector<int>& which);
   void upload_list(const std::vector<int>& which);
   void eigen_step(const ScfSettings& s);
@@ -99,6 +140,11 @@ class Batch {
   Engine* eng_;
   cudaStream_t stream_;
   int diis_m_;
+  bool pool_ = false;
+  BatchCapacity cap_;
+  ArenaAlloc a_atoms_, a_pairs_, a_blocks_, a_mat_, a_vec_;
+  std::vector<int> free_slots_;
+  std::vector<long long> slot_blocks_;   // block-arena length of each occupied slot
   size_t bytes_ = 0;
   long long mat_total_ = 0, vec_total_ = 0;
   int max_n_ = 0, max_iter_alloc_ = 0;
@@ -123,6 +169,8 @@ class Batch {
   double *d_G64 = nullptr, *d_T64 = nullptr;
   double* d_S[6] = {};
   float *d_jA32 = nullptr, *d_jV32 = nullptr;
+  void* d_bj_ws = nullptr;               // block-Jacobi workspace (bases above kSmallJacobiMaxN)
+  int* h_bj_pending = nullptr;           // pinned: molecules still rotating after a block-Jacobi sweep
   double *d_jA64 = nullptr, *d_jV64 = nullptr;
   long long jws_stride_ = 0;
   MolState* d_state = nullptr;
@@ -135,9 +183,14 @@ class Batch {
   // current molecule list and its GEMM job tables
   std::vector<int> cur_list_;
   std::vector<std::vector<int>> buckets_;      // jacobi size buckets (indices into cur_list_)
-  std::vector<int*> d_bucket_lists_;
+  std::vector<int*> d_bucket_lists_;     // persistent, one per size bucket, `slots` entries each
+  std::vector<int*> bucket_dev_;         // device list of each non-empty bucket of the current list
+  void run_jacobi(bool fp32, const ScfSettings& s, const double* Cin);
   std::vector<int> bucket_max_n_;
-  struct JobSet { GemmJob* d = nullptr; int n = 0; int tiles = 0; };
+  struct JobSet { GemmJob* d = nullptr; int n = 0; int tiles = 0; int cap = 0; };
+  GemmJob* h_jobs_ = nullptr;             // pinned staging of the job tables
+  int* h_lists_ = nullptr;                // pinned staging of the molecule / bucket lists
+  int job_cap_ = 0;
   JobSet j_trans1_, j_trans2_, j_dens_, j_w_, j_kt_, j_yt_, j_m_, j_d2_, j_z_, j_p_, j_ns1_, j_ns2_, j_ov_;
   void free_jobs();
   void make_jobset(JobSet* js, const std::vector<GemmJob>& jobs);

@@ -298,7 +298,9 @@ void launch_jacobi_impl(const DevMol* mols, const int* mol_list, int nlist, int 
     if (jacobi_smem_bytes(max_n, elem, false, true) > limit) a_sm = false;
   }
   const size_t bytes = jacobi_smem_bytes(max_n, elem, v_sm, a_sm);
-  cudaFuncSetAttribute(jacobi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  // the opt-in bound is set to the device limit (the same value on every call),
+  // so launches from several host threads never race on it
+  cudaFuncSetAttribute(jacobi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
   jacobi_kernel<T><<<nlist, kJacobiThreads, bytes, s>>>(mols, mol_list, st, require_active, G, Cin, use_basis,
                                                         Cout, eps, Aws, Vws, ws_stride, a_sm ? 1 : 0,
                                                         v_sm ? 1 : 0, max_sweeps, sweeps_out);

@@ -20,6 +20,17 @@ struct GemmJob {
 
 int gemm_tiles(int M, int N);
 int gemm_tiles_sym(int N);
+// block Jacobi (block_jacobi.cu) for bases above the one-CTA Jacobi's limit
+constexpr int kSmallJacobiMaxN = 194;
+size_t block_jacobi_workspace(int max_n, int nslots, int elem, long long* stride, long long* qstride);
+int launch_block_jacobi_f32(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
+                            const float* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
+                            int* sweeps_out, int* h_pending, cudaStream_t s);
+int launch_block_jacobi_f64(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
+                            const double* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
+                            int* sweeps_out, int* h_pending, cudaStream_t s);
+void launch_copy_matrices(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, const double* src,
+                          double* dst, cudaStream_t s);
 int gemm_tiles_n(int N);
 
 // pair_fock.cu

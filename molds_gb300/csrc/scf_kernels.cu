@@ -415,4 +415,22 @@ void launch_copy_occ_rows(const DevMol* mols, const int* mol_list, int nlist, co
   copy_rows_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, src, dst);
 }
 
+// copy each listed active molecule's N x N block (src -> dst, same offsets)
+__global__ void copy_matrices_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+                                     const MolState* __restrict__ st, const double* __restrict__ src,
+                                     double* __restrict__ dst) {
+  const int m = mol_list[blockIdx.y];
+  if (st[m].status != kActive) return;
+  const DevMol mol = mols[m];
+  const long long cnt = (long long)mol.nao * mol.nao;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x)
+    dst[mol.mat0 + e] = src[mol.mat0 + e];
+}
+
+void launch_copy_matrices(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, const double* src,
+                          double* dst, cudaStream_t s) {
+  if (nlist <= 0) return;
+  copy_matrices_kernel<<<dim3(16, nlist), 256, 0, s>>>(mols, mol_list, st, src, dst);
+}
+
 }  // namespace nddo

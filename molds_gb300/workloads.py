@@ -141,8 +141,29 @@ def _graph_distance(nat, bonds):
     return D
 
 
+_gen_lib = None
+
+
+def _generator():
+    """The C alkane generator (molds_gb300/_build/libworkloads.so, built with the CUDA library)."""
+    global _gen_lib
+    if _gen_lib is None:
+        import ctypes
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libworkloads.so")
+        if not os.path.exists(path):
+            raise ImportError(f"{path} is missing: build with `python -m molds_gb300.build`")
+        L = ctypes.CDLL(path)
+        L.alkane_generate.restype = ctypes.c_int
+        L.alkane_generate.argtypes = [ctypes.c_ulonglong, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                      ctypes.c_longlong, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        _gen_lib = L
+    return _gen_lib
+
+
 def random_alkane(seed: int, n: int | None = None, n_range=(3, 60), min_dist=1.8, min_dist_h=1.0,
-                  max_tries=100) -> Molecule:
+                  attempts=48, budget=200000, max_trees=400) -> Molecule:
     """A random saturated acyclic alkane CnH(2n+2).
 
     Topology: each new carbon attaches to a uniformly chosen carbon with < 4
@@ -156,27 +177,26 @@ def random_alkane(seed: int, n: int | None = None, n_range=(3, 60), min_dist=1.8
     carbons when dihedrals are uniform (hydrogens 5-6 bonds apart meet below
     1.8 A in about half of random hexane conformations), so hydrogens get the
     looser floor.  A carbon that cannot be placed sends the search back to the
-    carbon that owns a clashing atom; a tree that cannot be placed at all is
-    redrawn."""
+    carbon that owns a clashing atom; a tree that cannot be placed within
+    `budget` draws is redrawn.  The growth runs in C (csrc/alkane_gen.c); n is
+    drawn here from the seed."""
+    import ctypes
     rng = np.random.default_rng(seed)
     if n is None:
         n = int(rng.integers(n_range[0], n_range[1] + 1))
-    for _ in range(max_tries):
-        parent = [-1]
-        deg = [0]
-        for k in range(1, n):
-            cand = [c for c in range(k) if deg[c] < 4]
-            p = int(cand[rng.integers(len(cand))])
-            parent.append(p)
-            deg[p] += 1
-            deg.append(1)
-        mol = _grow_alkane(parent, rng, min_dist, min_dist_h)
-        if mol is not None:
-            return mol
-    raise RuntimeError(f"no acceptable geometry for n={n} after {max_tries} tries")
+    total = 3 * n + 2
+    Z = np.zeros(total, dtype=np.int32)
+    xyz = np.zeros((total, 3))
+    k = _generator().alkane_generate(int(seed) & 0xFFFFFFFFFFFFFFFF, int(n), float(min_dist), float(min_dist_h),
+                                     int(attempts), int(budget), int(max_trees),
+                                     Z.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                     xyz.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), total)
+    if k != total:
+        raise RuntimeError(f"no acceptable geometry for n={n} (generator returned {k})")
+    return Molecule(Z, xyz * ANG2AU)
 
 
-def _grow_alkane(parent, rng, min_dist, min_dist_h, attempts=48, budget=40000):
+def _grow_alkane(parent, rng, min_dist, min_dist_h, attempts=48, budget=40000, depth_first=False):
     """Places the carbons of a tree breadth first, drawing each carbon's
     dihedral uniformly; `attempts` draws are tested at once and one clash-free
     draw is kept.  When none is clash-free the search jumps back to the most
@@ -188,11 +208,18 @@ def _grow_alkane(parent, rng, min_dist, min_dist_h, attempts=48, budget=40000):
     for k in range(1, n):
         children[parent[k]].append(k)
     order = []
-    queue = list(children[0])
-    while queue:
-        c = queue.pop(0)
-        order.append(c)
-        queue += children[c]
+    if depth_first:
+        stack = list(reversed(children[0]))
+        while stack:
+            c = stack.pop()
+            order.append(c)
+            stack += list(reversed(children[c]))
+    else:
+        queue = list(children[0])
+        while queue:
+            c = queue.pop(0)
+            order.append(c)
+            queue += children[c]
     total = 3 * n + 2
     Z = np.zeros(total, dtype=np.int32)
     pos = np.zeros((total, 3))
@@ -256,10 +283,9 @@ def _grow_alkane(parent, rng, min_dist, min_dist_h, attempts=48, budget=40000):
             good = np.arange(attempts)
         if good.size == 0:
             culprits = owner[far[np.any(bad, axis=(0, 1))]]
-            back = int(culprits.max()) if culprits.size else -1
-            if back < 0:
-                return None
-            t = back
+            # jump back to the latest carbon that placed a clashing atom (atoms
+            # placed with the root belong to no draw: start over from the first)
+            t = max(0, int(culprits.max())) if culprits.size else 0
             continue
         cand = cands[good[0]]
         for s in range(3):
@@ -328,18 +354,21 @@ def water_cluster_k(k: int, seed: int, spacing=2.9, jitter=0.2) -> Molecule:
     return Molecule(np.array(Z, dtype=np.int32), np.array(xyz) * ANG2AU)
 
 
-def serving_stream(rate_hz: float, count: int, seed=5, min_atoms=5, max_atoms=500):
+def serving_stream(rate_hz: float, count: int, seed=5, min_atoms=5, max_atoms=500, max_alkane_n=60):
     """Poisson arrivals of single-point requests with sizes log-uniform in
-    [min_atoms, max_atoms]: half alkanes (n from the size, A = 3n + 2), half
-    water clusters (k = round(A / 3)).  Returns [(arrival_s, Molecule)]."""
+    [min_atoms, max_atoms]: even requests are alkanes (n from the size,
+    A = 3n + 2), odd ones water clusters (k = round(A / 3)).  The alkanes are
+    those of the uneven-batch workload, whose n stops at max_alkane_n (182
+    atoms); an alkane request above that size becomes a water cluster of the
+    same size.  Returns [(arrival_s, Molecule)]."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
     for i in range(count):
         t += rng.exponential(1.0 / rate_hz)
         a = math.exp(rng.uniform(math.log(min_atoms), math.log(max_atoms)))
-        if i % 2 == 0:
-            n = max(1, int(round((a - 2) / 3)))
+        n = max(1, int(round((a - 2) / 3)))
+        if i % 2 == 0 and n <= max_alkane_n:
             mol = random_alkane(seed * 1000003 + i, n=n)
         else:
             k = max(1, int(round(a / 3)))

@@ -105,6 +105,43 @@ def test_octane_geometry_is_ideal():
     c = np.nonzero(o.Z == 6)[0]
     for i in range(7):
         assert abs(d[c[i], c[i + 1]] - 1.54) < 1e-12
-    # all-trans: C1...C4 separation of an anti dihedral
-    anti = np.sqrt(1.54 ** 2 * (3 + 2 * 2 * (1 / 3) + 2 * (1 / 3) ** 2 * 0) )
+    # all-trans: C1...C4 of an anti dihedral are 3.9 A apart (gauche: 2.5-3.2 A)
     assert d[c[0], c[3]] > 3.8
+
+
+def _bond_graph_distances(Z, d):
+    """Graph distances of an alkane from its ideal bond lengths."""
+    n = len(Z)
+    bonded = (np.abs(d - 1.54) < 1e-9) & (Z[:, None] == 6) & (Z[None] == 6)
+    bonded |= (np.abs(d - 1.09) < 1e-9) & (((Z[:, None] == 6) & (Z[None] == 1)) | ((Z[:, None] == 1) & (Z[None] == 6)))
+    G = np.full((n, n), 99)
+    np.fill_diagonal(G, 0)
+    G[bonded] = 1
+    for k in range(n):
+        G = np.minimum(G, G[:, k:k + 1] + G[k:k + 1, :])
+    return G
+
+
+@pytest.mark.parametrize("seed", [3000000, 3000001, 3000002, 3000003])
+def test_random_alkane_rules(seed):
+    """Tree of CnH2n+2 with ideal bonds and angles; non-bonded pairs >= 3 bonds
+    apart respect the C-C 1.8 A and 1.0 A floors; deterministic per seed."""
+    a = workloads.random_alkane(seed)
+    b = workloads.random_alkane(seed)
+    assert np.array_equal(a.Z, b.Z) and np.array_equal(a.xyz, b.xyz)
+    nc = int((a.Z == 6).sum())
+    assert 3 <= nc <= 60 and (a.Z == 1).sum() == 2 * nc + 2
+    x = a.xyz / inputfile.ANG2AU
+    d = np.sqrt(((x[:, None] - x[None]) ** 2).sum(-1))
+    G = _bond_graph_distances(a.Z, d)
+    assert G.max() < 99                                   # connected
+    assert (G == 1).sum() // 2 == a.natoms - 1            # a tree
+    for i in np.nonzero(a.Z == 6)[0]:                     # every carbon has four bonds
+        assert (G[i] == 1).sum() == 4
+    ang13 = d[G == 2]                                     # tetrahedral 1-3 distances
+    assert np.all(np.isin(np.round(ang13, 6), np.round([2 * 1.54 * np.sin(np.arccos(-1 / 3) / 2),
+                                                        np.sqrt(1.54 ** 2 + 1.09 ** 2 + 2 * 1.54 * 1.09 / 3),
+                                                        2 * 1.09 * np.sin(np.arccos(-1 / 3) / 2)], 6)))
+    far = G >= 3
+    cc = far & (a.Z[:, None] == 6) & (a.Z[None] == 6)
+    assert np.all(d[cc] >= 1.8) and np.all(d[far] >= 1.0)
