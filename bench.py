@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=400, help="serving: requests per rate")
     ap.add_argument("--hbm-gb", type=float, default=96.0, help="serving: HBM budget of the server")
     ap.add_argument("--max-basis", type=int, default=1024, help="serving: largest basis accepted")
+    ap.add_argument("--alkanes", type=int, default=4096, help="alkanes: molecules in the uneven batch")
+    ap.add_argument("--repeats", type=int, default=200, help="octane: timed solves")
     return ap.parse_args()
 
 
@@ -387,6 +389,163 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+
+# ---------------------------------------------------------------------------
+# Uneven batch: random alkanes CnH2n+2, n uniform 3..60, PM3, precision ramp
+# ---------------------------------------------------------------------------
+def _gen_alkane(j):
+    from molds_gb300 import workloads as W
+    m = W.random_alkane(3_000_000 + j)
+    return m.Z, m.xyz
+
+
+def _cpu_worker_pm3(args):
+    Z, xyz = args
+    from oracle import oracle as O
+    mol = O.make_molecule("pm3", Z, xyz)
+    try:
+        r = O.scf(mol, O.SCFParams(**SCF))
+        return r.energy, r.iterations, True
+    except O.NotConverged:
+        return None, SCF["max_iter"], False
+
+
+def run_alkanes(args):
+    """All molecules in one device-resident batch; a step = integrals + SCF +
+    energies of all of them.  Mixed precision (FP32 eigen phase, FP64 after the
+    DIIS error drops below 1e-4); each molecule's |dE| and max|dP| against the
+    FP64 GPU path of the same batch."""
+    import numpy as np
+    from molds_gb300.inputfile import Molecule
+    os.environ.update(OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
+    cores = host_cores()
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(cores) as pool:      # before any CUDA call
+        gen = pool.map(_gen_alkane, range(args.alkanes), chunksize=16)
+    t_gen = time.perf_counter() - t0
+    mols = [Molecule(Z, xyz) for Z, xyz in gen]
+    import molds_gb300 as M
+    from molds_gb300 import build
+    build.build()
+    ctx = M.Context(0)
+    nao = np.array([int(sum(4 if z > 1 else 1 for z in m.Z)) for m in mols])
+    steps = args.steps if args.steps != 10 else 2
+    warm = args.warmup if args.warmup != 3 else 1
+    params = M.SCFParams(**SCF, precision=args.precision)
+    batch = M.ResidentBatch("pm3", mols, context=ctx)
+    for _ in range(warm):
+        batch.run(params)
+    clocks = Clocks(0)
+    clocks.start()
+    batch.profile(True)
+    l0 = batch.launch_count()
+    batch.timer(0)
+    for _ in range(steps):
+        batch.run(params)
+    batch.timer(1)
+    ms = batch.timer(2) / steps
+    clk = clocks.stop()
+    launches = (batch.launch_count() - l0) // steps
+    kt = batch.kernel_times()
+    batch.profile(False)
+    res, q = batch.results()
+    ref = M.ResidentBatch("pm3", mols, context=ctx)
+    ref.run(M.SCFParams(**SCF, precision="fp64"))
+    res64, q64 = ref.results()
+    conv = np.array([r["status"] == M.STATUS_CONVERGED for r in res])
+    conv64 = np.array([r["status"] == M.STATUS_CONVERGED for r in res64])
+    both = np.nonzero(conv & conv64)[0]
+    de = np.array([abs(res[i]["energy"] - res64[i]["energy"]) for i in both])
+    rng = np.random.default_rng(0)
+    samp = rng.choice(both, size=min(256, both.size), replace=False) if both.size else []
+    dp = np.array([float(np.max(np.abs(batch.density(i, nao[i]) - ref.density(i, nao[i])))) for i in samp])
+    its = np.array([r["iterations"] for r in res])
+    value = conv.sum() / (ms * 1e-3)
+    # CPU baseline: the oracle on a bounded sample, all host cores
+    cpu = None
+    if not args.no_cpu_baseline:
+        sample = mols[:args.cpu_sample]
+        t1 = time.perf_counter()
+        with mp.get_context("spawn").Pool(cores) as pool:
+            out = pool.map(_cpu_worker_pm3, [(m.Z, m.xyz) for m in sample], chunksize=1)
+        dt = time.perf_counter() - t1
+        ok = sum(1 for o in out if o[2])
+        cpu = {"value": ok / dt, "unit": "converged solves/s", "cores": cores, "kind": "port",
+               "sample": f"first {len(sample)} alkanes, spawn pool of {cores} single-thread processes running the "
+                         f"oracle; {ok} converged in {dt:.1f} s",
+               "max_abs_dE_gpu_vs_cpu_Eh": max((abs(o[0] - res[i]["energy"]) for i, o in enumerate(out)
+                                                if o[2] and res[i]["status"] == M.STATUS_CONVERGED), default=None)}
+    line = {"metric": "converged SCF solves/s, uneven batch of random alkanes with the precision ramp",
+            "value": value, "unit": "solves/s", "n_gpus": 1, "steps": steps, "warmup": warm, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32+fp64" if args.precision == "mixed" else "f64",
+            "data": f"synthetic: {args.alkanes} seeded random alkanes (seed 3e6 + j), generated in {t_gen:.1f} s",
+            "config": {"workload": f"{args.alkanes} alkanes CnH2n+2, n uniform 3..60, PM3, one batch",
+                       "basis_min_median_max": [int(nao.min()), int(np.median(nao)), int(nao.max())],
+                       "precision": args.precision, "scf": SCF,
+                       "l2": f"inputs larger than L2: {batch.device_bytes() / 1e9:.2f} GB resident"},
+            "gpu_launches": launches, "kernels_ms": {k: round(v["ms"] / steps, 3) for k, v in kt.items()},
+            "convergence": {"converged": int(conv.sum()), "fp64_converged": int(conv64.sum()),
+                            "not_converged_both": int((~conv & ~conv64).sum()),
+                            "iterations_median": float(np.median(its)), "iterations_max": int(its.max())},
+            "accuracy": {"molecules_compared": int(both.size),
+                         "max_abs_dE_vs_fp64_gpu_Eh": float(de.max()) if de.size else None,
+                         "p99_abs_dE_Eh": float(np.percentile(de, 99)) if de.size else None,
+                         "max_abs_dP_sample": float(dp.max()) if dp.size else None, "dP_sample": int(dp.size)},
+            "cpu_baseline": cpu, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    batch.close()
+    ref.close()
+
+
+# ---------------------------------------------------------------------------
+# Plain path: one PM3 n-octane solve at a time, FP64
+# ---------------------------------------------------------------------------
+def run_octane(args):
+    import numpy as np
+    import molds_gb300 as M
+    from molds_gb300 import build, workloads as W
+    build.build()
+    ctx = M.Context(0)
+    mol = W.octane()
+    es = M.ElectronicStructure("pm3", M.SCFParams(**SCF, precision="fp64"), context=ctx)
+    for _ in range(5):
+        es.SetMolecule(mol)
+        es.DoSCF()
+    lat = []
+    for _ in range(args.repeats):
+        t0 = time.perf_counter()
+        es.SetMolecule(mol)
+        es.DoSCF()
+        q = es.GetMullikenCharges()
+        lat.append(time.perf_counter() - t0)
+    e = es.GetElectronicEnergy()
+    its = es.GetIterations()
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        om = O.make_molecule("pm3", mol.Z, mol.xyz)
+        O.scf(om, O.SCFParams(**SCF))
+        tl = []
+        for _ in range(20):
+            t0 = time.perf_counter()
+            r = O.scf(om, O.SCFParams(**SCF))
+            tl.append(time.perf_counter() - t0)
+        cpu = {"value": 1.0 / float(np.median(tl)), "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": "20 octane solves, one process (oracle: C integrals/Fock + LAPACK dsyevd/dsysv)",
+               "p50_ms": 1e3 * float(np.median(tl)), "abs_dE_gpu_vs_cpu_Eh": abs(r.energy - e)}
+    line = {"metric": "plain one-molecule PM3 SCF (n-octane), latency", "value": 1.0 / float(np.median(lat)),
+            "unit": "solves/s", "n_gpus": 1, "steps": args.repeats, "warmup": 5,
+            "ms_per_step": 1e3 * float(np.median(lat)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic: ideal all-trans n-octane",
+            "config": {"workload": "C8H18 PM3, 26 atoms, 50 basis functions, FP64", "scf": SCF},
+            "latency_ms": {"p50": 1e3 * percentile(lat, 50), "p99": 1e3 * percentile(lat, 99)},
+            "e2e": {"value": 1.0 / float(np.mean(lat)), "unit": "solves/s",
+                    "call": "SetMolecule + DoSCF + GetMullikenCharges (host arrays)"},
+            "energy_Eh": e, "iterations": its, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
 # ---------------------------------------------------------------------------
 # Serving: Poisson stream of PM3 single-point requests (energy + Mulliken)
 # ---------------------------------------------------------------------------
@@ -485,5 +644,7 @@ if __name__ == "__main__":
         run_serving(a)
     elif a.workload == "water32":
         run_ours(a)
+    elif a.workload == "alkanes":
+        run_alkanes(a)
     else:
-        raise SystemExit(f"workload {a.workload} is not wired into bench.py yet")
+        run_octane(a)

@@ -119,6 +119,9 @@ int nddo_batch_run(nddo_batch* b, const nddo_scf_params* params);
 /* New coordinates for all atoms (same atoms, batch order), bohr. */
 int nddo_batch_set_coordinates(nddo_batch* b, const double* xyz_bohr);
 int nddo_batch_results(nddo_batch* b, nddo_scf_result* results, double* charges);
+/* Density P (which 0) or eigenvector rows C (which 1) of molecule m of the
+ * batch after nddo_batch_run: n_ao(m) x n_ao(m) doubles, row-major. */
+int nddo_batch_get_matrix(nddo_batch* b, int which, int m, double* out);
 size_t nddo_batch_device_bytes(const nddo_batch* b);
 void nddo_batch_destroy(nddo_batch* b);
 /* Per-kernel-class CUDA-event timing on the launching stream: after enabling,

@@ -91,6 +91,7 @@ SIGNATURES = {
     "nddo_batch_set_coordinates": (ctypes.c_int, [ctypes.c_void_p, _DP]),
     "nddo_batch_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScfResultC), _DP]),
     "nddo_batch_device_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "nddo_batch_get_matrix": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _DP]),
     "nddo_batch_destroy": (None, [ctypes.c_void_p]),
     "nddo_batch_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nddo_batch_kernel_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _DP,
@@ -359,6 +360,11 @@ class ResidentBatch:
 
     def device_bytes(self) -> int:
         return int(self.ctx.lib.nddo_batch_device_bytes(self.h))
+
+    def density(self, m: int, nao: int) -> np.ndarray:
+        out = np.zeros((nao, nao))
+        self.ctx.check(self.ctx.lib.nddo_batch_get_matrix(self.h, 0, int(m), _dp(out)))
+        return out
 
     def jacobi_sweeps(self) -> int:
         return int(self.ctx.lib.nddo_batch_jacobi_sweeps(self.h))

@@ -52,6 +52,8 @@ struct BjCtl {
   int done;         // 1 once a sweep found nothing to rotate
   unsigned int offmax_bits;   // max |off-diagonal| seen in the current sweep (float bits)
   int sweeps;
+  float prev_off;   // offmax of the previous sweep
+  int pad[3];
 };
 
 // ---- setup: pad G into A, the basis into V, the stopping scale ----------------------
@@ -86,6 +88,7 @@ __global__ void bj_init_kernel(const DevMol* __restrict__ mols, const int* __res
       ctl[slot].done = 0;
       ctl[slot].offmax_bits = 0u;
       ctl[slot].sweeps = 0;
+      ctl[slot].prev_off = 3.0e38f;
     }
   }
 }
@@ -305,9 +308,15 @@ __global__ void bj_sweep_end_kernel(const DevMol* __restrict__ mols, const int* 
     const int m = list[slot];
     if (st[m].status != kActive || ctl[slot].done) continue;
     const float off = __uint_as_float(ctl[slot].offmax_bits);
+    const float tol = (float)(BjTol<T>::rel * (T)ctl[slot].scale);
     ctl[slot].sweeps += 1;
-    if (off <= (float)(BjTol<T>::rel * (T)ctl[slot].scale)) ctl[slot].done = 1;
+    // done when nothing was above the threshold, or when the off-diagonal
+    // stopped shrinking within a few thresholds of it (the tile updates'
+    // round-off floor; Jacobi's quadratic convergence otherwise divides it by
+    // far more than 2 per sweep)
+    if (off <= tol || (off <= 16.f * tol && off > 0.5f * ctl[slot].prev_off)) ctl[slot].done = 1;
     else ++cnt;
+    ctl[slot].prev_off = off;
     ctl[slot].offmax_bits = 0u;
   }
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);

@@ -176,13 +176,47 @@ int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* Z, cons
     in.theory = theory;
     in.Z.assign(Z, Z + n_atoms);
     in.xyz.assign(xyz, xyz + 3 * (size_t)n_atoms);
-    ctx->mol.reset();
     ctx->has_scf = false;
-    std::unique_ptr<nddo::Batch> b(new nddo::Batch(ctx->engine.get(), {in}, 5));
-    if (ctx->budget && b->device_bytes() > ctx->budget)
-      return fail(ctx, NDDO_ERR_BUDGET, "molecule needs " + std::to_string(b->device_bytes()) + " bytes of HBM, budget is " + std::to_string(ctx->budget));
-    b->integrals();
-    ctx->mol = std::move(b);
+    // The molecule lives in a one-slot pool that is kept between calls: a new
+    // molecule that fits the pool's arenas reuses them (no device allocation
+    // on the repeated SetMolecule/DoSCF path); a larger one grows the pool.
+    int nao = 0;
+    for (int a = 0; a < n_atoms; ++a) {
+      const int e = nddo_element_index(Z[a]);
+      nao += e < 0 ? 1 : nddo_elements[e].n_ao;
+    }
+    int slot = -1;
+    if (ctx->mol) {
+      ctx->mol->release(0);
+      if (nao <= ctx->mol->max_n()) {
+        try {
+          slot = ctx->mol->admit(in);
+        } catch (...) {
+          ctx->mol.reset();   // an invalid molecule leaves no molecule set
+          throw;
+        }
+      }
+    }
+    if (slot < 0) {
+      ctx->mol.reset();
+      nddo::BatchCapacity c;
+      const long long na = n_atoms, np = na * (na - 1) / 2;
+      c.slots = 1;
+      c.atoms = na;
+      c.pairs = np;
+      c.blocks = 100 * np;
+      c.mat = ((long long)nao * nao + 31) / 32 * 32;
+      c.vec = (nao + 31) / 32 * 32;
+      c.max_n = nao;
+      c.ws_slots = 1;
+      std::unique_ptr<nddo::Batch> b(new nddo::Batch(ctx->engine.get(), c, 5, nullptr));
+      if (ctx->budget && b->device_bytes() > ctx->budget)
+        return fail(ctx, NDDO_ERR_BUDGET, "molecule needs " + std::to_string(b->device_bytes()) + " bytes of HBM, budget is " + std::to_string(ctx->budget));
+      slot = b->admit(in);      // throws for an invalid molecule (nothing is kept then)
+      if (slot != 0) return fail(ctx, NDDO_ERR_STATE, "molecule does not fit its own pool");
+      ctx->mol = std::move(b);
+    }
+    ctx->mol->integrals(std::vector<int>{0});
     return (int)NDDO_OK;
   });
 }
@@ -392,6 +426,16 @@ int nddo_batch_results(nddo_batch* h, nddo_scf_result* results, double* charges)
     }
     if (rc != NDDO_OK) h->ctx->err = "SCF did not met convergence criterion for at least one molecule";
     return rc;
+  });
+}
+
+int nddo_batch_get_matrix(nddo_batch* h, int which, int m, double* out) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() -> int {
+    if (!out || m < 0 || m >= h->b->size() || (which != 0 && which != 1))
+      return fail(h->ctx, NDDO_ERR_ARGUMENT, "bad matrix request");
+    h->b->copy_matrix(which == 0 ? 2 : 3, m, out);
+    return (int)NDDO_OK;
   });
 }
 

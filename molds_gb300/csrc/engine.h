@@ -76,6 +76,7 @@ class Batch {
   Batch& operator=(const Batch&) = delete;
 
   int size() const { return (int)h_mols.size(); }
+  int max_n() const { return cap_.max_n; }
   cudaStream_t stream() const { return stream_; }
 
   // pool mode: place a molecule (slot index, or -1 when an arena or the slot

@@ -24,7 +24,7 @@
 
 namespace nddo {
 
-constexpr int kJacobiThreads = 512;
+constexpr int kJacobiThreads = 1024;
 
 __host__ __device__ inline long long jac_pk(int i, int j, int n) {   // packed upper, i <= j
   return (long long)i * (2 * n - i + 1) / 2 + (j - i);
