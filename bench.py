@@ -177,14 +177,20 @@ class Clocks:
 
 # ---------------------------------------------------------------------------
 def dist_setup():
+    """Rank, world size and local rank from the torchrun environment; the
+    process group is NCCL on GPUs (gloo where CUDA is absent: the host-side
+    sharding logic is tested that way on CPU)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
         return rank, world, local, dist
     return rank, world, local, None
 
@@ -193,16 +199,23 @@ def barrier_sync(dist):
     import torch
     if dist is not None:
         dist.barrier()
-    torch.cuda.synchronize()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
 
 
 def max_over_ranks(x, dist):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_throughput(world: int, per_rank_units: int, max_ms_per_step: float) -> float:
+    """Whole-job units/s: every rank's units over the slowest rank's step time."""
+    return world * per_rank_units / (max_ms_per_step * 1e-3)
 
 
 def run_reference(args):
@@ -273,7 +286,7 @@ def run_ours(args):
     res, charges = batch.results()
     ms_max = max_over_ranks(ms, dist)
     per_step_ms = ms_max / args.steps
-    value = world * args.nmol / (per_step_ms * 1e-3)
+    value = aggregate_throughput(world, args.nmol, per_step_ms)
 
     # ---- end to end through the public batched call (host buffers) --------
     e2e_steps = max(1, min(args.steps, 3))
