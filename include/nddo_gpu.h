@@ -50,6 +50,7 @@ typedef struct {
   double diis_end_error;       /* diis_end_error                            */
   int precision;               /* NDDO_PRECISION_FP64 or NDDO_PRECISION_MIXED */
   double fp64_switch_error;    /* mixed: FP64 phase once the DIIS error is below this */
+  int tensor_cores;            /* mixed: FP32-phase GEMMs on the tensor cores (1, default) or CUDA cores (0) */
 } nddo_scf_params;
 
 typedef struct {

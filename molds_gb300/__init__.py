@@ -46,7 +46,7 @@ class ScfParamsC(ctypes.Structure):
                 ("damping_thresh", ctypes.c_double), ("damping_weight", ctypes.c_double),
                 ("diis_num_error_vect", ctypes.c_int), ("diis_start_error", ctypes.c_double),
                 ("diis_end_error", ctypes.c_double), ("precision", ctypes.c_int),
-                ("fp64_switch_error", ctypes.c_double)]
+                ("fp64_switch_error", ctypes.c_double), ("tensor_cores", ctypes.c_int)]
 
 
 class ScfResultC(ctypes.Structure):
@@ -155,6 +155,7 @@ def to_c_params(p: SCFParams) -> ScfParamsC:
     c.diis_end_error = float(p.diis_end_error)
     c.precision = 1 if str(p.precision).lower() == "mixed" else 0
     c.fp64_switch_error = float(p.fp64_switch_error)
+    c.tensor_cores = 1 if getattr(p, "tensor_cores", True) else 0
     return c
 
 

@@ -95,6 +95,7 @@ nddo::ScfSettings to_settings(const nddo_scf_params* p) {
     s.diis_end_error = p->diis_end_error;
     s.precision = p->precision;
     s.switch_error = p->fp64_switch_error;
+    s.tensor_cores = p->tensor_cores;
   }
   return s;
 }
@@ -140,6 +141,7 @@ void nddo_default_params(nddo_scf_params* p) {
   p->diis_end_error = 1e-8;
   p->precision = NDDO_PRECISION_FP64;
   p->fp64_switch_error = 1e-4;
+  p->tensor_cores = 1;
 }
 
 int nddo_create(int device, size_t hbm_budget_bytes, nddo_ctx** out) {

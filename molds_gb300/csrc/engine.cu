@@ -299,9 +299,11 @@ void Batch::allocate(const BatchCapacity& cap) {
   d_charges = dalloc<double>(cap.atoms, &bytes_);
   d_sweeps = dalloc<int>(nm, &bytes_);
   d_count = dalloc<int>(1, &bytes_);
+  d_tc_err = dalloc<int>(1, &bytes_);
   d_active = dalloc<char>(nm, &bytes_);
   cuda_check(cudaMemsetAsync(d_state, 0, nm * sizeof(MolState), stream_), "memset state");
   cuda_check(cudaMemsetAsync(d_sweeps, 0, nm * sizeof(int), stream_), "memset sweeps");
+  cuda_check(cudaMemsetAsync(d_tc_err, 0, sizeof(int), stream_), "memset tc err");
   cuda_check(cudaMemsetAsync(d_H, 0, mat * sizeof(double), stream_), "memset H");
   cuda_check(cudaMemsetAsync(d_P, 0, mat * sizeof(double), stream_), "memset P");
   cuda_check(cudaMemsetAsync(d_hist_dens, 0, std::max(diis_m_, 1) * mat * sizeof(double), stream_), "memset hist");
@@ -416,7 +418,7 @@ Batch::~Batch() {
   if (d_bj_ws) cudaFree(d_bj_ws);
   void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
                   d_hist_dens, d_hist_err, d_G32, d_T32, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
-                  d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs};
+                  d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs, d_tc_err};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
 }
@@ -433,16 +435,22 @@ void Batch::make_jobset(JobSet* js, const std::vector<GemmJob>& jobs_in) {
   while (all[idx] != js) ++idx;
   GemmJob* stage = h_jobs_ + (size_t)idx * job_cap_;
   if ((int)jobs_in.size() > js->cap) throw std::logic_error("GEMM job table overflow");
-  int tiles = 0;
+  int tiles = 0, tc_tiles = 0;
   for (size_t k = 0; k < jobs_in.size(); ++k) {
     GemmJob j = jobs_in[k];
     j.tile0 = tiles;
     j.tiles_n = gemm_tiles_n(j.N);
-    if (j.M > 0 && j.N > 0) tiles += j.sym ? gemm_tiles_sym(j.N) : gemm_tiles(j.M, j.N);
+    j.tc_tile0 = tc_tiles;
+    j.tc_tiles_n = tc_gemm_tiles_n(j.N);
+    if (j.M > 0 && j.N > 0) {
+      tiles += j.sym ? gemm_tiles_sym(j.N) : gemm_tiles(j.M, j.N);
+      tc_tiles += j.sym ? tc_gemm_tiles_sym(j.N) : tc_gemm_tiles(j.M, j.N);
+    }
     stage[k] = j;
   }
   js->n = (int)jobs_in.size();
   js->tiles = tiles;
+  js->tc_tiles = tc_tiles;
   if (jobs_in.empty()) return;
   cuda_check(cudaMemcpyAsync(js->d, stage, jobs_in.size() * sizeof(GemmJob), cudaMemcpyHostToDevice, stream_), "upload jobs");
 }
@@ -764,12 +772,24 @@ void Batch::eigen_step(const ScfSettings& s) {
     launches_ += 5;
     int h = prof_begin(kKOrtho, active_work_estimate(kKOrtho));
     launch_copy_matrices(d_mols, d_list, (int)cur_list_.size(), d_state, d_C, Cn, stream_);
-    launch_gemm(j_ns1_.d, j_ns1_.n, j_ns1_.tiles, d_C, d_C, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
-    launch_gemm(j_ns2_.d, j_ns2_.n, j_ns2_.tiles, d_T32, d_C, Cn, false, false, 0.0f, d_state, 1, -1, stream_);
+    if (s.tensor_cores) {
+      launch_tc_gemm(j_ns1_.d, j_ns1_.n, j_ns1_.tc_tiles, d_C, d_C, d_T32, false, true, d_state, 1, -1, d_tc_err, stream_);
+      launch_tc_gemm(j_ns2_.d, j_ns2_.n, j_ns2_.tc_tiles, d_T32, d_C, Cn, false, false, d_state, 1, -1, d_tc_err, stream_);
+    } else {
+      launch_gemm(j_ns1_.d, j_ns1_.n, j_ns1_.tiles, d_C, d_C, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
+      launch_gemm(j_ns2_.d, j_ns2_.n, j_ns2_.tiles, d_T32, d_C, Cn, false, false, 0.0f, d_state, 1, -1, stream_);
+    }
     prof_end(h);
     h = prof_begin(kKTransform, active_work_estimate(kKTransform));
-    launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, Cn, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
-    launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, Cn, d_T32, d_G32, false, false, 0.0f, d_state, 1, -1, stream_);
+    if (s.tensor_cores) {
+      launch_tc_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tc_tiles, d_F, Cn, d_T32, false, true, d_state, 1, -1, d_tc_err,
+                     stream_);
+      launch_tc_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tc_tiles, Cn, d_T32, d_G32, false, false, d_state, 1, -1,
+                     d_tc_err, stream_);
+    } else {
+      launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, Cn, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
+      launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, Cn, d_T32, d_G32, false, false, 0.0f, d_state, 1, -1, stream_);
+    }
     prof_end(h);
     h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
     run_jacobi(true, s, Cn);
@@ -788,7 +808,10 @@ void Batch::density_step(const ScfSettings& s) {
     // FP32 phase: density from the FP32 eigenvectors
     launches_ += 12;
     int h = prof_begin(kKDensity, active_work_estimate(kKDensity));
-    launch_gemm(j_dens_.d, j_dens_.n, j_dens_.tiles, d_C, d_C, d_P, true, false, 0.0f, d_state, 1, 0, stream_);
+    if (s.tensor_cores)
+      launch_tc_gemm(j_dens_.d, j_dens_.n, j_dens_.tc_tiles, d_C, d_C, d_P, true, false, d_state, 1, 0, d_tc_err, stream_);
+    else
+      launch_gemm(j_dens_.d, j_dens_.n, j_dens_.tiles, d_C, d_C, d_P, true, false, 0.0f, d_state, 1, 0, stream_);
     prof_end(h);
     h = prof_begin(kKRefine, active_work_estimate(kKRefine));
     // FP64 phase: one Newton step on the occupied subspace, then P = 2 Y (Y^T Y)^-1 Y^T
@@ -883,7 +906,10 @@ void Batch::scf(const ScfSettings& s, bool requires_guess) {
     if (count_active(all) == 0) break;
   }
   finish(s, all);
+  int tc_err = 0;
+  cuda_check(cudaMemcpyAsync(&tc_err, d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, stream_), "tc err");
   cuda_check(cudaStreamSynchronize(stream_), "scf");
+  if (tc_err) throw std::runtime_error("tensor-core GEMM: an MMA completion wait ran out");
 }
 
 void Batch::results(std::vector<MolResult>* out) {

@@ -28,6 +28,7 @@ struct ScfSettings {
   double switch_error = 1e-4;   // mixed: FP64 phase once the DIIS error is below this
   int max_sweeps = 30;
   int keep_trace = 1;
+  int tensor_cores = 1;         // mixed: FP32-phase GEMMs on tcgen05 (3xTF32) instead of CUDA cores
 };
 
 // kernel classes timed by the optional per-launch CUDA-event profiler
@@ -179,6 +180,7 @@ class Batch {
   double* d_charges = nullptr;
   int* d_sweeps = nullptr;
   int* d_count = nullptr;
+  int* d_tc_err = nullptr;               // set by a tensor-core GEMM whose MMA wait ran out
   char* d_active = nullptr;
 
   // current molecule list and its GEMM job tables
@@ -188,7 +190,7 @@ class Batch {
   std::vector<int*> bucket_dev_;         // device list of each non-empty bucket of the current list
   void run_jacobi(bool fp32, const ScfSettings& s, const double* Cin);
   std::vector<int> bucket_max_n_;
-  struct JobSet { GemmJob* d = nullptr; int n = 0; int tiles = 0; int cap = 0; };
+  struct JobSet { GemmJob* d = nullptr; int n = 0; int tiles = 0; int tc_tiles = 0; int cap = 0; };
   GemmJob* h_jobs_ = nullptr;             // pinned staging of the job tables
   int* h_lists_ = nullptr;                // pinned staging of the molecule / bucket lists
   int job_cap_ = 0;

@@ -15,11 +15,25 @@ struct GemmJob {
   int tile0;
   double alpha, beta;
   int sym;          // 1: C is symmetric; only tiles on/above the diagonal are computed and mirrored
+  int tc_tiles_n;   // the same job in 128 x 128 tiles (tensor-core kernel)
+  int tc_tile0;
   int pad;
 };
 
 int gemm_tiles(int M, int N);
 int gemm_tiles_sym(int N);
+// tensor-core (tcgen05, 3xTF32) batched GEMM, tc_gemm.cu
+int tc_gemm_tiles(int M, int N);
+int tc_gemm_tiles_n(int N);
+int tc_gemm_tiles_sym(int N);
+void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, float* C, bool ta,
+                    bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
+void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, const double* B, double* C, bool ta,
+                    bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
+void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const float* B, float* C, bool ta,
+                    bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
+void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C, bool ta,
+                    bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
 // block Jacobi (block_jacobi.cu) for bases above the one-CTA Jacobi's limit
 constexpr int kSmallJacobiMaxN = 194;
 size_t block_jacobi_workspace(int max_n, int nslots, int elem, long long* stride, long long* qstride);

@@ -37,6 +37,7 @@ class SCFParams:
     diis_end_error: float = 1e-8
     precision: str = "fp64"          # "fp64" or "mixed" (not a MolDS key)
     fp64_switch_error: float = 1e-4
+    tensor_cores: bool = True        # mixed: FP32-phase GEMMs on tcgen05 (not a MolDS key)
 
 
 @dataclass
