@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=16,
                     help="molecules solved one at a time on the plain FP64 path (0 = skip)")
-    ap.add_argument("--workload", default="water32", choices=["water32", "serving", "alkanes", "octane"],
+    ap.add_argument("--workload", default="water32", choices=["water32", "serving", "alkanes", "octane", "water512"],
                     help="water32: 256 x (H2O)32 AM1 batched (the headline); serving: Poisson stream of PM3 "
                          "requests through the continuous-batching server; alkanes: uneven batch of random "
                          "alkanes with the precision ramp; octane: the plain one-molecule path")
@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--max-basis", type=int, default=1024, help="serving: largest basis accepted")
     ap.add_argument("--alkanes", type=int, default=4096, help="alkanes: molecules in the uneven batch")
     ap.add_argument("--repeats", type=int, default=200, help="octane: timed solves")
+    ap.add_argument("--max-iter", type=int, default=500, help="water512: SCF iteration cap")
     return ap.parse_args()
 
 
@@ -559,6 +560,52 @@ def run_octane(args):
             "energy_Eh": e, "iterations": its, "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
 
+
+# ---------------------------------------------------------------------------
+# Large single molecule: (H2O)512 MNDO, N = 3072
+# ---------------------------------------------------------------------------
+def run_water512(args):
+    """One SCF of a 512-water cluster (8x8x8 jittered lattice, seed 4) under
+    MNDO through the plain ElectronicStructure path (block Jacobi for
+    N = 3072), with the RMS / DIIS-error trace."""
+    import numpy as np
+    import molds_gb300 as M
+    from molds_gb300 import build, workloads as W
+    build.build()
+    ctx = M.Context(0)
+    mol = W.water_cluster(shape=(8, 8, 8), spacing=2.9, jitter=0.2, seed=4)
+    scf = dict(SCF, max_iter=args.max_iter)
+    out = {}
+    clocks = Clocks(0)
+    clocks.start()
+    for prec in ([args.precision] if args.precision == "fp64" else ["mixed"]):
+        es = M.ElectronicStructure("mndo", M.SCFParams(**scf, precision=prec), context=ctx)
+        t0 = time.perf_counter()
+        es.SetMolecule(mol)
+        t1 = time.perf_counter()
+        try:
+            es.DoSCF()
+            status = "converged"
+        except M.SCFNotConverged:
+            status = "not converged"
+        t2 = time.perf_counter()
+        tr = es.GetTrace()
+        its = es.GetIterations()
+        out[prec] = {"status": status, "iterations": its, "set_molecule_s": t1 - t0, "scf_s": t2 - t1,
+                     "s_per_iteration": (t2 - t1) / max(1, its), "energy_Eh": es.GetElectronicEnergy(),
+                     "rms_trace": [float(f"{t[1]:.3e}") for t in tr[:its]],
+                     "diis_error_trace": [float(f"{t[2]:.3e}") for t in tr[:its]]}
+    clk = clocks.stop()
+    first = next(iter(out.values()))
+    line = {"metric": "large single SCF: (H2O)512 MNDO, seconds per SCF iteration", "value": first["s_per_iteration"],
+            "unit": "s/iteration", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * first["scf_s"],
+            "higher_is_better": False, "scaling": "replicas only", "vs_baseline": None,
+            "dtype": "fp32+fp64" if "mixed" in out else "f64",
+            "data": "synthetic: (H2O)512 on a jittered 8x8x8 lattice, seed 4",
+            "config": {"workload": "(H2O)512 MNDO, 1536 atoms, 3072 basis functions, 2048 occupied", "scf": scf},
+            "runs": out, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
 # ---------------------------------------------------------------------------
 # Serving: Poisson stream of PM3 single-point requests (energy + Mulliken)
 # ---------------------------------------------------------------------------
@@ -659,5 +706,7 @@ if __name__ == "__main__":
         run_ours(a)
     elif a.workload == "alkanes":
         run_alkanes(a)
+    elif a.workload == "water512":
+        run_water512(a)
     else:
         run_octane(a)
