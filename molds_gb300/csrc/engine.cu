@@ -529,6 +529,12 @@ void Batch::upload_list(const std::vector<int>& which) {
   }
 }
 
+int Batch::list_max_atoms() const {
+  int mx = 1;
+  for (int m : cur_list_) mx = std::max(mx, h_mols[m].natoms);
+  return mx;
+}
+
 const char* kernel_class_name(int k) {
   static const char* names[kKNumClasses] = {"pair_integrals", "core_hamiltonian", "fock_build", "basis_orthonormalise",
                                             "warm_start_transform", "jacobi_eigensolver", "density", "fp64_refinement",
@@ -840,7 +846,8 @@ void Batch::iterate(const ScfSettings& s, const std::vector<int>& which) {
   const int nl = (int)which.size();
   launches_ += 2;   // fock + diis
   int h = prof_begin(kKFock, active_work_estimate(kKFock));
-  launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, d_blocks, d_H, d_P, d_F, d_Pold, d_state, -1, 1, 1, stream_);
+  launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, list_max_atoms(), d_blocks, d_H, d_P, d_F, d_Pold, d_state, -1,
+                     1, 1, stream_);
   prof_end(h);
   cuda_check(cudaGetLastError(), "fock_kernel");
   eigen_step(s);
@@ -891,7 +898,8 @@ void Batch::finish(const ScfSettings& s, const std::vector<int>& which) {
   const int nl = (int)which.size();
   launches_ += 2;
   int h = prof_begin(kKEnergy, 0.0);
-  launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0, 0, 0, stream_);
+  launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, list_max_atoms(), d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0,
+                     0, 0, stream_);
   launch_energy_kernel(d_atoms, d_mols, d_list, nl, d_P, d_F, d_H, d_state, d_charges, stream_);
   prof_end(h);
   cuda_check(cudaGetLastError(), "finish");

@@ -134,6 +134,7 @@ class Batch {
 
  private:
   void allocate(const BatchCapacity& cap);
+  int list_max_atoms() const;   // largest molecule (atoms) of the current list
   void build_jobs(const std::vector<int>& which);
   void upload_list(const std::vector<int>& which);
   void eigen_step(const ScfSettings& s);

@@ -62,7 +62,7 @@ void launch_hcore_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMo
                          int nlist, const double* blocks, const double* ecore_pair, double* H, MolState* st,
                          cudaStream_t s);
 void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
-                        int nlist, const double* blocks, const double* H, const double* P, double* F,
+                        int nlist, int max_atoms, const double* blocks, const double* H, const double* P, double* F,
                         double* Pold, const MolState* st, int mode_override, int copy_old, int require_active,
                         cudaStream_t s);
 void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* mol_list, int nlist,

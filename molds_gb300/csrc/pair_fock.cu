@@ -419,7 +419,8 @@ fock_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
             const int* __restrict__ mol_list, const double* __restrict__ blocks, const double* __restrict__ H,
             const double* __restrict__ P, double* __restrict__ F, double* __restrict__ Pold,
             const MolState* __restrict__ st, int mode_override, int copy_old, int require_active) {
-  const int m = mol_list[blockIdx.x];
+  // grid: x = groups of atom rows (a warp per atom row), y = molecule
+  const int m = mol_list[blockIdx.y];
   const DevMol mol = mols[m];
   const MolState s = st[m];
   if (require_active && s.status != kActive) return;
@@ -431,15 +432,16 @@ fock_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs
   const double* Hm = H + mol.mat0;
   double* Fm = F + mol.mat0;
   const long long n2 = ld * ld;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, tstep = (long long)gridDim.x * blockDim.x;
   if (copy_old) {
     double* Po = Pold + mol.mat0;
-    for (long long i = threadIdx.x; i < n2; i += blockDim.x) Po[i] = Pm[i];
+    for (long long i = t0; i < n2; i += tstep) Po[i] = Pm[i];
   }
   if (mode == 2) {
-    for (long long i = threadIdx.x; i < n2; i += blockDim.x) Fm[i] = Hm[i];
+    for (long long i = t0; i < n2; i += tstep) Fm[i] = Hm[i];
     return;
   }
-  for (int ia = warp; ia < mol.natoms; ia += nwarps) {
+  for (int ia = blockIdx.x * nwarps + warp; ia < mol.natoms; ia += gridDim.x * nwarps) {
     const DevAtom A = atoms[mol.atom0 + ia];
     const nddo_atom_params& pa = c_params[A.pidx];
     const int nA = A.nao, dA = nA == 4 ? 10 : 1;
@@ -571,12 +573,14 @@ void launch_hcore_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMo
 }
 
 void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
-                        int nlist, const double* blocks, const double* H, const double* P, double* F,
+                        int nlist, int max_atoms, const double* blocks, const double* H, const double* P, double* F,
                         double* Pold, const MolState* st, int mode_override, int copy_old, int require_active,
                         cudaStream_t s) {
   if (nlist <= 0) return;
-  fock_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, pairs, mols, mol_list, blocks, H, P, F, Pold, st,
-                                             mode_override, copy_old, require_active);
+  const int rows = kFockThreads / 32;
+  dim3 grid((max_atoms + rows - 1) / rows, nlist);
+  fock_kernel<<<grid, kFockThreads, 0, s>>>(atoms, pairs, mols, mol_list, blocks, H, P, F, Pold, st, mode_override,
+                                            copy_old, require_active);
 }
 
 // E = 1/2 sum P (F + H) + E_core (Cndo2::CalcElecSCFEnergy, src/cndo/Cndo2.cpp:1324-1416),
