@@ -57,9 +57,9 @@ struct BjCtl {
 };
 
 // ---- setup: pad G into A, the basis into V, the stopping scale ----------------------
-template <typename T>
+template <typename T, typename TCin>
 __global__ void bj_init_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list,
-                               const MolState* __restrict__ st, const T* __restrict__ G, const double* __restrict__ Cin,
+                               const MolState* __restrict__ st, const T* __restrict__ G, const TCin* __restrict__ Cin,
                                T* __restrict__ Aws, T* __restrict__ Vws, long long stride, BjCtl* __restrict__ ctl) {
   const int slot = blockIdx.y;
   const int m = list[slot];
@@ -380,9 +380,9 @@ size_t block_jacobi_workspace(int max_n, int nslots, int elem, long long* stride
   return mats + ctl + ord + 1024;
 }
 
-template <typename T>
+template <typename T, typename TCin>
 int launch_block_jacobi_impl(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
-                             const T* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
+                             const T* G, const TCin* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
                              int* sweeps_out, int* h_pending, cudaStream_t s) {
   if (nlist <= 0) return 0;
   long long stride, qstride;
@@ -400,7 +400,7 @@ int launch_block_jacobi_impl(const DevMol* mols, const int* list, int nlist, int
   cudaFuncSetAttribute(bj_sub_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(bj_rows_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(bj_cols_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  bj_init_kernel<T><<<dim3(32, nlist), kBjThreads, 0, s>>>(mols, list, st, G, Cin, A, V, stride, ctl);
+  bj_init_kernel<T, TCin><<<dim3(32, nlist), kBjThreads, 0, s>>>(mols, list, st, G, Cin, A, V, stride, ctl);
   int launches = 1, sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     for (int r = 0; r < nb - 1; ++r) {
@@ -426,14 +426,21 @@ int launch_block_jacobi_impl(const DevMol* mols, const int* list, int nlist, int
 int launch_block_jacobi_f32(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                             const float* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
                             int* sweeps_out, int* h_pending, cudaStream_t s) {
-  return launch_block_jacobi_impl<float>(mols, list, nlist, max_n, st, G, Cin, Cout, eps, ws, max_sweeps, sweeps_out,
+  return launch_block_jacobi_impl<float, double>(mols, list, nlist, max_n, st, G, Cin, Cout, eps, ws, max_sweeps, sweeps_out,
                                          h_pending, s);
+}
+
+int launch_block_jacobi_f32(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
+                            const float* G, const float* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
+                            int* sweeps_out, int* h_pending, cudaStream_t s) {
+  return launch_block_jacobi_impl<float, float>(mols, list, nlist, max_n, st, G, Cin, Cout, eps, ws, max_sweeps,
+                                                sweeps_out, h_pending, s);
 }
 
 int launch_block_jacobi_f64(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                             const double* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
                             int* sweeps_out, int* h_pending, cudaStream_t s) {
-  return launch_block_jacobi_impl<double>(mols, list, nlist, max_n, st, G, Cin, Cout, eps, ws, max_sweeps, sweeps_out,
+  return launch_block_jacobi_impl<double, double>(mols, list, nlist, max_n, st, G, Cin, Cout, eps, ws, max_sweeps, sweeps_out,
                                           h_pending, s);
 }
 

@@ -194,8 +194,9 @@ inline long long round32(long long x) { return (x + 31) / 32 * 32; }
 }  // namespace
 
 size_t Batch::bytes_per_mat_element(int diis_m) {
-  // H F P P_old C G64 T64 + six refinement buffers (FP64), G32 T32 (FP32), DIIS history
-  return 13 * sizeof(double) + 2 * sizeof(float) + 2 * (size_t)std::max(diis_m, 1) * sizeof(double);
+  // H F P P_old C G64 T64 + six refinement buffers (FP64), G32 T32 + three tensor-core
+  // shadows (FP32), DIIS history
+  return 13 * sizeof(double) + 5 * sizeof(float) + 2 * (size_t)std::max(diis_m, 1) * sizeof(double);
 }
 
 Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
@@ -292,6 +293,9 @@ void Batch::allocate(const BatchCapacity& cap) {
   d_hist_err = dalloc<double>((size_t)std::max(diis_m_, 1) * mat, &bytes_);
   d_G32 = dalloc<float>(mat, &bytes_);
   d_T32 = dalloc<float>(mat, &bytes_);
+  d_Cf = dalloc<float>(mat, &bytes_);
+  d_Cnf = dalloc<float>(mat, &bytes_);
+  d_Ff = dalloc<float>(mat, &bytes_);
   d_G64 = dalloc<double>(mat, &bytes_);
   d_T64 = dalloc<double>(mat, &bytes_);
   for (int i = 0; i < 6; ++i) d_S[i] = dalloc<double>(mat, &bytes_);
@@ -417,7 +421,7 @@ Batch::~Batch() {
   if (h_bj_pending) cudaFreeHost(h_bj_pending);
   if (d_bj_ws) cudaFree(d_bj_ws);
   void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
-                  d_hist_dens, d_hist_err, d_G32, d_T32, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
+                  d_hist_dens, d_hist_err, d_G32, d_T32, d_Cf, d_Cnf, d_Ff, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
                   d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs, d_tc_err};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
@@ -729,7 +733,7 @@ void Batch::begin(const ScfSettings& s, const std::vector<int>& which, bool requ
 
 // One Jacobi launch per size bucket; buckets whose molecules need a
 // global-memory workspace are split into launches of at most ws_slots CTAs.
-void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin) {
+void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const float* Cin32) {
   for (size_t b = 0; b < buckets_.size(); ++b) {
     bool ag, vg;
     const int nb = (int)buckets_[b].size();
@@ -737,7 +741,11 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin) {
       // block Jacobi, many CTAs per molecule, at most ws_slots molecules per call
       for (int k0 = 0; k0 < nb; k0 += cap_.ws_slots) {
         const int cnt = std::min(cap_.ws_slots, nb - k0);
-        if (fp32)
+        if (fp32 && Cin32)
+          launches_ += launch_block_jacobi_f32(d_mols, bucket_dev_[b] + k0, cnt, bucket_max_n_[b], d_state, d_G32,
+                                               Cin32, d_C, d_eps, d_bj_ws, s.max_sweeps, d_sweeps, h_bj_pending,
+                                               stream_);
+        else if (fp32)
           launches_ += launch_block_jacobi_f32(d_mols, bucket_dev_[b] + k0, cnt, bucket_max_n_[b], d_state, d_G32, Cin,
                                                d_C, d_eps, d_bj_ws, s.max_sweeps, d_sweeps, h_bj_pending, stream_);
         else
@@ -750,7 +758,10 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin) {
     for (int k0 = 0; k0 < nb; k0 += chunk) {
       const int cnt = std::min(chunk, nb - k0);
       launches_ += 1;
-      if (fp32)
+      if (fp32 && Cin32)
+        launch_jacobi_f32(d_mols, bucket_dev_[b] + k0, cnt, bucket_max_n_[b], d_state, 1, d_G32, Cin32, 1, d_C, d_eps,
+                          d_jA32, d_jV32, jws_stride_, s.max_sweeps, d_sweeps, stream_);
+      else if (fp32)
         launch_jacobi_f32(d_mols, bucket_dev_[b] + k0, cnt, bucket_max_n_[b], d_state, 1, d_G32, Cin, 1, d_C, d_eps,
                           d_jA32, d_jV32, jws_stride_, s.max_sweeps, d_sweeps, stream_);
       else
@@ -774,32 +785,43 @@ void Batch::eigen_step(const ScfSettings& s) {
     // The FP32 rotations of each iteration erode the orthonormality of the
     // warm-start basis; one Newton-Schulz step C <- 1.5 C - 0.5 (C C^T) C
     // (FP32 accumulation) restores it to FP32 round-off before it is reused.
-    double* Cn = d_T64;
-    launches_ += 5;
-    int h = prof_begin(kKOrtho, active_work_estimate(kKOrtho));
-    launch_copy_matrices(d_mols, d_list, (int)cur_list_.size(), d_state, d_C, Cn, stream_);
     if (s.tensor_cores) {
-      launch_tc_gemm(j_ns1_.d, j_ns1_.n, j_ns1_.tc_tiles, d_C, d_C, d_T32, false, true, d_state, 1, -1, d_tc_err, stream_);
-      launch_tc_gemm(j_ns2_.d, j_ns2_.n, j_ns2_.tc_tiles, d_T32, d_C, Cn, false, false, d_state, 1, -1, d_tc_err, stream_);
+      // tensor-core chain on FP32 shadows: Cf = Cnf = float(C), Ff = float(F);
+      // M = Cf Cf^T, Cnf = 1.5 Cnf - 0.5 M Cf, T = Ff Cnf^T, G = Cnf T
+      launches_ += 6;
+      int h = prof_begin(kKOrtho, active_work_estimate(kKOrtho));
+      launch_tc_shadows(d_mols, d_list, (int)cur_list_.size(), d_state, d_C, d_F, d_Cf, d_Cnf, d_Ff, stream_);
+      launch_tc_gemm(j_ns1_.d, j_ns1_.n, j_ns1_.tc_tiles, d_Cf, d_Cf, d_T32, false, true, d_state, 1, -1, d_tc_err,
+                     stream_);
+      launch_tc_gemm(j_ns2_.d, j_ns2_.n, j_ns2_.tc_tiles, d_T32, d_Cf, d_Cnf, false, false, d_state, 1, -1, d_tc_err,
+                     stream_);
+      prof_end(h);
+      h = prof_begin(kKTransform, active_work_estimate(kKTransform));
+      launch_tc_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tc_tiles, d_Ff, d_Cnf, d_T32, false, true, d_state, 1, -1,
+                     d_tc_err, stream_);
+      launch_tc_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tc_tiles, d_Cnf, d_T32, d_G32, false, false, d_state, 1, -1,
+                     d_tc_err, stream_);
+      prof_end(h);
+      h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
+      run_jacobi(true, s, nullptr, d_Cnf);
+      prof_end(h);
     } else {
+      double* Cn = d_T64;
+      launches_ += 5;
+      int h = prof_begin(kKOrtho, active_work_estimate(kKOrtho));
+      launch_copy_matrices(d_mols, d_list, (int)cur_list_.size(), d_state, d_C, Cn, stream_);
       launch_gemm(j_ns1_.d, j_ns1_.n, j_ns1_.tiles, d_C, d_C, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
       launch_gemm(j_ns2_.d, j_ns2_.n, j_ns2_.tiles, d_T32, d_C, Cn, false, false, 0.0f, d_state, 1, -1, stream_);
-    }
-    prof_end(h);
-    h = prof_begin(kKTransform, active_work_estimate(kKTransform));
-    if (s.tensor_cores) {
-      launch_tc_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tc_tiles, d_F, Cn, d_T32, false, true, d_state, 1, -1, d_tc_err,
-                     stream_);
-      launch_tc_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tc_tiles, Cn, d_T32, d_G32, false, false, d_state, 1, -1,
-                     d_tc_err, stream_);
-    } else {
+      prof_end(h);
+      h = prof_begin(kKTransform, active_work_estimate(kKTransform));
       launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, Cn, d_T32, false, true, 0.0f, d_state, 1, -1, stream_);
-      launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, Cn, d_T32, d_G32, false, false, 0.0f, d_state, 1, -1, stream_);
+      launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, Cn, d_T32, d_G32, false, false, 0.0f, d_state, 1, -1,
+                  stream_);
+      prof_end(h);
+      h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
+      run_jacobi(true, s, Cn);
+      prof_end(h);
     }
-    prof_end(h);
-    h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
-    run_jacobi(true, s, Cn);
-    prof_end(h);
   }
   cuda_check(cudaGetLastError(), "eigen step");
 }

@@ -169,6 +169,7 @@ class Batch {
   double *d_H = nullptr, *d_F = nullptr, *d_P = nullptr, *d_Pold = nullptr, *d_C = nullptr, *d_eps = nullptr;
   double *d_hist_dens = nullptr, *d_hist_err = nullptr;
   float *d_G32 = nullptr, *d_T32 = nullptr;
+  float *d_Cf = nullptr, *d_Cnf = nullptr, *d_Ff = nullptr;   // FP32 shadows of the tensor-core chain
   double *d_G64 = nullptr, *d_T64 = nullptr;
   double* d_S[6] = {};
   float *d_jA32 = nullptr, *d_jV32 = nullptr;
@@ -189,7 +190,7 @@ class Batch {
   std::vector<std::vector<int>> buckets_;      // jacobi size buckets (indices into cur_list_)
   std::vector<int*> d_bucket_lists_;     // persistent, one per size bucket, `slots` entries each
   std::vector<int*> bucket_dev_;         // device list of each non-empty bucket of the current list
-  void run_jacobi(bool fp32, const ScfSettings& s, const double* Cin);
+  void run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const float* Cin32 = nullptr);
   std::vector<int> bucket_max_n_;
   struct JobSet { GemmJob* d = nullptr; int n = 0; int tiles = 0; int tc_tiles = 0; int cap = 0; };
   GemmJob* h_jobs_ = nullptr;             // pinned staging of the job tables

@@ -76,10 +76,10 @@ size_t jacobi_smem_bytes(int n, int elem, bool v_in_smem, bool a_in_smem) {
   return (size_t)((b + 15) & ~15LL);
 }
 
-template <typename T>
+template <typename T, typename TCin>
 __global__ void __launch_bounds__(kJacobiThreads)
 jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list, const MolState* __restrict__ st,
-              int require_active, const T* __restrict__ G, const double* __restrict__ Cin, int use_basis,
+              int require_active, const T* __restrict__ G, const TCin* __restrict__ Cin, int use_basis,
               double* __restrict__ Cout, double* __restrict__ eps_out, T* __restrict__ Aws, T* __restrict__ Vws,
               long long ws_stride, int a_in_smem, int v_in_smem, int max_sweeps, int* __restrict__ sweeps_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -109,7 +109,7 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
 
   const int tid = threadIdx.x, nth = blockDim.x;
   const T* Gm = G + mol.mat0;
-  const double* Cm = Cin + mol.mat0;
+  const TCin* Cm = Cin + mol.mat0;
 
   // ---- load ------------------------------------------------------------------
   for (long long e = tid; e < npk; e += nth) {
@@ -284,9 +284,9 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
   if (tid == 0 && sweeps_out) sweeps_out[m] += sweep;   // cumulative over the SCF
 }
 
-template <typename T>
+template <typename T, typename TCin>
 void launch_jacobi_impl(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
-                        int require_active, const T* G, const double* Cin, int use_basis, double* Cout,
+                        int require_active, const T* G, const TCin* Cin, int use_basis, double* Cout,
                         double* eps, T* Aws, T* Vws, long long ws_stride, int max_sweeps, int* sweeps_out,
                         cudaStream_t s) {
   if (nlist <= 0) return;
@@ -300,8 +300,8 @@ void launch_jacobi_impl(const DevMol* mols, const int* mol_list, int nlist, int 
   const size_t bytes = jacobi_smem_bytes(max_n, elem, v_sm, a_sm);
   // the opt-in bound is set to the device limit (the same value on every call),
   // so launches from several host threads never race on it
-  cudaFuncSetAttribute(jacobi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
-  jacobi_kernel<T><<<nlist, kJacobiThreads, bytes, s>>>(mols, mol_list, st, require_active, G, Cin, use_basis,
+  cudaFuncSetAttribute(jacobi_kernel<T, TCin>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
+  jacobi_kernel<T, TCin><<<nlist, kJacobiThreads, bytes, s>>>(mols, mol_list, st, require_active, G, Cin, use_basis,
                                                         Cout, eps, Aws, Vws, ws_stride, a_sm ? 1 : 0,
                                                         v_sm ? 1 : 0, max_sweeps, sweeps_out);
 }
@@ -310,15 +310,23 @@ void launch_jacobi_f32(const DevMol* mols, const int* mol_list, int nlist, int m
                        int require_active, const float* G, const double* Cin, int use_basis, double* Cout,
                        double* eps, float* Aws, float* Vws, long long ws_stride, int max_sweeps,
                        int* sweeps_out, cudaStream_t s) {
-  launch_jacobi_impl<float>(mols, mol_list, nlist, max_n, st, require_active, G, Cin, use_basis, Cout, eps, Aws,
+  launch_jacobi_impl<float, double>(mols, mol_list, nlist, max_n, st, require_active, G, Cin, use_basis, Cout, eps, Aws,
                             Vws, ws_stride, max_sweeps, sweeps_out, s);
+}
+
+void launch_jacobi_f32(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                       int require_active, const float* G, const float* Cin, int use_basis, double* Cout,
+                       double* eps, float* Aws, float* Vws, long long ws_stride, int max_sweeps,
+                       int* sweeps_out, cudaStream_t s) {
+  launch_jacobi_impl<float, float>(mols, mol_list, nlist, max_n, st, require_active, G, Cin, use_basis, Cout, eps,
+                                   Aws, Vws, ws_stride, max_sweeps, sweeps_out, s);
 }
 
 void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
                        int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
                        double* eps, double* Aws, double* Vws, long long ws_stride, int max_sweeps,
                        int* sweeps_out, cudaStream_t s) {
-  launch_jacobi_impl<double>(mols, mol_list, nlist, max_n, st, require_active, G, Cin, use_basis, Cout, eps, Aws,
+  launch_jacobi_impl<double, double>(mols, mol_list, nlist, max_n, st, require_active, G, Cin, use_basis, Cout, eps, Aws,
                              Vws, ws_stride, max_sweeps, sweeps_out, s);
 }
 

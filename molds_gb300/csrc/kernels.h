@@ -32,6 +32,8 @@ void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, 
                     bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
 void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const float* B, float* C, bool ta,
                     bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
+void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, const float* B, float* C, bool ta,
+                    bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
 void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C, bool ta,
                     bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
 // block Jacobi (block_jacobi.cu) for bases above the one-CTA Jacobi's limit
@@ -40,9 +42,15 @@ size_t block_jacobi_workspace(int max_n, int nslots, int elem, long long* stride
 int launch_block_jacobi_f32(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                             const float* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
                             int* sweeps_out, int* h_pending, cudaStream_t s);
+int launch_block_jacobi_f32(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
+                            const float* G, const float* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
+                            int* sweeps_out, int* h_pending, cudaStream_t s);
 int launch_block_jacobi_f64(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                             const double* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
                             int* sweeps_out, int* h_pending, cudaStream_t s);
+// FP32 shadows for the tensor-core chain: Cf = Cf2 = float(C), Ff = float(F)
+void launch_tc_shadows(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, const double* C,
+                       const double* F, float* Cf, float* Cf2, float* Ff, cudaStream_t s);
 void launch_copy_matrices(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, const double* src,
                           double* dst, cudaStream_t s);
 int gemm_tiles_n(int N);
@@ -73,6 +81,10 @@ void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* m
 bool jacobi_needs_workspace(int max_n, int elem, bool* a_global, bool* v_global);
 void launch_jacobi_f32(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
                        int require_active, const float* G, const double* Cin, int use_basis, double* Cout,
+                       double* eps, float* Aws, float* Vws, long long ws_stride, int max_sweeps,
+                       int* sweeps_out, cudaStream_t s);
+void launch_jacobi_f32(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                       int require_active, const float* G, const float* Cin, int use_basis, double* Cout,
                        double* eps, float* Aws, float* Vws, long long ws_stride, int max_sweeps,
                        int* sweeps_out, cudaStream_t s);
 void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,

@@ -415,6 +415,31 @@ void launch_copy_occ_rows(const DevMol* mols, const int* mol_list, int nlist, co
   copy_rows_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, src, dst);
 }
 
+// FP32 shadows of the basis C (twice: operand and Newton-Schulz output) and of
+// F for the tensor-core chain of the FP32 phase: one conversion per element
+// and iteration instead of one per tile that loads it
+__global__ void tc_shadows_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+                                  const MolState* __restrict__ st, const double* __restrict__ C,
+                                  const double* __restrict__ F, float* __restrict__ Cf, float* __restrict__ Cf2,
+                                  float* __restrict__ Ff) {
+  const int m = mol_list[blockIdx.y];
+  if (st[m].status != kActive) return;
+  const DevMol mol = mols[m];
+  const long long cnt = (long long)mol.nao * mol.nao;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x) {
+    const float c = (float)C[mol.mat0 + e];
+    Cf[mol.mat0 + e] = c;
+    Cf2[mol.mat0 + e] = c;
+    Ff[mol.mat0 + e] = (float)F[mol.mat0 + e];
+  }
+}
+
+void launch_tc_shadows(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, const double* C,
+                       const double* F, float* Cf, float* Cf2, float* Ff, cudaStream_t s) {
+  if (nlist <= 0) return;
+  tc_shadows_kernel<<<dim3(16, nlist), 256, 0, s>>>(mols, mol_list, st, C, F, Cf, Cf2, Ff);
+}
+
 // copy each listed active molecule's N x N block (src -> dst, same offsets)
 __global__ void copy_matrices_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
                                      const MolState* __restrict__ st, const double* __restrict__ src,

@@ -203,14 +203,19 @@ tc_gemm_kernel(const GemmJob* __restrict__ jobs, int njobs, const TA* __restrict
       const int i = e / kTcT, j = e % kTcT;
       const int gi = row0 + i, gj = col0 + j;
       if (gi < job.M && gj < job.N) {
-        const double a = job.alpha * (double)S[i * kTcOutLd + j];
         TC* c = Cj + (long long)gi * job.ldc + gj;
-        *c = (TC)(job.beta != 0.0 ? a + job.beta * (double)(*c) : a);
+        if (sizeof(TC) == 4) {            // FP32 output: FP32 arithmetic (GB300's FP64 pipe is 1/64 rate)
+          const float a = (float)job.alpha * S[i * kTcOutLd + j];
+          *c = (TC)(job.beta != 0.0 ? a + (float)job.beta * (float)(*c) : a);
+        } else {
+          const double a = job.alpha * (double)S[i * kTcOutLd + j];
+          *c = (TC)(job.beta != 0.0 ? a + job.beta * (double)(*c) : a);
+        }
       }
       if (job.sym && tm != tn) {
         // mirror tile (beta is zero for symmetric jobs): C[col0 + i][row0 + j] = acc[j][i]
         const int mi = col0 + i, mj = row0 + j;
-        if (mi < job.N && mj < job.M) Cj[(long long)mi * job.ldc + mj] = (TC)(job.alpha * (double)S[j * kTcOutLd + i]);
+        if (mi < job.N && mj < job.M) Cj[(long long)mi * job.ldc + mj] = (TC)((float)job.alpha * S[j * kTcOutLd + i]);
       }
     }
   }
@@ -243,6 +248,7 @@ static void tc_launch(const GemmJob* jobs, int njobs, int ntiles, const TA* A, c
     else if (!ta && tb) tc_launch<TA, TB, TC, false, true>(jobs, njobs, ntiles, A, B, C, st, require_active, require_phase, err, s); \
     else tc_launch<TA, TB, TC, true, true>(jobs, njobs, ntiles, A, B, C, st, require_active, require_phase, err, s); \
   }
+TC_LAUNCH(float, float, float)
 TC_LAUNCH(double, double, float)
 TC_LAUNCH(float, double, double)
 TC_LAUNCH(double, float, float)
