@@ -486,7 +486,7 @@ void Batch::build_jobs(const std::vector<int>& which) {
       yt.push_back(job(b, b + (long long)o * n, b, o, n, v, o, n, n, m, 1.0, 1.0));  // Yt = C_o + K^T C_v (A transposed)
       mm.push_back(job(b, b, b, o, o, n, n, n, o, m, 1.0, 0.0, 1));         // M = Yt Yt^T   (B transposed, symmetric)
       d2.push_back(job(b, b, b, o, o, o, o, o, o, m));                      // D2 = D D
-      z.push_back(job(b, b, b, o, n, o, o, n, n, m));                       // Z = Minv Yt
+      z.push_back(job(b, b, b, o, n, o, o, n, n, m, -1.0, 1.0));            // Z = Yt - D Yt
       pp.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0, 0.0, 1));         // P = 2 Yt^T Z  (A transposed, symmetric)
     }
   }
@@ -611,7 +611,7 @@ double Batch::active_work_estimate(int cls) const {
       case kKTransform: w += 4.0 * n * n * n; break;
       case kKOrtho: w += 4.0 * n * n * n; break;
       case kKDensity: w += 2.0 * n * n * o; break;
-      case kKRefine: w += 2 * n * n * o + 6 * n * v * o + 2 * n * o * o + 2 * o * o * n + 2 * n * n * o; break;
+      case kKRefine: w += 2 * n * n * o + 4 * n * v * o + 2 * n * o * o + 2 * n * n * o; break;   // FP64 products
       case kKDiis: w += 8.0 * n * n * (2.0 * diis_m_ + 3.0); break;
       case kKFock: {
         double blk = 0.0;
@@ -849,14 +849,18 @@ void Batch::density_step(const ScfSettings& s) {
     launch_gemm(j_kt_.d, j_kt_.n, j_kt_.tiles, d_C, W, K, false, false, 0.0, d_state, 1, 1, stream_);
     launch_gemm(j_ov_.d, j_ov_.n, j_ov_.tiles, d_C, d_C, D2, false, true, 0.0, d_state, 1, 1, stream_);
     launch_newton_scale(d_mols, d_list, nl, d_state, 1, K, D2, d_eps, stream_);
+    // Yt = C_o + K^T C_v: K is ~1e-7, so its product needs only FP32
+    // accumulation (error ~1e-14 absolute); the sum is formed in FP64
     launch_copy_occ_rows(d_mols, d_list, nl, d_state, 1, d_C, Yt, stream_);
-    launch_gemm(j_yt_.d, j_yt_.n, j_yt_.tiles, K, d_C, Yt, true, false, 0.0, d_state, 1, 1, stream_);
+    launch_gemm(j_yt_.d, j_yt_.n, j_yt_.tiles, K, d_C, Yt, true, false, 0.0f, d_state, 1, 1, stream_);
     launch_gemm(j_m_.d, j_m_.n, j_m_.tiles, Yt, Yt, Mm, false, true, 0.0, d_state, 1, 1, stream_);
     // (Y^T Y)^-1 = I - D + O(D^2) with D = Y^T Y - I: D is at the FP32 round-off
-    // of the orthonormalised basis (~1e-7), so the second-order term is ~1e-14
+    // of the orthonormalised basis (~1e-7), so the second-order term is ~1e-14;
+    // Z = (I - D) Yt = Yt - D Yt, where D Yt (~1e-7) again needs only FP32
+    // accumulation
     launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, D2, 0, stream_);
-    launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, nullptr, 1, stream_);
-    launch_gemm(j_z_.d, j_z_.n, j_z_.tiles, Mm, Yt, Z, false, false, 0.0, d_state, 1, 1, stream_);
+    launch_copy_occ_rows(d_mols, d_list, nl, d_state, 1, Yt, Z, stream_);
+    launch_gemm(j_z_.d, j_z_.n, j_z_.tiles, Mm, Yt, Z, false, false, 0.0f, d_state, 1, 1, stream_);
     launch_gemm(j_p_.d, j_p_.n, j_p_.tiles, Yt, Z, d_P, true, false, 0.0, d_state, 1, 1, stream_);
     prof_end(h);
   }

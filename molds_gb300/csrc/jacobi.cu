@@ -301,7 +301,10 @@ void launch_jacobi_impl(const DevMol* mols, const int* mol_list, int nlist, int 
   // the opt-in bound is set to the device limit (the same value on every call),
   // so launches from several host threads never race on it
   cudaFuncSetAttribute(jacobi_kernel<T, TCin>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
-  jacobi_kernel<T, TCin><<<nlist, kJacobiThreads, bytes, s>>>(mols, mol_list, st, require_active, G, Cin, use_basis,
+  // block size from the bucket's basis: the per-round barriers cost more with
+  // more warps, and a small matrix has too little work per round for 32 warps
+  const int threads = max_n <= 64 ? 256 : (max_n <= 128 ? 512 : kJacobiThreads);
+  jacobi_kernel<T, TCin><<<nlist, threads, bytes, s>>>(mols, mol_list, st, require_active, G, Cin, use_basis,
                                                         Cout, eps, Aws, Vws, ws_stride, a_sm ? 1 : 0,
                                                         v_sm ? 1 : 0, max_sweeps, sweeps_out);
 }
