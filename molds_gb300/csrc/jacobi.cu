@@ -160,6 +160,17 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
 
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
+    // A sweep that would rotate nothing is replaced by one parallel scan of
+    // every off-diagonal element: when all are at the threshold or below, the
+    // matrix is already diagonal to the accuracy the sweep would certify.
+    if (sweep > 0) {
+      T m = 0;
+      for (int i = tid; i < n; i += nth) {
+        const int oi = rowoff[i];
+        for (int j = i + 1; j < n; ++j) { const T a = fabs(A[oi + (j - i)]); m = a > m ? a : m; }
+      }
+      if (!__syncthreads_or(m > thresh)) break;
+    }
     T offmax = 0;
     for (int r = 0; r < np - 1; ++r) {
       // pairs and rotations of this round; rotations below the stopping
