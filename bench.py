@@ -264,13 +264,14 @@ def run_ours(args):
     params = M.SCFParams(**SCF, precision=args.precision)
     batch = M.ResidentBatch("am1", mols, context=ctx)
 
+    batch.profile(True)            # the per-class event pool is created during the warm-up
     for _ in range(args.warmup):
         batch.run(params)
     res_w, q_w = batch.results()
 
     # ---- timed region: K steps on device-resident inputs ------------------
     clocks = Clocks(local)
-    batch.profile(True)
+    batch.profile(True)            # resets the accumulated times, keeps the event pool
     l0 = batch.launch_count()
     barrier_sync(dist)
     clocks.start()
@@ -447,6 +448,7 @@ def run_alkanes(args):
     warm = args.warmup if args.warmup != 3 else 1
     params = M.SCFParams(**SCF, precision=args.precision)
     batch = M.ResidentBatch("pm3", mols, context=ctx)
+    batch.profile(True)
     for _ in range(warm):
         batch.run(params)
     clocks = Clocks(0)

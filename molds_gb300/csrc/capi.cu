@@ -13,13 +13,8 @@
 
 struct nddo_batch {
   nddo_ctx* ctx;
-  std::unique_ptr<nddo::Batch> b;
+  std::unique_ptr<nddo::GroupedBatch> b;
   std::vector<int> n_atoms;
-  cudaEvent_t t0 = nullptr, t1 = nullptr;
-  ~nddo_batch() {
-    if (t0) cudaEventDestroy(t0);
-    if (t1) cudaEventDestroy(t1);
-  }
 };
 
 namespace {
@@ -329,11 +324,10 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
       mols[i].xyz.assign(xyz + 3 * off, xyz + 3 * (off + n_atoms[i]));
       off += n_atoms[i];
     }
-    nddo::Batch b(ctx->engine.get(), mols, s.diis_num_error_vect);
+    nddo::GroupedBatch b(ctx->engine.get(), mols, s.diis_num_error_vect, nddo::GroupedBatch::default_groups(n_mol));
     if (ctx->budget && b.device_bytes() > ctx->budget)
       return fail(ctx, NDDO_ERR_BUDGET, "batch needs " + std::to_string(b.device_bytes()) + " bytes of HBM, budget is " + std::to_string(ctx->budget));
-    b.integrals();
-    b.scf(s, true);
+    b.run(s);
     std::vector<nddo::MolResult> r;
     b.results(&r);
     int rc = NDDO_OK;
@@ -372,7 +366,8 @@ int nddo_batch_create(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, 
       mols[i].xyz.assign(xyz + 3 * off, xyz + 3 * (off + n_atoms[i]));
       off += n_atoms[i];
     }
-    std::unique_ptr<nddo::Batch> b(new nddo::Batch(ctx->engine.get(), mols, diis_m));
+    std::unique_ptr<nddo::GroupedBatch> b(
+        new nddo::GroupedBatch(ctx->engine.get(), mols, diis_m, nddo::GroupedBatch::default_groups(n_mol)));
     if (ctx->budget && b->device_bytes() > ctx->budget)
       return fail(ctx, NDDO_ERR_BUDGET, "batch needs " + std::to_string(b->device_bytes()) + " bytes of HBM, budget is " + std::to_string(ctx->budget));
     nddo_batch* h = new nddo_batch();
@@ -391,8 +386,7 @@ int nddo_batch_run(nddo_batch* h, const nddo_scf_params* params) {
     if (!valid_params(params, &why)) return fail(h->ctx, NDDO_ERR_ARGUMENT, why);
     nddo::ScfSettings s = to_settings(params);
     s.keep_trace = 0;
-    h->b->integrals();
-    h->b->scf(s, true);
+    h->b->run(s);
     return (int)NDDO_OK;
   });
 }
@@ -487,19 +481,7 @@ const char* nddo_kernel_class_name(int k) { return nddo::kernel_class_name(k); }
 int nddo_batch_timer(nddo_batch* h, int op, double* ms) {
   if (!h) return NDDO_ERR_ARGUMENT;
   return guarded(h->ctx, [&]() {
-    cudaStream_t s = h->ctx->engine->stream();
-    if (!h->t0) {
-      nddo::cuda_check(cudaEventCreate(&h->t0), "cudaEventCreate");
-      nddo::cuda_check(cudaEventCreate(&h->t1), "cudaEventCreate");
-    }
-    if (op == 0) nddo::cuda_check(cudaEventRecord(h->t0, s), "cudaEventRecord");
-    else if (op == 1) nddo::cuda_check(cudaEventRecord(h->t1, s), "cudaEventRecord");
-    else {
-      nddo::cuda_check(cudaEventSynchronize(h->t1), "cudaEventSynchronize");
-      float t = 0.f;
-      nddo::cuda_check(cudaEventElapsedTime(&t, h->t0, h->t1), "cudaEventElapsedTime");
-      if (ms) *ms = t;
-    }
+    h->b->timer(op, ms);
     return (int)NDDO_OK;
   });
 }

@@ -199,8 +199,8 @@ size_t Batch::bytes_per_mat_element(int diis_m) {
   return 13 * sizeof(double) + 5 * sizeof(float) + 2 * (size_t)std::max(diis_m, 1) * sizeof(double);
 }
 
-Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m)
-    : eng_(eng), stream_(eng->stream()), diis_m_(diis_m) {
+Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m, cudaStream_t stream)
+    : eng_(eng), stream_(stream ? stream : eng->stream()), diis_m_(diis_m) {
   if (diis_m_ < 0 || diis_m_ > kMaxDiis) throw std::invalid_argument("diis_num_error_vect out of range (0..8)");
   if (mols.empty()) throw std::invalid_argument("empty batch");
   long long mat = 0, vec = 0;

@@ -70,7 +70,7 @@ class ArenaAlloc {
 // one at a time (the serving loop).
 class Batch {
  public:
-  Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m);
+  Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m, cudaStream_t stream = nullptr);
   Batch(Engine* eng, const BatchCapacity& cap, int diis_m, cudaStream_t stream);
   ~Batch();
   Batch(const Batch&) = delete;
@@ -216,6 +216,42 @@ class Batch {
   // algorithmic work of the molecules still active (flop counts, see engine.cu)
   double active_work_estimate(int cls) const;
   std::vector<char> active_host_;
+};
+
+// A fixed batch split into groups of molecules, each a Batch with its own
+// stream, run concurrently by one host thread per group: the latency-bound
+// one-CTA Jacobi of one group overlaps the FP64-bound refinement and the
+// memory-bound Fock build of the others, and the tail wave of a group's
+// launches no longer leaves SMs idle.  Molecule results do not depend on the
+// grouping (every kernel works per molecule).
+class GroupedBatch {
+ public:
+  GroupedBatch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m, int groups);
+  ~GroupedBatch();
+  static int default_groups(int n_mol);
+  int size() const { return n_; }
+  int groups() const { return (int)g_.size(); }
+  void run(const ScfSettings& s);                 // integrals + SCF + energies of every molecule
+  void results(std::vector<MolResult>* out);
+  void copy_charges(int m, double* host) const;
+  void copy_matrix(int which_matrix, int m, double* host) const;
+  void set_coordinates(const double* xyz);
+  size_t device_bytes() const;
+  long long launches() const;
+  long long jacobi_sweeps() const;
+  void set_profiling(bool on);
+  void profile_reset();
+  void profile_collect(double* ms, long long* launches, double* work);   // summed over the groups' streams
+  void timer(int op, double* ms);                 // 0 start, 1 stop, 2 elapsed wall time over all streams
+
+ private:
+  const Batch& locate(int m, int* local) const;
+  int n_ = 0;
+  std::vector<std::unique_ptr<Batch>> g_;
+  std::vector<cudaStream_t> streams_;
+  std::vector<int> first_mol_, first_atom_;
+  std::vector<cudaEvent_t> t0_, t1_;
+  int device_ = 0;
 };
 
 class Engine {
