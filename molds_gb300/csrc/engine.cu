@@ -546,6 +546,17 @@ const char* kernel_class_name(int k) {
   return (k >= 0 && k < kKNumClasses) ? names[k] : "?";
 }
 
+void Batch::set_profiling(bool on) {
+  constexpr size_t kProfEvents = 8192;   // about 14 SCF runs of 14 iterations
+  if (on)
+    while (ev_pool_.size() < kProfEvents) {
+      cudaEvent_t e;
+      cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+      ev_pool_.push_back(e);
+    }
+  prof_on_ = on;
+}
+
 cudaEvent_t Batch::next_event() {
   if (ev_used_ == ev_pool_.size()) {
     cudaEvent_t e;

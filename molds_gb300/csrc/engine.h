@@ -124,7 +124,9 @@ class Batch {
   const std::vector<DevMol>& mol_table() const { return h_mols; }
   void set_coordinates(const double* xyz);          // bohr, 3 per atom, batch order
   // per-kernel-class timing with CUDA events on the launching stream
-  void set_profiling(bool on) { prof_on_ = on; }
+  // Enabling creates the event pool up front (kProfEvents), so the timed
+  // region that follows does not pay for cudaEventCreate.
+  void set_profiling(bool on);
   void profile_collect(double* ms, long long* launches, double* work);  // accumulates since last reset
   void profile_reset();
   long long launches() const { return launches_; }
