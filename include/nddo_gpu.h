@@ -103,7 +103,9 @@ int nddo_get_pair_blocks(nddo_ctx* ctx, double* out, size_t* count);
  * repeated-DoSCF callers (RPMD beads, src/rpmd/RPMD.cpp:78-84; MD/MC/optimiser
  * steps) and throughput runs.  Molecule i has n_atoms[i] atoms; Z and xyz are
  * concatenated over molecules.  results has n_mol entries, charges has
- * sum(n_atoms) entries (may be NULL). */
+ * sum(n_atoms) entries (may be NULL).  The context keeps the device arrays of
+ * the last call: a call with the same molecules (theory, DIIS window, atom
+ * counts, elements) uploads only the new coordinates. */
 int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, const int* atomic_numbers,
                    const double* xyz_bohr, const nddo_scf_params* params, nddo_scf_result* results,
                    double* charges);

@@ -1,6 +1,7 @@
 // extern "C" boundary (include/nddo_gpu.h) over the batched engine.
 #include "../../include/nddo_gpu.h"
 
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -69,6 +70,12 @@ struct nddo_server {
 
 struct nddo_ctx {
   std::unique_ptr<nddo::Engine> engine;
+  // nddo_batch_scf keeps its last batch: a call with the same molecules
+  // (theory, DIIS window, atom counts and elements) reuses the device arrays
+  // and uploads only the new coordinates
+  std::unique_ptr<nddo::GroupedBatch> batch_cache;
+  std::vector<int> cache_natoms, cache_Z;
+  int cache_theory = -1, cache_diis = -1;
   std::unique_ptr<nddo::Batch> mol;      // current molecule (SetMolecule / DoSCF API)
   nddo::ScfSettings last_settings;
   bool has_scf = false;
@@ -158,6 +165,7 @@ int nddo_create(int device, size_t hbm_budget_bytes, nddo_ctx** out) {
 
 void nddo_destroy(nddo_ctx* ctx) {
   if (!ctx) return;
+  ctx->batch_cache.reset();
   ctx->mol.reset();
   ctx->engine.reset();
   delete ctx;
@@ -324,9 +332,30 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
       mols[i].xyz.assign(xyz + 3 * off, xyz + 3 * (off + n_atoms[i]));
       off += n_atoms[i];
     }
-    nddo::GroupedBatch b(ctx->engine.get(), mols, s.diis_num_error_vect, nddo::GroupedBatch::default_groups(n_mol));
-    if (ctx->budget && b.device_bytes() > ctx->budget)
-      return fail(ctx, NDDO_ERR_BUDGET, "batch needs " + std::to_string(b.device_bytes()) + " bytes of HBM, budget is " + std::to_string(ctx->budget));
+    const bool hit = ctx->batch_cache && ctx->cache_theory == theory && ctx->cache_diis == s.diis_num_error_vect &&
+                     ctx->cache_natoms.size() == (size_t)n_mol &&
+                     std::equal(n_atoms, n_atoms + n_mol, ctx->cache_natoms.begin()) &&
+                     ctx->cache_Z.size() == off && std::equal(Z, Z + off, ctx->cache_Z.begin());
+    if (hit) {
+      try {
+        ctx->batch_cache->set_coordinates(xyz);
+      } catch (...) {
+        ctx->batch_cache.reset();   // a rejected geometry leaves no half-updated batch behind
+        throw;
+      }
+    } else {
+      ctx->batch_cache.reset();
+      std::unique_ptr<nddo::GroupedBatch> nb(new nddo::GroupedBatch(ctx->engine.get(), mols, s.diis_num_error_vect,
+                                                                    nddo::GroupedBatch::default_groups(n_mol)));
+      if (ctx->budget && nb->device_bytes() > ctx->budget)
+        return fail(ctx, NDDO_ERR_BUDGET, "batch needs " + std::to_string(nb->device_bytes()) + " bytes of HBM, budget is " + std::to_string(ctx->budget));
+      ctx->batch_cache = std::move(nb);
+      ctx->cache_theory = theory;
+      ctx->cache_diis = s.diis_num_error_vect;
+      ctx->cache_natoms.assign(n_atoms, n_atoms + n_mol);
+      ctx->cache_Z.assign(Z, Z + off);
+    }
+    nddo::GroupedBatch& b = *ctx->batch_cache;
     b.run(s);
     std::vector<nddo::MolResult> r;
     b.results(&r);

@@ -234,3 +234,21 @@ def test_large_basis_block_jacobi(ctx, precision):
         if precision == "fp64":
             assert r["iterations"] == rf.iterations
     assert checked >= 1
+
+
+def test_batch_scf_reuses_arrays_for_new_coordinates(ctx):
+    """A second nddo_batch_scf call with the same molecules and new coordinates
+    reuses the context's batch and gives what a fresh context gives."""
+    base = W.water_cluster(shape=(2, 2, 1), seed=3)
+    a = W.water_replicas(base, 4, seed0=10)
+    b = W.water_replicas(base, 4, seed0=20)
+    p = M.SCFParams(**{**BENCH_SCF.__dict__, "precision": "fp64"})
+    M.batch_scf("am1", a, p, context=ctx)
+    r1, q1 = M.batch_scf("am1", b, p, context=ctx)
+    fresh = M.Context(0)
+    r2, q2 = M.batch_scf("am1", b, p, context=fresh)
+    fresh.close()
+    for x, y, qa, qb in zip(r1, r2, q1, q2):
+        assert x["status"] == M.STATUS_CONVERGED
+        assert x["energy"] == y["energy"] and x["iterations"] == y["iterations"]
+        assert np.array_equal(qa, qb)
