@@ -304,6 +304,11 @@ void Batch::allocate(const BatchCapacity& cap) {
   d_sweeps = dalloc<int>(nm, &bytes_);
   d_count = dalloc<int>(1, &bytes_);
   d_tc_err = dalloc<int>(1, &bytes_);
+  {
+    const size_t b = diis_scratch_bytes(nm);
+    cuda_check(cudaMalloc(&d_diis_ws, b), "cudaMalloc DIIS scratch");
+    bytes_ += b;
+  }
   d_active = dalloc<char>(nm, &bytes_);
   cuda_check(cudaMemsetAsync(d_state, 0, nm * sizeof(MolState), stream_), "memset state");
   cuda_check(cudaMemsetAsync(d_sweeps, 0, nm * sizeof(int), stream_), "memset sweeps");
@@ -420,6 +425,7 @@ Batch::~Batch() {
   if (h_lists_) cudaFreeHost(h_lists_);
   if (h_bj_pending) cudaFreeHost(h_bj_pending);
   if (d_bj_ws) cudaFree(d_bj_ws);
+  if (d_diis_ws) cudaFree(d_diis_ws);
   void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
                   d_hist_dens, d_hist_err, d_G32, d_T32, d_Cf, d_Cnf, d_Ff, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
                   d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs, d_tc_err};
@@ -881,7 +887,7 @@ void Batch::density_step(const ScfSettings& s) {
 void Batch::iterate(const ScfSettings& s, const std::vector<int>& which) {
   upload_list(which);
   const int nl = (int)which.size();
-  launches_ += 2;   // fock + diis
+  launches_ += 4;   // fock + three DIIS kernels
   int h = prof_begin(kKFock, active_work_estimate(kKFock));
   launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, list_max_atoms(), d_blocks, d_H, d_P, d_F, d_Pold, d_state, -1,
                      1, 1, stream_);
@@ -891,7 +897,7 @@ void Batch::iterate(const ScfSettings& s, const std::vector<int>& which) {
   density_step(s);
   h = prof_begin(kKDiis, active_work_estimate(kKDiis));
   launch_diis(d_mols, d_list, nl, d_state, to_dev(s), d_P, d_Pold, d_hist_dens, d_hist_err, mat_total_,
-              s.keep_trace ? d_trace : nullptr, max_iter_alloc_, stream_);
+              s.keep_trace ? d_trace : nullptr, max_iter_alloc_, d_diis_ws, stream_);
   prof_end(h);
   cuda_check(cudaGetLastError(), "diis_kernel");
 }

@@ -184,7 +184,8 @@ class Batch {
   double* d_charges = nullptr;
   int* d_sweeps = nullptr;
   int* d_count = nullptr;
-  int* d_tc_err = nullptr;               // set by a tensor-core GEMM whose MMA wait ran out
+  int* d_tc_err = nullptr;
+  void* d_diis_ws = nullptr;             // DIIS partial sums and decisions (diis_scratch_bytes)               // set by a tensor-core GEMM whose MMA wait ran out
   char* d_active = nullptr;
 
   // current molecule list and its GEMM job tables

@@ -111,9 +111,12 @@ void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, co
 void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, const double* B, double* C,
                  bool ta, bool tb, float acc_tag, const MolState* st, int require_active, int require_phase,
                  cudaStream_t s);
+// DIIS in three launches (partial sums, per-molecule solve, apply); scratch
+// holds diis_scratch_bytes(nlist) bytes
+size_t diis_scratch_bytes(int slots);
 void launch_diis(const DevMol* mols, const int* mol_list, int nlist, MolState* st, const ScfParamsDev& prm,
                  double* P, const double* Pold, double* hist_dens, double* hist_err, long long hist_stride,
-                 TraceEntry* trace, int trace_len, cudaStream_t s);
+                 TraceEntry* trace, int trace_len, void* scratch, cudaStream_t s);
 void launch_convert_f64_f32(const DevMol* mols, const int* mol_list, int nlist, const MolState* st,
                             int require_active, const double* src, float* dst, cudaStream_t s);
 void launch_newton_scale(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,

@@ -9,7 +9,7 @@
 //     parameter: FP32 in the early iterations, FP64 after the switch and on the
 //     plain FP64 path.
 //
-// (e) diis_kernel -- one CTA per molecule: RMS density change and convergence
+// (e) DIIS -- partial / solve / apply kernels: RMS density change and convergence
 //     test (Cndo2::SatisfyConvergenceCriterion, src/cndo/Cndo2.cpp:1472-1517),
 //     density DIIS with MolDS's exact window/acceptance rules (Cndo2::DoDIIS,
 //     :920-1028) and damping (Cndo2::DoDamp, :1030-1061).  The DIIS history is
@@ -176,37 +176,58 @@ __device__ __forceinline__ double block_max(double v, double* scratch) {
   return r;
 }
 
-// One SCF bookkeeping step per molecule, after the new density P is formed.
+// One SCF bookkeeping step per molecule, after the new density P is formed,
+// in three launches so that each molecule's N^2 streams are spread over many
+// CTAs: (1) partial sums over fixed chunks of the molecule's matrix (sum e^2,
+// max |e|, the new B row) while the new history entry is written; (2) one
+// thread per molecule reduces the chunks in order and runs the convergence
+// test, the DIIS solve, damping and the phase switch; (3) the extrapolation
+// and damping over the same chunks.  The chunking depends only on N, and the
+// chunk partials are reduced in a fixed order, so a molecule's result does not
+// depend on the rest of the batch.
+constexpr int kDiisChunksMax = 64;
+constexpr int kDiisPart = 2 + kMaxDiis;     // sum e^2, max |e|, dots
+
+__device__ __forceinline__ int diis_chunks(long long n2) {
+  const long long c = (n2 + 4095) / 4096;
+  return (int)(c < kDiisChunksMax ? (c < 1 ? 1 : c) : kDiisChunksMax);
+}
+
+struct DiisStep {          // decisions of kernel (2) read by kernel (3)
+  double coef[kMaxDiis];
+  int apply, damp, active, pad;
+};
+
 __global__ void __launch_bounds__(kDiisThreads)
-diis_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list, MolState* __restrict__ st,
-            ScfParamsDev prm, double* __restrict__ P, const double* __restrict__ Pold,
-            double* __restrict__ hist_dens, double* __restrict__ hist_err, long long hist_stride,
-            TraceEntry* __restrict__ trace, int trace_len) {
+diis_partial_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list, const MolState* __restrict__ st,
+                    ScfParamsDev prm, const double* __restrict__ P, const double* __restrict__ Pold,
+                    double* __restrict__ hist_dens, double* __restrict__ hist_err, long long hist_stride,
+                    double* __restrict__ part) {
   __shared__ double scratch[40];
-  __shared__ double coef[kMaxDiis + 1];
-  __shared__ int flags[3];
-  const int m = mol_list[blockIdx.x];
-  MolState* s = st + m;
-  if (s->status != kActive) return;
+  const int li = blockIdx.y;
+  const int m = mol_list[li];
+  const MolState s = st[m];
+  if (s.status != kActive) return;
   const DevMol mol = mols[m];
   const long long n2 = (long long)mol.nao * mol.nao;
-  double* Pm = P + mol.mat0;
-  const double* Po = Pold + mol.mat0;
-  const int iter = s->iter;
-  const bool is_guess = (iter == 0 && s->requires_guess);
+  const int chunks = diis_chunks(n2);
+  if ((int)blockIdx.x >= chunks) return;
+  const long long len = (n2 + chunks - 1) / chunks;
+  const long long lo = blockIdx.x * len, hi = (lo + len < n2) ? lo + len : n2;
+  const bool is_guess = (s.iter == 0 && s.requires_guess);
   const int M = prm.diis_m;
   const bool do_diis = !is_guess && M > 0;
-  const int slot = do_diis ? (s->diis_count % M) : 0;
-  const int count = do_diis ? min(s->diis_count + 1, M) : 0;
-
-  // one pass: e = P - P_old, sum e^2, max |e|, push history, dot products
+  const int slot = do_diis ? (s.diis_count % M) : 0;
+  const int count = do_diis ? min(s.diis_count + 1, M) : 0;
+  const double* Pm = P + mol.mat0;
+  const double* Po = Pold + mol.mat0;
+  double* dslot = hist_dens + slot * hist_stride + mol.mat0;
+  double* eslot = hist_err + slot * hist_stride + mol.mat0;
   double sq = 0.0, mx = 0.0;
   double dots[kMaxDiis];
 #pragma unroll
   for (int k = 0; k < kMaxDiis; ++k) dots[k] = 0.0;
-  double* dslot = hist_dens + slot * hist_stride + mol.mat0;
-  double* eslot = hist_err + slot * hist_stride + mol.mat0;
-  for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const double p = Pm[i];
     const double e = p - Po[i];
     sq += e * e;
@@ -222,107 +243,165 @@ diis_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list, M
   }
   const double sumsq = block_sum(sq, scratch);
   const double maxe = block_max(mx, scratch);
-  const double rms = sqrt(sumsq / (double)n2);
   double dsum[kMaxDiis];
 #pragma unroll
   for (int k = 0; k < kMaxDiis; ++k) dsum[k] = (k < count) ? block_sum(dots[k], scratch) : 0.0;
-
   if (threadIdx.x == 0) {
-    if (trace && iter < trace_len) {
-      TraceEntry te;
-      te.rms = rms; te.diis_err = s->diis_err; te.diis_on = s->diis_on; te.damp_on = s->damp_on;
-      trace[(long long)m * trace_len + iter] = te;
-    }
-    s->rms = rms;
-    flags[0] = 0; flags[1] = 0; flags[2] = 0;
-    if (rms < prm.rms_density) {
-      s->status = kConverged;
-      flags[0] = 1;
-    } else if (!is_guess) {
-      if (do_diis) {
-        for (int k = 0; k < count; ++k) { s->B[k * kMaxDiis + slot] = dsum[k]; s->B[slot * kMaxDiis + k] = dsum[k]; }
-        s->diis_count += 1;
-        s->diis_head = slot;
-        s->diis_err = maxe;
-        bool apply = (M <= iter) && (prm.diis_end < maxe) && (maxe < prm.diis_start) && (count == M);
-        if (apply) {
-          // chronological order: oldest ... newest
-          int chron[kMaxDiis];
-          for (int k = 0; k < M; ++k) chron[k] = (slot + 1 + k) % M;
-          double a[(kMaxDiis + 1) * (kMaxDiis + 1)], b[kMaxDiis + 1];
-          const int n = M + 1;
-          for (int i = 0; i < M; ++i)
-            for (int j = 0; j < M; ++j) a[i * n + j] = s->B[chron[i] * kMaxDiis + chron[j]];
-          for (int i = 0; i < M; ++i) { a[i * n + M] = -1.0; a[M * n + i] = -1.0; b[i] = 0.0; }
-          a[M * n + M] = 0.0;
-          b[M] = -1.0;
-          // Gaussian elimination with partial pivoting; an exactly zero pivot
-          // means a singular system, which MolDS answers by skipping the step
-          bool singular = false;
-          for (int c = 0; c < n && !singular; ++c) {
-            int piv = c;
-            for (int r = c + 1; r < n; ++r) if (fabs(a[r * n + c]) > fabs(a[piv * n + c])) piv = r;
-            if (a[piv * n + c] == 0.0) { singular = true; break; }
-            if (piv != c) {
-              for (int j = 0; j < n; ++j) { double t = a[c * n + j]; a[c * n + j] = a[piv * n + j]; a[piv * n + j] = t; }
-              double t = b[c]; b[c] = b[piv]; b[piv] = t;
-            }
-            for (int r = c + 1; r < n; ++r) {
-              const double f = a[r * n + c] / a[c * n + c];
-              for (int j = c; j < n; ++j) a[r * n + j] -= f * a[c * n + j];
-              b[r] -= f * b[c];
-            }
+    double* o = part + ((long long)li * kDiisChunksMax + blockIdx.x) * kDiisPart;
+    o[0] = sumsq;
+    o[1] = maxe;
+    for (int k = 0; k < kMaxDiis; ++k) o[2 + k] = dsum[k];
+  }
+}
+
+__global__ void diis_solve_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list, int nlist,
+                                  MolState* __restrict__ st, ScfParamsDev prm, const double* __restrict__ part,
+                                  DiisStep* __restrict__ steps, TraceEntry* __restrict__ trace, int trace_len) {
+  const int li = blockIdx.x * blockDim.x + threadIdx.x;
+  if (li >= nlist) return;
+  DiisStep out;
+  for (int k = 0; k < kMaxDiis; ++k) out.coef[k] = 0.0;
+  out.apply = 0; out.damp = 0; out.active = 0; out.pad = 0;
+  const int m = mol_list[li];
+  MolState* s = st + m;
+  if (s->status != kActive) { steps[li] = out; return; }
+  out.active = 1;
+  const DevMol mol = mols[m];
+  const long long n2 = (long long)mol.nao * mol.nao;
+  const int chunks = diis_chunks(n2);
+  const int iter = s->iter;
+  const bool is_guess = (iter == 0 && s->requires_guess);
+  const int M = prm.diis_m;
+  const bool do_diis = !is_guess && M > 0;
+  const int slot = do_diis ? (s->diis_count % M) : 0;
+  const int count = do_diis ? min(s->diis_count + 1, M) : 0;
+  double sumsq = 0.0, maxe = 0.0, dsum[kMaxDiis];
+  for (int k = 0; k < kMaxDiis; ++k) dsum[k] = 0.0;
+  for (int c = 0; c < chunks; ++c) {      // fixed order
+    const double* p = part + ((long long)li * kDiisChunksMax + c) * kDiisPart;
+    sumsq += p[0];
+    maxe = p[1] > maxe ? p[1] : maxe;
+    for (int k = 0; k < kMaxDiis; ++k) dsum[k] += p[2 + k];
+  }
+  const double rms = sqrt(sumsq / (double)n2);
+  if (trace && iter < trace_len) {
+    TraceEntry te;
+    te.rms = rms; te.diis_err = s->diis_err; te.diis_on = s->diis_on; te.damp_on = s->damp_on;
+    trace[(long long)m * trace_len + iter] = te;
+  }
+  s->rms = rms;
+  if (rms < prm.rms_density) {
+    s->status = kConverged;
+    out.active = 0;
+    steps[li] = out;
+    return;
+  }
+  if (!is_guess) {
+    if (do_diis) {
+      for (int k = 0; k < count; ++k) { s->B[k * kMaxDiis + slot] = dsum[k]; s->B[slot * kMaxDiis + k] = dsum[k]; }
+      s->diis_count += 1;
+      s->diis_head = slot;
+      s->diis_err = maxe;
+      const bool apply = (M <= iter) && (prm.diis_end < maxe) && (maxe < prm.diis_start) && (count == M);
+      if (apply) {
+        // chronological order: oldest ... newest
+        int chron[kMaxDiis];
+        for (int k = 0; k < M; ++k) chron[k] = (slot + 1 + k) % M;
+        double a[(kMaxDiis + 1) * (kMaxDiis + 1)], b[kMaxDiis + 1];
+        const int n = M + 1;
+        for (int i = 0; i < M; ++i)
+          for (int j = 0; j < M; ++j) a[i * n + j] = s->B[chron[i] * kMaxDiis + chron[j]];
+        for (int i = 0; i < M; ++i) { a[i * n + M] = -1.0; a[M * n + i] = -1.0; b[i] = 0.0; }
+        a[M * n + M] = 0.0;
+        b[M] = -1.0;
+        // Gaussian elimination with partial pivoting; an exactly zero pivot
+        // means a singular system, which MolDS answers by skipping the step
+        bool singular = false;
+        for (int c = 0; c < n && !singular; ++c) {
+          int piv = c;
+          for (int r = c + 1; r < n; ++r) if (fabs(a[r * n + c]) > fabs(a[piv * n + c])) piv = r;
+          if (a[piv * n + c] == 0.0) { singular = true; break; }
+          if (piv != c) {
+            for (int j = 0; j < n; ++j) { double t = a[c * n + j]; a[c * n + j] = a[piv * n + j]; a[piv * n + j] = t; }
+            double t = b[c]; b[c] = b[piv]; b[piv] = t;
           }
-          if (!singular) {
-            for (int c = n - 1; c >= 0; --c) {
-              double v = b[c];
-              for (int j = c + 1; j < n; ++j) v -= a[c * n + j] * b[j];
-              b[c] = v / a[c * n + c];
-            }
-            for (int k = 0; k < M; ++k) coef[k] = b[k];
-            flags[1] = 1;
+          for (int r = c + 1; r < n; ++r) {
+            const double f = a[r * n + c] / a[c * n + c];
+            for (int j = c; j < n; ++j) a[r * n + j] -= f * a[c * n + j];
+            b[r] -= f * b[c];
           }
         }
-        s->diis_on = flags[1];
+        if (!singular) {
+          for (int c = n - 1; c >= 0; --c) {
+            double v = b[c];
+            for (int j = c + 1; j < n; ++j) v -= a[c * n + j] * b[j];
+            b[c] = v / a[c * n + c];
+          }
+          for (int k = 0; k < M; ++k) out.coef[k] = b[k];
+          out.apply = 1;
+        }
       }
-      flags[2] = (prm.damping_weight > 0.0 && prm.damping_thresh < rms) ? 1 : 0;
-      s->damp_on = flags[2];
-      if (prm.precision == 1 && s->phase == 0 && do_diis && maxe < prm.switch_error) s->phase = 1;
+      s->diis_on = out.apply;
     }
+    out.damp = (prm.damping_weight > 0.0 && prm.damping_thresh < rms) ? 1 : 0;
+    s->damp_on = out.damp;
+    if (prm.precision == 1 && s->phase == 0 && do_diis && maxe < prm.switch_error) s->phase = 1;
   }
-  __syncthreads();
-  if (flags[0]) return;
-  if (flags[1]) {
-    // P = sum_k c_k P_k in chronological order (MolDS sums the stored
-    // densities in slot order through Dgemv)
-    const int newest = slot;
-    for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
-      double v = 0.0;
+  s->iter = iter + 1;
+  if (s->iter >= prm.max_iter) s->status = kNotConverged;
+  steps[li] = out;
+}
+
+__global__ void __launch_bounds__(kDiisThreads)
+diis_apply_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list, const MolState* __restrict__ st,
+                  ScfParamsDev prm, double* __restrict__ P, const double* __restrict__ Pold,
+                  const double* __restrict__ hist_dens, long long hist_stride, const DiisStep* __restrict__ steps) {
+  const int li = blockIdx.y;
+  const DiisStep d = steps[li];
+  if (!d.active || (!d.apply && !d.damp)) return;
+  const int m = mol_list[li];
+  const DevMol mol = mols[m];
+  const long long n2 = (long long)mol.nao * mol.nao;
+  const int chunks = diis_chunks(n2);
+  if ((int)blockIdx.x >= chunks) return;
+  const long long len = (n2 + chunks - 1) / chunks;
+  const long long lo = blockIdx.x * len, hi = (lo + len < n2) ? lo + len : n2;
+  const int M = prm.diis_m;
+  double* Pm = P + mol.mat0;
+  const double* Po = Pold + mol.mat0;
+  // the newest entry is the one this iteration pushed (diis_head)
+  const int newest = st[m].diis_head;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    double v = Pm[i];
+    if (d.apply) {
+      // P = sum_k c_k P_k in chronological order (MolDS sums the stored
+      // densities in slot order through Dgemv)
+      v = 0.0;
       for (int k = 0; k < M; ++k) {
         const int rs = (newest + 1 + k) % M;
-        v += coef[k] * hist_dens[rs * hist_stride + mol.mat0 + i];
+        v += d.coef[k] * hist_dens[rs * hist_stride + mol.mat0 + i];
       }
-      Pm[i] = v;
     }
-  }
-  if (flags[2]) {
-    const double w = prm.damping_weight;
-    __syncthreads();
-    for (long long i = threadIdx.x; i < n2; i += blockDim.x) Pm[i] = Pm[i] * (1.0 - w) + w * Po[i];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    s->iter = iter + 1;
-    if (s->iter >= prm.max_iter) s->status = kNotConverged;
+    if (d.damp) v = v * (1.0 - prm.damping_weight) + prm.damping_weight * Po[i];
+    Pm[i] = v;
   }
 }
 
 void launch_diis(const DevMol* mols, const int* mol_list, int nlist, MolState* st, const ScfParamsDev& prm,
                  double* P, const double* Pold, double* hist_dens, double* hist_err, long long hist_stride,
-                 TraceEntry* trace, int trace_len, cudaStream_t s) {
+                 TraceEntry* trace, int trace_len, void* scratch, cudaStream_t s) {
   if (nlist <= 0) return;
-  diis_kernel<<<nlist, kDiisThreads, 0, s>>>(mols, mol_list, st, prm, P, Pold, hist_dens, hist_err, hist_stride,
-                                             trace, trace_len);
+  double* part = static_cast<double*>(scratch);
+  DiisStep* steps = reinterpret_cast<DiisStep*>(part + (size_t)nlist * kDiisChunksMax * kDiisPart);
+  diis_partial_kernel<<<dim3(kDiisChunksMax, nlist), kDiisThreads, 0, s>>>(mols, mol_list, st, prm, P, Pold, hist_dens,
+                                                                          hist_err, hist_stride, part);
+  diis_solve_kernel<<<(nlist + 63) / 64, 64, 0, s>>>(mols, mol_list, nlist, st, prm, part, steps, trace, trace_len);
+  diis_apply_kernel<<<dim3(kDiisChunksMax, nlist), kDiisThreads, 0, s>>>(mols, mol_list, st, prm, P, Pold, hist_dens,
+                                                                        hist_stride, steps);
+}
+
+size_t diis_scratch_bytes(int slots) {
+  return (size_t)slots * kDiisChunksMax * kDiisPart * sizeof(double) + (size_t)slots * sizeof(DiisStep) + 256;
 }
 
 // ---------------------------------------------------------------------------
