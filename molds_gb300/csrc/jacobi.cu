@@ -53,6 +53,43 @@ template <> struct Vec4<double> {
   }
 };
 
+// Rotation that annihilates a_pq: t = tan(phi) is the root of
+// a_pq t^2 + (a_qq - a_pp) t - a_pq = 0 with |t| <= 1, c = 1 / sqrt(1 + t^2).
+__device__ __forceinline__ void jac_rotation(float app, float aqq, float apq, float* t_out, float* c, float* s) {
+  const float theta = (aqq - app) / (2.f * apq);
+  float t;
+  if (fabsf(theta) > 1e15f) t = 0.5f / theta;
+  else t = (theta >= 0.f ? 1.f : -1.f) / (fabsf(theta) + sqrtf(theta * theta + 1.f));
+  *c = 1.f / sqrtf(t * t + 1.f);
+  *s = t * *c;
+  *t_out = t;
+}
+// FP64: GB300 runs FP64 at 1/64 of the FP32 rate and FP64 divides and square
+// roots are long dependent sequences, so t starts from the FP32 formula (with
+// a_qq - a_pp formed in FP64) and takes one Newton step on the quadratic
+// (error (1e-7)^2), and c = rsqrt(1 + t^2) takes two Newton steps from the FP32
+// reciprocal square root: one FP64 divide instead of three divides and two
+// square roots.
+__device__ __forceinline__ void jac_rotation(double app, double aqq, double apq, double* t_out, double* c,
+                                             double* s) {
+  const double d = aqq - app;
+  const float thetaf = (float)d / (2.f * (float)apq);
+  float tf;
+  if (fabsf(thetaf) > 1e15f) tf = 0.5f / thetaf;
+  else tf = (thetaf >= 0.f ? 1.f : -1.f) / (fabsf(thetaf) + sqrtf(thetaf * thetaf + 1.f));
+  double t = (double)tf;
+  const double g = fma(apq * t, t, fma(d, t, -apq));
+  const double gp = fma(2.0 * apq, t, d);
+  t -= g / gp;
+  const double x = fma(t, t, 1.0);
+  double cc = (double)rsqrtf((float)x);
+  cc = cc * fma(-0.5 * x, cc * cc, 1.5);
+  cc = cc * fma(-0.5 * x, cc * cc, 1.5);
+  *c = cc;
+  *s = t * cc;
+  *t_out = t;
+}
+
 template <typename T> struct JacTol;
 template <> struct JacTol<float> { static constexpr float rel = 3e-7f; };
 template <> struct JacTol<double> { static constexpr double rel = 2e-14; };
@@ -188,12 +225,8 @@ jacobi_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
         const int doit = aa > thresh;
         if (doit) {
           const T app = A[rowoff[p]], aqq = A[rowoff[q]];
-          const T theta = (aqq - app) / (2 * apq);
           T t;
-          if (fabs(theta) > (T)1e15) t = (T)0.5 / theta;
-          else t = (theta >= 0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt(theta * theta + (T)1));
-          c = (T)1 / sqrt(t * t + (T)1);
-          s = t * c;
+          jac_rotation(app, aqq, apq, &t, &c, &s);
           // diagonal block: exact update, off-diagonal element annihilated
           A[rowoff[p]] = app - t * apq;
           A[rowoff[q]] = aqq + t * apq;
