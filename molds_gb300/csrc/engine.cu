@@ -491,7 +491,6 @@ void Batch::build_jobs(const std::vector<int>& which) {
       ov.push_back(job(b + (long long)o * n, b, b, v, o, n, n, n, o, m));   // O = C_v C_o^T (B transposed)
       yt.push_back(job(b, b + (long long)o * n, b, o, n, v, o, n, n, m, 1.0, 1.0));  // Yt = C_o + K^T C_v (A transposed)
       mm.push_back(job(b, b, b, o, o, n, n, n, o, m, 1.0, 0.0, 1));         // M = Yt Yt^T   (B transposed, symmetric)
-      d2.push_back(job(b, b, b, o, o, o, o, o, o, m));                      // D2 = D D
       z.push_back(job(b, b, b, o, n, o, o, n, n, m, -1.0, 1.0));            // Z = Yt - D Yt
       pp.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0, 0.0, 1));         // P = 2 Yt^T Z  (A transposed, symmetric)
     }
@@ -861,11 +860,11 @@ void Batch::density_step(const ScfSettings& s) {
     h = prof_begin(kKRefine, active_work_estimate(kKRefine));
     // FP64 phase: one Newton step on the occupied subspace, then P = 2 Y (Y^T Y)^-1 Y^T
     const int nl = (int)cur_list_.size();
-    double *W = d_S[0], *K = d_S[1], *Yt = d_S[2], *Mm = d_S[3], *D2 = d_S[4], *Z = d_S[5];
+    double *W = d_S[0], *K = d_S[1], *Yt = d_S[2], *Mm = d_S[3], *O = d_S[4], *Z = d_S[5];
     launch_gemm(j_w_.d, j_w_.n, j_w_.tiles, d_F, d_C, W, false, true, 0.0, d_state, 1, 1, stream_);
     launch_gemm(j_kt_.d, j_kt_.n, j_kt_.tiles, d_C, W, K, false, false, 0.0, d_state, 1, 1, stream_);
-    launch_gemm(j_ov_.d, j_ov_.n, j_ov_.tiles, d_C, d_C, D2, false, true, 0.0, d_state, 1, 1, stream_);
-    launch_newton_scale(d_mols, d_list, nl, d_state, 1, K, D2, d_eps, stream_);
+    launch_gemm(j_ov_.d, j_ov_.n, j_ov_.tiles, d_C, d_C, O, false, true, 0.0, d_state, 1, 1, stream_);
+    launch_newton_scale(d_mols, d_list, nl, d_state, 1, K, O, d_eps, stream_);
     // Yt = C_o + K^T C_v: K is ~1e-7, so its product needs only FP32
     // accumulation (error ~1e-14 absolute); the sum is formed in FP64
     launch_copy_occ_rows(d_mols, d_list, nl, d_state, 1, d_C, Yt, stream_);
@@ -875,7 +874,7 @@ void Batch::density_step(const ScfSettings& s) {
     // of the orthonormalised basis (~1e-7), so the second-order term is ~1e-14;
     // Z = (I - D) Yt = Yt - D Yt, where D Yt (~1e-7) again needs only FP32
     // accumulation
-    launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, D2, 0, stream_);
+    launch_neumann(d_mols, d_list, nl, d_state, 1, Mm, stream_);
     launch_copy_occ_rows(d_mols, d_list, nl, d_state, 1, Yt, Z, stream_);
     launch_gemm(j_z_.d, j_z_.n, j_z_.tiles, Mm, Yt, Z, false, false, 0.0f, d_state, 1, 1, stream_);
     launch_gemm(j_p_.d, j_p_.n, j_p_.tiles, Yt, Z, d_P, true, false, 0.0, d_state, 1, 1, stream_);

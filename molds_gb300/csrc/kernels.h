@@ -117,12 +117,11 @@ size_t diis_scratch_bytes(int slots);
 void launch_diis(const DevMol* mols, const int* mol_list, int nlist, MolState* st, const ScfParamsDev& prm,
                  double* P, const double* Pold, double* hist_dens, double* hist_err, long long hist_stride,
                  TraceEntry* trace, int trace_len, void* scratch, cudaStream_t s);
-void launch_convert_f64_f32(const DevMol* mols, const int* mol_list, int nlist, const MolState* st,
-                            int require_active, const double* src, float* dst, cudaStream_t s);
+
 void launch_newton_scale(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
                          double* K, const double* O, const double* eps, cudaStream_t s);
 void launch_neumann(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
-                    double* M, const double* D2, int mode, cudaStream_t s);
+                    double* M, cudaStream_t s);
 void launch_copy_occ_rows(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
                           const double* src, double* dst, cudaStream_t s);
 

@@ -407,24 +407,6 @@ size_t diis_scratch_bytes(int slots) {
 // ---------------------------------------------------------------------------
 // small elementwise helpers
 // ---------------------------------------------------------------------------
-__global__ void convert_f64_to_f32_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
-                                          const MolState* __restrict__ st, int require_active,
-                                          const double* __restrict__ src, float* __restrict__ dst) {
-  const int m = mol_list[blockIdx.y];
-  if (require_active && st[m].status != kActive) return;
-  const DevMol mol = mols[m];
-  const long long n2 = (long long)mol.nao * mol.nao;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x)
-    dst[mol.mat0 + i] = (float)src[mol.mat0 + i];
-}
-
-void launch_convert_f64_f32(const DevMol* mols, const int* mol_list, int nlist, const MolState* st,
-                            int require_active, const double* src, float* dst, cudaStream_t s) {
-  if (nlist <= 0) return;
-  dim3 grid(8, nlist);
-  convert_f64_to_f32_kernel<<<grid, 256, 0, s>>>(mols, mol_list, st, require_active, src, dst);
-}
-
 // FP64 refinement (one Newton step of Ogita & Aishima's eigenvector refinement,
 // restricted to the occupied columns): with approximate eigenvectors x and
 // eigenvalues lam, K_ai = -(x_a^T F x_i - lam_i x_a^T x_i) / (lam_a - lam_i),
@@ -452,11 +434,10 @@ void launch_newton_scale(const DevMol* mols, const int* mol_list, int nlist, con
   newton_scale_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, K, O, eps);
 }
 
-// Minv = I - D + D2 with D = M - I (o x o); D2 computed separately as D*D.
-// mode 0: M <- M - I (so M holds D); mode 1: M <- I - M + D2
+// D = M - I in place (o x o): the first-order (Y^T Y)^-1 = I - D is applied by
+// the caller as Z = Y - D Y.
 __global__ void neumann_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
-                               const MolState* __restrict__ st, int require_phase, double* __restrict__ Mm,
-                               const double* __restrict__ D2, int mode) {
+                               const MolState* __restrict__ st, int require_phase, double* __restrict__ Mm) {
   const int m = mol_list[blockIdx.y];
   if (st[m].status != kActive || (require_phase >= 0 && st[m].phase != require_phase)) return;
   const DevMol mol = mols[m];
@@ -464,16 +445,14 @@ __global__ void neumann_kernel(const DevMol* __restrict__ mols, const int* __res
   const long long cnt = (long long)o * o;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(e / o), j = (int)(e % o);
-    double* x = Mm + mol.mat0 + e;
-    if (mode == 0) *x = *x - (i == j ? 1.0 : 0.0);
-    else *x = (i == j ? 1.0 : 0.0) - *x + (D2 ? D2[mol.mat0 + e] : 0.0);
+    if (i == j) Mm[mol.mat0 + e] -= 1.0;
   }
 }
 
 void launch_neumann(const DevMol* mols, const int* mol_list, int nlist, const MolState* st, int require_phase,
-                    double* M, const double* D2, int mode, cudaStream_t s) {
+                    double* M, cudaStream_t s) {
   if (nlist <= 0) return;
-  neumann_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, M, D2, mode);
+  neumann_kernel<<<dim3(8, nlist), 256, 0, s>>>(mols, mol_list, st, require_phase, M);
 }
 
 // copy the first `rows` rows of C (n x n, row-major) into dst (rows x n)

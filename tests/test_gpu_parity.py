@@ -252,3 +252,25 @@ def test_batch_scf_reuses_arrays_for_new_coordinates(ctx):
         assert x["status"] == M.STATUS_CONVERGED
         assert x["energy"] == y["energy"] and x["iterations"] == y["iterations"]
         assert np.array_equal(qa, qb)
+
+
+def test_grouped_batch_new_coordinates_match_plain_path(ctx):
+    """A resident batch of 100 molecules runs as concurrent groups; after
+    nddo_batch_set_coordinates its results equal the plain one-molecule path."""
+    base = W.water_cluster(shape=(2, 1, 1), seed=5)
+    first = W.water_replicas(base, 100, seed0=500)
+    moved = W.water_replicas(base, 100, seed0=900)
+    p = M.SCFParams(**{**BENCH_SCF.__dict__, "precision": "fp64"})
+    rb = M.ResidentBatch("am1", first, context=ctx)
+    rb.run(p)
+    rb.set_coordinates(np.concatenate([m.xyz for m in moved]))
+    rb.run(p)
+    res, q = rb.results()
+    rb.close()
+    es = M.ElectronicStructure("am1", p, context=ctx)
+    for i in (0, 37, 63, 99):
+        es.SetMolecule(moved[i])
+        es.DoSCF()
+        assert res[i]["status"] == M.STATUS_CONVERGED
+        assert abs(res[i]["energy"] - es.GetElectronicEnergy()) <= 1e-10
+        assert np.max(np.abs(q[i] - es.GetMullikenCharges())) <= 1e-10
