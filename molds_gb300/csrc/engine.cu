@@ -486,8 +486,8 @@ void Batch::build_jobs(const std::vector<int>& which) {
     t2.push_back(job(b, b, b, n, n, n, n, n, n, m));            // G = C T
     dn.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0, 0.0, 1)); // P = 2 C_o^T C_o  (A transposed, symmetric)
     if (o > 0 && v > 0) {
-      w.push_back(job(b, b, b, n, o, n, n, n, o, m));                       // W = F C_o^T   (B transposed)
-      kt.push_back(job(b + (long long)o * n, b, b, v, o, n, n, o, o, m));   // Kt = C_v W
+      w.push_back(job(b + (long long)o * n, b, b, v, n, n, n, n, n, m));   // U = C_v F  (v x n)
+      kt.push_back(job(b, b, b, v, o, n, n, n, o, m));                      // Kt = U C_o^T  (B transposed)
       ov.push_back(job(b + (long long)o * n, b, b, v, o, n, n, n, o, m));   // O = C_v C_o^T (B transposed)
       yt.push_back(job(b, b + (long long)o * n, b, o, n, v, o, n, n, m, 1.0, 1.0));  // Yt = C_o + K^T C_v (A transposed)
       mm.push_back(job(b, b, b, o, o, n, n, n, o, m, 1.0, 0.0, 1));         // M = Yt Yt^T   (B transposed, symmetric)
@@ -627,7 +627,7 @@ double Batch::active_work_estimate(int cls) const {
       case kKTransform: w += 4.0 * n * n * n; break;
       case kKOrtho: w += 4.0 * n * n * n; break;
       case kKDensity: w += 2.0 * n * n * o; break;
-      case kKRefine: w += 2 * n * n * o + 4 * n * v * o + 2 * n * o * o + 2 * n * n * o; break;   // FP64 products
+      case kKRefine: w += 2 * v * n * n + 4 * n * v * o + 2 * n * o * o + 2 * n * n * o; break;   // FP64 products
       case kKDiis: w += 8.0 * n * n * (2.0 * diis_m_ + 3.0); break;
       case kKFock: {
         double blk = 0.0;
@@ -861,8 +861,9 @@ void Batch::density_step(const ScfSettings& s) {
     // FP64 phase: one Newton step on the occupied subspace, then P = 2 Y (Y^T Y)^-1 Y^T
     const int nl = (int)cur_list_.size();
     double *W = d_S[0], *K = d_S[1], *Yt = d_S[2], *Mm = d_S[3], *O = d_S[4], *Z = d_S[5];
-    launch_gemm(j_w_.d, j_w_.n, j_w_.tiles, d_F, d_C, W, false, true, 0.0, d_state, 1, 1, stream_);
-    launch_gemm(j_kt_.d, j_kt_.n, j_kt_.tiles, d_C, W, K, false, false, 0.0, d_state, 1, 1, stream_);
+    // Kt = C_v F C_o^T as (C_v F) C_o^T: 2 v n^2 + 2 v n o flops instead of 2 n^2 o + 2 v n o
+    launch_gemm(j_w_.d, j_w_.n, j_w_.tiles, d_C, d_F, W, false, false, 0.0, d_state, 1, 1, stream_);
+    launch_gemm(j_kt_.d, j_kt_.n, j_kt_.tiles, W, d_C, K, false, true, 0.0, d_state, 1, 1, stream_);
     launch_gemm(j_ov_.d, j_ov_.n, j_ov_.tiles, d_C, d_C, O, false, true, 0.0, d_state, 1, 1, stream_);
     launch_newton_scale(d_mols, d_list, nl, d_state, 1, K, O, d_eps, stream_);
     // Yt = C_o + K^T C_v: K is ~1e-7, so its product needs only FP32
