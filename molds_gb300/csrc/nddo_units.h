@@ -10,6 +10,7 @@
 
 #include <math.h>
 #include "nddo_elements.h"
+#include "nddo_dipole.h"
 
 #define NDDO_EV2AU   0.03674903
 #define NDDO_ANG2AU  (1.0 / 0.5291772)
@@ -28,6 +29,7 @@ typedef struct {
   double gk[4], gl[4], gm[4];   /* Gaussian core-core terms (a.u.)     */
   double e_atom, dhf_atom;      /* MNDO heat-of-formation bookkeeping  */
   double sto_norm[2];   /* Slater normalisation (2 zeta)^(n+1/2) / sqrt((2n)!) of s and p */
+  double core_mass;     /* atomic mass [a.u.] - valence electrons: weight of the dipole origin */
   int n_ao;             /* 1 or 4                                      */
   int principal_n;      /* 1, 2 or 3                                   */
   int atomic_number;
@@ -75,6 +77,7 @@ static inline int nddo_fill_atom_params(int theory, int atomic_number, nddo_atom
     out->sto_norm[0] = pow(2.0 * t->zeta_s, el->principal_n + 0.5) / sqrt(f);
     out->sto_norm[1] = (t->zeta_p > 0.0) ? pow(2.0 * t->zeta_p, el->principal_n + 0.5) / sqrt(f) : 0.0;
   }
+  out->core_mass = nddo_atomic_mass_gmol(atomic_number) * NDDO_GMOLIN2AU - (double)el->core_charge;
   out->n_ao = el->n_ao;
   out->principal_n = el->principal_n;
   out->atomic_number = atomic_number;

@@ -17,6 +17,8 @@
  *   Fock elements .......................... src/mndo/Mndo.cpp:422-650, src/cndo/Cndo2.cpp:1526-1636
  *   core-core (MNDO + H-N/H-O rule) ........ src/mndo/Mndo.cpp:223-240, 319-327
  *   AM1/PM3 Gaussian core-core terms ....... src/am1/Am1.cpp:145-170, src/am1/Am1.h:45-47
+ *   Cartesian (dipole) matrix, STO-6G ...... src/cndo/Cndo2.cpp:1946-2057, 2068-2130, 2149-2400
+ *   Gaussian overlaps (s, p) ............... src/cndo/Cndo2.cpp:4563-4575, 4601-5153
  *
  * The STO overlap is evaluated here by my own expansion in prolate-spheroidal
  * coordinates (the integrand is a polynomial in xi, eta times exp(-p xi - q eta),
@@ -485,6 +487,113 @@ int oracle_atom_info(int theory, int natoms, const int* Z, double* out) {
     out[4 * a + 1] = p.n_ao;
     out[4 * a + 2] = p.e_atom;
     out[4 * a + 3] = p.dhf_atom;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Cartesian (dipole) matrix <mu| r_k |nu> by the STO-6G expansion           */
+/* ------------------------------------------------------------------------ */
+
+/* axis of each orbital in MolDS's order (s, py, pz, px); -1 for s */
+static const int axis_of_orb[4] = {-1, 1, 2, 0};
+
+/* (s_A|s_B) of two normalised s Gaussians (Cndo2.cpp:4563-4575) */
+static double gto_sasb(double a, double b, double R) {
+  double t1 = 2.0 * sqrt(a * b) / (a + b);
+  double t2 = -1.0 * (a * b) / (a + b);
+  return t1 * sqrt(t1) * exp(t2 * R * R);
+}
+
+/* Overlap of normalised s / p Gaussians, p given by its axis (-1 = s);
+ * d = A - B (Cndo2.cpp:4601-5153, the s and p cases). */
+static double gto_overlap(int ia, double a, int ib, double b, const double* d, double sasb) {
+  double p = a + b, ab = a * b, v;
+  if (ia < 0 && ib < 0) v = 1.0;
+  else if (ia < 0) v = 2.0 * a * sqrt(b) * d[ib] / p;
+  else if (ib < 0) v = -2.0 * sqrt(a) * b * d[ia] / p;
+  else if (ia == ib) v = 4.0 * sqrt(ab) / p * (-1.0 * (d[ia] * d[ia]) * ab / p + 0.5);
+  else v = -4.0 * ab * sqrt(ab) / (p * p) * d[ia] * d[ib];
+  return v * sasb;
+}
+
+/* <g_A| r_k |g_B> of normalised s / p Gaussians in absolute coordinates
+ * (Cndo2.cpp:2149-2400, the s and p cases). */
+static double gto_cartesian(int ia, double a, const double* ra, int ib, double b, const double* rb,
+                            int k, double sasb) {
+  const double p = a + b, ab = a * b;
+  const double d[3] = {ra[0] - rb[0], ra[1] - rb[1], ra[2] - rb[2]};
+  if (ia < 0 && ib < 0) return (a * ra[k] + b * rb[k]) / p * sasb;
+  if (ia < 0)   /* r_k g_s(A) = g_pk(A) / (2 sqrt a) + A_k g_s(A) */
+    return gto_overlap(k, a, ib, b, d, sasb) / (2.0 * sqrt(a)) + ra[k] * gto_overlap(-1, a, ib, b, d, sasb);
+  if (ib < 0)
+    return gto_overlap(ia, a, k, b, d, sasb) / (2.0 * sqrt(b)) + rb[k] * gto_overlap(ia, a, -1, b, d, sasb);
+  const double f = 4.0 * sqrt(ab) / (p * p);
+  if (ia == ib && k == ia) {
+    double t1 = a * ra[k] + b * rb[k], t2 = a * ra[k] - a * rb[k], t3 = b * ra[k] - b * rb[k];
+    return (0.5 * (t1 + t2 - t3) - t1 * t2 * t3 / p) * f * sasb;
+  }
+  if (ia == ib) {
+    double t1 = a * ra[ia] - a * rb[ia], t2 = b * ra[ia] - b * rb[ia];
+    return (0.5 - t1 * t2 / p) * (a * ra[k] + b * rb[k]) * f * sasb;
+  }
+  if (k == ib) {
+    double t1 = a * ra[k] + b * rb[k], t2 = a * ra[k] - a * rb[k];
+    return (0.5 + t1 * t2 / p) * (b * ra[ia] - b * rb[ia]) * (-f) * sasb;
+  }
+  if (k == ia) {
+    double t1 = a * ra[k] + b * rb[k], t2 = b * ra[k] - b * rb[k];
+    return (0.5 - t1 * t2 / p) * (a * ra[ib] - a * rb[ib]) * f * sasb;
+  }
+  {
+    double t1 = b * ra[ia] - b * rb[ia], t2 = a * ra[k] + b * rb[k], t3 = a * ra[ib] - a * rb[ib];
+    return -f / p * (t1 * t2 * t3) * sasb;
+  }
+}
+
+/* X[3][N][N]: every AO pair, same atom included, each element summed over the
+ * 6 x 6 primitive pairs (Cndo2.cpp:1946-2057, 2068-2130).  Returns N. */
+int oracle_cartesian(int theory, int natoms, const int* Z, const double* xyz, double* X) {
+  nddo_atom_params* P = (nddo_atom_params*)malloc(sizeof(nddo_atom_params) * (natoms > 0 ? natoms : 1));
+  int* first = (int*)malloc(sizeof(int) * (natoms > 0 ? natoms : 1));
+  int N = fill_params(theory, natoms, Z, P, first);
+  if (N < 0) { free(P); free(first); return -1; }
+  const size_t NN = (size_t)N * N;
+  for (int A = 0; A < natoms; ++A)
+    for (int B = 0; B < natoms; ++B) {
+      const double* ra = xyz + 3 * A; const double* rb = xyz + 3 * B;
+      const double dx = ra[0] - rb[0], dy = ra[1] - rb[1], dz = ra[2] - rb[2];
+      const double R = sqrt(dx * dx + dy * dy + dz * dz);
+      const int shA = P[A].principal_n - 1, shB = P[B].principal_n - 1;
+      for (int mu = 0; mu < P[A].n_ao; ++mu)
+        for (int nu = 0; nu < P[B].n_ao; ++nu) {
+          const int la = mu == 0 ? 0 : 1, lb = nu == 0 ? 0 : 1;
+          const double zA = P[A].zeta[la], zB = P[B].zeta[lb];
+          double acc[3] = {0.0, 0.0, 0.0};
+          for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+              const double c = nddo_sto6g_coef[shA][la][i] * nddo_sto6g_coef[shB][lb][j];
+              const double a = (zA * zA) * nddo_sto6g_exp[shA][la][i];
+              const double b = (zB * zB) * nddo_sto6g_exp[shB][lb][j];
+              const double sasb = gto_sasb(a, b, R);
+              for (int k = 0; k < 3; ++k)
+                acc[k] += c * gto_cartesian(axis_of_orb[mu], a, ra, axis_of_orb[nu], b, rb, k, sasb);
+            }
+          const size_t e = (size_t)(first[A] + mu) * N + first[B] + nu;
+          for (int k = 0; k < 3; ++k) X[k * NN + e] = acc[k];
+        }
+    }
+  free(P); free(first);
+  return N;
+}
+
+/* Core mass of every atom: atomic mass [a.u.] - valence electrons
+ * (src/base/atoms/Atom.h:34). */
+int oracle_core_masses(int theory, int natoms, const int* Z, double* out) {
+  for (int a = 0; a < natoms; ++a) {
+    nddo_atom_params p;
+    if (nddo_fill_atom_params(theory, Z[a], &p) != 0) return -1;
+    out[a] = p.core_mass;
   }
   return 0;
 }

@@ -21,6 +21,9 @@ Reference semantics restated here (file:line in the MolDS tree):
   * E = 1/2 sum P (F + H) + E_core, F and H rebuilt ............. Cndo2.cpp:1324-1416
   * Mulliken q_A = Z_A - sum_mu P_mu,mu ......................... Cndo2.cpp:1187-1199, 1733-1747
   * MNDO heat of formation ...................................... mndo/Mndo.cpp:395-404
+  * dipole: STO-6G Cartesian matrix (C restatement), origin at the
+    centre of core mass, -sum P X + origin * sum P S, core part ... Cndo2.cpp:1871-1944,
+                                                                    base/Molecule.cpp:396-419
 """
 from __future__ import annotations
 
@@ -76,6 +79,8 @@ def lib():
             L.oracle_integrals.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp, dp, dp]
             L.oracle_fock.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp, dp, ctypes.c_int, dp]
             L.oracle_atom_info.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp]
+            L.oracle_cartesian.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp]
+            L.oracle_core_masses.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp]
             L.oracle_sto_overlap_local.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                    ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                    ctypes.c_double]
@@ -127,6 +132,7 @@ class SCFResult:
     charges: np.ndarray
     heat_of_formation: float | None
     trace: list = field(default_factory=list)   # (iter, rms, diis_error, diis_on, damp_on)
+    dipole: np.ndarray | None = None   # (3, 3): total, electronic, core; x y z [a.u.]
 
 
 class NotConverged(RuntimeError):
@@ -166,6 +172,36 @@ def integrals(mol: Molecule):
     if r < 0:
         raise ValueError("oracle_integrals failed")
     return S, eri[:npairs], float(ecore[0])
+
+
+def cartesian_matrix(mol: Molecule) -> np.ndarray:
+    """<mu| r_k |nu> over all AO pairs, (3, N, N) [bohr] (Cndo2.cpp:1946-2130)."""
+    N = num_aos(mol)
+    X = np.zeros((3, N, N))
+    if lib().oracle_cartesian(mol.theory, mol.natoms, _ip(mol.Z), _dp(mol.xyz), _dp(X)) < 0:
+        raise ValueError("element without NDDO parameters")
+    return X
+
+
+def dipole(mol: Molecule, S, P, X=None) -> np.ndarray:
+    """Total, electronic and core dipole moments (rows), x y z [a.u.]:
+    origin c = centre of core mass (base/Molecule.cpp:396-419), core part
+    sum_A Z_A (R_A - c) (Cndo2.cpp:1871-1882), electronic part
+    -sum P X + c sum P S (Cndo2.cpp:1906-1936)."""
+    X = cartesian_matrix(mol) if X is None else X
+    info = atom_info(mol)
+    mass = np.zeros(mol.natoms)
+    lib().oracle_core_masses(mol.theory, mol.natoms, _ip(mol.Z), _dp(mass))
+    center = np.zeros(3)
+    for k in range(3):
+        for a in range(mol.natoms):
+            center[k] += mol.xyz[a, k] * mass[a]
+    center /= mass.sum()
+    core = np.array([sum(info[a, 0] * (mol.xyz[a, k] - center[k]) for a in range(mol.natoms))
+                     for k in range(3)])
+    pop = float(np.dot(P.ravel(), S.ravel()))
+    elec = np.array([-float(np.dot(P.ravel(), X[k].ravel())) + center[k] * pop for k in range(3)])
+    return np.stack([elec + core, elec, core])
 
 
 def fock(mol: Molecule, S, eri, P, guess=False):
@@ -284,7 +320,8 @@ def _properties(mol, S, eri, ecore, P, eps, C, info, iters, trace) -> SCFResult:
     hof = None
     if mol.theory == THEORIES["mndo"]:
         hof = energy - float(info[:, 2].sum()) + float(info[:, 3].sum())
-    return SCFResult(True, iters, energy, ecore, eps, C, P, charges, hof, trace)
+    return SCFResult(True, iters, energy, ecore, eps, C, P, charges, hof, trace,
+                     dipole(mol, S, P))
 
 
 # --------------------------------------------------------------------------

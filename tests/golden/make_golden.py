@@ -4,8 +4,9 @@ Reads the reference's own golden input/output pairs (test/<case>.in and
 test/<case>.dat of the MolDS tree, registered in test/Test_Of_MolDS.rb) and
 keeps, per case, the input text and the printed values that pin the NDDO SCF
 path: the per-iteration RMS density and DIIS error, MO energies, electronic
-energy (incl. core repulsion), core repulsion, Mulliken charges and, for MNDO,
-the heat of formation.  MolDS prints these with %e (7 significant digits,
+energy (incl. core repulsion), core repulsion, Mulliken charges, the total,
+electronic and core dipole moments (x, y, z in a.u.) and, for MNDO, the heat of
+formation.  MolDS prints these with %e (7 significant digits,
 src/cndo/Cndo2.cpp:1087-1089, 1193-1198), so they pin results to ~5e-7 relative.
 
 Usage:  python tests/golden/make_golden.py [/path/to/molds/test]
@@ -36,8 +37,13 @@ def parse_dat(text, natoms):
     ec = float(re.search(r"Core repulsion energy:\t(\S+)", body).group(1))
     q = [float(x) for x in re.findall(r"Mulliken charge\(SCF\):\t0\t\d+\t\S+\t\S+\t(\S+)", body)][:natoms]
     hof = re.search(r"Heats of formation:\t(\S+)", body)
+    dip = []
+    for label in (r"Total Dipole moment\(SCF\):", r"Electronic Dipole moment\(SCF\):",
+                  r"Core Dipole moment:"):
+        m = re.search(label + r"\t+(\S+)\t(\S+)\t(\S+)", body)
+        dip.append([float(m.group(i)) for i in (1, 2, 3)])
     out = {"trace": trace, "mo_energies": mo, "energy": e, "core_repulsion": ec,
-           "mulliken": q}
+           "mulliken": q, "dipole": dip}
     if hof:
         out["heat_of_formation"] = float(hof.group(1))
     return out

@@ -1,7 +1,8 @@
 """The oracle against the golden values of MolDS's own test suite.
 
 tests/golden/reference_fixtures.json holds the reference's printed results
-(7 significant digits) for its 12 SCF-only NDDO cases
+(7 significant digits: energies, MO energies, Mulliken charges, dipole
+moments, iteration trace) for its 12 SCF-only NDDO cases
 (test/{ch4,c2h6,ch3f,ch3cl}_{mndo,am1,pm3}) plus the first SCF of two PM3
 frequency cases (water: O and the H-O core-core rule; ethylene).  Passing here
 is what pins the oracle before it is used to check the CUDA path.
@@ -74,6 +75,17 @@ def test_heat_of_formation(case):
         assert close(r.heat_of_formation, c["heat_of_formation"])
     else:
         assert r.heat_of_formation is None
+
+
+def test_dipole_moments(case):
+    """Total, electronic and core dipole (Cndo2.cpp:1126-1185 prints x, y, z in
+    a.u.): every component to the printed 7 digits; components that are
+    round-off noise in the reference (|mu_k| ~ 1e-11 or below) to 1e-9 a.u."""
+    c, mol, r = case
+    ref = np.array(c["dipole"])
+    assert r.dipole.shape == (3, 3)
+    for mine, theirs in zip(r.dipole.ravel(), ref.ravel()):
+        assert close(mine, theirs, rel=PRINT_REL, abs_=1e-9), (mine, theirs)
 
 
 def test_aos_match(case):
