@@ -16,6 +16,7 @@ replicas (weak scaling) and rank 0 reports the max-over-ranks time.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import multiprocessing as mp
@@ -42,6 +43,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--nmol", type=int, default=N_MOL)
+    ap.add_argument("--dipole", default="on", choices=["on", "off"],
+                    help="dipole moment after convergence (on: as the reference's DoSCF)")
     ap.add_argument("--cpu-sample", type=int, default=48, help="molecules in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=16,
@@ -261,7 +264,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     ctx = M.Context(local)
     mols = workload(rank, args.nmol)
-    params = M.SCFParams(**SCF, precision=args.precision)
+    params = M.SCFParams(**SCF, precision=args.precision, dipole=args.dipole == "on")
     batch = M.ResidentBatch("am1", mols, context=ctx)
 
     batch.profile(True)            # the per-class event pool is created during the warm-up
@@ -296,7 +299,7 @@ def run_ours(args):
     # the context keeps the batch between calls with the same molecules: after
     # the first call a step uploads the coordinates only
     h2d = int(Z.size * 3 * 8)
-    d2h = int(args.nmol * 7 * 8 + Z.size * 8)
+    d2h = int(args.nmol * ctypes.sizeof(M.ScfResultC) + Z.size * 8)
     M.batch_scf("am1", mols, params, context=ctx)       # warm-up: allocates the context's batch
     barrier_sync(dist)
     t0 = time.perf_counter()
@@ -321,7 +324,8 @@ def run_ours(args):
     # ---- plain path: one molecule at a time, FP64, ElectronicStructure ------
     plain = None
     if rank == 0 and args.plain_sample > 0:
-        es = M.ElectronicStructure("am1", M.SCFParams(**SCF, precision="fp64"), context=ctx)
+        es = M.ElectronicStructure("am1", M.SCFParams(**SCF, precision="fp64", dipole=args.dipole == "on"),
+                                   context=ctx)
         lat = []
         for i, m in enumerate(mols[:args.plain_sample] * 2):
             t0 = time.perf_counter()
@@ -386,7 +390,7 @@ def run_ours(args):
                 "data": "synthetic: seeded (H2O)32 replicas (no public dataset is named for this path)",
                 "config": {"workload": f"{args.nmol} replicas of (H2O)32 per GPU, AM1, batched SCF to RMS 1e-8",
                            "molecules_per_gpu": args.nmol, "atoms": 96, "basis_functions": 192, "occupied": 128,
-                           "precision": args.precision, "scf": SCF,
+                           "precision": args.precision, "scf": SCF, "dipole": args.dipole == "on",
                            "l2": f"inputs larger than L2: {batch.device_bytes() / 1e9:.2f} GB resident per GPU",
                            "parallelism": f"replicas x{world} (molecules sharded, no collective)"},
                 "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -452,7 +456,7 @@ def run_alkanes(args):
     nao = np.array([int(sum(4 if z > 1 else 1 for z in m.Z)) for m in mols])
     steps = args.steps if args.steps != 10 else 2
     warm = args.warmup if args.warmup != 3 else 1
-    params = M.SCFParams(**SCF, precision=args.precision)
+    params = M.SCFParams(**SCF, precision=args.precision, dipole=args.dipole == "on")
     batch = M.ResidentBatch("pm3", mols, context=ctx)
     batch.profile(True)
     for _ in range(warm):
@@ -504,7 +508,7 @@ def run_alkanes(args):
             "data": f"synthetic: {args.alkanes} seeded random alkanes (seed 3e6 + j), generated in {t_gen:.1f} s",
             "config": {"workload": f"{args.alkanes} alkanes CnH2n+2, n uniform 3..60, PM3, one batch",
                        "basis_min_median_max": [int(nao.min()), int(np.median(nao)), int(nao.max())],
-                       "precision": args.precision, "scf": SCF,
+                       "precision": args.precision, "scf": SCF, "dipole": args.dipole == "on",
                        "l2": f"inputs larger than L2: {batch.device_bytes() / 1e9:.2f} GB resident"},
             "gpu_launches": launches, "kernels_ms": {k: round(v["ms"] / steps, 3) for k, v in kt.items()},
             "convergence": {"converged": int(conv.sum()), "fp64_converged": int(conv64.sum()),
@@ -632,7 +636,7 @@ def run_serving(args):
     mols = [m for _, m in stream]
     nao = [int(sum(4 if z > 1 else 1 for z in m.Z)) for m in mols]
     ctx = M.Context(0)
-    params = M.SCFParams(**SCF, precision=args.precision)
+    params = M.SCFParams(**SCF, precision=args.precision, dipole=args.dipole == "on")
     srv = M.Server(params, hbm_budget_bytes=int(args.hbm_gb * (1 << 30)), max_basis=args.max_basis, context=ctx)
     # warm-up: one small and one large request
     srv.submit("pm3", W.water_cluster_k(8, 1))

@@ -51,6 +51,7 @@ typedef struct {
   int precision;               /* NDDO_PRECISION_FP64 or NDDO_PRECISION_MIXED */
   double fp64_switch_error;    /* mixed: FP64 phase once the DIIS error is below this */
   int tensor_cores;            /* mixed: FP32-phase GEMMs on the tensor cores (1, default) or CUDA cores (0) */
+  int dipole;                  /* dipole moment after convergence (1, default, as DoSCF) or skipped (0) */
 } nddo_scf_params;
 
 typedef struct {
@@ -61,6 +62,8 @@ typedef struct {
   double heat_of_formation;    /* [Eh]; meaningful for MNDO only             */
   double final_rms;            /* last RMS density change                    */
   double final_diis_error;     /* last DIIS error (max |P_new - P_old|)      */
+  double dipole[9];            /* total, electronic, core dipole (x, y, z) [a.u.]; 0 with dipole = 0
+                                  (Cndo2::OutputSCFDipole, src/cndo/Cndo2.cpp:1126-1185) */
 } nddo_scf_result;
 
 /* Defaults of src/base/Parameters.cpp:133-139 (precision = FP64). */
@@ -91,6 +94,15 @@ int nddo_get_fock_matrix(nddo_ctx* ctx, double* out_nn);         /* GetFockMatri
 int nddo_get_density(nddo_ctx* ctx, double* out_nn);             /* orbital electron population P   */
 int nddo_get_mulliken(nddo_ctx* ctx, double* out_natoms);        /* Mulliken charges (Cndo2.cpp:1187-1199) */
 int nddo_get_core_hamiltonian(nddo_ctx* ctx, double* out_nn);    /* H = F(P = 0) (Cndo2.cpp:1359-1367) */
+/* Total, electronic and core dipole moments (x, y, z each) [a.u.] of the last
+ * SCF: origin at the centre of core mass, electronic part -sum P X + c sum P S
+ * (Cndo2::CalcElectronicDipoleMomentGroundState / CalcCoreDipoleMoment,
+ * src/cndo/Cndo2.cpp:1871-1944). */
+int nddo_get_dipole(nddo_ctx* ctx, double* out9);
+/* STO-6G Cartesian matrix <mu| r_k |nu> [bohr], 3 x N x N doubles (k = x, y, z):
+ * MolDS's cartesianMatrix (Cndo2::CalcCartesianMatrixByGTOExpansion,
+ * src/cndo/Cndo2.cpp:1946-2130).  Needs only a molecule. */
+int nddo_get_cartesian_matrix(nddo_ctx* ctx, double* out_3nn);
 /* Per-iteration log of Cndo2::SatisfyConvergenceCriterion (Cndo2.cpp:1505-1510). */
 int nddo_get_trace(nddo_ctx* ctx, int max_entries, double* rms, double* diis_error, int* diis_on, int* damp_on);
 /* Packed space-frame (mu nu|la si) blocks of all atom pairs a < b, row-major

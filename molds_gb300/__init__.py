@@ -46,13 +46,15 @@ class ScfParamsC(ctypes.Structure):
                 ("damping_thresh", ctypes.c_double), ("damping_weight", ctypes.c_double),
                 ("diis_num_error_vect", ctypes.c_int), ("diis_start_error", ctypes.c_double),
                 ("diis_end_error", ctypes.c_double), ("precision", ctypes.c_int),
-                ("fp64_switch_error", ctypes.c_double), ("tensor_cores", ctypes.c_int)]
+                ("fp64_switch_error", ctypes.c_double), ("tensor_cores", ctypes.c_int),
+                ("dipole", ctypes.c_int)]
 
 
 class ScfResultC(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("energy", ctypes.c_double),
                 ("core_repulsion", ctypes.c_double), ("heat_of_formation", ctypes.c_double),
-                ("final_rms", ctypes.c_double), ("final_diis_error", ctypes.c_double)]
+                ("final_rms", ctypes.c_double), ("final_diis_error", ctypes.c_double),
+                ("dipole", ctypes.c_double * 9)]
 
 
 class ServeResultC(ctypes.Structure):
@@ -81,6 +83,8 @@ SIGNATURES = {
     "nddo_get_density": (ctypes.c_int, [_CTX, _DP]),
     "nddo_get_mulliken": (ctypes.c_int, [_CTX, _DP]),
     "nddo_get_core_hamiltonian": (ctypes.c_int, [_CTX, _DP]),
+    "nddo_get_dipole": (ctypes.c_int, [_CTX, _DP]),
+    "nddo_get_cartesian_matrix": (ctypes.c_int, [_CTX, _DP]),
     "nddo_get_trace": (ctypes.c_int, [_CTX, ctypes.c_int, _DP, _DP, _IP, _IP]),
     "nddo_get_pair_blocks": (ctypes.c_int, [_CTX, _DP, ctypes.POINTER(ctypes.c_size_t)]),
     "nddo_batch_scf": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, ctypes.POINTER(ScfParamsC),
@@ -156,7 +160,13 @@ def to_c_params(p: SCFParams) -> ScfParamsC:
     c.precision = 1 if str(p.precision).lower() == "mixed" else 0
     c.fp64_switch_error = float(p.fp64_switch_error)
     c.tensor_cores = 1 if getattr(p, "tensor_cores", True) else 0
+    c.dipole = 1 if getattr(p, "dipole", True) else 0
     return c
+
+
+def _dipole3(r) -> np.ndarray:
+    """(3, 3): total, electronic, core dipole rows, x y z [a.u.]."""
+    return np.array(r.dipole[:], dtype=np.float64).reshape(3, 3)
 
 
 class Context:
@@ -269,6 +279,15 @@ class ElectronicStructure:
     def GetMullikenCharges(self) -> np.ndarray:
         return self._vec(self.ctx.lib.nddo_get_mulliken, self.molecule.natoms)
 
+    def GetDipoleMoments(self) -> np.ndarray:
+        """(3, 3): total, electronic and core dipole (rows), x y z [a.u.]
+        (the three lines of Cndo2::OutputSCFDipole, src/cndo/Cndo2.cpp:1126-1185)."""
+        return self._vec(self.ctx.lib.nddo_get_dipole, 9).reshape(3, 3)
+
+    def GetCartesianMatrix(self) -> np.ndarray:
+        """STO-6G <mu| r_k |nu>, (3, N, N) [bohr] (Cndo2.cpp:1946-2130)."""
+        return self._vec(self.ctx.lib.nddo_get_cartesian_matrix, 3 * self.n * self.n).reshape(3, self.n, self.n)
+
     def GetCoreHamiltonian(self) -> np.ndarray:
         return self._vec(self.ctx.lib.nddo_get_core_hamiltonian, self.n * self.n).reshape(self.n, self.n)
 
@@ -317,7 +336,7 @@ def batch_scf(theory, molecules, params: SCFParams | None = None, context: Conte
         ctx.check(rc)
     out = [dict(status=r.status, iterations=r.iterations, energy=r.energy, core_repulsion=r.core_repulsion,
                 heat_of_formation=r.heat_of_formation, final_rms=r.final_rms,
-                final_diis_error=r.final_diis_error) for r in res]
+                final_diis_error=r.final_diis_error, dipole=_dipole3(r)) for r in res]
     offs = np.concatenate([[0], np.cumsum(nat)])
     return out, [ch[offs[i]:offs[i + 1]] for i in range(len(molecules))]
 
@@ -356,7 +375,7 @@ class ResidentBatch:
         offs = np.concatenate([[0], np.cumsum(self.nat)])
         out = [dict(status=r.status, iterations=r.iterations, energy=r.energy, core_repulsion=r.core_repulsion,
                     heat_of_formation=r.heat_of_formation, final_rms=r.final_rms,
-                    final_diis_error=r.final_diis_error) for r in res]
+                    final_diis_error=r.final_diis_error, dipole=_dipole3(r)) for r in res]
         return out, [ch[offs[i]:offs[i + 1]] for i in range(self.n)]
 
     def device_bytes(self) -> int:

@@ -16,6 +16,7 @@ struct nddo_batch {
   nddo_ctx* ctx;
   std::unique_ptr<nddo::GroupedBatch> b;
   std::vector<int> n_atoms;
+  bool dipole = false;          // the last nddo_batch_run computed dipole moments
 };
 
 namespace {
@@ -98,6 +99,7 @@ nddo::ScfSettings to_settings(const nddo_scf_params* p) {
     s.precision = p->precision;
     s.switch_error = p->fp64_switch_error;
     s.tensor_cores = p->tensor_cores;
+    s.dipole = p->dipole;
   }
   return s;
 }
@@ -144,6 +146,7 @@ void nddo_default_params(nddo_scf_params* p) {
   p->precision = NDDO_PRECISION_FP64;
   p->fp64_switch_error = 1e-4;
   p->tensor_cores = 1;
+  p->dipole = 1;
 }
 
 int nddo_create(int device, size_t hbm_budget_bytes, nddo_ctx** out) {
@@ -254,6 +257,7 @@ int nddo_scf(nddo_ctx* ctx, const nddo_scf_params* params, int requires_guess, n
       result->heat_of_formation = r[0].heat_of_formation;
       result->final_rms = r[0].final_rms;
       result->final_diis_error = r[0].final_diis_error;
+      for (int k = 0; k < 9; ++k) result->dipole[k] = s.dipole ? r[0].dipole[k] : 0.0;
     }
     if (r[0].status != nddo::kConverged)
       return fail(ctx, NDDO_NOT_CONVERGED,
@@ -277,6 +281,27 @@ int nddo_get_energies_mo(nddo_ctx* ctx, double* out) { return getter(ctx, out, 1
 int nddo_get_fock_matrix(nddo_ctx* ctx, double* out) { return getter(ctx, out, 3); }
 int nddo_get_density(nddo_ctx* ctx, double* out) { return getter(ctx, out, 2); }
 int nddo_get_mulliken(nddo_ctx* ctx, double* out) { return getter(ctx, out, 11); }
+
+int nddo_get_dipole(nddo_ctx* ctx, double* out) {
+  return guarded(ctx, [&]() {
+    if (!ctx->mol || !ctx->has_scf) return fail(ctx, NDDO_ERR_STATE, "no SCF result");
+    if (!out) return fail(ctx, NDDO_ERR_ARGUMENT, "null output buffer");
+    if (!ctx->last_settings.dipole) return fail(ctx, NDDO_ERR_STATE, "the last SCF ran with dipole = 0");
+    std::vector<nddo::MolResult> r;
+    ctx->mol->results(&r);
+    for (int k = 0; k < 9; ++k) out[k] = r[0].dipole[k];
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_get_cartesian_matrix(nddo_ctx* ctx, double* out) {
+  return guarded(ctx, [&]() {
+    if (!ctx->mol) return fail(ctx, NDDO_ERR_STATE, "A molecule is not set.");
+    if (!out) return fail(ctx, NDDO_ERR_ARGUMENT, "null output buffer");
+    ctx->mol->cartesian_matrix(0, out);
+    return (int)NDDO_OK;
+  });
+}
 
 int nddo_get_core_hamiltonian(nddo_ctx* ctx, double* out) {
   return guarded(ctx, [&]() {
@@ -369,6 +394,7 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
       results[i].heat_of_formation = r[i].heat_of_formation;
       results[i].final_rms = r[i].final_rms;
       results[i].final_diis_error = r[i].final_diis_error;
+      for (int k = 0; k < 9; ++k) results[i].dipole[k] = s.dipole ? r[i].dipole[k] : 0.0;
       if (r[i].status != nddo::kConverged) rc = NDDO_NOT_CONVERGED;
       if (charges) b.copy_charges(i, charges + off);
       off += n_atoms[i];
@@ -415,7 +441,9 @@ int nddo_batch_run(nddo_batch* h, const nddo_scf_params* params) {
     if (!valid_params(params, &why)) return fail(h->ctx, NDDO_ERR_ARGUMENT, why);
     nddo::ScfSettings s = to_settings(params);
     s.keep_trace = 0;
+    h->dipole = false;
     h->b->run(s);
+    h->dipole = s.dipole != 0;
     return (int)NDDO_OK;
   });
 }
@@ -445,6 +473,7 @@ int nddo_batch_results(nddo_batch* h, nddo_scf_result* results, double* charges)
       results[i].heat_of_formation = r[i].heat_of_formation;
       results[i].final_rms = r[i].final_rms;
       results[i].final_diis_error = r[i].final_diis_error;
+      for (int k = 0; k < 9; ++k) results[i].dipole[k] = h->dipole ? r[i].dipole[k] : 0.0;
       if (r[i].status != nddo::kConverged) rc = NDDO_NOT_CONVERGED;
       if (charges) h->b->copy_charges((int)i, charges + off);
       off += h->n_atoms[i];

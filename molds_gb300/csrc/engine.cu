@@ -309,6 +309,7 @@ void Batch::allocate(const BatchCapacity& cap) {
     cuda_check(cudaMalloc(&d_diis_ws, b), "cudaMalloc DIIS scratch");
     bytes_ += b;
   }
+  d_dip_ws = dalloc<double>((size_t)nm * kDipChunks * 4, &bytes_);
   d_active = dalloc<char>(nm, &bytes_);
   cuda_check(cudaMemsetAsync(d_state, 0, nm * sizeof(MolState), stream_), "memset state");
   cuda_check(cudaMemsetAsync(d_sweeps, 0, nm * sizeof(int), stream_), "memset sweeps");
@@ -428,7 +429,7 @@ Batch::~Batch() {
   if (d_diis_ws) cudaFree(d_diis_ws);
   void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
                   d_hist_dens, d_hist_err, d_G32, d_T32, d_Cf, d_Cnf, d_Ff, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
-                  d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs, d_tc_err};
+                  d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs, d_tc_err, d_dip_ws};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
 }
@@ -547,7 +548,7 @@ int Batch::list_max_atoms() const {
 const char* kernel_class_name(int k) {
   static const char* names[kKNumClasses] = {"pair_integrals", "core_hamiltonian", "fock_build", "basis_orthonormalise",
                                             "warm_start_transform", "jacobi_eigensolver", "density", "fp64_refinement",
-                                            "diis", "energy"};
+                                            "diis", "energy", "dipole"};
   return (k >= 0 && k < kKNumClasses) ? names[k] : "?";
 }
 
@@ -936,15 +937,21 @@ void Batch::copy_charges_async(int m, double* host) {
 }
 
 void Batch::finish(const ScfSettings& s, const std::vector<int>& which) {
-  (void)s;
   upload_list(which);
   const int nl = (int)which.size();
+  const int max_atoms = list_max_atoms();
   launches_ += 2;
   int h = prof_begin(kKEnergy, 0.0);
-  launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, list_max_atoms(), d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0,
+  launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, max_atoms, d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0,
                      0, 0, stream_);
   launch_energy_kernel(d_atoms, d_mols, d_list, nl, d_P, d_F, d_H, d_state, d_charges, stream_);
   prof_end(h);
+  if (s.dipole) {
+    launches_ += 2;
+    h = prof_begin(kKDipole, 0.0);
+    launch_dipole(d_atoms, d_pairs, d_mols, d_list, nl, max_atoms, d_P, d_H, d_dip_ws, d_state, stream_);
+    prof_end(h);
+  }
   cuda_check(cudaGetLastError(), "finish");
 }
 
@@ -977,7 +984,21 @@ void Batch::results(std::vector<MolResult>* out) {
     r.heat_of_formation = st[m].heat_of_formation;
     r.final_rms = st[m].rms;
     r.final_diis_error = st[m].diis_err;
+    for (int k = 0; k < 9; ++k) r.dipole[k] = st[m].dipole[k];
   }
+}
+
+void Batch::cartesian_matrix(int m, double* host) const {
+  const DevMol& d = h_mols[m];
+  const size_t bytes = 3 * (size_t)d.nao * d.nao * sizeof(double);
+  double* X = nullptr;
+  cuda_check(cudaMalloc(&X, bytes), "cudaMalloc cartesian matrix");
+  launch_cartesian_matrix(d_atoms, d_pairs, d_mols, m, d.natoms, X, stream_);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, X, bytes, cudaMemcpyDeviceToHost, stream_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  cudaFree(X);
+  cuda_check(e, "cartesian matrix");
 }
 
 void Batch::copy_matrix(int which, int m, double* host) const {

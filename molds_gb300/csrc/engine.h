@@ -29,11 +29,13 @@ struct ScfSettings {
   int max_sweeps = 30;
   int keep_trace = 1;
   int tensor_cores = 1;         // mixed: FP32-phase GEMMs on tcgen05 (3xTF32) instead of CUDA cores
+  int dipole = 1;               // dipole moment after convergence (MolDS DoSCF always computes it)
 };
 
 // kernel classes timed by the optional per-launch CUDA-event profiler
 enum KernelClass {
-  kKPair = 0, kKHcore, kKFock, kKOrtho, kKTransform, kKJacobi, kKDensity, kKRefine, kKDiis, kKEnergy, kKNumClasses
+  kKPair = 0, kKHcore, kKFock, kKOrtho, kKTransform, kKJacobi, kKDensity, kKRefine, kKDiis, kKEnergy, kKDipole,
+  kKNumClasses
 };
 const char* kernel_class_name(int k);
 
@@ -41,6 +43,7 @@ struct MolResult {
   int status = 0;               // MolStatus
   int iterations = 0;
   double energy = 0, core_repulsion = 0, heat_of_formation = 0, final_rms = 0, final_diis_error = 0;
+  double dipole[9] = {};        // total, electronic, core (x, y, z) [a.u.] when ScfSettings::dipole
 };
 
 class Engine;
@@ -119,6 +122,8 @@ class Batch {
   void copy_charges(int m, double* host) const;
   void copy_blocks(int m, double* host, size_t* count) const;
   void copy_trace(int m, std::vector<TraceEntry>* out) const;
+  // STO-6G Cartesian matrix <mu| r_k |nu> of molecule m, 3 x N x N doubles (synchronises)
+  void cartesian_matrix(int m, double* host) const;
   void set_density(int m, const double* host);
 
   const std::vector<DevMol>& mol_table() const { return h_mols; }
@@ -184,8 +189,9 @@ class Batch {
   double* d_charges = nullptr;
   int* d_sweeps = nullptr;
   int* d_count = nullptr;
-  int* d_tc_err = nullptr;
-  void* d_diis_ws = nullptr;             // DIIS partial sums and decisions (diis_scratch_bytes)               // set by a tensor-core GEMM whose MMA wait ran out
+  int* d_tc_err = nullptr;               // set by a tensor-core GEMM whose MMA wait ran out
+  void* d_diis_ws = nullptr;             // DIIS partial sums and decisions (diis_scratch_bytes)
+  double* d_dip_ws = nullptr;            // dipole partial sums (slots x kDipChunks x 4)
   char* d_active = nullptr;
 
   // current molecule list and its GEMM job tables
@@ -238,6 +244,7 @@ class GroupedBatch {
   void results(std::vector<MolResult>* out);
   void copy_charges(int m, double* host) const;
   void copy_matrix(int which_matrix, int m, double* host) const;
+  void cartesian_matrix(int m, double* host) const;
   void set_coordinates(const double* xyz);
   size_t device_bytes() const;
   long long launches() const;

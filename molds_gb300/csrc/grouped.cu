@@ -98,6 +98,12 @@ void GroupedBatch::copy_matrix(int which, int m, double* host) const {
   b.copy_matrix(which, l, host);
 }
 
+void GroupedBatch::cartesian_matrix(int m, double* host) const {
+  int l = 0;
+  const Batch& b = locate(m, &l);
+  b.cartesian_matrix(l, host);
+}
+
 void GroupedBatch::set_coordinates(const double* xyz) {
   for (size_t g = 0; g < g_.size(); ++g) g_[g]->set_coordinates(xyz + 3 * (size_t)first_atom_[g]);
 }

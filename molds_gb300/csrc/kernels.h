@@ -76,6 +76,14 @@ void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol
 void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* mol_list, int nlist,
                           const double* P, const double* F, const double* H, MolState* st, double* charges,
                           cudaStream_t s);
+// dipole moment of the listed molecules into MolState::dipole; partial holds
+// nlist * kDipChunks * 4 doubles
+constexpr int kDipChunks = 64;
+void launch_dipole(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list, int nlist,
+                   int max_atoms, const double* P, const double* H, double* partial, MolState* st, cudaStream_t s);
+// STO-6G Cartesian matrix of molecule m: X = 3 x N x N doubles
+void launch_cartesian_matrix(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, int m, int natoms,
+                             double* X, cudaStream_t s);
 
 // jacobi.cu
 bool jacobi_needs_workspace(int max_n, int elem, bool* a_global, bool* v_global);

@@ -52,6 +52,7 @@ struct MolState {
   int flags;
   double rms, diis_err, ecore, energy, heat_of_formation, energy_electronic;
   double B[kMaxDiis * kMaxDiis];   // <e_i, e_j> over ring slots
+  double dipole[9];   // total, electronic, core dipole (x, y, z each) [a.u.] after convergence
 };
 
 struct TraceEntry {

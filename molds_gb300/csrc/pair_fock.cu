@@ -24,6 +24,7 @@
 //     (:490-580), GetCoulombInt/GetExchangeInt (:583-639), GetElectronCoreAttraction
 //     (:643-650).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include "nddo_batch.cuh"
 #include "kernels.h"
 
@@ -31,6 +32,8 @@ namespace nddo {
 
 __constant__ nddo_atom_params c_params[kNumParamSlots];
 __constant__ double c_inv[128];   // c_inv[j] = 1 / j
+__constant__ double c_sto_exp[3][2][6];    // STO-6G exponents (zeta = 1), shell K/L/M, s/p
+__constant__ double c_sto_coef[3][2][6];   // STO-6G contraction coefficients
 
 void upload_params(const nddo_atom_params* p, cudaStream_t s) {
   static double inv[128];
@@ -39,6 +42,8 @@ void upload_params(const nddo_atom_params* p, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_params, p, sizeof(nddo_atom_params) * kNumParamSlots, 0,
                           cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_inv, inv, sizeof(inv), 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_sto_exp, nddo_sto6g_exp, sizeof(nddo_sto6g_exp), 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_sto_coef, nddo_sto6g_coef, sizeof(nddo_sto6g_coef), 0, cudaMemcpyHostToDevice, s);
 }
 
 __device__ __forceinline__ double sel3(int i, double a, double b, double c) {
@@ -628,6 +633,299 @@ void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* m
                           cudaStream_t s) {
   if (nlist <= 0) return;
   energy_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, mols, mol_list, P, F, H, st, charges);
+}
+
+// ---------------------------------------------------------------------------
+// (c) Dipole moment after convergence.
+//
+// MolDS builds the Cartesian matrix X_k,mu,nu = <mu| r_k |nu> of every AO pair
+// (same atom included) from the STO-6G expansion of each Slater orbital
+// (Cndo2::CalcCartesianMatrixByGTOExpansion, src/cndo/Cndo2.cpp:1946-2130) and
+// then forms mu_elec = -sum P X + c sum P S with c the centre of core mass,
+// and mu_core = sum_A Z_A (R_A - c) (Cndo2.cpp:1871-1944).  Here the matrix is
+// never stored: each thread takes one atom pair (or one atom), evaluates the
+// pair's X block shell pair by shell pair and contracts it with P on the fly.
+//
+// Primitive integrals: normalised Cartesian Gaussians, s = N e^{-a|r-A|^2},
+// p_i = 2 sqrt(a) (r_i - A_i) s.  With p = a + b, the product centre Pc,
+// PA = Pc - A, PB = Pc - B and h = 1/(2p), the one-dimensional moments of
+// (x-A)^i (x-B)^j follow from the Obara-Saika recurrence:
+//   s10 = PA, s01 = PB, s11 = PA PB + h, s02 = PB^2 + h, s12 = PA PB^2 + (PA + 2 PB) h,
+// and x = (x - B) + B turns them into moments of the position operator:
+//   m00 = Pc, m10 = s11 + B PA, m01 = s02 + B PB, m11 = s12 + B s11.
+// The three-dimensional integral is (s|s) times the product over directions.
+// ---------------------------------------------------------------------------
+constexpr int kDipThreads = 256;
+
+// X block of one shell pair, summed over the 6 x 6 primitive pairs:
+// out[k][i][j], k the axis of r, i / j the p axis (0 for an s shell).
+template <int LA, int LB>
+__device__ __forceinline__ void cart_shell_block(const double* ra, const double* rb, const double* d, double R2,
+                                                 int shA, double zA, int shB, double zB,
+                                                 double (&out)[3][LA ? 3 : 1][LB ? 3 : 1]) {
+  constexpr int NA = LA ? 3 : 1, NB = LB ? 3 : 1;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int i = 0; i < NA; ++i)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) out[k][i][j] = 0.0;
+  const double zA2 = zA * zA, zB2 = zB * zB;
+#pragma unroll 1
+  for (int i6 = 0; i6 < 6; ++i6) {
+    const double a = zA2 * c_sto_exp[shA][LA][i6];
+    const double ca = c_sto_coef[shA][LA][i6] * (LA ? 2.0 * sqrt(a) : 1.0);
+#pragma unroll 1
+    for (int j6 = 0; j6 < 6; ++j6) {
+      const double b = zB2 * c_sto_exp[shB][LB][j6];
+      const double ip = 1.0 / (a + b);
+      const double t = 2.0 * sqrt(a * b) * ip;
+      const double w = ca * c_sto_coef[shB][LB][j6] * (LB ? 2.0 * sqrt(b) : 1.0) * (t * sqrt(t)) *
+                       exp(-(a * b * ip) * R2);
+      const double h = 0.5 * ip;
+      double Pc[3], PA[3], PB[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        Pc[q] = (a * ra[q] + b * rb[q]) * ip;
+        PA[q] = -b * ip * d[q];
+        PB[q] = a * ip * d[q];
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int i = 0; i < NA; ++i)
+#pragma unroll
+          for (int j = 0; j < NB; ++j) {
+            double v;
+            if (!LA && !LB) {
+              v = Pc[k];
+            } else if (!LA) {
+              v = (k == j) ? PB[j] * PB[j] + h + rb[j] * PB[j] : PB[j] * Pc[k];
+            } else if (!LB) {
+              v = (k == i) ? PA[i] * PB[i] + h + rb[i] * PA[i] : PA[i] * Pc[k];
+            } else if (i == j) {
+              const double s11 = PA[i] * PB[i] + h;
+              v = (k == i) ? PA[i] * PB[i] * PB[i] + (PA[i] + 2.0 * PB[i]) * h + rb[i] * s11 : s11 * Pc[k];
+            } else {
+              v = (k == i)   ? (PA[i] * PB[i] + h + rb[i] * PA[i]) * PB[j]
+                  : (k == j) ? PA[i] * (PB[j] * PB[j] + h + rb[j] * PB[j])
+                             : PA[i] * PB[j] * Pc[k];
+            }
+            out[k][i][j] += w * v;
+          }
+    }
+  }
+}
+
+// AO index within an atom of p axis i (MolDS order s, py, pz, px)
+__device__ __forceinline__ int ao_of_axis(int i) { return i == 0 ? 3 : i; }
+
+// acc[k] += sum over the shell pair of W_mu,nu X_k,mu,nu
+template <int LA, int LB>
+__device__ __forceinline__ void cart_shell_contract(const double* ra, const double* rb, const double* d, double R2,
+                                                    int shA, double zA, int shB, double zB, const double (&W)[4][4],
+                                                    double* acc) {
+  double blk[3][LA ? 3 : 1][LB ? 3 : 1];
+  cart_shell_block<LA, LB>(ra, rb, d, R2, shA, zA, shB, zB, blk);
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int i = 0; i < (LA ? 3 : 1); ++i)
+#pragma unroll
+      for (int j = 0; j < (LB ? 3 : 1); ++j)
+        acc[k] += W[LA ? ao_of_axis(i) : 0][LB ? ao_of_axis(j) : 0] * blk[k][i][j];
+}
+
+// CTAs of one molecule's dipole sums: a function of the molecule alone, so a
+// molecule's result does not depend on the batch it runs in.
+__host__ __device__ __forceinline__ int dipole_chunks(int natoms) {
+  const long long items = (long long)natoms + (long long)natoms * (natoms - 1) / 2;
+  const long long c = (items + 2LL * kDipThreads - 1) / (2LL * kDipThreads);
+  return (int)(c < 1 ? 1 : (c > kDipChunks ? kDipChunks : c));
+}
+
+// One work item: atom t of the molecule (t < natoms, the same-atom block) or
+// atom pair t - natoms (a < b).  Returns the batch-global atom indices.
+__device__ __forceinline__ void dipole_item(const DevMol& mol, const DevPair* __restrict__ pairs, long long t,
+                                            int* ia, int* ib) {
+  if (t < mol.natoms) {
+    *ia = *ib = mol.atom0 + (int)t;
+  } else {
+    const DevPair pr = pairs[mol.pair0 + (t - mol.natoms)];
+    *ia = pr.a;
+    *ib = pr.b;
+  }
+}
+
+// Partial sums per CTA: sum W X (x, y, z) and sum P S.  W = P_mu,nu + P_nu,mu
+// for two different atoms (both triangles of MolDS's full-matrix dot product),
+// P_mu,nu within one atom.  The inter-atom block of H is exactly
+// 1/2 (beta_mu + beta_nu) S_mu,nu, so S is read back from H; within an atom S
+// is the identity (Cndo2.cpp:4135-4140).
+__global__ void __launch_bounds__(kDipThreads)
+dipole_partial_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs,
+                      const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+                      const double* __restrict__ P, const double* __restrict__ H, double* __restrict__ partial) {
+  __shared__ double red[kDipThreads / 32][4];
+  const DevMol mol = mols[mol_list[blockIdx.y]];
+  const int chunks = dipole_chunks(mol.natoms);
+  if ((int)blockIdx.x >= chunks) return;
+  const long long items = (long long)mol.natoms + mol.npairs;
+  const long long ld = mol.nao;
+  const double* Pm = P + mol.mat0;
+  const double* Hm = H + mol.mat0;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < items;
+       t += (long long)chunks * blockDim.x) {
+    int ia, ib;
+    dipole_item(mol, pairs, t, &ia, &ib);
+    const DevAtom A = atoms[ia], B = atoms[ib];
+    const nddo_atom_params& pa = c_params[A.pidx];
+    const nddo_atom_params& pb = c_params[B.pidx];
+    const bool same = ia == ib;
+    double W[4][4];
+#pragma unroll
+    for (int mu = 0; mu < 4; ++mu)
+#pragma unroll
+      for (int nu = 0; nu < 4; ++nu) {
+        double w = 0.0;
+        if (mu < A.nao && nu < B.nao) {
+          const long long r = A.ao0 + mu, c = B.ao0 + nu;
+          w = Pm[r * ld + c];
+          if (!same) {
+            w += Pm[c * ld + r];
+            acc[3] += w * (2.0 * Hm[r * ld + c] / (pa.beta[mu == 0 ? 0 : 1] + pb.beta[nu == 0 ? 0 : 1]));
+          } else if (mu == nu) {
+            acc[3] += w;
+          }
+        }
+        W[mu][nu] = w;
+      }
+    const double ra[3] = {A.x, A.y, A.z}, rb[3] = {B.x, B.y, B.z};
+    const double d[3] = {ra[0] - rb[0], ra[1] - rb[1], ra[2] - rb[2]};
+    const double R2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const int shA = pa.principal_n - 1, shB = pb.principal_n - 1;
+    cart_shell_contract<0, 0>(ra, rb, d, R2, shA, pa.zeta[0], shB, pb.zeta[0], W, acc);
+    if (B.nao > 1) cart_shell_contract<0, 1>(ra, rb, d, R2, shA, pa.zeta[0], shB, pb.zeta[1], W, acc);
+    if (A.nao > 1) cart_shell_contract<1, 0>(ra, rb, d, R2, shA, pa.zeta[1], shB, pb.zeta[0], W, acc);
+    if (A.nao > 1 && B.nao > 1) cart_shell_contract<1, 1>(ra, rb, d, R2, shA, pa.zeta[1], shB, pb.zeta[1], W, acc);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const double v = warp_sum(acc[q]);
+    if (lane == 0) red[warp][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double v = 0.0;
+    for (int w = 0; w < kDipThreads / 32; ++w) v += red[w][threadIdx.x];
+    partial[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 4 + threadIdx.x] = v;
+  }
+}
+
+// One thread per molecule: chunk sums in a fixed order, the centre of core
+// mass (src/base/Molecule.cpp:396-419), the core dipole and the electronic
+// dipole; MolState::dipole = total, electronic, core (x, y, z each).
+__global__ void dipole_finish_kernel(const DevAtom* __restrict__ atoms, const DevMol* __restrict__ mols,
+                                     const int* __restrict__ mol_list, int nlist, int grid_chunks,
+                                     const double* __restrict__ partial, MolState* __restrict__ st) {
+  const int li = blockIdx.x * blockDim.x + threadIdx.x;
+  if (li >= nlist) return;
+  const int m = mol_list[li];
+  const DevMol mol = mols[m];
+  const int chunks = dipole_chunks(mol.natoms);
+  double sum[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int c = 0; c < chunks; ++c)
+    for (int q = 0; q < 4; ++q) sum[q] += partial[((long long)li * grid_chunks + c) * 4 + q];
+  double center[3] = {0.0, 0.0, 0.0}, mass = 0.0;
+  for (int a = 0; a < mol.natoms; ++a) {
+    const DevAtom A = atoms[mol.atom0 + a];
+    const double cm = c_params[A.pidx].core_mass;
+    mass += cm;
+    center[0] += A.x * cm;
+    center[1] += A.y * cm;
+    center[2] += A.z * cm;
+  }
+  for (int k = 0; k < 3; ++k) center[k] /= mass;
+  double core[3] = {0.0, 0.0, 0.0};
+  for (int a = 0; a < mol.natoms; ++a) {
+    const DevAtom A = atoms[mol.atom0 + a];
+    const double z = c_params[A.pidx].core_charge;
+    core[0] += z * (A.x - center[0]);
+    core[1] += z * (A.y - center[1]);
+    core[2] += z * (A.z - center[2]);
+  }
+  MolState* s = st + m;
+  for (int k = 0; k < 3; ++k) {
+    const double elec = -sum[k] + center[k] * sum[3];
+    s->dipole[k] = elec + core[k];
+    s->dipole[3 + k] = elec;
+    s->dipole[6 + k] = core[k];
+  }
+}
+
+
+void launch_dipole(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list, int nlist,
+                   int max_atoms, const double* P, const double* H, double* partial, MolState* st, cudaStream_t s) {
+  if (nlist <= 0) return;
+  const int chunks = dipole_chunks(max_atoms);   // the largest molecule's count sets the grid
+  dipole_partial_kernel<<<dim3(chunks, nlist), kDipThreads, 0, s>>>(atoms, pairs, mols, mol_list, P, H, partial);
+  dipole_finish_kernel<<<(nlist + 127) / 128, 128, 0, s>>>(atoms, mols, mol_list, nlist, chunks, partial, st);
+}
+
+// Stores the X block of one shell pair at (mu, nu) and (nu, mu).
+template <int LA, int LB>
+__device__ __forceinline__ void cart_shell_store(const double* ra, const double* rb, const double* d, double R2,
+                                                 int shA, double zA, int shB, double zB, int ao0A, int ao0B,
+                                                 long long N, double* __restrict__ X) {
+  double blk[3][LA ? 3 : 1][LB ? 3 : 1];
+  cart_shell_block<LA, LB>(ra, rb, d, R2, shA, zA, shB, zB, blk);
+  const long long NN = N * N;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int i = 0; i < (LA ? 3 : 1); ++i)
+#pragma unroll
+      for (int j = 0; j < (LB ? 3 : 1); ++j) {
+        const long long r = ao0A + (LA ? ao_of_axis(i) : 0), c = ao0B + (LB ? ao_of_axis(j) : 0);
+        X[k * NN + r * N + c] = blk[k][i][j];
+        X[k * NN + c * N + r] = blk[k][i][j];
+      }
+}
+
+// X[k][mu][nu] of molecule m (3 x N x N doubles, row-major), both triangles:
+// the matrix MolDS keeps as cartesianMatrix (Cndo2.cpp:1946-2057).
+__global__ void __launch_bounds__(kDipThreads)
+cartesian_matrix_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs,
+                        const DevMol* __restrict__ mols, int m, double* __restrict__ X) {
+  const DevMol mol = mols[m];
+  const long long items = (long long)mol.natoms + mol.npairs;
+  const long long N = mol.nao;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < items;
+       t += (long long)gridDim.x * blockDim.x) {
+    int ia, ib;
+    dipole_item(mol, pairs, t, &ia, &ib);
+    const DevAtom A = atoms[ia], B = atoms[ib];
+    const nddo_atom_params& pa = c_params[A.pidx];
+    const nddo_atom_params& pb = c_params[B.pidx];
+    const double ra[3] = {A.x, A.y, A.z}, rb[3] = {B.x, B.y, B.z};
+    const double d[3] = {ra[0] - rb[0], ra[1] - rb[1], ra[2] - rb[2]};
+    const double R2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const int shA = pa.principal_n - 1, shB = pb.principal_n - 1;
+    cart_shell_store<0, 0>(ra, rb, d, R2, shA, pa.zeta[0], shB, pb.zeta[0], A.ao0, B.ao0, N, X);
+    if (B.nao > 1) cart_shell_store<0, 1>(ra, rb, d, R2, shA, pa.zeta[0], shB, pb.zeta[1], A.ao0, B.ao0, N, X);
+    if (A.nao > 1) cart_shell_store<1, 0>(ra, rb, d, R2, shA, pa.zeta[1], shB, pb.zeta[0], A.ao0, B.ao0, N, X);
+    if (A.nao > 1 && B.nao > 1)
+      cart_shell_store<1, 1>(ra, rb, d, R2, shA, pa.zeta[1], shB, pb.zeta[1], A.ao0, B.ao0, N, X);
+  }
+}
+
+void launch_cartesian_matrix(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, int m, int natoms,
+                             double* X, cudaStream_t s) {
+  const long long items = (long long)natoms + (long long)natoms * (natoms - 1) / 2;
+  const int blocks = (int)std::max(1LL, std::min<long long>(4096, (items + kDipThreads - 1) / kDipThreads));
+  cartesian_matrix_kernel<<<blocks, kDipThreads, 0, s>>>(atoms, pairs, mols, m, X);
 }
 
 }  // namespace nddo

@@ -38,6 +38,7 @@ class SCFParams:
     precision: str = "fp64"          # "fp64" or "mixed" (not a MolDS key)
     fp64_switch_error: float = 1e-4
     tensor_cores: bool = True        # mixed: FP32-phase GEMMs on tcgen05 (not a MolDS key)
+    dipole: bool = True              # dipole moment after convergence, as DoSCF (not a MolDS key)
 
 
 @dataclass

@@ -4,6 +4,9 @@ Bars (from the reference's own correctness targets):
   * plain FP64 path: total energy within 1e-8 Eh, Mulliken charges within 1e-6
   * mixed precision: total energy within 1e-6 Eh
   * one-time integrals (pair blocks, core Hamiltonian): 1e-11 absolute
+  * dipole moments (total, electronic, core): 1e-6 a.u., the Mulliken bar
+    times a bohr; the STO-6G Cartesian matrix: 1e-11 relative to its largest
+    element
 """
 import json
 import os
@@ -22,6 +25,7 @@ FIX = json.load(open(os.path.join(HERE, "golden", "reference_fixtures.json")))["
 E_TOL_FP64 = 1e-8
 Q_TOL = 1e-6
 E_TOL_MIXED = 1e-6
+DIP_TOL = 1e-6
 
 
 @pytest.fixture(scope="module")
@@ -95,6 +99,19 @@ def test_pair_blocks_and_core_hamiltonian(ctx, name):
     assert np.max(np.abs(H - H_ref)) < 1e-11
 
 
+@pytest.mark.parametrize("name", sorted(MOLS) + ["octane_pm3"])
+def test_cartesian_matrix(ctx, name):
+    """<mu| r_k |nu> of the STO-6G expansion (Cndo2.cpp:1946-2130) against the
+    oracle's case-by-case restatement, every AO pair including same-atom ones."""
+    mol = O.make_molecule("pm3", W.octane().Z, W.octane().xyz) if name == "octane_pm3" else MOLS[name]()
+    es = M.ElectronicStructure(mol.theory, context=ctx)
+    es.SetMolecule(M.Molecule(mol.Z, mol.xyz))
+    X = es.GetCartesianMatrix()
+    X_ref = O.cartesian_matrix(mol)
+    assert X.shape == X_ref.shape
+    assert np.max(np.abs(X - X_ref)) <= 1e-11 * max(1.0, np.max(np.abs(X_ref)))
+
+
 @pytest.mark.parametrize("case", FIX, ids=[c["name"] for c in FIX])
 def test_reference_fixtures_fp64(ctx, case):
     mol, p = O.parse_input(case["input"])
@@ -109,8 +126,12 @@ def test_reference_fixtures_fp64(ctx, case):
     assert abs(es.GetCoreRepulsionEnergy() - ref.core_repulsion) < 1e-10
     assert np.max(np.abs(es.GetMullikenCharges() - ref.charges)) < Q_TOL
     assert np.max(np.abs(es.GetEnergiesMO() - ref.eps)) < 1e-7
+    D = es.GetDipoleMoments()
+    assert np.max(np.abs(D - ref.dipole)) < DIP_TOL
     # the printed values of the reference itself (7 significant digits)
     assert abs(es.GetElectronicEnergy(0) - case["energy"]) <= 1e-6 * abs(case["energy"])
+    for mine, theirs in zip(D.ravel(), np.array(case["dipole"]).ravel()):
+        assert abs(mine - theirs) <= max(1e-6 * abs(theirs), 1e-9), (mine, theirs)
     if p.rms_density >= 1e-12:
         assert es.GetIterations() == ref.iterations
         tr = es.GetTrace()
@@ -159,6 +180,7 @@ def test_water_cluster_am1(ctx, precision):
     tol = E_TOL_FP64 if precision == "fp64" else E_TOL_MIXED
     assert abs(es.GetElectronicEnergy(0) - ref.energy) < tol
     assert np.max(np.abs(es.GetMullikenCharges() - ref.charges)) < Q_TOL
+    assert np.max(np.abs(es.GetDipoleMoments() - ref.dipole)) < DIP_TOL
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -173,10 +195,16 @@ def test_batch_matches_oracle_and_is_invariant(ctx, precision):
         assert r["status"] == M.STATUS_CONVERGED
         assert abs(r["energy"] - ref.energy) < tol
         assert np.max(np.abs(q - ref.charges)) < Q_TOL
+        assert np.max(np.abs(r["dipole"] - ref.dipole)) < DIP_TOL
     # each molecule's result is the same alone and in the batch (bitwise)
     alone, qa = M.batch_scf("am1", [mols[3]], p, context=ctx)
     assert alone[0]["energy"] == res[3]["energy"]
     assert np.array_equal(qa[0], charges[3])
+    assert np.array_equal(alone[0]["dipole"], res[3]["dipole"])
+    # dipole = 0 skips the property and reports zeros
+    skip, _ = M.batch_scf("am1", [mols[3]], M.SCFParams(**{**vars(p), "dipole": False}), context=ctx)
+    assert skip[0]["energy"] == res[3]["energy"]
+    assert not np.any(skip[0]["dipole"])
 
 
 def test_uneven_batch(ctx):
@@ -188,7 +216,11 @@ def test_uneven_batch(ctx):
         ref = O.scf(O.make_molecule("pm3", m.Z, m.xyz), oracle_params(BENCH_SCF))
         assert abs(r["energy"] - ref.energy) < E_TOL_FP64
         assert np.max(np.abs(q - ref.charges)) < Q_TOL
+        assert np.max(np.abs(r["dipole"] - ref.dipole)) < DIP_TOL
         assert r["iterations"] == ref.iterations
+    # a molecule's dipole does not depend on the sizes of its batch partners
+    alone, _ = M.batch_scf("pm3", [mols[0]], BENCH_SCF, context=ctx)
+    assert np.array_equal(alone[0]["dipole"], res[0]["dipole"])
 
 
 def test_errors(ctx):
