@@ -25,6 +25,7 @@
 //     (:643-650).
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cmath>
 #include "nddo_batch.cuh"
 #include "kernels.h"
 
@@ -32,8 +33,8 @@ namespace nddo {
 
 __constant__ nddo_atom_params c_params[kNumParamSlots];
 __constant__ double c_inv[128];   // c_inv[j] = 1 / j
-__constant__ double c_sto_exp[3][2][6];    // STO-6G exponents (zeta = 1), shell K/L/M, s/p
-__constant__ double c_sto_coef[3][2][6];   // STO-6G contraction coefficients
+
+void upload_primitives(const nddo_atom_params* p, cudaStream_t s);
 
 void upload_params(const nddo_atom_params* p, cudaStream_t s) {
   static double inv[128];
@@ -42,8 +43,7 @@ void upload_params(const nddo_atom_params* p, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_params, p, sizeof(nddo_atom_params) * kNumParamSlots, 0,
                           cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_inv, inv, sizeof(inv), 0, cudaMemcpyHostToDevice, s);
-  cudaMemcpyToSymbolAsync(c_sto_exp, nddo_sto6g_exp, sizeof(nddo_sto6g_exp), 0, cudaMemcpyHostToDevice, s);
-  cudaMemcpyToSymbolAsync(c_sto_coef, nddo_sto6g_coef, sizeof(nddo_sto6g_coef), 0, cudaMemcpyHostToDevice, s);
+  upload_primitives(p, s);
 }
 
 __device__ __forceinline__ double sel3(int i, double a, double b, double c) {
@@ -643,8 +643,9 @@ void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* m
 // (Cndo2::CalcCartesianMatrixByGTOExpansion, src/cndo/Cndo2.cpp:1946-2130) and
 // then forms mu_elec = -sum P X + c sum P S with c the centre of core mass,
 // and mu_core = sum_A Z_A (R_A - c) (Cndo2.cpp:1871-1944).  Here the matrix is
-// never stored: each thread takes one atom pair (or one atom), evaluates the
-// pair's X block shell pair by shell pair and contracts it with P on the fly.
+// never stored: one warp takes one atom pair (or one atom), its lanes take the
+// 6 x 6 primitive pairs of each shell pair, and every primitive block is
+// contracted with P at once.
 //
 // Primitive integrals: normalised Cartesian Gaussians, s = N e^{-a|r-A|^2},
 // p_i = 2 sqrt(a) (r_i - A_i) s.  With p = a + b, the product centre Pc,
@@ -653,94 +654,113 @@ void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* m
 //   s10 = PA, s01 = PB, s11 = PA PB + h, s02 = PB^2 + h, s12 = PA PB^2 + (PA + 2 PB) h,
 // and x = (x - B) + B turns them into moments of the position operator:
 //   m00 = Pc, m10 = s11 + B PA, m01 = s02 + B PB, m11 = s12 + B s11.
-// The three-dimensional integral is (s|s) times the product over directions.
+// The three-dimensional integral is (s|s) times the product over directions,
+// (s|s) = (2 sqrt(ab) / p)^{3/2} e^{-mu R^2}, mu = ab / p.
+//
+// Screen: a primitive pair with mu R^2 > 46 (e^{-46} = 1e-20) is skipped.
+// Its elements are below 1e-17 (coefficients, normalisation and moments are
+// O(1..100)), far below the FP64 rounding of the sums they would join.
 // ---------------------------------------------------------------------------
 constexpr int kDipThreads = 256;
+constexpr double kDipScreen = 46.0;
 
-// X block of one shell pair, summed over the 6 x 6 primitive pairs:
-// out[k][i][j], k the axis of r, i / j the p axis (0 for an s shell).
+// Per parameter slot and shell (s, p): the six primitive exponents a_i =
+// zeta^2 alpha_i and factors f_i = d_i (2 sqrt(a_i) for p) a_i^{3/4}, so that a
+// primitive pair's weight is 2^{3/2} f_i f_j p^{-3/2} e^{-mu R^2}.
+__device__ double g_prim[kNumParamSlots][2][2][6];
+
+void upload_primitives(const nddo_atom_params* p, cudaStream_t s) {
+  static double prim[kNumParamSlots][2][2][6];
+  for (int slot = 0; slot < kNumParamSlots; ++slot)
+    for (int l = 0; l < 2; ++l)
+      for (int i = 0; i < 6; ++i) {
+        const int sh = p[slot].principal_n - 1;
+        const double z = p[slot].zeta[l];
+        const bool ok = sh >= 0 && sh < 3 && (l == 0 || p[slot].n_ao > 1) && z > 0.0;
+        const double a = ok ? z * z * nddo_sto6g_exp[sh][l][i] : 0.0;
+        double f = ok ? nddo_sto6g_coef[sh][l][i] * std::pow(a, 0.75) : 0.0;
+        if (ok && l == 1) f *= 2.0 * std::sqrt(a);
+        prim[slot][l][0][i] = a;
+        prim[slot][l][1][i] = f;
+      }
+  cudaMemcpyToSymbolAsync(g_prim, prim, sizeof(prim), 0, cudaMemcpyHostToDevice, s);
+}
+
+// One primitive pair's X block (weighted), out[k][i][j]: k the axis of r, i / j
+// the p axis (0 for an s shell).  Returns false when the pair is screened.
 template <int LA, int LB>
-__device__ __forceinline__ void cart_shell_block(const double* ra, const double* rb, const double* d, double R2,
-                                                 int shA, double zA, int shB, double zB,
-                                                 double (&out)[3][LA ? 3 : 1][LB ? 3 : 1]) {
+__device__ __forceinline__ bool prim_block(const double* ra, const double* rb, const double* d, double R2, double a,
+                                           double fa, double b, double fb,
+                                           double (&out)[3][LA ? 3 : 1][LB ? 3 : 1]) {
   constexpr int NA = LA ? 3 : 1, NB = LB ? 3 : 1;
+  const double r = rsqrt(a + b);          // p^{-1/2}
+  const double ip = r * r;
+  const double x = a * b * ip * R2;
+  if (x > kDipScreen) return false;
+  const double w = 2.8284271247461903 * fa * fb * (r * ip) * exp(-x);
+  const double h = 0.5 * ip;
+  double Pc[3], PA[3], PB[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    Pc[q] = (a * ra[q] + b * rb[q]) * ip;
+    PA[q] = -b * ip * d[q];
+    PB[q] = a * ip * d[q];
+  }
 #pragma unroll
   for (int k = 0; k < 3; ++k)
 #pragma unroll
     for (int i = 0; i < NA; ++i)
 #pragma unroll
-      for (int j = 0; j < NB; ++j) out[k][i][j] = 0.0;
-  const double zA2 = zA * zA, zB2 = zB * zB;
-#pragma unroll 1
-  for (int i6 = 0; i6 < 6; ++i6) {
-    const double a = zA2 * c_sto_exp[shA][LA][i6];
-    const double ca = c_sto_coef[shA][LA][i6] * (LA ? 2.0 * sqrt(a) : 1.0);
-#pragma unroll 1
-    for (int j6 = 0; j6 < 6; ++j6) {
-      const double b = zB2 * c_sto_exp[shB][LB][j6];
-      const double ip = 1.0 / (a + b);
-      const double t = 2.0 * sqrt(a * b) * ip;
-      const double w = ca * c_sto_coef[shB][LB][j6] * (LB ? 2.0 * sqrt(b) : 1.0) * (t * sqrt(t)) *
-                       exp(-(a * b * ip) * R2);
-      const double h = 0.5 * ip;
-      double Pc[3], PA[3], PB[3];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        Pc[q] = (a * ra[q] + b * rb[q]) * ip;
-        PA[q] = -b * ip * d[q];
-        PB[q] = a * ip * d[q];
+      for (int j = 0; j < NB; ++j) {
+        double v;
+        if (!LA && !LB) {
+          v = Pc[k];
+        } else if (!LA) {
+          v = (k == j) ? PB[j] * PB[j] + h + rb[j] * PB[j] : PB[j] * Pc[k];
+        } else if (!LB) {
+          v = (k == i) ? PA[i] * PB[i] + h + rb[i] * PA[i] : PA[i] * Pc[k];
+        } else if (i == j) {
+          const double s11 = PA[i] * PB[i] + h;
+          v = (k == i) ? PA[i] * PB[i] * PB[i] + (PA[i] + 2.0 * PB[i]) * h + rb[i] * s11 : s11 * Pc[k];
+        } else {
+          v = (k == i)   ? (PA[i] * PB[i] + h + rb[i] * PA[i]) * PB[j]
+              : (k == j) ? PA[i] * (PB[j] * PB[j] + h + rb[j] * PB[j])
+                         : PA[i] * PB[j] * Pc[k];
+        }
+        out[k][i][j] = w * v;
       }
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int i = 0; i < NA; ++i)
-#pragma unroll
-          for (int j = 0; j < NB; ++j) {
-            double v;
-            if (!LA && !LB) {
-              v = Pc[k];
-            } else if (!LA) {
-              v = (k == j) ? PB[j] * PB[j] + h + rb[j] * PB[j] : PB[j] * Pc[k];
-            } else if (!LB) {
-              v = (k == i) ? PA[i] * PB[i] + h + rb[i] * PA[i] : PA[i] * Pc[k];
-            } else if (i == j) {
-              const double s11 = PA[i] * PB[i] + h;
-              v = (k == i) ? PA[i] * PB[i] * PB[i] + (PA[i] + 2.0 * PB[i]) * h + rb[i] * s11 : s11 * Pc[k];
-            } else {
-              v = (k == i)   ? (PA[i] * PB[i] + h + rb[i] * PA[i]) * PB[j]
-                  : (k == j) ? PA[i] * (PB[j] * PB[j] + h + rb[j] * PB[j])
-                             : PA[i] * PB[j] * Pc[k];
-            }
-            out[k][i][j] += w * v;
-          }
-    }
-  }
+  return true;
 }
 
 // AO index within an atom of p axis i (MolDS order s, py, pz, px)
 __device__ __forceinline__ int ao_of_axis(int i) { return i == 0 ? 3 : i; }
 
-// acc[k] += sum over the shell pair of W_mu,nu X_k,mu,nu
+// acc[k] += sum_{mu, nu} W_mu,nu X_k,mu,nu of the shell pair (LA, LB); the
+// warp's lanes split the 36 primitive pairs
 template <int LA, int LB>
-__device__ __forceinline__ void cart_shell_contract(const double* ra, const double* rb, const double* d, double R2,
-                                                    int shA, double zA, int shB, double zB, const double (&W)[4][4],
+__device__ __forceinline__ void shell_contract_warp(const double* ra, const double* rb, const double* d, double R2,
+                                                    const double* pa_a, const double* pa_f, const double* pb_a,
+                                                    const double* pb_f, const double (&W)[4][4], int lane,
                                                     double* acc) {
-  double blk[3][LA ? 3 : 1][LB ? 3 : 1];
-  cart_shell_block<LA, LB>(ra, rb, d, R2, shA, zA, shB, zB, blk);
+  for (int e = lane; e < 36; e += 32) {
+    const int i6 = e / 6, j6 = e - 6 * (e / 6);
+    double blk[3][LA ? 3 : 1][LB ? 3 : 1];
+    if (!prim_block<LA, LB>(ra, rb, d, R2, pa_a[i6], pa_f[i6], pb_a[j6], pb_f[j6], blk)) continue;
 #pragma unroll
-  for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 3; ++k)
 #pragma unroll
-    for (int i = 0; i < (LA ? 3 : 1); ++i)
+      for (int i = 0; i < (LA ? 3 : 1); ++i)
 #pragma unroll
-      for (int j = 0; j < (LB ? 3 : 1); ++j)
-        acc[k] += W[LA ? ao_of_axis(i) : 0][LB ? ao_of_axis(j) : 0] * blk[k][i][j];
+        for (int j = 0; j < (LB ? 3 : 1); ++j)
+          acc[k] += W[LA ? ao_of_axis(i) : 0][LB ? ao_of_axis(j) : 0] * blk[k][i][j];
+  }
 }
 
 // CTAs of one molecule's dipole sums: a function of the molecule alone, so a
 // molecule's result does not depend on the batch it runs in.
 __host__ __device__ __forceinline__ int dipole_chunks(int natoms) {
   const long long items = (long long)natoms + (long long)natoms * (natoms - 1) / 2;
-  const long long c = (items + 2LL * kDipThreads - 1) / (2LL * kDipThreads);
+  const long long c = (items + 4LL * (kDipThreads / 32) - 1) / (4LL * (kDipThreads / 32));
   return (int)(c < 1 ? 1 : (c > kDipChunks ? kDipChunks : c));
 }
 
@@ -761,27 +781,29 @@ __device__ __forceinline__ void dipole_item(const DevMol& mol, const DevPair* __
 // for two different atoms (both triangles of MolDS's full-matrix dot product),
 // P_mu,nu within one atom.  The inter-atom block of H is exactly
 // 1/2 (beta_mu + beta_nu) S_mu,nu, so S is read back from H; within an atom S
-// is the identity (Cndo2.cpp:4135-4140).
-__global__ void __launch_bounds__(kDipThreads)
+// is the identity (Cndo2.cpp:4135-4140).  One warp per item.
+__global__ void __launch_bounds__(kDipThreads, 2)
 dipole_partial_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs,
                       const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
                       const double* __restrict__ P, const double* __restrict__ H, double* __restrict__ partial) {
+  __shared__ double s_prim[kNumParamSlots][2][2][6];
   __shared__ double red[kDipThreads / 32][4];
   const DevMol mol = mols[mol_list[blockIdx.y]];
   const int chunks = dipole_chunks(mol.natoms);
   if ((int)blockIdx.x >= chunks) return;
+  for (int i = threadIdx.x; i < kNumParamSlots * 24; i += blockDim.x) (&s_prim[0][0][0][0])[i] = (&g_prim[0][0][0][0])[i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int kWarps = kDipThreads / 32;
   const long long items = (long long)mol.natoms + mol.npairs;
   const long long ld = mol.nao;
   const double* Pm = P + mol.mat0;
   const double* Hm = H + mol.mat0;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < items;
-       t += (long long)chunks * blockDim.x) {
+  for (long long t = (long long)blockIdx.x * kWarps + warp; t < items; t += (long long)chunks * kWarps) {
     int ia, ib;
     dipole_item(mol, pairs, t, &ia, &ib);
     const DevAtom A = atoms[ia], B = atoms[ib];
-    const nddo_atom_params& pa = c_params[A.pidx];
-    const nddo_atom_params& pb = c_params[B.pidx];
     const bool same = ia == ib;
     double W[4][4];
 #pragma unroll
@@ -792,25 +814,39 @@ dipole_partial_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restri
         if (mu < A.nao && nu < B.nao) {
           const long long r = A.ao0 + mu, c = B.ao0 + nu;
           w = Pm[r * ld + c];
-          if (!same) {
-            w += Pm[c * ld + r];
-            acc[3] += w * (2.0 * Hm[r * ld + c] / (pa.beta[mu == 0 ? 0 : 1] + pb.beta[nu == 0 ? 0 : 1]));
-          } else if (mu == nu) {
-            acc[3] += w;
-          }
+          if (!same) w += Pm[c * ld + r];
         }
         W[mu][nu] = w;
       }
+    // sum P S: lane e takes element (e / 4, e % 4) of the block
+    if (lane < 16) {
+      const int mu = lane >> 2, nu = lane & 3;
+      if (mu < A.nao && nu < B.nao) {
+        const long long r = A.ao0 + mu, c = B.ao0 + nu;
+        if (!same) {
+          const double bs = c_params[A.pidx].beta[mu == 0 ? 0 : 1] + c_params[B.pidx].beta[nu == 0 ? 0 : 1];
+          acc[3] += (Pm[r * ld + c] + Pm[c * ld + r]) * (2.0 * Hm[r * ld + c] / bs);
+        } else if (mu == nu) {
+          acc[3] += Pm[r * ld + c];
+        }
+      }
+    }
     const double ra[3] = {A.x, A.y, A.z}, rb[3] = {B.x, B.y, B.z};
     const double d[3] = {ra[0] - rb[0], ra[1] - rb[1], ra[2] - rb[2]};
     const double R2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-    const int shA = pa.principal_n - 1, shB = pb.principal_n - 1;
-    cart_shell_contract<0, 0>(ra, rb, d, R2, shA, pa.zeta[0], shB, pb.zeta[0], W, acc);
-    if (B.nao > 1) cart_shell_contract<0, 1>(ra, rb, d, R2, shA, pa.zeta[0], shB, pb.zeta[1], W, acc);
-    if (A.nao > 1) cart_shell_contract<1, 0>(ra, rb, d, R2, shA, pa.zeta[1], shB, pb.zeta[0], W, acc);
-    if (A.nao > 1 && B.nao > 1) cart_shell_contract<1, 1>(ra, rb, d, R2, shA, pa.zeta[1], shB, pb.zeta[1], W, acc);
+    const double* As = s_prim[A.pidx][0][0];
+    const double* Af = s_prim[A.pidx][0][1];
+    const double* Bs = s_prim[B.pidx][0][0];
+    const double* Bf = s_prim[B.pidx][0][1];
+    const double* Ap = s_prim[A.pidx][1][0];
+    const double* Apf = s_prim[A.pidx][1][1];
+    const double* Bp = s_prim[B.pidx][1][0];
+    const double* Bpf = s_prim[B.pidx][1][1];
+    shell_contract_warp<0, 0>(ra, rb, d, R2, As, Af, Bs, Bf, W, lane, acc);
+    if (B.nao > 1) shell_contract_warp<0, 1>(ra, rb, d, R2, As, Af, Bp, Bpf, W, lane, acc);
+    if (A.nao > 1) shell_contract_warp<1, 0>(ra, rb, d, R2, Ap, Apf, Bs, Bf, W, lane, acc);
+    if (A.nao > 1 && B.nao > 1) shell_contract_warp<1, 1>(ra, rb, d, R2, Ap, Apf, Bp, Bpf, W, lane, acc);
   }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const double v = warp_sum(acc[q]);
@@ -819,7 +855,7 @@ dipole_partial_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restri
   __syncthreads();
   if (threadIdx.x < 4) {
     double v = 0.0;
-    for (int w = 0; w < kDipThreads / 32; ++w) v += red[w][threadIdx.x];
+    for (int w = 0; w < kWarps; ++w) v += red[w][threadIdx.x];
     partial[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 4 + threadIdx.x] = v;
   }
 }
@@ -865,7 +901,6 @@ __global__ void dipole_finish_kernel(const DevAtom* __restrict__ atoms, const De
   }
 }
 
-
 void launch_dipole(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list, int nlist,
                    int max_atoms, const double* P, const double* H, double* partial, MolState* st, cudaStream_t s) {
   if (nlist <= 0) return;
@@ -874,28 +909,34 @@ void launch_dipole(const DevAtom* atoms, const DevPair* pairs, const DevMol* mol
   dipole_finish_kernel<<<(nlist + 127) / 128, 128, 0, s>>>(atoms, mols, mol_list, nlist, chunks, partial, st);
 }
 
-// Stores the X block of one shell pair at (mu, nu) and (nu, mu).
+// X[k][mu][nu] of molecule m (3 x N x N doubles, row-major), both triangles:
+// the matrix MolDS keeps as cartesianMatrix (Cndo2.cpp:1946-2057).  One thread
+// per atom pair (or atom) and shell pair; not on the SCF path.
 template <int LA, int LB>
-__device__ __forceinline__ void cart_shell_store(const double* ra, const double* rb, const double* d, double R2,
-                                                 int shA, double zA, int shB, double zB, int ao0A, int ao0B,
-                                                 long long N, double* __restrict__ X) {
-  double blk[3][LA ? 3 : 1][LB ? 3 : 1];
-  cart_shell_block<LA, LB>(ra, rb, d, R2, shA, zA, shB, zB, blk);
+__device__ __forceinline__ void shell_store(const double* ra, const double* rb, const double* d, double R2,
+                                            const double* pa_a, const double* pa_f, const double* pb_a,
+                                            const double* pb_f, int ao0A, int ao0B, long long N,
+                                            double* __restrict__ X) {
+  constexpr int NA = LA ? 3 : 1, NB = LB ? 3 : 1;
+  double sum[3][NA][NB] = {};
+  for (int i6 = 0; i6 < 6; ++i6)
+    for (int j6 = 0; j6 < 6; ++j6) {
+      double blk[3][NA][NB];
+      if (!prim_block<LA, LB>(ra, rb, d, R2, pa_a[i6], pa_f[i6], pb_a[j6], pb_f[j6], blk)) continue;
+      for (int k = 0; k < 3; ++k)
+        for (int i = 0; i < NA; ++i)
+          for (int j = 0; j < NB; ++j) sum[k][i][j] += blk[k][i][j];
+    }
   const long long NN = N * N;
-#pragma unroll
   for (int k = 0; k < 3; ++k)
-#pragma unroll
-    for (int i = 0; i < (LA ? 3 : 1); ++i)
-#pragma unroll
-      for (int j = 0; j < (LB ? 3 : 1); ++j) {
+    for (int i = 0; i < NA; ++i)
+      for (int j = 0; j < NB; ++j) {
         const long long r = ao0A + (LA ? ao_of_axis(i) : 0), c = ao0B + (LB ? ao_of_axis(j) : 0);
-        X[k * NN + r * N + c] = blk[k][i][j];
-        X[k * NN + c * N + r] = blk[k][i][j];
+        X[k * NN + r * N + c] = sum[k][i][j];
+        X[k * NN + c * N + r] = sum[k][i][j];
       }
 }
 
-// X[k][mu][nu] of molecule m (3 x N x N doubles, row-major), both triangles:
-// the matrix MolDS keeps as cartesianMatrix (Cndo2.cpp:1946-2057).
 __global__ void __launch_bounds__(kDipThreads)
 cartesian_matrix_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs,
                         const DevMol* __restrict__ mols, int m, double* __restrict__ X) {
@@ -907,17 +948,21 @@ cartesian_matrix_kernel(const DevAtom* __restrict__ atoms, const DevPair* __rest
     int ia, ib;
     dipole_item(mol, pairs, t, &ia, &ib);
     const DevAtom A = atoms[ia], B = atoms[ib];
-    const nddo_atom_params& pa = c_params[A.pidx];
-    const nddo_atom_params& pb = c_params[B.pidx];
     const double ra[3] = {A.x, A.y, A.z}, rb[3] = {B.x, B.y, B.z};
     const double d[3] = {ra[0] - rb[0], ra[1] - rb[1], ra[2] - rb[2]};
     const double R2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-    const int shA = pa.principal_n - 1, shB = pb.principal_n - 1;
-    cart_shell_store<0, 0>(ra, rb, d, R2, shA, pa.zeta[0], shB, pb.zeta[0], A.ao0, B.ao0, N, X);
-    if (B.nao > 1) cart_shell_store<0, 1>(ra, rb, d, R2, shA, pa.zeta[0], shB, pb.zeta[1], A.ao0, B.ao0, N, X);
-    if (A.nao > 1) cart_shell_store<1, 0>(ra, rb, d, R2, shA, pa.zeta[1], shB, pb.zeta[0], A.ao0, B.ao0, N, X);
-    if (A.nao > 1 && B.nao > 1)
-      cart_shell_store<1, 1>(ra, rb, d, R2, shA, pa.zeta[1], shB, pb.zeta[1], A.ao0, B.ao0, N, X);
+    const double* As = g_prim[A.pidx][0][0];
+    const double* Af = g_prim[A.pidx][0][1];
+    const double* Bs = g_prim[B.pidx][0][0];
+    const double* Bf = g_prim[B.pidx][0][1];
+    const double* Ap = g_prim[A.pidx][1][0];
+    const double* Apf = g_prim[A.pidx][1][1];
+    const double* Bp = g_prim[B.pidx][1][0];
+    const double* Bpf = g_prim[B.pidx][1][1];
+    shell_store<0, 0>(ra, rb, d, R2, As, Af, Bs, Bf, A.ao0, B.ao0, N, X);
+    if (B.nao > 1) shell_store<0, 1>(ra, rb, d, R2, As, Af, Bp, Bpf, A.ao0, B.ao0, N, X);
+    if (A.nao > 1) shell_store<1, 0>(ra, rb, d, R2, Ap, Apf, Bs, Bf, A.ao0, B.ao0, N, X);
+    if (A.nao > 1 && B.nao > 1) shell_store<1, 1>(ra, rb, d, R2, Ap, Apf, Bp, Bpf, A.ao0, B.ao0, N, X);
   }
 }
 
