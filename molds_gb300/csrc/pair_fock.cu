@@ -735,24 +735,105 @@ __device__ __forceinline__ bool prim_block(const double* ra, const double* rb, c
 // AO index within an atom of p axis i (MolDS order s, py, pz, px)
 __device__ __forceinline__ int ao_of_axis(int i) { return i == 0 ? 3 : i; }
 
-// acc[k] += sum_{mu, nu} W_mu,nu X_k,mu,nu of the shell pair (LA, LB); the
-// warp's lanes split the 36 primitive pairs
+// acc[k] += sum_{i, j} Wa_ij X_k,ij of one primitive pair, Wa in axis order
+// (Wa[0][*] for an s shell on A, Wa[*][0] for an s shell on B).  The sums over
+// i, j are folded into row / column sums: with U_k = sum_j Wa_kj PB_j,
+// V_k = sum_i Wa_ik PA_i, Q = sum_k PA_k U_k, D = sum_i Wa_ii PA_i PB_i and
+// T = sum_i Wa_ii s11_i, the p-p contraction for axis k is
+//   Wa_kk m11_k + (T - Wa_kk s11_k) Pc_k + U'_k m10_k + V'_k m01_k
+//   + (Q - D - PA_k U'_k - PB_k V'_k) Pc_k,  U'_k = U_k - Wa_kk PB_k, V'_k = V_k - Wa_kk PA_k,
+// the terms of the block with k = i = j, i = j != k, k = i != j, k = j != i and
+// i, j, k all different.
+template <int LA, int LB>
+__device__ __forceinline__ void prim_contract(const double* ra, const double* rb, const double* d, double R2,
+                                              double a, double fa, double b, double fb, const double (&Wa)[3][3],
+                                              double* acc) {
+  const double r = rsqrt(a + b);          // p^{-1/2}
+  const double ip = r * r;
+  const double x = a * b * ip * R2;
+  const double w = 2.8284271247461903 * fa * fb * (r * ip) * exp(-x);
+  const double h = 0.5 * ip;
+  double Pc[3], PA[3], PB[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    Pc[q] = (a * ra[q] + b * rb[q]) * ip;
+    PA[q] = -b * ip * d[q];
+    PB[q] = a * ip * d[q];
+  }
+  if (!LA && !LB) {
+    const double ws = w * Wa[0][0];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc[k] += ws * Pc[k];
+  } else if (!LA) {
+    const double sPB = Wa[0][0] * PB[0] + Wa[0][1] * PB[1] + Wa[0][2] * PB[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double m01 = PB[k] * PB[k] + h + rb[k] * PB[k];
+      acc[k] += w * (Wa[0][k] * m01 + Pc[k] * (sPB - Wa[0][k] * PB[k]));
+    }
+  } else if (!LB) {
+    const double sPA = Wa[0][0] * PA[0] + Wa[1][0] * PA[1] + Wa[2][0] * PA[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double m10 = PA[k] * PB[k] + h + rb[k] * PA[k];
+      acc[k] += w * (Wa[k][0] * m10 + Pc[k] * (sPA - Wa[k][0] * PA[k]));
+    }
+  } else {
+    double s11[3], U[3], V[3];
+    double T = 0.0, D = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      s11[i] = PA[i] * PB[i] + h;
+      T += Wa[i][i] * s11[i];
+      D += Wa[i][i] * PA[i] * PB[i];
+      U[i] = Wa[i][0] * PB[0] + Wa[i][1] * PB[1] + Wa[i][2] * PB[2];
+      V[i] = Wa[0][i] * PA[0] + Wa[1][i] * PA[1] + Wa[2][i] * PA[2];
+    }
+    const double Q = PA[0] * U[0] + PA[1] * U[1] + PA[2] * U[2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double m10 = s11[k] + rb[k] * PA[k];
+      const double m01 = PB[k] * PB[k] + h + rb[k] * PB[k];
+      const double m11 = PA[k] * PB[k] * PB[k] + (PA[k] + 2.0 * PB[k]) * h + rb[k] * s11[k];
+      const double Ur = U[k] - Wa[k][k] * PB[k];
+      const double Vr = V[k] - Wa[k][k] * PA[k];
+      acc[k] += w * (Wa[k][k] * m11 + (T - Wa[k][k] * s11[k]) * Pc[k] + Ur * m10 + Vr * m01 +
+                     (Q - D - PA[k] * Ur - PB[k] * Vr) * Pc[k]);
+    }
+  }
+}
+
+// acc[k] += sum_{mu, nu} W_mu,nu X_k,mu,nu of the shell pair (LA, LB).  The
+// warp screens the 36 primitive pairs (mu R^2 > 46, tested without a divide
+// as a b R^2 > 46 (a + b)) and hands the survivors out lane by lane, so a
+// distant atom pair with few survivors takes one pass.  Called by all lanes.
 template <int LA, int LB>
 __device__ __forceinline__ void shell_contract_warp(const double* ra, const double* rb, const double* d, double R2,
                                                     const double* pa_a, const double* pa_f, const double* pb_a,
                                                     const double* pb_f, const double (&W)[4][4], int lane,
                                                     double* acc) {
-  for (int e = lane; e < 36; e += 32) {
+  double Wa[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Wa[i][j] = W[LA ? ao_of_axis(i) : 0][LB ? ao_of_axis(j) : 0];
+  const double a0 = pa_a[lane / 6], b0 = pb_a[lane % 6];
+  const bool keep0 = !(a0 * b0 * R2 > kDipScreen * (a0 + b0));
+  bool keep1 = false;
+  if (lane < 4) {
+    const double a1 = pa_a[(lane + 32) / 6], b1 = pb_a[(lane + 32) % 6];
+    keep1 = !(a1 * b1 * R2 > kDipScreen * (a1 + b1));
+  }
+  const unsigned m0 = __ballot_sync(0xffffffffu, keep0);
+  const unsigned m1 = __ballot_sync(0xffffffffu, keep1);
+  const int n0 = __popc(m0), n = n0 + __popc(m1);
+  for (int slot = lane; slot < n; slot += 32) {
+    // position of the (slot)-th set bit (0-based) of m0, then of m1
+    unsigned m = slot < n0 ? m0 : m1;
+    for (int q = slot < n0 ? slot : slot - n0; q > 0; --q) m &= m - 1;
+    const int e = (slot < n0 ? 0 : 32) + __ffs(m) - 1;
     const int i6 = e / 6, j6 = e - 6 * (e / 6);
-    double blk[3][LA ? 3 : 1][LB ? 3 : 1];
-    if (!prim_block<LA, LB>(ra, rb, d, R2, pa_a[i6], pa_f[i6], pb_a[j6], pb_f[j6], blk)) continue;
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int i = 0; i < (LA ? 3 : 1); ++i)
-#pragma unroll
-        for (int j = 0; j < (LB ? 3 : 1); ++j)
-          acc[k] += W[LA ? ao_of_axis(i) : 0][LB ? ao_of_axis(j) : 0] * blk[k][i][j];
+    prim_contract<LA, LB>(ra, rb, d, R2, pa_a[i6], pa_f[i6], pb_a[j6], pb_f[j6], Wa, acc);
   }
 }
 
