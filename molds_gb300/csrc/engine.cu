@@ -771,6 +771,15 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const
       }
       continue;
     }
+    // FP64, few molecules (the plain one-molecule path): one cluster of CTAs
+    // per molecule puts several SMs' FP64 units on each diagonalisation
+    if (!fp32 && bucket_max_n_[b] >= kClusterJacobiMinN && nb <= kClusterJacobiMaxMols &&
+        jacobi_cluster_capacity(bucket_max_n_[b]) > 0) {
+      launches_ += 1;
+      launch_jacobi_cluster_f64(d_mols, bucket_dev_[b], nb, bucket_max_n_[b], d_state, 1, d_G64, Cin, 1, d_C, d_eps,
+                                s.max_sweeps, d_sweeps, stream_);
+      continue;
+    }
     const int chunk = jacobi_needs_workspace(bucket_max_n_[b], fp32 ? 4 : 8, &ag, &vg) ? cap_.ws_slots : nb;
     for (int k0 = 0; k0 < nb; k0 += chunk) {
       const int cnt = std::min(chunk, nb - k0);

@@ -18,6 +18,7 @@
 // Warm start: V starts from the previous iteration's eigenvectors and the
 // matrix from C_prev F C_prev^T (computed by the transform GEMMs), so late SCF
 // iterations converge in one or two sweeps.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include "nddo_batch.cuh"
 #include "kernels.h"
@@ -385,6 +386,282 @@ bool jacobi_needs_workspace(int max_n, int elem, bool* a_global, bool* v_global)
     if (jacobi_smem_bytes(max_n, elem, false, true) > limit) *a_global = true;
   }
   return *a_global || *v_global;
+}
+
+// ---------------------------------------------------------------------------
+// One molecule on a cluster of kJcCluster CTAs (FP64, the plain one-molecule
+// path): the same round-robin two-sided Jacobi as jacobi_kernel, with the
+// matrix and the eigenvector rows spread over the cluster's shared memory, so
+// a single diagonalisation runs on kJcCluster SMs instead of one.
+//
+// Layout: row i of the upper triangle of A (entries j >= i) and row i of V
+// live in CTA i % kJcCluster at local row i / kJcCluster; every element is
+// reached through the cluster's distributed shared memory.  Each round:
+//   1. every CTA computes all rotations of the round from the same elements
+//      (identical tables in every CTA, no exchange), then cluster barrier;
+//   2. the 2x2 diagonal blocks (by the owner of row p), the off-diagonal 2x2
+//      blocks and the column slices of the V rows are updated, the work spread
+//      over all CTAs, then cluster barrier.
+// Every branch around a barrier depends only on values all CTAs computed
+// identically, so all CTAs of a cluster pass the same barriers.
+// ---------------------------------------------------------------------------
+constexpr int kJcCluster = 8;
+
+struct JcView {
+  double* A[kJcCluster];
+  double* V[kJcCluster];
+  int np;
+  __device__ __forceinline__ double* a(int x, int y) const {   // upper-triangle element (x, y)
+    const int i = x < y ? x : y, j = x < y ? y : x;
+    return A[i % kJcCluster] + (long long)(i / kJcCluster) * np + j;
+  }
+  __device__ __forceinline__ double* v(int i, int mu) const {
+    return V[i % kJcCluster] + (long long)(i / kJcCluster) * np + mu;
+  }
+};
+
+size_t jacobi_cluster_smem_bytes(int n) {
+  const long long np = jac_np(n), half = np / 2;
+  const long long rows = (np + kJcCluster - 1) / kJcCluster;
+  long long b = 2 * rows * np * 8;     // A and V rows
+  b += half * (2 * 8 + 2 * 4 + 4 + 4 * 8);   // c, s; p, q; flag; t, app, aqq, apq
+  b += sizeof(JcView) + kJcCluster * 4 + 64;   // DSMEM pointers, cluster flags, alignment
+  b += 64 * 8;                         // reduction scratch
+  return (size_t)((b + 15) & ~15LL);
+}
+
+__global__ void __cluster_dims__(kJcCluster, 1, 1) __launch_bounds__(512)
+jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
+                      const MolState* __restrict__ st, int require_active, const double* __restrict__ G,
+                      const double* __restrict__ Cin, int use_basis, double* __restrict__ Cout,
+                      double* __restrict__ eps_out, int max_sweeps, int* __restrict__ sweeps_out) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int m = mol_list[blockIdx.x / kJcCluster];
+  if (require_active && st[m].status != kActive) return;   // the whole cluster returns
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const DevMol mol = mols[m];
+  const int n = mol.nao, np = jac_np(n), half = np / 2;
+  const int rows = (np + kJcCluster - 1) / kJcCluster;
+  unsigned char* ptr = smem_raw;
+  double* Aloc = reinterpret_cast<double*>(ptr); ptr += (size_t)rows * np * 8;
+  double* Vloc = reinterpret_cast<double*>(ptr); ptr += (size_t)rows * np * 8;
+  double* cs = reinterpret_cast<double*>(ptr); ptr += (size_t)half * 16;
+  double* dg = reinterpret_cast<double*>(ptr); ptr += (size_t)half * 32;   // t, app, aqq, apq
+  int* pq = reinterpret_cast<int*>(ptr); ptr += (size_t)half * 8;
+  int* rot = reinterpret_cast<int*>(ptr); ptr += (size_t)half * 4;
+  JcView* view = reinterpret_cast<JcView*>(((uintptr_t)ptr + 15) & ~(uintptr_t)15);
+  ptr = reinterpret_cast<unsigned char*>(view + 1);
+  int* cflag = reinterpret_cast<int*>(ptr); ptr += kJcCluster * 4;
+  double* red = reinterpret_cast<double*>(((uintptr_t)ptr + 7) & ~(uintptr_t)7);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  if (tid == 0) {
+    for (int r = 0; r < kJcCluster; ++r) {
+      view->A[r] = cluster.map_shared_rank(Aloc, r);
+      view->V[r] = cluster.map_shared_rank(Vloc, r);
+    }
+    view->np = np;
+  }
+  // ---- load this CTA's rows ------------------------------------------------
+  const double* Gm = G + mol.mat0;
+  const double* Cm = Cin + mol.mat0;
+  for (long long e = tid; e < (long long)rows * np; e += nth) {
+    const int lr = (int)(e / np), j = (int)(e % np);
+    const int i = lr * kJcCluster + rank;
+    double a = 0.0, v = (i == j) ? 1.0 : 0.0;
+    if (i < np) {
+      if (i < n && j < n && j >= i) a = Gm[(long long)i * n + j];
+      if (i < n && j < n && use_basis) v = Cm[(long long)i * n + j];
+    }
+    Aloc[e] = a;
+    Vloc[e] = v;
+  }
+  cluster.sync();
+  const JcView& W = *view;
+  // scale for the stopping test: every CTA reads every diagonal element
+  double scale = 0.0;
+  for (int i = tid; i < n; i += nth) { const double d = fabs(*W.a(i, i)); scale = d > scale ? d : scale; }
+  for (int o = 16; o > 0; o >>= 1) { const double t = __shfl_xor_sync(0xffffffffu, scale, o); scale = t > scale ? t : scale; }
+  if ((tid & 31) == 0) red[tid >> 5] = scale;
+  __syncthreads();
+  if (tid == 0) {
+    double sc = 0.0;
+    for (int w = 0; w < (nth >> 5); ++w) sc = red[w] > sc ? red[w] : sc;
+    red[32] = sc > 1e-30 ? sc : 1.0;
+  }
+  __syncthreads();
+  const double thresh = JacTol<double>::rel * red[32];
+  const int groups = half / 2;                 // row-pair groups (I, half-1-I): half - 1 blocks each
+  const long long nblk = (long long)groups * (half - 1);
+  const int cw = (np + kJcCluster - 1) / kJcCluster;   // V columns per CTA
+  const int c0 = rank * cw, c1 = min(np, c0 + cw);
+
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (sweep > 0) {
+      // any off-diagonal element above the threshold in this CTA's rows?
+      int big = 0;
+      for (int lr = tid; lr < rows; lr += nth) {
+        const int i = lr * kJcCluster + rank;
+        if (i >= n) continue;
+        for (int j = i + 1; j < n; ++j) big |= fabs(Aloc[(long long)lr * np + j]) > thresh;
+      }
+      big = __syncthreads_or(big);
+      if (tid < kJcCluster) cluster.map_shared_rank(cflag, tid)[rank] = big;
+      cluster.sync();
+      int any = 0;
+      for (int r = 0; r < kJcCluster; ++r) any |= cflag[r];
+      cluster.sync();                          // flags read before the next write
+      if (!any) break;
+    }
+    double offmax = 0.0;
+    for (int r = 0; r < np - 1; ++r) {
+      int any = 0;
+      for (int k = tid; k < half; k += nth) {
+        const int i1 = k, i2 = np - 1 - k;
+        const int p1 = (i1 == 0) ? 0 : ((i1 - 1 + r) % (np - 1)) + 1;
+        const int p2 = (i2 == 0) ? 0 : ((i2 - 1 + r) % (np - 1)) + 1;
+        const int p = p1 < p2 ? p1 : p2, q = p1 < p2 ? p2 : p1;
+        const double apq = *W.a(p, q);
+        double c = 1.0, sn = 0.0, t = 0.0, app = 0.0, aqq = 0.0;
+        const double aa = fabs(apq);
+        offmax = aa > offmax ? aa : offmax;
+        const int doit = aa > thresh;
+        if (doit) {
+          app = *W.a(p, p);
+          aqq = *W.a(q, q);
+          jac_rotation(app, aqq, apq, &t, &c, &sn);
+        }
+        cs[2 * k] = c; cs[2 * k + 1] = sn;
+        dg[4 * k] = t; dg[4 * k + 1] = app; dg[4 * k + 2] = aqq; dg[4 * k + 3] = apq;
+        pq[2 * k] = p; pq[2 * k + 1] = q;
+        rot[k] = doit;
+        any |= doit;
+      }
+      // identical in every CTA: the whole cluster skips or rotates together
+      if (!__syncthreads_or(any)) continue;
+      cluster.sync();                          // all reads of the round's inputs done
+      // diagonal 2x2 blocks: the owner of row p writes them
+      for (int k = tid; k < half; k += nth) {
+        if (!rot[k] || (pq[2 * k] % kJcCluster) != rank) continue;
+        const int p = pq[2 * k], q = pq[2 * k + 1];
+        const double t = dg[4 * k], app = dg[4 * k + 1], aqq = dg[4 * k + 2], apq = dg[4 * k + 3];
+        *W.a(p, p) = app - t * apq;
+        *W.a(q, q) = aqq + t * apq;
+        *W.a(p, q) = 0.0;
+      }
+      // off-diagonal 2x2 blocks (I < K) over the whole cluster
+      for (long long b = (long long)rank * nth + tid; b < nblk; b += (long long)kJcCluster * nth) {
+        const int g = (int)(b / (half - 1)), e = (int)(b % (half - 1));
+        const int I1 = g, I2 = half - 1 - g;
+        int I, K;
+        if (e < half - 1 - I1) { I = I1; K = I1 + 1 + e; } else { I = I2; K = I2 + 1 + (e - (half - 1 - I1)); }
+        if (!(rot[I] | rot[K])) continue;
+        const int p = pq[2 * I], q = pq[2 * I + 1], r2 = pq[2 * K], s2 = pq[2 * K + 1];
+        const double c = cs[2 * I], sn = cs[2 * I + 1], c2 = cs[2 * K], s2n = cs[2 * K + 1];
+        double* e_pr = W.a(p, r2);
+        double* e_ps = W.a(p, s2);
+        double* e_qr = W.a(q, r2);
+        double* e_qs = W.a(q, s2);
+        const double b00 = *e_pr, b01 = *e_ps, b10 = *e_qr, b11 = *e_qs;
+        const double y00 = c * b00 - sn * b10, y01 = c * b01 - sn * b11;
+        const double y10 = sn * b00 + c * b10, y11 = sn * b01 + c * b11;
+        *e_pr = y00 * c2 - y01 * s2n;
+        *e_ps = y00 * s2n + y01 * c2;
+        *e_qr = y10 * c2 - y11 * s2n;
+        *e_qs = y10 * s2n + y11 * c2;
+      }
+      // V rows p, q: this CTA's column slice of every rotated pair
+      if (c1 > c0) {
+        const int w = c1 - c0;
+        for (int e = tid; e < half * w; e += nth) {
+          const int k = e / w, mu = c0 + (e - k * w);
+          if (!rot[k]) continue;
+          const int p = pq[2 * k], q = pq[2 * k + 1];
+          const double c = cs[2 * k], sn = cs[2 * k + 1];
+          double* vp = W.v(p, mu);
+          double* vq = W.v(q, mu);
+          const double a = *vp, bq = *vq;
+          *vp = c * a - sn * bq;
+          *vq = sn * a + c * bq;
+        }
+      }
+      cluster.sync();                          // the round's writes visible everywhere
+    }
+    // converged when every rotation the sweep applied was at round-off level
+    // (offmax is identical in every CTA: all of them saw every pivot)
+    for (int o = 16; o > 0; o >>= 1) { const double t = __shfl_xor_sync(0xffffffffu, offmax, o); offmax = t > offmax ? t : offmax; }
+    if ((tid & 31) == 0) red[tid >> 5] = offmax;
+    __syncthreads();
+    if (tid == 0) {
+      double mx = 0.0;
+      for (int w = 0; w < (nth >> 5); ++w) mx = red[w] > mx ? red[w] : mx;
+      red[33] = mx;
+    }
+    __syncthreads();
+    const bool done = red[33] <= thresh;
+    __syncthreads();
+    if (done) { ++sweep; break; }
+  }
+
+  // ---- rank by eigenvalue, sign fix, write this CTA's rows ------------------
+  for (int lr = tid; lr < rows; lr += nth) {
+    const int i = lr * kJcCluster + rank;
+    if (i >= n) continue;
+    const double li = Aloc[(long long)lr * np + i];
+    int rk = 0;
+    for (int j = 0; j < n; ++j) {
+      const double lj = *W.a(j, j);
+      rk += (lj < li) || (lj == li && j < i);
+    }
+    double sum = 0.0;
+    for (int mu = 0; mu < n; ++mu) sum += Vloc[(long long)lr * np + mu];
+    const double sg = sum < 0.0 ? -1.0 : 1.0;
+    eps_out[mol.vec0 + rk] = li;
+    double* Co = Cout + mol.mat0 + (long long)rk * n;
+    for (int mu = 0; mu < n; ++mu) Co[mu] = sg * Vloc[(long long)lr * np + mu];
+  }
+  if (rank == 0 && tid == 0 && sweeps_out) sweeps_out[m] += sweep;
+  cluster.sync();                              // no CTA leaves while others read its diagonal
+}
+
+// Clusters that fit at once on this device for the cluster kernel at basis n
+// (0: not launchable, use the one-CTA kernel).
+int jacobi_cluster_capacity(int n) {
+  static int cached_n = -1, cached_val = 0;
+  if (n == cached_n) return cached_val;
+  const size_t bytes = jacobi_cluster_smem_bytes(n);
+  int val = 0;
+  if (bytes <= 232448) {
+    cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kJcCluster, 1, 1);
+    cfg.blockDim = dim3(jac_np(n) <= 64 ? 256 : 512, 1, 1);
+    cfg.dynamicSmemBytes = bytes;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = kJcCluster;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    if (cudaOccupancyMaxActiveClusters(&val, jacobi_cluster_kernel, &cfg) != cudaSuccess) val = 0;
+    cudaGetLastError();
+  }
+  cached_n = n;
+  cached_val = val;
+  return val;
+}
+
+void launch_jacobi_cluster_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                               int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
+                               double* eps, int max_sweeps, int* sweeps_out, cudaStream_t s) {
+  if (nlist <= 0) return;
+  const size_t bytes = jacobi_cluster_smem_bytes(max_n);
+  const int threads = jac_np(max_n) <= 64 ? 256 : 512;
+  jacobi_cluster_kernel<<<nlist * kJcCluster, threads, bytes, s>>>(mols, mol_list, st, require_active, G, Cin,
+                                                                   use_basis, Cout, eps, max_sweeps, sweeps_out);
 }
 
 }  // namespace nddo

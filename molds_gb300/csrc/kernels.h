@@ -38,6 +38,10 @@ void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A,
                     bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
 // block Jacobi (block_jacobi.cu) for bases above the one-CTA Jacobi's limit
 constexpr int kSmallJacobiMaxN = 194;
+// FP64 lists of at most this many molecules with a basis of at least
+// kClusterJacobiMinN use the cluster Jacobi (one 8-CTA cluster per molecule)
+constexpr int kClusterJacobiMaxMols = 8;
+constexpr int kClusterJacobiMinN = 32;
 size_t block_jacobi_workspace(int max_n, int nslots, int elem, long long* stride, long long* qstride);
 int launch_block_jacobi_f32(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                             const float* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
@@ -95,6 +99,12 @@ void launch_jacobi_f32(const DevMol* mols, const int* mol_list, int nlist, int m
                        int require_active, const float* G, const float* Cin, int use_basis, double* Cout,
                        double* eps, float* Aws, float* Vws, long long ws_stride, int max_sweeps,
                        int* sweeps_out, cudaStream_t s);
+// one molecule per cluster of 8 CTAs (FP64); jacobi_cluster_capacity(n) > 0
+// when the cluster kernel can run at basis n on this device
+int jacobi_cluster_capacity(int n);
+void launch_jacobi_cluster_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
+                               int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
+                               double* eps, int max_sweeps, int* sweeps_out, cudaStream_t s);
 void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
                        int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
                        double* eps, double* Aws, double* Vws, long long ws_stride, int max_sweeps,

@@ -159,6 +159,8 @@ def test_density_and_eigenvectors_fp64(ctx):
 
 
 def test_octane_pm3_fp64(ctx):
+    """The plain one-molecule FP64 path at N = 50 (the cluster Jacobi: one
+    8-CTA cluster per molecule) against the oracle's LAPACK dsyevd run."""
     mol = W.octane()
     ref = O.scf(O.make_molecule("pm3", mol.Z, mol.xyz), oracle_params(BENCH_SCF))
     es = M.ElectronicStructure("pm3", BENCH_SCF, context=ctx)
@@ -167,6 +169,26 @@ def test_octane_pm3_fp64(ctx):
     assert abs(es.GetElectronicEnergy(0) - ref.energy) < E_TOL_FP64
     assert np.max(np.abs(es.GetMullikenCharges() - ref.charges)) < Q_TOL
     assert es.GetIterations() == ref.iterations
+    assert np.max(np.abs(es.GetEnergiesMO() - ref.eps)) < 1e-9
+    assert np.max(np.abs(es.GetOrbitalElectronPopulation() - ref.P)) < 1e-8
+    C = es.GetFockMatrix()
+    assert np.max(np.abs(C @ C.T - np.eye(C.shape[0]))) < 1e-10
+    assert np.all(C.sum(axis=1) >= 0)
+    assert np.max(np.abs(es.GetDipoleMoments() - ref.dipole)) < DIP_TOL
+
+
+def test_plain_water32_fp64(ctx):
+    """(H2O)32 AM1 (N = 192) on the plain path: the largest basis the cluster
+    Jacobi serves."""
+    mol = W.water_replicas(W.water_cluster(shape=(4, 4, 2), seed=2), 1)[0]
+    ref = O.scf(O.make_molecule("am1", mol.Z, mol.xyz), oracle_params(BENCH_SCF))
+    es = M.ElectronicStructure("am1", BENCH_SCF, context=ctx)
+    es.SetMolecule(mol)
+    es.DoSCF(True)
+    assert abs(es.GetElectronicEnergy(0) - ref.energy) < E_TOL_FP64
+    assert np.max(np.abs(es.GetMullikenCharges() - ref.charges)) < Q_TOL
+    assert es.GetIterations() == ref.iterations
+    assert np.max(np.abs(es.GetEnergiesMO() - ref.eps)) < 1e-9
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
