@@ -396,16 +396,12 @@ bool jacobi_needs_workspace(int max_n, int elem, bool* a_global, bool* v_global)
 //
 // Layout: row i of the upper triangle of A (entries j >= i) and row i of V
 // live in CTA i % kJcCluster at local row i / kJcCluster; every element is
-// reached through the cluster's distributed shared memory.  Every CTA also
-// keeps a replicated copy of the diagonal and of the next round's pivots
-// a_pq, double-buffered by round parity.  Each round:
-//   1. every CTA computes all rotations of the round from its local copies
-//      (identical tables in every CTA, no exchange, no barrier);
-//   2. the 2x2 diagonal blocks, the off-diagonal 2x2 blocks and the column
-//      slices of the V rows are updated, the work spread over all CTAs; the
-//      thread that produces a diagonal element or a next-round pivot writes it
-//      into every CTA's copy of the other parity;
-//   3. one cluster barrier.
+// reached through the cluster's distributed shared memory.  Each round:
+//   1. every CTA computes all rotations of the round from the same elements
+//      (identical tables in every CTA, no exchange), then cluster barrier;
+//   2. the 2x2 diagonal blocks (by the owner of row p), the off-diagonal 2x2
+//      blocks and the column slices of the V rows are updated, the work spread
+//      over all CTAs, then cluster barrier.
 // Every branch around a barrier depends only on values all CTAs computed
 // identically, so all CTAs of a cluster pass the same barriers.
 // ---------------------------------------------------------------------------
@@ -414,8 +410,6 @@ constexpr int kJcCluster = 8;
 struct JcView {
   double* A[kJcCluster];
   double* V[kJcCluster];
-  double* diag[kJcCluster];   // replicated diagonal, [2][np]
-  double* piv[kJcCluster];    // replicated next-round pivots, [2][half]
   int np;
   __device__ __forceinline__ double* a(int x, int y) const {   // upper-triangle element (x, y)
     const int i = x < y ? x : y, j = x < y ? y : x;
@@ -426,23 +420,10 @@ struct JcView {
   }
 };
 
-// index at tournament position i in round r (np indices, np - 1 rounds)
-__device__ __forceinline__ int jc_at(int i, int r, int np) { return i == 0 ? 0 : ((i - 1 + r) % (np - 1)) + 1; }
-// tournament position of index x in round r
-__device__ __forceinline__ int jc_pos(int x, int r, int np) {
-  return x == 0 ? 0 : ((x - 1 - r) % (np - 1) + (np - 1)) % (np - 1) + 1;
-}
-// pair index of (x, y) in round r when x and y are paired there, else -1
-__device__ __forceinline__ int jc_pair_of(int x, int y, int r, int np) {
-  const int i = jc_pos(x, r, np), j = np - 1 - i;
-  return jc_at(j, r, np) == y ? (i < j ? i : j) : -1;
-}
-
 size_t jacobi_cluster_smem_bytes(int n) {
   const long long np = jac_np(n), half = np / 2;
   const long long rows = (np + kJcCluster - 1) / kJcCluster;
   long long b = 2 * rows * np * 8;     // A and V rows
-  b += 2 * np * 8 + 2 * half * 8;      // replicated diagonal and pivots, two parities
   b += half * (2 * 8 + 2 * 4 + 4 + 4 * 8);   // c, s; p, q; flag; t, app, aqq, apq
   b += sizeof(JcView) + kJcCluster * 4 + 64;   // DSMEM pointers, cluster flags, alignment
   b += 64 * 8;                         // reduction scratch
@@ -466,8 +447,6 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
   unsigned char* ptr = smem_raw;
   double* Aloc = reinterpret_cast<double*>(ptr); ptr += (size_t)rows * np * 8;
   double* Vloc = reinterpret_cast<double*>(ptr); ptr += (size_t)rows * np * 8;
-  double* rdiag = reinterpret_cast<double*>(ptr); ptr += (size_t)2 * np * 8;
-  double* rpiv = reinterpret_cast<double*>(ptr); ptr += (size_t)2 * half * 8;
   double* cs = reinterpret_cast<double*>(ptr); ptr += (size_t)half * 16;
   double* dg = reinterpret_cast<double*>(ptr); ptr += (size_t)half * 32;   // t, app, aqq, apq
   int* pq = reinterpret_cast<int*>(ptr); ptr += (size_t)half * 8;
@@ -481,8 +460,6 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
     for (int r = 0; r < kJcCluster; ++r) {
       view->A[r] = cluster.map_shared_rank(Aloc, r);
       view->V[r] = cluster.map_shared_rank(Vloc, r);
-      view->diag[r] = cluster.map_shared_rank(rdiag, r);
-      view->piv[r] = cluster.map_shared_rank(rpiv, r);
     }
     view->np = np;
   }
@@ -502,15 +479,12 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
   }
   cluster.sync();
   const JcView& W = *view;
-  // replicated copies for round 0 (parity 0), read before anyone writes A
-  for (int i = tid; i < np; i += nth) rdiag[i] = *W.a(i, i);
-  for (int k = tid; k < half; k += nth) rpiv[k] = *W.a(jc_at(k, 0, np), jc_at(np - 1 - k, 0, np));
-  // scale for the stopping test
+  // scale for the stopping test: every CTA reads every diagonal element
   double scale = 0.0;
   for (int i = tid; i < n; i += nth) { const double d = fabs(*W.a(i, i)); scale = d > scale ? d : scale; }
   for (int o = 16; o > 0; o >>= 1) { const double t = __shfl_xor_sync(0xffffffffu, scale, o); scale = t > scale ? t : scale; }
   if ((tid & 31) == 0) red[tid >> 5] = scale;
-  cluster.sync();                              // copies complete everywhere before round 0 writes
+  __syncthreads();
   if (tid == 0) {
     double sc = 0.0;
     for (int w = 0; w < (nth >> 5); ++w) sc = red[w] > sc ? red[w] : sc;
@@ -523,7 +497,6 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
   const int cw = (np + kJcCluster - 1) / kJcCluster;   // V columns per CTA
   const int c0 = rank * cw, c1 = min(np, c0 + cw);
 
-  int par = 0;                                 // parity of the current round's copies
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (sweep > 0) {
@@ -544,77 +517,62 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
     }
     double offmax = 0.0;
     for (int r = 0; r < np - 1; ++r) {
-      const double* dcur = rdiag + par * np;
-      const double* pcur = rpiv + par * half;
-      const int nxt = 1 - par, rn = (r + 1) % (np - 1);
-      // 1. rotations of this round from the local copies
+      int any = 0;
       for (int k = tid; k < half; k += nth) {
-        const int p1 = jc_at(k, r, np), p2 = jc_at(np - 1 - k, r, np);
+        const int i1 = k, i2 = np - 1 - k;
+        const int p1 = (i1 == 0) ? 0 : ((i1 - 1 + r) % (np - 1)) + 1;
+        const int p2 = (i2 == 0) ? 0 : ((i2 - 1 + r) % (np - 1)) + 1;
         const int p = p1 < p2 ? p1 : p2, q = p1 < p2 ? p2 : p1;
-        const double apq = pcur[k], app = dcur[p], aqq = dcur[q];
-        double c = 1.0, sn = 0.0, t = 0.0;
+        const double apq = *W.a(p, q);
+        double c = 1.0, sn = 0.0, t = 0.0, app = 0.0, aqq = 0.0;
         const double aa = fabs(apq);
         offmax = aa > offmax ? aa : offmax;
         const int doit = aa > thresh;
-        if (doit) jac_rotation(app, aqq, apq, &t, &c, &sn);
+        if (doit) {
+          app = *W.a(p, p);
+          aqq = *W.a(q, q);
+          jac_rotation(app, aqq, apq, &t, &c, &sn);
+        }
         cs[2 * k] = c; cs[2 * k + 1] = sn;
         dg[4 * k] = t; dg[4 * k + 1] = app; dg[4 * k + 2] = aqq; dg[4 * k + 3] = apq;
         pq[2 * k] = p; pq[2 * k + 1] = q;
         rot[k] = doit;
+        any |= doit;
       }
-      __syncthreads();
-      // 2a. diagonal 2x2 blocks (pair k by CTA k % kJcCluster): write A and
-      //     the next round's diagonal copies
-      for (int k = rank + kJcCluster * tid; k < half; k += kJcCluster * nth) {
+      // identical in every CTA: the whole cluster skips or rotates together
+      if (!__syncthreads_or(any)) continue;
+      cluster.sync();                          // all reads of the round's inputs done
+      // diagonal 2x2 blocks: the owner of row p writes them
+      for (int k = tid; k < half; k += nth) {
+        if (!rot[k] || (pq[2 * k] % kJcCluster) != rank) continue;
         const int p = pq[2 * k], q = pq[2 * k + 1];
-        const double t = dg[4 * k], apq = dg[4 * k + 3];
-        double app = dg[4 * k + 1], aqq = dg[4 * k + 2];
-        if (rot[k]) {
-          app -= t * apq;
-          aqq += t * apq;
-          *W.a(p, p) = app;
-          *W.a(q, q) = aqq;
-          *W.a(p, q) = 0.0;
-        }
-        for (int c = 0; c < kJcCluster; ++c) {
-          W.diag[c][nxt * np + p] = app;
-          W.diag[c][nxt * np + q] = aqq;
-        }
+        const double t = dg[4 * k], app = dg[4 * k + 1], aqq = dg[4 * k + 2], apq = dg[4 * k + 3];
+        *W.a(p, p) = app - t * apq;
+        *W.a(q, q) = aqq + t * apq;
+        *W.a(p, q) = 0.0;
       }
-      // 2b. off-diagonal 2x2 blocks (I < K) over the whole cluster; the
-      //     elements that pair up in the next round go to every CTA's copy
+      // off-diagonal 2x2 blocks (I < K) over the whole cluster
       for (long long b = (long long)rank * nth + tid; b < nblk; b += (long long)kJcCluster * nth) {
         const int g = (int)(b / (half - 1)), e = (int)(b % (half - 1));
         const int I1 = g, I2 = half - 1 - g;
         int I, K;
         if (e < half - 1 - I1) { I = I1; K = I1 + 1 + e; } else { I = I2; K = I2 + 1 + (e - (half - 1 - I1)); }
+        if (!(rot[I] | rot[K])) continue;
         const int p = pq[2 * I], q = pq[2 * I + 1], r2 = pq[2 * K], s2 = pq[2 * K + 1];
-        const int xs[4] = {p, p, q, q}, ys[4] = {r2, s2, r2, s2};
-        int kn[4];
-        bool need = false;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) { kn[u] = jc_pair_of(xs[u], ys[u], rn, np); need |= kn[u] >= 0; }
-        const bool rotated = rot[I] | rot[K];
-        if (!rotated && !need) continue;
-        double* el[4] = {W.a(p, r2), W.a(p, s2), W.a(q, r2), W.a(q, s2)};
-        double val[4] = {*el[0], *el[1], *el[2], *el[3]};
-        if (rotated) {
-          const double c = cs[2 * I], sn = cs[2 * I + 1], c2 = cs[2 * K], s2n = cs[2 * K + 1];
-          const double y00 = c * val[0] - sn * val[2], y01 = c * val[1] - sn * val[3];
-          const double y10 = sn * val[0] + c * val[2], y11 = sn * val[1] + c * val[3];
-          val[0] = y00 * c2 - y01 * s2n;
-          val[1] = y00 * s2n + y01 * c2;
-          val[2] = y10 * c2 - y11 * s2n;
-          val[3] = y10 * s2n + y11 * c2;
-#pragma unroll
-          for (int u = 0; u < 4; ++u) *el[u] = val[u];
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (kn[u] >= 0)
-            for (int c = 0; c < kJcCluster; ++c) W.piv[c][nxt * half + kn[u]] = val[u];
+        const double c = cs[2 * I], sn = cs[2 * I + 1], c2 = cs[2 * K], s2n = cs[2 * K + 1];
+        double* e_pr = W.a(p, r2);
+        double* e_ps = W.a(p, s2);
+        double* e_qr = W.a(q, r2);
+        double* e_qs = W.a(q, s2);
+        const double b00 = *e_pr, b01 = *e_ps, b10 = *e_qr, b11 = *e_qs;
+        const double y00 = c * b00 - sn * b10, y01 = c * b01 - sn * b11;
+        const double y10 = sn * b00 + c * b10, y11 = sn * b01 + c * b11;
+        *e_pr = y00 * c2 - y01 * s2n;
+        *e_ps = y00 * s2n + y01 * c2;
+        *e_qr = y10 * c2 - y11 * s2n;
+        *e_qs = y10 * s2n + y11 * c2;
       }
-      // 2c. V rows p, q: this CTA's column slice of every rotated pair
+      // V rows p, q: this CTA's column slice of every rotated pair
       if (c1 > c0) {
         const int w = c1 - c0;
         for (int e = tid; e < half * w; e += nth) {
@@ -629,8 +587,7 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
           *vq = sn * a + c * bq;
         }
       }
-      cluster.sync();                          // 3. the round's writes visible everywhere
-      par = nxt;
+      cluster.sync();                          // the round's writes visible everywhere
     }
     // converged when every rotation the sweep applied was at round-off level
     // (offmax is identical in every CTA: all of them saw every pivot)
@@ -649,14 +606,13 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
   }
 
   // ---- rank by eigenvalue, sign fix, write this CTA's rows ------------------
-  const double* dfin = rdiag + par * np;
   for (int lr = tid; lr < rows; lr += nth) {
     const int i = lr * kJcCluster + rank;
     if (i >= n) continue;
-    const double li = dfin[i];
+    const double li = Aloc[(long long)lr * np + i];
     int rk = 0;
     for (int j = 0; j < n; ++j) {
-      const double lj = dfin[j];
+      const double lj = *W.a(j, j);
       rk += (lj < li) || (lj == li && j < i);
     }
     double sum = 0.0;
@@ -667,7 +623,7 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
     for (int mu = 0; mu < n; ++mu) Co[mu] = sg * Vloc[(long long)lr * np + mu];
   }
   if (rank == 0 && tid == 0 && sweeps_out) sweeps_out[m] += sweep;
-  cluster.sync();                              // no CTA leaves while others may address its memory
+  cluster.sync();                              // no CTA leaves while others read its diagonal
 }
 
 // Clusters that fit at once on this device for the cluster kernel at basis n
