@@ -541,7 +541,10 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
       }
       // identical in every CTA: the whole cluster skips or rotates together
       if (!__syncthreads_or(any)) continue;
-      cluster.sync();                          // all reads of the round's inputs done
+      // all reads of the round's inputs done before any CTA writes: the values
+      // are already consumed (the tables above hold their results), so the
+      // arrive needs no release fence
+      asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
       // diagonal 2x2 blocks: the owner of row p writes them
       for (int k = tid; k < half; k += nth) {
         if (!rot[k] || (pq[2 * k] % kJcCluster) != rank) continue;
