@@ -968,9 +968,14 @@ void Batch::scf(const ScfSettings& s, bool requires_guess) {
   std::vector<int> all(h_mols.size());
   for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
   begin(s, all, requires_guess);
+  // One molecule: its iterations are short, so the host enqueues three before
+  // it waits for the convergence count.  Every kernel of an iteration skips
+  // molecules that are no longer active, so iterations enqueued past
+  // convergence change nothing.
+  const int every = all.size() == 1 ? 3 : 1;
   for (int it = 0; it < s.max_iter; ++it) {
     iterate(s, all);
-    if (count_active(all) == 0) break;
+    if (((it + 1) % every == 0 || it + 1 == s.max_iter) && count_active(all) == 0) break;
   }
   finish(s, all);
   int tc_err = 0;
