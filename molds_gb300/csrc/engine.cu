@@ -750,7 +750,12 @@ void Batch::begin(const ScfSettings& s, const std::vector<int>& which, bool requ
 
 // One Jacobi launch per size bucket; buckets whose molecules need a
 // global-memory workspace are split into launches of at most ws_slots CTAs.
-void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const float* Cin32) {
+bool Batch::cluster_jacobi(int b) const {
+  return bucket_max_n_[b] >= kClusterJacobiMinN && bucket_max_n_[b] <= kSmallJacobiMaxN &&
+         (int)buckets_[b].size() <= kClusterJacobiMaxMols && jacobi_cluster_capacity(bucket_max_n_[b]) > 0;
+}
+
+void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const float* Cin32, const double* F) {
   for (size_t b = 0; b < buckets_.size(); ++b) {
     bool ag, vg;
     const int nb = (int)buckets_[b].size();
@@ -773,13 +778,13 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const
     }
     // FP64, few molecules (the plain one-molecule path): one cluster of CTAs
     // per molecule puts several SMs' FP64 units on each diagonalisation
-    if (!fp32 && bucket_max_n_[b] >= kClusterJacobiMinN && nb <= kClusterJacobiMaxMols &&
-        jacobi_cluster_capacity(bucket_max_n_[b]) > 0) {
+    if (!fp32 && cluster_jacobi((int)b)) {
       launches_ += 1;
-      launch_jacobi_cluster_f64(d_mols, bucket_dev_[b], nb, bucket_max_n_[b], d_state, 1, d_G64, Cin, 1, d_C, d_eps,
-                                s.max_sweeps, d_sweeps, stream_);
+      launch_jacobi_cluster_f64(d_mols, bucket_dev_[b], nb, bucket_max_n_[b], d_state, 1, F ? nullptr : d_G64, F, Cin,
+                                1, d_C, d_eps, s.max_sweeps, d_sweeps, stream_);
       continue;
     }
+    if (F) throw std::logic_error("fused warm-start transform without the cluster Jacobi");
     const int chunk = jacobi_needs_workspace(bucket_max_n_[b], fp32 ? 4 : 8, &ag, &vg) ? cap_.ws_slots : nb;
     for (int k0 = 0; k0 < nb; k0 += chunk) {
       const int cnt = std::min(chunk, nb - k0);
@@ -799,14 +804,25 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const
 
 void Batch::eigen_step(const ScfSettings& s) {
   if (s.precision == 0) {
-    int h = prof_begin(kKTransform, active_work_estimate(kKTransform));
-    launches_ += 2;
-    launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, d_C, d_T64, false, true, 0.0, d_state, 1, -1, stream_);
-    launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, d_C, d_T64, d_G64, false, false, 0.0, d_state, 1, -1, stream_);
-    prof_end(h);
-    h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
-    run_jacobi(false, s, d_C);
-    prof_end(h);
+    // every size bucket on the cluster Jacobi (a few molecules): it forms
+    // G = C F C^T itself on the cluster's SMs
+    bool fuse = !buckets_.empty();
+    for (size_t b = 0; b < buckets_.size(); ++b) fuse = fuse && cluster_jacobi((int)b);
+    if (fuse) {
+      int h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
+      run_jacobi(false, s, d_C, nullptr, d_F);
+      prof_end(h);
+    } else {
+      int h = prof_begin(kKTransform, active_work_estimate(kKTransform));
+      launches_ += 2;
+      launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, d_C, d_T64, false, true, 0.0, d_state, 1, -1, stream_);
+      launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, d_C, d_T64, d_G64, false, false, 0.0, d_state, 1, -1,
+                  stream_);
+      prof_end(h);
+      h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
+      run_jacobi(false, s, d_C);
+      prof_end(h);
+    }
   } else {
     // The FP32 rotations of each iteration erode the orthonormality of the
     // warm-start basis; one Newton-Schulz step C <- 1.5 C - 0.5 (C C^T) C

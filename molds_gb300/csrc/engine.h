@@ -199,7 +199,9 @@ class Batch {
   std::vector<std::vector<int>> buckets_;      // jacobi size buckets (indices into cur_list_)
   std::vector<int*> d_bucket_lists_;     // persistent, one per size bucket, `slots` entries each
   std::vector<int*> bucket_dev_;         // device list of each non-empty bucket of the current list
-  void run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const float* Cin32 = nullptr);
+  void run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const float* Cin32 = nullptr,
+                  const double* F = nullptr);
+  bool cluster_jacobi(int bucket) const;   // FP64 bucket served by the cluster Jacobi
   std::vector<int> bucket_max_n_;
   struct JobSet { GemmJob* d = nullptr; int n = 0; int tiles = 0; int tc_tiles = 0; int cap = 0; };
   GemmJob* h_jobs_ = nullptr;             // pinned staging of the job tables

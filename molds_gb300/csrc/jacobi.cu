@@ -433,8 +433,9 @@ size_t jacobi_cluster_smem_bytes(int n) {
 __global__ void __cluster_dims__(kJcCluster, 1, 1) __launch_bounds__(512)
 jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
                       const MolState* __restrict__ st, int require_active, const double* __restrict__ G,
-                      const double* __restrict__ Cin, int use_basis, double* __restrict__ Cout,
-                      double* __restrict__ eps_out, int max_sweeps, int* __restrict__ sweeps_out) {
+                      const double* __restrict__ F, const double* __restrict__ Cin, int use_basis,
+                      double* __restrict__ Cout, double* __restrict__ eps_out, int max_sweeps,
+                      int* __restrict__ sweeps_out) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
@@ -464,18 +465,48 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
     view->np = np;
   }
   // ---- load this CTA's rows ------------------------------------------------
-  const double* Gm = G + mol.mat0;
   const double* Cm = Cin + mol.mat0;
-  for (long long e = tid; e < (long long)rows * np; e += nth) {
-    const int lr = (int)(e / np), j = (int)(e % np);
-    const int i = lr * kJcCluster + rank;
-    double a = 0.0, v = (i == j) ? 1.0 : 0.0;
-    if (i < np) {
-      if (i < n && j < n && j >= i) a = Gm[(long long)i * n + j];
-      if (i < n && j < n && use_basis) v = Cm[(long long)i * n + j];
+  if (F) {
+    // warm-start transform G = C F C^T fused in (G == nullptr): rows of
+    // T = C F into A, then the upper part of G's rows, G_ij = T_i . C_j, into V
+    const double* Fm = F + mol.mat0;
+    for (long long e = tid; e < (long long)rows * np; e += nth) {
+      const int lr = (int)(e / np), b = (int)(e % np);
+      const int i = lr * kJcCluster + rank;
+      double t = 0.0;
+      if (i < n && b < n)
+        for (int a = 0; a < n; ++a) t = fma(Cm[(long long)i * n + a], Fm[(long long)a * n + b], t);
+      Aloc[e] = t;
     }
-    Aloc[e] = a;
-    Vloc[e] = v;
+    __syncthreads();
+    for (long long e = tid; e < (long long)rows * np; e += nth) {
+      const int lr = (int)(e / np), j = (int)(e % np);
+      const int i = lr * kJcCluster + rank;
+      double g = 0.0;
+      if (i < n && j < n && j >= i)
+        for (int b = 0; b < n; ++b) g = fma(Aloc[(long long)lr * np + b], Cm[(long long)j * n + b], g);
+      Vloc[e] = g;
+    }
+    __syncthreads();
+    for (long long e = tid; e < (long long)rows * np; e += nth) Aloc[e] = Vloc[e];
+    for (long long e = tid; e < (long long)rows * np; e += nth) {
+      const int lr = (int)(e / np), j = (int)(e % np);
+      const int i = lr * kJcCluster + rank;
+      Vloc[e] = (i < n && j < n) ? Cm[(long long)i * n + j] : ((i == j) ? 1.0 : 0.0);
+    }
+  } else {
+    const double* Gm = G + mol.mat0;
+    for (long long e = tid; e < (long long)rows * np; e += nth) {
+      const int lr = (int)(e / np), j = (int)(e % np);
+      const int i = lr * kJcCluster + rank;
+      double a = 0.0, v = (i == j) ? 1.0 : 0.0;
+      if (i < np) {
+        if (i < n && j < n && j >= i) a = Gm[(long long)i * n + j];
+        if (i < n && j < n && use_basis) v = Cm[(long long)i * n + j];
+      }
+      Aloc[e] = a;
+      Vloc[e] = v;
+    }
   }
   cluster.sync();
   const JcView& W = *view;
@@ -658,12 +689,12 @@ int jacobi_cluster_capacity(int n) {
 }
 
 void launch_jacobi_cluster_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
-                               int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
-                               double* eps, int max_sweeps, int* sweeps_out, cudaStream_t s) {
+                               int require_active, const double* G, const double* F, const double* Cin, int use_basis,
+                               double* Cout, double* eps, int max_sweeps, int* sweeps_out, cudaStream_t s) {
   if (nlist <= 0) return;
   const size_t bytes = jacobi_cluster_smem_bytes(max_n);
   const int threads = jac_np(max_n) <= 64 ? 256 : 512;
-  jacobi_cluster_kernel<<<nlist * kJcCluster, threads, bytes, s>>>(mols, mol_list, st, require_active, G, Cin,
+  jacobi_cluster_kernel<<<nlist * kJcCluster, threads, bytes, s>>>(mols, mol_list, st, require_active, G, F, Cin,
                                                                    use_basis, Cout, eps, max_sweeps, sweeps_out);
 }
 

@@ -100,11 +100,12 @@ void launch_jacobi_f32(const DevMol* mols, const int* mol_list, int nlist, int m
                        double* eps, float* Aws, float* Vws, long long ws_stride, int max_sweeps,
                        int* sweeps_out, cudaStream_t s);
 // one molecule per cluster of 8 CTAs (FP64); jacobi_cluster_capacity(n) > 0
-// when the cluster kernel can run at basis n on this device
+// when the cluster kernel can run at basis n on this device.  With F given
+// (and G null) the kernel forms G = Cin F Cin^T itself.
 int jacobi_cluster_capacity(int n);
 void launch_jacobi_cluster_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
-                               int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
-                               double* eps, int max_sweeps, int* sweeps_out, cudaStream_t s);
+                               int require_active, const double* G, const double* F, const double* Cin, int use_basis,
+                               double* Cout, double* eps, int max_sweeps, int* sweeps_out, cudaStream_t s);
 void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
                        int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
                        double* eps, double* Aws, double* Vws, long long ws_stride, int max_sweeps,
