@@ -784,7 +784,6 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const
                                 1, d_C, d_eps, s.max_sweeps, d_sweeps, stream_);
       continue;
     }
-    if (F) throw std::logic_error("fused warm-start transform without the cluster Jacobi");
     const int chunk = jacobi_needs_workspace(bucket_max_n_[b], fp32 ? 4 : 8, &ag, &vg) ? cap_.ws_slots : nb;
     for (int k0 = 0; k0 < nb; k0 += chunk) {
       const int cnt = std::min(chunk, nb - k0);
@@ -804,25 +803,23 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const
 
 void Batch::eigen_step(const ScfSettings& s) {
   if (s.precision == 0) {
-    // every size bucket on the cluster Jacobi (a few molecules): it forms
-    // G = C F C^T itself on the cluster's SMs
-    bool fuse = !buckets_.empty();
-    for (size_t b = 0; b < buckets_.size(); ++b) fuse = fuse && cluster_jacobi((int)b);
-    if (fuse) {
-      int h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
-      run_jacobi(false, s, d_C, nullptr, d_F);
-      prof_end(h);
-    } else {
+    // size buckets on the cluster Jacobi (a few molecules) form G = C F C^T
+    // inside it on the cluster's SMs; the transform GEMMs run only when some
+    // bucket uses the one-CTA Jacobi (a molecule's path depends on its bucket
+    // alone, not on whether other buckets need the GEMMs)
+    bool gemms = false;
+    for (size_t b = 0; b < buckets_.size(); ++b) gemms = gemms || !cluster_jacobi((int)b);
+    if (gemms) {
       int h = prof_begin(kKTransform, active_work_estimate(kKTransform));
       launches_ += 2;
       launch_gemm(j_trans1_.d, j_trans1_.n, j_trans1_.tiles, d_F, d_C, d_T64, false, true, 0.0, d_state, 1, -1, stream_);
       launch_gemm(j_trans2_.d, j_trans2_.n, j_trans2_.tiles, d_C, d_T64, d_G64, false, false, 0.0, d_state, 1, -1,
                   stream_);
       prof_end(h);
-      h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
-      run_jacobi(false, s, d_C);
-      prof_end(h);
     }
+    int h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
+    run_jacobi(false, s, d_C, nullptr, d_F);
+    prof_end(h);
   } else {
     // The FP32 rotations of each iteration erode the orthonormality of the
     // warm-start basis; one Newton-Schulz step C <- 1.5 C - 0.5 (C C^T) C
