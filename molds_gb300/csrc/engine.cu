@@ -346,8 +346,9 @@ void Batch::allocate(const BatchCapacity& cap) {
   JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_};
   for (JobSet* j : all) { j->d = dalloc<GemmJob>(job_cap_, &bytes_); j->cap = job_cap_; }
   cuda_check(cudaHostAlloc(&h_jobs_, sizeof(GemmJob) * (size_t)job_cap_ * 13, cudaHostAllocDefault), "cudaHostAlloc jobs");
-  cuda_check(cudaHostAlloc(&h_lists_, sizeof(int) * (size_t)nm * 9, cudaHostAllocDefault), "cudaHostAlloc lists");
-  for (int b = 0; b < 8; ++b) d_bucket_lists_.push_back(dalloc<int>(nm, &bytes_));
+  cuda_check(cudaHostAlloc(&h_lists_, sizeof(int) * (size_t)nm * (kJacobiBuckets + 1), cudaHostAllocDefault),
+             "cudaHostAlloc lists");
+  for (int b = 0; b < kJacobiBuckets; ++b) d_bucket_lists_.push_back(dalloc<int>(nm, &bytes_));
   cuda_check(cudaStreamSynchronize(stream_), "allocate");
 }
 
@@ -513,11 +514,13 @@ void Batch::upload_list(const std::vector<int>& which) {
   if (!which.empty())
     cuda_check(cudaMemcpyAsync(d_list, h_lists_, which.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload list");
   build_jobs(which);
-  // Jacobi size buckets: smaller molecules get a smaller shared-memory footprint
+  // Jacobi size buckets: smaller molecules get a smaller shared-memory
+  // footprint; the first edge keeps bases below the cluster Jacobi's minimum
+  // apart from the ones it serves, so a molecule's kernel follows its own size
   buckets_.clear();
   bucket_max_n_.clear();
   bucket_dev_.clear();
-  const int edges[] = {64, 96, 128, 160, 194, 256, 338, 1 << 30};
+  const int edges[kJacobiBuckets] = {kClusterJacobiMinN - 1, 64, 96, 128, 160, 194, 256, 338, 1 << 30};
   int lo = 0, bi = 0;
   for (int hi : edges) {
     std::vector<int> b;

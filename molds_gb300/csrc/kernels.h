@@ -42,6 +42,7 @@ constexpr int kSmallJacobiMaxN = 194;
 // kClusterJacobiMinN use the cluster Jacobi (one 8-CTA cluster per molecule)
 constexpr int kClusterJacobiMaxMols = 8;
 constexpr int kClusterJacobiMinN = 32;
+constexpr int kJacobiBuckets = 9;   // size buckets of a molecule list (edges in Batch::upload_list)
 size_t block_jacobi_workspace(int max_n, int nslots, int elem, long long* stride, long long* qstride);
 int launch_block_jacobi_f32(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                             const float* G, const double* Cin, double* Cout, double* eps, void* ws, int max_sweeps,
