@@ -19,6 +19,7 @@
 // matrix from C_prev F C_prev^T (computed by the transform GEMMs), so late SCF
 // iterations converge in one or two sweeps.
 #include <cooperative_groups.h>
+#include <mutex>
 #include <cuda_runtime.h>
 #include "nddo_batch.cuh"
 #include "kernels.h"
@@ -661,31 +662,35 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
 }
 
 // Clusters that fit at once on this device for the cluster kernel at basis n
-// (0: not launchable, use the one-CTA kernel).
+// (0: not launchable, use the one-CTA kernel).  Queried once, for the largest
+// basis the kernel serves (the largest shared-memory footprint), under
+// std::call_once: lanes of the server call this from several host threads.
 int jacobi_cluster_capacity(int n) {
-  static int cached_n = -1, cached_val = 0;
-  if (n == cached_n) return cached_val;
-  const size_t bytes = jacobi_cluster_smem_bytes(n);
-  int val = 0;
-  if (bytes <= 232448) {
-    cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kJcCluster, 1, 1);
-    cfg.blockDim = dim3(jac_np(n) <= 64 ? 256 : 512, 1, 1);
-    cfg.dynamicSmemBytes = bytes;
-    cudaLaunchAttribute attr;
-    attr.id = cudaLaunchAttributeClusterDimension;
-    attr.val.clusterDim.x = kJcCluster;
-    attr.val.clusterDim.y = 1;
-    attr.val.clusterDim.z = 1;
-    cfg.attrs = &attr;
-    cfg.numAttrs = 1;
-    if (cudaOccupancyMaxActiveClusters(&val, jacobi_cluster_kernel, &cfg) != cudaSuccess) val = 0;
+  static std::once_flag once;
+  static int capacity = 0;
+  std::call_once(once, []() {
+    const size_t bytes = jacobi_cluster_smem_bytes(kSmallJacobiMaxN);
+    int val = 0;
+    if (bytes <= 232448 &&
+        cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) ==
+            cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(kJcCluster, 1, 1);
+      cfg.blockDim = dim3(512, 1, 1);
+      cfg.dynamicSmemBytes = bytes;
+      cudaLaunchAttribute attr;
+      attr.id = cudaLaunchAttributeClusterDimension;
+      attr.val.clusterDim.x = kJcCluster;
+      attr.val.clusterDim.y = 1;
+      attr.val.clusterDim.z = 1;
+      cfg.attrs = &attr;
+      cfg.numAttrs = 1;
+      if (cudaOccupancyMaxActiveClusters(&val, jacobi_cluster_kernel, &cfg) != cudaSuccess) val = 0;
+    }
     cudaGetLastError();
-  }
-  cached_n = n;
-  cached_val = val;
-  return val;
+    capacity = val;
+  });
+  return n <= kSmallJacobiMaxN ? capacity : 0;
 }
 
 void launch_jacobi_cluster_f64(const DevMol* mols, const int* mol_list, int nlist, int max_n, const MolState* st,
