@@ -555,14 +555,16 @@ jacobi_cluster_kernel(const DevMol* __restrict__ mols, const int* __restrict__ m
         const int p1 = (i1 == 0) ? 0 : ((i1 - 1 + r) % (np - 1)) + 1;
         const int p2 = (i2 == 0) ? 0 : ((i2 - 1 + r) % (np - 1)) + 1;
         const int p = p1 < p2 ? p1 : p2, q = p1 < p2 ? p2 : p1;
-        const double apq = *W.a(p, q);
+        // the three loads are issued together: one distributed-shared-memory
+        // round trip per round instead of two
+        const double apq = *W.a(p, q), app_in = *W.a(p, p), aqq_in = *W.a(q, q);
         double c = 1.0, sn = 0.0, t = 0.0, app = 0.0, aqq = 0.0;
         const double aa = fabs(apq);
         offmax = aa > offmax ? aa : offmax;
         const int doit = aa > thresh;
         if (doit) {
-          app = *W.a(p, p);
-          aqq = *W.a(q, q);
+          app = app_in;
+          aqq = aqq_in;
           jac_rotation(app, aqq, apq, &t, &c, &sn);
         }
         cs[2 * k] = c; cs[2 * k + 1] = sn;
