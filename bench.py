@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=16,
                     help="molecules solved one at a time on the plain FP64 path (0 = skip)")
-    ap.add_argument("--workload", default="water32", choices=["water32", "serving", "alkanes", "octane", "water512"],
+    ap.add_argument("--workload", default="water32",
+                    choices=["water32", "serving", "alkanes", "octane", "water512", "md"],
                     help="water32: 256 x (H2O)32 AM1 batched (the headline); serving: Poisson stream of PM3 "
                          "requests through the continuous-batching server; alkanes: uneven batch of random "
                          "alkanes with the precision ramp; octane: the plain one-molecule path")
@@ -574,6 +575,71 @@ def run_octane(args):
 
 
 # ---------------------------------------------------------------------------
+# Moving molecules: warm-started SCF steps (the MD / RPMD pattern)
+# ---------------------------------------------------------------------------
+def run_md(args):
+    """The (H2O)32 replicas take random-walk steps (0.01 A per coordinate and
+    step); after each step the resident batch is re-solved from the previous
+    densities (DoSCF(false), as MolDS's MD loop, src/md/MD.cpp:108, and RPMD
+    beads, src/rpmd/RPMD.cpp:78-84).  Timed: the coordinate upload, integrals,
+    SCF and properties of every step; a cold (guess) solve of the last
+    geometry checks the warm results and gives the iteration count it saves."""
+    import numpy as np
+    import molds_gb300 as M
+    from molds_gb300 import build
+    build.build()
+    ctx = M.Context(0)
+    mols = workload(0, args.nmol)
+    params = M.SCFParams(**SCF, precision=args.precision, dipole=args.dipole == "on")
+    b = M.ResidentBatch("am1", mols, context=ctx)
+    rng = np.random.default_rng(7)
+    x = np.concatenate([m.xyz for m in mols])
+    steps = [x]
+    for _ in range(args.warmup + args.steps):
+        steps.append(steps[-1] + rng.normal(scale=0.01 * M.ANG2AU, size=x.shape))
+    b.run(params)                                   # first step from the guess
+    for k in range(1, args.warmup + 1):
+        b.set_coordinates(steps[k])
+        b.run(params, requires_guess=False)
+    clocks = Clocks(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    its = []
+    for k in range(args.warmup + 1, args.warmup + 1 + args.steps):
+        b.set_coordinates(steps[k])
+        b.run(params, requires_guess=False)
+        res, _ = b.results()
+        its.append(float(np.mean([r["iterations"] for r in res])))
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    warm_e = np.array([r["energy"] for r in res])
+    ok = all(r["status"] == M.STATUS_CONVERGED for r in res)
+    t1 = time.perf_counter()
+    b.run(params)                                   # the same geometry from the guess
+    cold_s = time.perf_counter() - t1
+    cold, _ = b.results()
+    cold_e = np.array([r["energy"] for r in cold])
+    value = args.nmol * args.steps / wall
+    line = {"metric": "warm-started SCF solves/s (MD / RPMD steps of resident molecules)", "value": value,
+            "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32+fp64" if args.precision == "mixed" else "f64",
+            "data": "synthetic: seeded (H2O)32 replicas on a random walk",
+            "config": {"workload": f"{args.nmol} replicas of (H2O)32, AM1, 0.01 A random-walk step, "
+                                   "SCF from the previous density", "precision": args.precision,
+                       "scf": SCF, "dipole": args.dipole == "on"},
+            "e2e": {"value": value, "unit": "solves/s",
+                    "h2d_bytes_per_step": int(x.size * 8), "d2h_bytes_per_step": int(args.nmol * ctypes.sizeof(M.ScfResultC)),
+                    "call": "nddo_batch_set_coordinates + nddo_batch_run_ex(requires_guess = 0) + nddo_batch_results, "
+                            "host wall clock"},
+            "iterations": {"warm_mean": float(np.mean(its)), "cold_mean": float(np.mean([r["iterations"] for r in cold]))},
+            "cold_step_ms": 1e3 * cold_s, "all_converged": ok,
+            "accuracy": {"max_abs_dE_warm_vs_cold_Eh": float(np.max(np.abs(warm_e - cold_e)))},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
 # Large single molecule: (H2O)512 MNDO, N = 3072
 # ---------------------------------------------------------------------------
 def run_water512(args):
@@ -720,5 +786,7 @@ if __name__ == "__main__":
         run_alkanes(a)
     elif a.workload == "water512":
         run_water512(a)
+    elif a.workload == "md":
+        run_md(a)
     else:
         run_octane(a)

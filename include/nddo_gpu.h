@@ -80,6 +80,12 @@ const char* nddo_last_error(const nddo_ctx* ctx);
  * the electron count (odd -> error, src/cndo/Cndo2.cpp:351-357) and computes
  * the one-time pair integrals, overlap and core-core terms. */
 int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* atomic_numbers, const double* xyz_bohr);
+/* New coordinates for the molecule already set (same atoms, bohr), as the MD /
+ * MC / optimiser drivers move MolDS's Molecule in place before calling
+ * DoSCF(false) (src/md/MD.cpp:108): the one-time integrals are recomputed and
+ * the density of the last SCF is kept, so nddo_scf(..., requires_guess = 0)
+ * starts from it. */
+int nddo_set_coordinates(nddo_ctx* ctx, const double* xyz_bohr);
 int nddo_num_aos(const nddo_ctx* ctx);
 int nddo_num_atoms(const nddo_ctx* ctx);
 
@@ -131,6 +137,11 @@ int nddo_batch_create(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, 
                       const double* xyz_bohr, int diis_num_error_vect, nddo_batch** out);
 /* Integrals + SCF + energies of every molecule, on the device only. */
 int nddo_batch_run(nddo_batch* b, const nddo_scf_params* params);
+/* As nddo_batch_run with DoSCF's requiresGuess: 0 starts every molecule from
+ * its density of the previous run (after nddo_batch_set_coordinates: the
+ * warm start of MD steps and RPMD beads, src/rpmd/RPMD.cpp:78-84); the first
+ * run of a batch always starts from the guess. */
+int nddo_batch_run_ex(nddo_batch* b, const nddo_scf_params* params, int requires_guess);
 /* New coordinates for all atoms (same atoms, batch order), bohr. */
 int nddo_batch_set_coordinates(nddo_batch* b, const double* xyz_bohr);
 int nddo_batch_results(nddo_batch* b, nddo_scf_result* results, double* charges);

@@ -75,6 +75,7 @@ SIGNATURES = {
     "nddo_destroy": (None, [_CTX]),
     "nddo_last_error": (ctypes.c_char_p, [_CTX]),
     "nddo_set_molecule": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _DP]),
+    "nddo_set_coordinates": (ctypes.c_int, [_CTX, _DP]),
     "nddo_num_aos": (ctypes.c_int, [_CTX]),
     "nddo_num_atoms": (ctypes.c_int, [_CTX]),
     "nddo_scf": (ctypes.c_int, [_CTX, ctypes.POINTER(ScfParamsC), ctypes.c_int, ctypes.POINTER(ScfResultC)]),
@@ -92,6 +93,7 @@ SIGNATURES = {
     "nddo_batch_create": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_void_p)]),
     "nddo_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScfParamsC)]),
+    "nddo_batch_run_ex": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScfParamsC), ctypes.c_int]),
     "nddo_batch_set_coordinates": (ctypes.c_int, [ctypes.c_void_p, _DP]),
     "nddo_batch_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScfResultC), _DP]),
     "nddo_batch_device_bytes": (ctypes.c_size_t, [ctypes.c_void_p]),
@@ -239,6 +241,14 @@ class ElectronicStructure:
         self.n = self.ctx.lib.nddo_num_aos(self.ctx.h)
         self.result = None
 
+    def SetCoordinates(self, xyz_bohr):
+        """Moves the molecule (same atoms): integrals are recomputed and the
+        last density is kept, so DoSCF(False) starts from it (the MD / MC /
+        optimiser pattern, src/md/MD.cpp:108)."""
+        x = np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1, 3)
+        self.ctx.check(self.ctx.lib.nddo_set_coordinates(self.ctx.h, _dp(x)))
+        self.molecule = Molecule(self.molecule.Z, x)
+
     def DoSCF(self, requiresGuess: bool = True, params: SCFParams | None = None):
         p = to_c_params(params or self.params)
         r = ScfResultC()
@@ -358,9 +368,11 @@ class ResidentBatch:
         self.h = h
         self.n = len(molecules)
 
-    def run(self, params: SCFParams):
+    def run(self, params: SCFParams, requires_guess: bool = True):
+        """Integrals + SCF + properties of every molecule; requires_guess=False
+        starts each molecule from its density of the previous run (DoSCF(false))."""
         p = to_c_params(params)
-        self.ctx.check(self.ctx.lib.nddo_batch_run(self.h, ctypes.byref(p)))
+        self.ctx.check(self.ctx.lib.nddo_batch_run_ex(self.h, ctypes.byref(p), 1 if requires_guess else 0))
 
     def set_coordinates(self, xyz):
         x = np.ascontiguousarray(xyz, dtype=np.float64)

@@ -17,6 +17,7 @@ struct nddo_batch {
   std::unique_ptr<nddo::GroupedBatch> b;
   std::vector<int> n_atoms;
   bool dipole = false;          // the last nddo_batch_run computed dipole moments
+  bool ran = false;             // a run completed: every molecule has a density to start from
 };
 
 namespace {
@@ -282,6 +283,16 @@ int nddo_get_fock_matrix(nddo_ctx* ctx, double* out) { return getter(ctx, out, 3
 int nddo_get_density(nddo_ctx* ctx, double* out) { return getter(ctx, out, 2); }
 int nddo_get_mulliken(nddo_ctx* ctx, double* out) { return getter(ctx, out, 11); }
 
+int nddo_set_coordinates(nddo_ctx* ctx, const double* xyz) {
+  return guarded(ctx, [&]() {
+    if (!ctx->mol) return fail(ctx, NDDO_ERR_STATE, "A molecule is not set.");
+    if (!xyz) return fail(ctx, NDDO_ERR_ARGUMENT, "null coordinates");
+    ctx->mol->set_molecule_coordinates(0, xyz);   // validates before it changes anything
+    ctx->mol->integrals(std::vector<int>{0});
+    return (int)NDDO_OK;
+  });
+}
+
 int nddo_get_dipole(nddo_ctx* ctx, double* out) {
   return guarded(ctx, [&]() {
     if (!ctx->mol || !ctx->has_scf) return fail(ctx, NDDO_ERR_STATE, "no SCF result");
@@ -434,7 +445,7 @@ int nddo_batch_create(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, 
   });
 }
 
-int nddo_batch_run(nddo_batch* h, const nddo_scf_params* params) {
+int nddo_batch_run_ex(nddo_batch* h, const nddo_scf_params* params, int requires_guess) {
   if (!h) return NDDO_ERR_ARGUMENT;
   return guarded(h->ctx, [&]() {
     std::string why;
@@ -442,11 +453,17 @@ int nddo_batch_run(nddo_batch* h, const nddo_scf_params* params) {
     nddo::ScfSettings s = to_settings(params);
     s.keep_trace = 0;
     h->dipole = false;
-    h->b->run(s);
+    // no previous density before the first run: the guess, as DoSCF's first call
+    const bool guess = requires_guess != 0 || !h->ran;
+    h->ran = false;
+    h->b->run(s, guess);
+    h->ran = true;
     h->dipole = s.dipole != 0;
     return (int)NDDO_OK;
   });
 }
+
+int nddo_batch_run(nddo_batch* h, const nddo_scf_params* params) { return nddo_batch_run_ex(h, params, 1); }
 
 int nddo_batch_set_coordinates(nddo_batch* h, const double* xyz) {
   if (!h) return NDDO_ERR_ARGUMENT;

@@ -49,11 +49,14 @@ __global__ void init_state_kernel(const DevMol* __restrict__ mols, const int* __
     st[m] = s;
     if (sweeps) sweeps[m] = 0;
   }
-  for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
-    const long long r = i / mol.nao, c = i % mol.nao;
-    C[mol.mat0 + i] = (r == c) ? 1.0 : 0.0;
-    if (reset_density) P[mol.mat0 + i] = 0.0;
-  }
+  // a run from the previous density (requires_guess = 0) also keeps the
+  // previous eigenvectors as the eigensolver's warm-start basis
+  if (reset_density)
+    for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
+      const long long r = i / mol.nao, c = i % mol.nao;
+      C[mol.mat0 + i] = (r == c) ? 1.0 : 0.0;
+      P[mol.mat0 + i] = 0.0;
+    }
   // the DIIS window starts zero-filled (as the reference's zero-initialised history)
   for (int k = 0; k < diis_m; ++k)
     for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
@@ -670,6 +673,25 @@ void Batch::set_coordinates(const double* xyz) {
   }
   cuda_check(cudaMemcpyAsync(d_atoms, h_atoms.data(), h_atoms.size() * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_),
              "upload atoms");
+}
+
+void Batch::set_molecule_coordinates(int m, const double* xyz) {
+  if (m < 0 || m >= (int)h_mols.size()) throw std::invalid_argument("molecule index out of range");
+  const DevMol& d = h_mols[m];
+  for (int a = 0; a < 3 * d.natoms; ++a)
+    if (!std::isfinite(xyz[a])) throw std::invalid_argument("non-finite coordinate");
+  for (int k = 0; k < d.npairs; ++k) {
+    const DevPair& p = h_pairs[d.pair0 + k];
+    const double* A = xyz + 3 * (p.a - d.atom0);
+    const double* B = xyz + 3 * (p.b - d.atom0);
+    if (A[0] == B[0] && A[1] == B[1] && A[2] == B[2]) throw std::invalid_argument("two atoms at the same position");
+  }
+  for (int a = 0; a < d.natoms; ++a) {
+    DevAtom& at = h_atoms[d.atom0 + a];
+    at.x = xyz[3 * a]; at.y = xyz[3 * a + 1]; at.z = xyz[3 * a + 2];
+  }
+  cuda_check(cudaMemcpyAsync(d_atoms + d.atom0, h_atoms.data() + d.atom0, d.natoms * sizeof(DevAtom),
+                             cudaMemcpyHostToDevice, stream_), "upload atoms");
 }
 
 void Batch::integrals() {

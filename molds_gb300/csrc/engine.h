@@ -128,6 +128,10 @@ class Batch {
 
   const std::vector<DevMol>& mol_table() const { return h_mols; }
   void set_coordinates(const double* xyz);          // bohr, 3 per atom, batch order
+  // new coordinates of one molecule (pool mode: the slot's atoms only); the
+  // density, eigenvectors and DIIS arrays are kept, so a following
+  // scf(..., requires_guess = false) starts from the previous density
+  void set_molecule_coordinates(int m, const double* xyz);
   // per-kernel-class timing with CUDA events on the launching stream
   // Enabling creates the event pool up front (kProfEvents), so the timed
   // region that follows does not pay for cudaEventCreate.
@@ -242,7 +246,9 @@ class GroupedBatch {
   static int default_groups(int n_mol);
   int size() const { return n_; }
   int groups() const { return (int)g_.size(); }
-  void run(const ScfSettings& s);                 // integrals + SCF + energies of every molecule
+  // integrals + SCF + energies of every molecule; requires_guess = false
+  // starts every molecule from its previous density (DoSCF(false))
+  void run(const ScfSettings& s, bool requires_guess = true);
   void results(std::vector<MolResult>* out);
   void copy_charges(int m, double* host) const;
   void copy_matrix(int which_matrix, int m, double* host) const;

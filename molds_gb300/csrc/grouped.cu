@@ -47,10 +47,10 @@ GroupedBatch::~GroupedBatch() {
   for (cudaStream_t s : streams_) cudaStreamDestroy(s);
 }
 
-void GroupedBatch::run(const ScfSettings& s) {
+void GroupedBatch::run(const ScfSettings& s, bool requires_guess) {
   if (g_.size() == 1) {
     g_[0]->integrals();
-    g_[0]->scf(s, true);
+    g_[0]->scf(s, requires_guess);
     return;
   }
   std::vector<std::exception_ptr> err(g_.size());
@@ -60,7 +60,7 @@ void GroupedBatch::run(const ScfSettings& s) {
       try {
         cuda_check(cudaSetDevice(device_), "cudaSetDevice");
         g_[g]->integrals();
-        g_[g]->scf(s, true);
+        g_[g]->scf(s, requires_guess);
       } catch (...) {
         err[g] = std::current_exception();
       }

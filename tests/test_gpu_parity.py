@@ -328,3 +328,42 @@ def test_grouped_batch_new_coordinates_match_plain_path(ctx):
         assert res[i]["status"] == M.STATUS_CONVERGED
         assert abs(res[i]["energy"] - es.GetElectronicEnergy()) <= 1e-10
         assert np.max(np.abs(q[i] - es.GetMullikenCharges())) <= 1e-10
+
+
+def test_warm_start_after_coordinate_change(ctx):
+    """The MD / MC step: the molecule moves and DoSCF(false) starts from the
+    previous density (Cndo2::DoSCF with requiresGuess = false,
+    src/cndo/Cndo2.cpp:585-729; src/md/MD.cpp:108), on the plain path and on a
+    resident batch, against the oracle started from its own previous density."""
+    base = W.water_cluster(shape=(2, 2, 2), seed=2)          # (H2O)8, 48 basis functions
+    rng = np.random.default_rng(11)
+    new_xyz = base.xyz + rng.normal(scale=0.02, size=base.xyz.shape)
+    r0 = O.scf(O.make_molecule("am1", base.Z, base.xyz), oracle_params(BENCH_SCF))
+    om1 = O.make_molecule("am1", base.Z, new_xyz)
+    ref = O.scf(om1, oracle_params(BENCH_SCF), requires_guess=False, P0=r0.P)
+    cold = O.scf(om1, oracle_params(BENCH_SCF))
+    assert ref.iterations < cold.iterations
+    es = M.ElectronicStructure("am1", BENCH_SCF, context=ctx)
+    es.SetMolecule(base)
+    es.DoSCF(True)
+    es.SetCoordinates(new_xyz)
+    es.DoSCF(False)
+    assert abs(es.GetElectronicEnergy(0) - ref.energy) < E_TOL_FP64
+    assert np.max(np.abs(es.GetMullikenCharges() - ref.charges)) < Q_TOL
+    assert es.GetIterations() == ref.iterations
+    # the same step for three replicas resident on the device
+    mols = W.water_replicas(base, 3)
+    b = M.ResidentBatch("am1", mols, context=ctx)
+    b.run(BENCH_SCF)
+    moved = [m.xyz + rng.normal(scale=0.02, size=m.xyz.shape) for m in mols]
+    b.set_coordinates(np.concatenate(moved))
+    b.run(BENCH_SCF, requires_guess=False)
+    res, charges = b.results()
+    for m, x, r, q in zip(mols, moved, res, charges):
+        p0 = O.scf(O.make_molecule("am1", m.Z, m.xyz), oracle_params(BENCH_SCF)).P
+        rr = O.scf(O.make_molecule("am1", m.Z, x), oracle_params(BENCH_SCF), requires_guess=False, P0=p0)
+        assert abs(r["energy"] - rr.energy) < E_TOL_FP64
+        assert np.max(np.abs(q - rr.charges)) < Q_TOL
+        assert r["iterations"] == rr.iterations
+    b.close()
+

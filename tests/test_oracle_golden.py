@@ -91,3 +91,18 @@ def test_dipole_moments(case):
 def test_aos_match(case):
     c, mol, r = case
     assert O.num_aos(mol) == c["n_ao"]
+
+
+def test_warm_start_from_previous_density():
+    """DoSCF(false) after the molecule moved (src/md/MD.cpp:108): the oracle
+    started from the previous density converges to the cold-start energy in
+    no more iterations."""
+    c = [c for c in FIX if c["name"] == "ch3f_pm3"][0]
+    mol, params = O.parse_input(c["input"])
+    r0 = O.scf(mol, params)
+    moved = O.make_molecule(mol.theory, mol.Z, mol.xyz + np.random.default_rng(3).normal(scale=0.01, size=mol.xyz.shape))
+    warm = O.scf(moved, params, requires_guess=False, P0=r0.P)
+    cold = O.scf(moved, params)
+    assert abs(warm.energy - cold.energy) < 1e-9
+    assert warm.iterations <= cold.iterations
+
