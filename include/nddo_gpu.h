@@ -26,7 +26,9 @@ extern "C" {
 
 typedef struct nddo_ctx nddo_ctx;
 
-enum { NDDO_THEORY_MNDO = 0, NDDO_THEORY_AM1 = 1, NDDO_THEORY_PM3 = 2 };
+/* AM1-D / PM3-D: MolDS's dispersion-corrected sets (THEORY am1-d / pm3-d;
+ * src/am1/Am1D.cpp, src/pm3/Pm3D.cpp), H, C, N, O and S only. */
+enum { NDDO_THEORY_MNDO = 0, NDDO_THEORY_AM1 = 1, NDDO_THEORY_PM3 = 2, NDDO_THEORY_AM1D = 3, NDDO_THEORY_PM3D = 4 };
 enum { NDDO_PRECISION_FP64 = 0, NDDO_PRECISION_MIXED = 1 };
 enum {
   NDDO_OK = 0,
@@ -52,6 +54,9 @@ typedef struct {
   double fp64_switch_error;    /* mixed: FP64 phase once the DIIS error is below this */
   int tensor_cores;            /* mixed: FP32-phase GEMMs on the tensor cores (1, default) or CUDA cores (0) */
   int dipole;                  /* dipole moment after convergence (1, default, as DoSCF) or skipped (0) */
+  int vdw;                     /* vdW yes/no: empirical dispersion energy (always on for AM1-D / PM3-D) */
+  double vdw_s6;               /* vdW_s6 (default 1.40; AM1-D / PM3-D use 1.40)  */
+  double vdw_d;                /* vdW_d  (default 23;  AM1-D / PM3-D use 23)    */
 } nddo_scf_params;
 
 typedef struct {
@@ -64,6 +69,7 @@ typedef struct {
   double final_diis_error;     /* last DIIS error (max |P_new - P_old|)      */
   double dipole[9];            /* total, electronic, core dipole (x, y, z) [a.u.]; 0 with dipole = 0
                                   (Cndo2::OutputSCFDipole, src/cndo/Cndo2.cpp:1126-1185) */
+  double vdw_energy;           /* empirical dispersion energy [Eh], included in energy (0 when off) */
 } nddo_scf_result;
 
 /* Defaults of src/base/Parameters.cpp:133-139 (precision = FP64). */

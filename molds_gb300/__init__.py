@@ -47,14 +47,15 @@ class ScfParamsC(ctypes.Structure):
                 ("diis_num_error_vect", ctypes.c_int), ("diis_start_error", ctypes.c_double),
                 ("diis_end_error", ctypes.c_double), ("precision", ctypes.c_int),
                 ("fp64_switch_error", ctypes.c_double), ("tensor_cores", ctypes.c_int),
-                ("dipole", ctypes.c_int)]
+                ("dipole", ctypes.c_int), ("vdw", ctypes.c_int), ("vdw_s6", ctypes.c_double),
+                ("vdw_d", ctypes.c_double)]
 
 
 class ScfResultC(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("energy", ctypes.c_double),
                 ("core_repulsion", ctypes.c_double), ("heat_of_formation", ctypes.c_double),
                 ("final_rms", ctypes.c_double), ("final_diis_error", ctypes.c_double),
-                ("dipole", ctypes.c_double * 9)]
+                ("dipole", ctypes.c_double * 9), ("vdw_energy", ctypes.c_double)]
 
 
 class ServeResultC(ctypes.Structure):
@@ -163,6 +164,9 @@ def to_c_params(p: SCFParams) -> ScfParamsC:
     c.fp64_switch_error = float(p.fp64_switch_error)
     c.tensor_cores = 1 if getattr(p, "tensor_cores", True) else 0
     c.dipole = 1 if getattr(p, "dipole", True) else 0
+    c.vdw = 1 if getattr(p, "vdw", False) else 0
+    c.vdw_s6 = float(getattr(p, "vdw_s6", 1.40))
+    c.vdw_d = float(getattr(p, "vdw_d", 23.0))
     return c
 
 
@@ -270,6 +274,10 @@ class ElectronicStructure:
     def GetCoreRepulsionEnergy(self) -> float:
         return self.result.core_repulsion
 
+    def GetVdWCorrectionEnergy(self) -> float:
+        """Empirical dispersion energy, included in GetElectronicEnergy (Cndo2.cpp:825)."""
+        return self.result.vdw_energy
+
     def GetHeatsFormation(self) -> float:
         return self.result.heat_of_formation
 
@@ -346,7 +354,7 @@ def batch_scf(theory, molecules, params: SCFParams | None = None, context: Conte
         ctx.check(rc)
     out = [dict(status=r.status, iterations=r.iterations, energy=r.energy, core_repulsion=r.core_repulsion,
                 heat_of_formation=r.heat_of_formation, final_rms=r.final_rms,
-                final_diis_error=r.final_diis_error, dipole=_dipole3(r)) for r in res]
+                final_diis_error=r.final_diis_error, dipole=_dipole3(r), vdw_energy=r.vdw_energy) for r in res]
     offs = np.concatenate([[0], np.cumsum(nat)])
     return out, [ch[offs[i]:offs[i + 1]] for i in range(len(molecules))]
 
@@ -387,7 +395,7 @@ class ResidentBatch:
         offs = np.concatenate([[0], np.cumsum(self.nat)])
         out = [dict(status=r.status, iterations=r.iterations, energy=r.energy, core_repulsion=r.core_repulsion,
                     heat_of_formation=r.heat_of_formation, final_rms=r.final_rms,
-                    final_diis_error=r.final_diis_error, dipole=_dipole3(r)) for r in res]
+                    final_diis_error=r.final_diis_error, dipole=_dipole3(r), vdw_energy=r.vdw_energy) for r in res]
         return out, [ch[offs[i]:offs[i + 1]] for i in range(self.n)]
 
     def device_bytes(self) -> int:

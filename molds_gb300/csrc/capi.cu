@@ -101,6 +101,9 @@ nddo::ScfSettings to_settings(const nddo_scf_params* p) {
     s.switch_error = p->fp64_switch_error;
     s.tensor_cores = p->tensor_cores;
     s.dipole = p->dipole;
+    s.vdw = p->vdw;
+    s.vdw_s6 = p->vdw_s6;
+    s.vdw_d = p->vdw_d;
   }
   return s;
 }
@@ -128,6 +131,7 @@ bool valid_params(const nddo_scf_params* p, std::string* why) {
   if (p->diis_num_error_vect < 0 || p->diis_num_error_vect > nddo::kMaxDiis) { *why = "diis_num_error_vect must be in 0..8"; return false; }
   if (p->precision != NDDO_PRECISION_FP64 && p->precision != NDDO_PRECISION_MIXED) { *why = "unknown precision"; return false; }
   if (!(p->rms_density > 0.0)) { *why = "rms_density must be > 0"; return false; }
+  if (p->vdw && !(p->vdw_s6 >= 0.0 && p->vdw_d > 0.0)) { *why = "vdw_s6 must be >= 0 and vdw_d > 0"; return false; }
   return true;
 }
 
@@ -148,6 +152,9 @@ void nddo_default_params(nddo_scf_params* p) {
   p->fp64_switch_error = 1e-4;
   p->tensor_cores = 1;
   p->dipole = 1;
+  p->vdw = 0;
+  p->vdw_s6 = 1.40;
+  p->vdw_d = 23.0;
 }
 
 int nddo_create(int device, size_t hbm_budget_bytes, nddo_ctx** out) {
@@ -259,6 +266,7 @@ int nddo_scf(nddo_ctx* ctx, const nddo_scf_params* params, int requires_guess, n
       result->final_rms = r[0].final_rms;
       result->final_diis_error = r[0].final_diis_error;
       for (int k = 0; k < 9; ++k) result->dipole[k] = s.dipole ? r[0].dipole[k] : 0.0;
+      result->vdw_energy = r[0].vdw_energy;
     }
     if (r[0].status != nddo::kConverged)
       return fail(ctx, NDDO_NOT_CONVERGED,
@@ -406,6 +414,7 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
       results[i].final_rms = r[i].final_rms;
       results[i].final_diis_error = r[i].final_diis_error;
       for (int k = 0; k < 9; ++k) results[i].dipole[k] = s.dipole ? r[i].dipole[k] : 0.0;
+      results[i].vdw_energy = r[i].vdw_energy;
       if (r[i].status != nddo::kConverged) rc = NDDO_NOT_CONVERGED;
       if (charges) b.copy_charges(i, charges + off);
       off += n_atoms[i];
@@ -491,6 +500,7 @@ int nddo_batch_results(nddo_batch* h, nddo_scf_result* results, double* charges)
       results[i].final_rms = r[i].final_rms;
       results[i].final_diis_error = r[i].final_diis_error;
       for (int k = 0; k < 9; ++k) results[i].dipole[k] = h->dipole ? r[i].dipole[k] : 0.0;
+      results[i].vdw_energy = r[i].vdw_energy;
       if (r[i].status != nddo::kConverged) rc = NDDO_NOT_CONVERGED;
       if (charges) h->b->copy_charges((int)i, charges + off);
       off += h->n_atoms[i];

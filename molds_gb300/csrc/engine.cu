@@ -96,7 +96,7 @@ Engine::Engine(int device) : device_(device) {
   nddo_atom_params params[kNumParamSlots];
   std::memset(params, 0, sizeof(params));
   static const int zs[NDDO_NUM_ELEMENTS] = {1, 6, 7, 8, 9, 16, 17};
-  for (int t = 0; t < NDDO_NUM_THEORIES; ++t)
+  for (int t = 0; t < NDDO_NUM_THEORY_SLOTS; ++t)
     for (int e = 0; e < NDDO_NUM_ELEMENTS; ++e) nddo_fill_atom_params(t, zs[e], &params[t * NDDO_NUM_ELEMENTS + e]);
   upload_params(params, stream_);
   cuda_check(cudaStreamSynchronize(stream_), "engine init");
@@ -158,11 +158,13 @@ MolLayout layout_molecule(const MoleculeInput& in) {
   const int na = (int)in.Z.size();
   if (na < 1) throw std::invalid_argument("molecule without atoms");
   if ((int)in.xyz.size() != 3 * na) throw std::invalid_argument("coordinate count does not match atom count");
-  if (in.theory < 0 || in.theory >= NDDO_NUM_THEORIES) throw std::invalid_argument("unknown theory");
+  if (in.theory < 0 || in.theory >= NDDO_NUM_THEORY_SLOTS) throw std::invalid_argument("unknown theory");
   int ao = 0, nelec = 0;
   for (int a = 0; a < na; ++a) {
     const int e = nddo_element_index(in.Z[a]);
-    if (e < 0) throw std::invalid_argument("element " + std::to_string(in.Z[a]) + " has no NDDO parameters");
+    nddo_atom_params probe;
+    if (e < 0 || nddo_fill_atom_params(in.theory, in.Z[a], &probe) != 0)
+      throw std::invalid_argument("element " + std::to_string(in.Z[a]) + " has no parameters for this theory");
     for (int k = 0; k < 3; ++k)
       if (!std::isfinite(in.xyz[3 * a + k])) throw std::invalid_argument("non-finite coordinate");
     DevAtom at;
@@ -991,7 +993,11 @@ void Batch::finish(const ScfSettings& s, const std::vector<int>& which) {
   int h = prof_begin(kKEnergy, 0.0);
   launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, max_atoms, d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0,
                      0, 0, stream_);
-  launch_energy_kernel(d_atoms, d_mols, d_list, nl, d_P, d_F, d_H, d_state, d_charges, stream_);
+  VdwParams vdw;
+  vdw.on = s.vdw;
+  vdw.s6 = s.vdw_s6;
+  vdw.d = s.vdw_d;
+  launch_energy_kernel(d_atoms, d_pairs, d_mols, d_list, nl, d_P, d_F, d_H, d_state, d_charges, vdw, stream_);
   prof_end(h);
   if (s.dipole) {
     launches_ += 2;
@@ -1037,6 +1043,7 @@ void Batch::results(std::vector<MolResult>* out) {
     r.final_rms = st[m].rms;
     r.final_diis_error = st[m].diis_err;
     for (int k = 0; k < 9; ++k) r.dipole[k] = st[m].dipole[k];
+    r.vdw_energy = st[m].vdw_energy;
   }
 }
 

@@ -30,6 +30,8 @@ struct ScfSettings {
   int keep_trace = 1;
   int tensor_cores = 1;         // mixed: FP32-phase GEMMs on tcgen05 (3xTF32) instead of CUDA cores
   int dipole = 1;               // dipole moment after convergence (MolDS DoSCF always computes it)
+  int vdw = 0;                  // empirical dispersion energy (SCF block "vdW yes"; always on for AM1-D / PM3-D)
+  double vdw_s6 = 1.40, vdw_d = 23.0;
 };
 
 // kernel classes timed by the optional per-launch CUDA-event profiler
@@ -44,6 +46,7 @@ struct MolResult {
   int iterations = 0;
   double energy = 0, core_repulsion = 0, heat_of_formation = 0, final_rms = 0, final_diis_error = 0;
   double dipole[9] = {};        // total, electronic, core (x, y, z) [a.u.] when ScfSettings::dipole
+  double vdw_energy = 0;        // empirical dispersion energy, included in energy
 };
 
 class Engine;

@@ -78,9 +78,14 @@ void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol
                         int nlist, int max_atoms, const double* blocks, const double* H, const double* P, double* F,
                         double* Pold, const MolState* st, int mode_override, int copy_old, int require_active,
                         cudaStream_t s);
-void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* mol_list, int nlist,
-                          const double* P, const double* F, const double* H, MolState* st, double* charges,
-                          cudaStream_t s);
+// empirical dispersion energy requested for the list (AM1-D / PM3-D always add it)
+struct VdwParams {
+  int on;
+  double s6, d;
+};
+void launch_energy_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
+                          int nlist, const double* P, const double* F, const double* H, MolState* st,
+                          double* charges, VdwParams vdw, cudaStream_t s);
 // dipole moment of the listed molecules into MolState::dipole; partial holds
 // nlist * kDipChunks * 4 doubles
 constexpr int kDipChunks = 64;

@@ -12,7 +12,7 @@
 
 namespace nddo {
 
-constexpr int kNumParamSlots = NDDO_NUM_THEORIES * NDDO_NUM_ELEMENTS;
+constexpr int kNumParamSlots = NDDO_NUM_THEORY_SLOTS * NDDO_NUM_ELEMENTS;
 constexpr int kMaxDiis = 8;
 
 struct DevAtom {
@@ -53,6 +53,7 @@ struct MolState {
   double rms, diis_err, ecore, energy, heat_of_formation, energy_electronic;
   double B[kMaxDiis * kMaxDiis];   // <e_i, e_j> over ring slots
   double dipole[9];   // total, electronic, core dipole (x, y, z each) [a.u.] after convergence
+  double vdw_energy;  // empirical dispersion energy (0 when off)
 };
 
 struct TraceEntry {

@@ -11,6 +11,7 @@
 #include <math.h>
 #include "nddo_elements.h"
 #include "nddo_dipole.h"
+#include "nddo_dispersion.h"
 
 #define NDDO_EV2AU   0.03674903
 #define NDDO_ANG2AU  (1.0 / 0.5291772)
@@ -30,6 +31,8 @@ typedef struct {
   double e_atom, dhf_atom;      /* MNDO heat-of-formation bookkeeping  */
   double sto_norm[2];   /* Slater normalisation (2 zeta)^(n+1/2) / sqrt((2n)!) of s and p */
   double core_mass;     /* atomic mass [a.u.] - valence electrons: weight of the dipole origin */
+  double vdw_c6;        /* dispersion C6 coefficient [a.u.] (0: none)  */
+  double vdw_r0;        /* van der Waals radius [bohr]                 */
   int n_ao;             /* 1 or 4                                      */
   int principal_n;      /* 1, 2 or 3                                   */
   int atomic_number;
@@ -41,9 +44,13 @@ typedef struct {
  * (e.g. alpha = a / angstrom2AU, L = l / angstrom2AU^2, M = m * angstrom2AU). */
 static inline int nddo_fill_atom_params(int theory, int atomic_number, nddo_atom_params* out) {
   int e = nddo_element_index(atomic_number);
-  if (e < 0 || theory < 0 || theory >= NDDO_NUM_THEORIES) return -1;
+  if (e < 0 || theory < 0 || theory >= NDDO_NUM_THEORY_SLOTS) return -1;
+  const nddo_dispersion_element* dsp = nddo_dispersion_lookup(atomic_number);
+  /* AM1-D / PM3-D: the AM1 / PM3 set with the overrides below (H, C, N, O, S) */
+  const int base = theory == NDDO_AM1D ? NDDO_AM1 : (theory == NDDO_PM3D ? NDDO_PM3 : theory);
+  if (base != theory && !dsp) return -1;
   const nddo_element* el = &nddo_elements[e];
-  const nddo_theory_params* t = &el->t[theory];
+  const nddo_theory_params* t = &el->t[base];
   int i;
   out->core_charge = (double)el->core_charge;
   out->u[0] = t->u_s * NDDO_EV2AU;
@@ -78,6 +85,16 @@ static inline int nddo_fill_atom_params(int theory, int atomic_number, nddo_atom
     out->sto_norm[1] = (t->zeta_p > 0.0) ? pow(2.0 * t->zeta_p, el->principal_n + 0.5) / sqrt(f) : 0.0;
   }
   out->core_mass = nddo_atomic_mass_gmol(atomic_number) * NDDO_GMOLIN2AU - (double)el->core_charge;
+  out->vdw_c6 = dsp ? dsp->c6 * NDDO_J2AU * pow(10.0 * NDDO_ANG2AU, 6.0) / NDDO_AVOGADRO : 0.0;
+  out->vdw_r0 = dsp ? dsp->r0 * NDDO_ANG2AU : 0.0;
+  if (base != theory) {
+    const double* o = theory == NDDO_AM1D ? dsp->am1d : dsp->pm3d;
+    out->u[0] = o[0] * NDDO_EV2AU;
+    out->u[1] = o[1] * NDDO_EV2AU;
+    out->beta[0] = o[2] * NDDO_EV2AU;
+    out->beta[1] = o[3] * NDDO_EV2AU;
+    out->alpha = o[4] / NDDO_ANG2AU;
+  }
   out->n_ao = el->n_ao;
   out->principal_n = el->principal_n;
   out->atomic_number = atomic_number;

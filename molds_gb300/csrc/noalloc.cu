@@ -115,7 +115,7 @@ int setup_device(int device, cudaStream_t s, unsigned char** out, char* err, siz
   nddo_atom_params params[kNumParamSlots];
   std::memset(params, 0, sizeof(params));
   static const int zs[NDDO_NUM_ELEMENTS] = {1, 6, 7, 8, 9, 16, 17};
-  for (int t = 0; t < NDDO_NUM_THEORIES; ++t)
+  for (int t = 0; t < NDDO_NUM_THEORY_SLOTS; ++t)
     for (int k = 0; k < NDDO_NUM_ELEMENTS; ++k) nddo_fill_atom_params(t, zs[k], &params[t * NDDO_NUM_ELEMENTS + k]);
   if (e == cudaSuccess) {
     upload_params(params, s);
@@ -137,7 +137,7 @@ extern "C" int nddo_pair_integrals_noalloc(int device, int theory, int n_atoms, 
                                            char* err, size_t err_len) {
   using namespace nddo;
   if (device < 0 || device >= kMaxDevices) return set_error(err, err_len, NDDO_ERR_ARGUMENT, "device index out of range");
-  if (theory < 0 || theory >= NDDO_NUM_THEORIES) return set_error(err, err_len, NDDO_ERR_ARGUMENT, "unknown theory");
+  if (theory < 0 || theory >= NDDO_NUM_THEORY_SLOTS) return set_error(err, err_len, NDDO_ERR_ARGUMENT, "unknown theory");
   if (n_atoms < 1 || !atomic_numbers || !xyz_bohr || !d_pair_blocks || !d_core_hamiltonian)
     return set_error(err, err_len, NDDO_ERR_ARGUMENT, "null argument or no atoms");
   if (n_atoms > kNoAllocMaxAtoms) {
@@ -152,7 +152,9 @@ extern "C" int nddo_pair_integrals_noalloc(int device, int theory, int n_atoms, 
   int ao = 0;
   for (int a = 0; a < n_atoms; ++a) {
     const int e = nddo_element_index(atomic_numbers[a]);
-    if (e < 0) return set_error(err, err_len, NDDO_ERR_ARGUMENT, "element has no NDDO parameters");
+    nddo_atom_params probe;
+    if (e < 0 || nddo_fill_atom_params(theory, atomic_numbers[a], &probe) != 0)
+      return set_error(err, err_len, NDDO_ERR_ARGUMENT, "element has no parameters for this theory");
     for (int k = 0; k < 3; ++k)
       if (!(xyz_bohr[3 * a + k] == xyz_bohr[3 * a + k]) || xyz_bohr[3 * a + k] - xyz_bohr[3 * a + k] != 0.0)
         return set_error(err, err_len, NDDO_ERR_ARGUMENT, "non-finite coordinate");

@@ -588,14 +588,17 @@ void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol
                                             copy_old, require_active);
 }
 
-// E = 1/2 sum P (F + H) + E_core (Cndo2::CalcElecSCFEnergy, src/cndo/Cndo2.cpp:1324-1416),
+// E = 1/2 sum P (F + H) + E_core + E_vdW (Cndo2::CalcElecSCFEnergy, src/cndo/Cndo2.cpp:1324-1416),
 // Mulliken charges q_A = Z_A - sum_{mu in A} P_mu,mu (Cndo2.cpp:1187-1199, 1733-1747)
 // and, for MNDO, the heat of formation (Mndo::CalcHeatsFormation, src/mndo/Mndo.cpp:395-404).
+// E_vdW: the empirical dispersion energy of Cndo2::CalcVdWCorrectionEnergy
+// (Cndo2.cpp:464-513), on when requested or for AM1-D / PM3-D (which fix
+// s6 = 1.40, d = 23).
 __global__ void __launch_bounds__(kFockThreads)
-energy_kernel(const DevAtom* __restrict__ atoms, const DevMol* __restrict__ mols, const int* __restrict__ mol_list,
-              const double* __restrict__ P, const double* __restrict__ F, const double* __restrict__ H,
-              MolState* __restrict__ st, double* __restrict__ charges) {
-  __shared__ double red[32];
+energy_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs, const DevMol* __restrict__ mols,
+              const int* __restrict__ mol_list, const double* __restrict__ P, const double* __restrict__ F,
+              const double* __restrict__ H, MolState* __restrict__ st, double* __restrict__ charges, VdwParams vdw) {
+  __shared__ double red[32], red_v[32];
   const int m = mol_list[blockIdx.x];
   const DevMol mol = mols[m];
   const long long n2 = (long long)mol.nao * mol.nao;
@@ -603,7 +606,26 @@ energy_kernel(const DevAtom* __restrict__ atoms, const DevMol* __restrict__ mols
   for (long long i = threadIdx.x; i < n2; i += blockDim.x)
     acc += P[mol.mat0 + i] * (F[mol.mat0 + i] + H[mol.mat0 + i]);
   acc = warp_sum(acc);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  const bool dtheory = mol.theory == NDDO_AM1D || mol.theory == NDDO_PM3D;
+  const bool vdw_on = vdw.on || dtheory;
+  const double s6 = dtheory ? NDDO_VDW_S6_D : vdw.s6, dd = dtheory ? NDDO_VDW_DAMP_D : vdw.d;
+  double ev = 0.0;
+  if (vdw_on)
+    for (int t = threadIdx.x; t < mol.npairs; t += blockDim.x) {
+      const DevPair pr = pairs[mol.pair0 + t];
+      const DevAtom A = atoms[pr.a], B = atoms[pr.b];
+      const nddo_atom_params& pa = c_params[A.pidx];
+      const nddo_atom_params& pb = c_params[B.pidx];
+      const double csum = pa.vdw_c6 + pb.vdw_c6;
+      if (csum <= 0.0) continue;
+      const double dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+      const double R = sqrt(dx * dx + dy * dy + dz * dz);
+      const double c6 = 2.0 * pa.vdw_c6 * pb.vdw_c6 / csum;
+      const double damp = 1.0 / (1.0 + exp(-1.0 * dd * (R / (pa.vdw_r0 + pb.vdw_r0) - 1.0)));
+      ev += -1.0 * s6 * c6 * damp / (R * R * R * R * R * R);
+    }
+  ev = warp_sum(ev);
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = acc; red_v[threadIdx.x >> 5] = ev; }
   __syncthreads();
   for (int a = threadIdx.x; a < mol.natoms; a += blockDim.x) {
     const DevAtom A = atoms[mol.atom0 + a];
@@ -612,12 +634,13 @@ energy_kernel(const DevAtom* __restrict__ atoms, const DevMol* __restrict__ mols
     charges[mol.atom0 + a] = c_params[A.pidx].core_charge - pop;
   }
   if (threadIdx.x == 0) {
-    double e = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) e += red[w];
+    double e = 0.0, v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { e += red[w]; v += red_v[w]; }
     e *= 0.5;
     MolState* s = st + m;
     s->energy_electronic = e;
-    s->energy = e + s->ecore;
+    s->vdw_energy = v;
+    s->energy = e + s->ecore + v;
     double hof = s->energy;
     for (int a = 0; a < mol.natoms; ++a) {
       const nddo_atom_params& pa = c_params[atoms[mol.atom0 + a].pidx];
@@ -628,11 +651,11 @@ energy_kernel(const DevAtom* __restrict__ atoms, const DevMol* __restrict__ mols
   }
 }
 
-void launch_energy_kernel(const DevAtom* atoms, const DevMol* mols, const int* mol_list, int nlist,
-                          const double* P, const double* F, const double* H, MolState* st, double* charges,
-                          cudaStream_t s) {
+void launch_energy_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
+                          int nlist, const double* P, const double* F, const double* H, MolState* st,
+                          double* charges, VdwParams vdw, cudaStream_t s) {
   if (nlist <= 0) return;
-  energy_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, mols, mol_list, P, F, H, st, charges);
+  energy_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, pairs, mols, mol_list, P, F, H, st, charges, vdw);
 }
 
 // ---------------------------------------------------------------------------

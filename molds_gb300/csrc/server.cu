@@ -119,16 +119,19 @@ long long Server::submit(const MoleculeInput& in) {
     std::lock_guard<std::mutex> g(done_mu_);
     if (!error_.empty()) throw std::runtime_error("server stopped: " + error_);
   }
+  if (in.theory < 0 || in.theory >= NDDO_NUM_THEORY_SLOTS) throw std::invalid_argument("unknown theory");
   int nao = 0, nelec = 0;
   for (int z : in.Z) {
     const int e = nddo_element_index(z);
-    if (e < 0) throw std::invalid_argument("element " + std::to_string(z) + " has no NDDO parameters");
+    nddo_atom_params probe;
+    if (e < 0 || nddo_fill_atom_params(in.theory, z, &probe) != 0)
+      throw std::invalid_argument("element " + std::to_string(z) + " has no parameters for this theory");
     nao += nddo_elements[e].n_ao;
     nelec += nddo_elements[e].core_charge;
   }
   if (in.Z.empty()) throw std::invalid_argument("molecule without atoms");
   if ((int)in.xyz.size() != 3 * (int)in.Z.size()) throw std::invalid_argument("coordinate count does not match atom count");
-  if (in.theory < 0 || in.theory >= NDDO_NUM_THEORIES) throw std::invalid_argument("unknown theory");
+  if (in.theory < 0 || in.theory >= NDDO_NUM_THEORY_SLOTS) throw std::invalid_argument("unknown theory");
   if (nelec % 2) throw std::invalid_argument("Total number of valence electrons is odd. totalNumberValenceElectrons=" + std::to_string(nelec));
   for (auto& L : lanes_) {
     if (nao > L->lo && nao <= L->hi) {

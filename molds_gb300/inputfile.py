@@ -15,8 +15,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 ANG2AU = 1.0 / 0.5291772             # src/base/Parameters.cpp:48
-THEORIES = {"mndo": 0, "am1": 1, "pm3": 2}
-THEORY_NAMES = {0: "MNDO", 1: "AM1", 2: "PM3"}
+THEORIES = {"mndo": 0, "am1": 1, "pm3": 2, "am1-d": 3, "pm3-d": 4}   # src/base/InputParser.cpp:286-292
+THEORY_NAMES = {0: "MNDO", 1: "AM1", 2: "PM3", 3: "AM1-D", 4: "PM3-D"}
 SYMBOL_TO_Z = {"h": 1, "c": 6, "n": 7, "o": 8, "f": 9, "s": 16, "cl": 17}
 Z_TO_SYMBOL = {1: "H", 6: "C", 7: "N", 8: "O", 9: "F", 16: "S", 17: "Cl"}
 
@@ -38,6 +38,9 @@ class SCFParams:
     precision: str = "fp64"          # "fp64" or "mixed" (not a MolDS key)
     fp64_switch_error: float = 1e-4
     tensor_cores: bool = True        # mixed: FP32-phase GEMMs on tcgen05 (not a MolDS key)
+    vdw: bool = False                # vdW yes/no (always on for AM1-D / PM3-D)
+    vdw_s6: float = 1.40             # vdW_s6 (src/base/Parameters.cpp:141)
+    vdw_d: float = 23.0              # vdW_d (src/base/Parameters.cpp:142)
     dipole: bool = True              # dipole moment after convergence, as DoSCF (not a MolDS key)
 
 
@@ -72,6 +75,8 @@ _SCF_KEYS = {
     "diis_num_error_vect": ("diis_num_error_vect", int),
     "diis_start_error": ("diis_start_error", float),
     "diis_end_error": ("diis_end_error", float),
+    "vdw_s6": ("vdw_s6", float),
+    "vdw_d": ("vdw_d", float),
 }
 
 
@@ -101,7 +106,7 @@ def parse(text: str) -> InputFile:
         if t == "theory":
             name = need(i + 1)
             if name not in THEORIES:
-                raise InputError(f"theory '{name}' is not an NDDO theory (mndo, am1, pm3)")
+                raise InputError(f"theory '{name}' is not an NDDO theory (mndo, am1, pm3, am1-d, pm3-d)")
             theory = THEORIES[name]
             i += 2
             if need(i) != "theory_end":
@@ -114,7 +119,10 @@ def parse(text: str) -> InputFile:
                     attr, conv = _SCF_KEYS[key]
                     setattr(scf, attr, conv(need(i + 1)))
                     i += 2
-                elif key in ("vdw", "vdw_s6", "vdw_d", "mpi", "scalapack"):
+                elif key == "vdw":                 # src/base/InputParser.cpp:684-693
+                    scf.vdw = need(i + 1) == "yes"
+                    i += 2
+                elif key in ("mpi", "scalapack"):
                     i += 2
                 else:
                     raise InputError(f"unknown SCF keyword '{key}'")

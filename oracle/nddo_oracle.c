@@ -597,3 +597,16 @@ int oracle_core_masses(int theory, int natoms, const int* Z, double* out) {
   }
   return 0;
 }
+
+/* Dispersion data of every atom: C6 [a.u.] and van der Waals radius [bohr]
+ * (src/base/atoms/<El>atom.cpp, e.g. Catom.cpp:60-63); 2 doubles per atom. */
+int oracle_vdw_params(int theory, int natoms, const int* Z, double* out) {
+  for (int a = 0; a < natoms; ++a) {
+    nddo_atom_params p;
+    if (nddo_fill_atom_params(theory, Z[a], &p) != 0) return -1;
+    out[2 * a] = p.vdw_c6;
+    out[2 * a + 1] = p.vdw_r0;
+  }
+  return 0;
+}
+

@@ -44,7 +44,7 @@ SOURCES = [os.path.join(HERE, "nddo_oracle.c")]
 HEADERS = [os.path.join(HERE, "..", "molds_gb300", "csrc", "nddo_units.h"),
            os.path.join(HERE, "..", "molds_gb300", "csrc", "nddo_elements.h")]
 
-THEORIES = {"mndo": 0, "am1": 1, "pm3": 2}
+THEORIES = {"mndo": 0, "am1": 1, "pm3": 2, "am1-d": 3, "pm3-d": 4}
 SYMBOL_TO_Z = {"h": 1, "c": 6, "n": 7, "o": 8, "f": 9, "s": 16, "cl": 17}
 ANG2AU = 1.0 / 0.5291772          # src/base/Parameters.cpp:48
 KCAL2AU = 0.00159360175           # src/base/Parameters.cpp:47
@@ -81,6 +81,7 @@ def lib():
             L.oracle_atom_info.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp]
             L.oracle_cartesian.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp]
             L.oracle_core_masses.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp]
+            L.oracle_vdw_params.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp]
             L.oracle_sto_overlap_local.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                    ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                    ctypes.c_double]
@@ -107,6 +108,9 @@ class SCFParams:
     diis_num_error_vect: int = 5
     diis_start_error: float = 1e-2
     diis_end_error: float = 1e-8
+    vdw: bool = False                 # Parameters.cpp:140-142
+    vdw_s6: float = 1.40
+    vdw_d: float = 23.0
 
 
 @dataclass
@@ -133,6 +137,7 @@ class SCFResult:
     heat_of_formation: float | None
     trace: list = field(default_factory=list)   # (iter, rms, diis_error, diis_on, damp_on)
     dipole: np.ndarray | None = None   # (3, 3): total, electronic, core; x y z [a.u.]
+    vdw_energy: float = 0.0            # empirical dispersion energy, included in energy
 
 
 class NotConverged(RuntimeError):
@@ -202,6 +207,26 @@ def dipole(mol: Molecule, S, P, X=None) -> np.ndarray:
     pop = float(np.dot(P.ravel(), S.ravel()))
     elec = np.array([-float(np.dot(P.ravel(), X[k].ravel())) + center[k] * pop for k in range(3)])
     return np.stack([elec + core, elec, core])
+
+
+def vdw_energy(mol: Molecule, s6: float, d: float) -> float:
+    """Cndo2::CalcVdWCorrectionEnergy / GetDiatomVdWCorrectionEnergy
+    (src/cndo/Cndo2.cpp:464-513): -s6 C6_AB f(R) / R^6 over atom pairs."""
+    prm = np.zeros(2 * mol.natoms)
+    if lib().oracle_vdw_params(mol.theory, mol.natoms, _ip(mol.Z), _dp(prm)) != 0:
+        raise ValueError("element without dispersion parameters")
+    c6, r0 = prm[0::2], prm[1::2]
+    value = 0.0
+    for i in range(mol.natoms):
+        for j in range(i + 1, mol.natoms):
+            dist = float(np.sqrt(np.sum((mol.xyz[i] - mol.xyz[j]) ** 2)))
+            tmp = c6[i] + c6[j]
+            if tmp <= 0.0:
+                continue
+            c = 2.0 * c6[i] * c6[j] / tmp
+            damping = 1.0 / (1.0 + np.exp(-1.0 * d * (dist / (r0[i] + r0[j]) - 1.0)))
+            value += -1.0 * s6 * c * damping / dist ** 6
+    return value
 
 
 def fock(mol: Molecule, S, eri, P, guess=False):
@@ -296,7 +321,7 @@ def scf(mol: Molecule, params: SCFParams | None = None, requires_guess=True, P0=
         if log is not None:
             log(it, rms, diis_err, diis_on, damp_on)
         if rms < params.rms_density:
-            return _properties(mol, S, eri, ecore, P, eps, C, info, it + 1, trace)
+            return _properties(mol, S, eri, ecore, P, eps, C, info, it + 1, trace, params)
         if not is_guess:
             if diis is not None:
                 P, diis_err, diis_on = diis.step(P, P_old, it, params.diis_start_error,
@@ -308,11 +333,17 @@ def scf(mol: Molecule, params: SCFParams | None = None, requires_guess=True, P0=
     raise NotConverged(f"SCF did not met convergence criterion. maxIterationsSCF={params.max_iter}")
 
 
-def _properties(mol, S, eri, ecore, P, eps, C, info, iters, trace) -> SCFResult:
+def _properties(mol, S, eri, ecore, P, eps, C, info, iters, trace, params) -> SCFResult:
     F = fock(mol, S, eri, P, guess=False)
     H = fock(mol, S, eri, np.zeros_like(P), guess=False)
     e_elec = 0.5 * float(np.sum(P * (F + H)))
-    energy = e_elec + ecore
+    # AM1-D / PM3-D switch the dispersion term on with s6 = 1.40, d = 23
+    # (InputParser::ValidateVdWConditions, src/base/InputParser.cpp:1657-1664)
+    dtheory = mol.theory in (THEORIES["am1-d"], THEORIES["pm3-d"])
+    evdw = 0.0
+    if params.vdw or dtheory:
+        evdw = vdw_energy(mol, 1.40 if dtheory else params.vdw_s6, 23.0 if dtheory else params.vdw_d)
+    energy = e_elec + ecore + evdw
     firsts = np.concatenate([[0], np.cumsum(info[:, 1].astype(int))[:-1]])
     diag = np.diag(P)
     pop = np.array([diag[f:f + int(n)].sum() for f, n in zip(firsts, info[:, 1])])
@@ -321,7 +352,7 @@ def _properties(mol, S, eri, ecore, P, eps, C, info, iters, trace) -> SCFResult:
     if mol.theory == THEORIES["mndo"]:
         hof = energy - float(info[:, 2].sum()) + float(info[:, 3].sum())
     return SCFResult(True, iters, energy, ecore, eps, C, P, charges, hof, trace,
-                     dipole(mol, S, P))
+                     dipole(mol, S, P), evdw)
 
 
 # --------------------------------------------------------------------------
@@ -360,6 +391,12 @@ def parse_input(text: str):
                     params.diis_start_error = float(v)
                 elif k == "diis_end_error":
                     params.diis_end_error = float(v)
+                elif k == "vdw":                     # InputParser.cpp:684-693
+                    params.vdw = v == "yes"
+                elif k == "vdw_s6":
+                    params.vdw_s6 = float(v)
+                elif k == "vdw_d":
+                    params.vdw_d = float(v)
                 else:
                     i -= 1
                 i += 2

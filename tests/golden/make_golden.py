@@ -5,8 +5,8 @@ test/<case>.dat of the MolDS tree, registered in test/Test_Of_MolDS.rb) and
 keeps, per case, the input text and the printed values that pin the NDDO SCF
 path: the per-iteration RMS density and DIIS error, MO energies, electronic
 energy (incl. core repulsion), core repulsion, Mulliken charges, the total,
-electronic and core dipole moments (x, y, z in a.u.) and, for MNDO, the heat of
-formation.  MolDS prints these with %e (7 significant digits,
+electronic and core dipole moments (x, y, z in a.u.), the empirical van der
+Waals energy where the run has one and, for MNDO, the heat of formation.  MolDS prints these with %e (7 significant digits,
 src/cndo/Cndo2.cpp:1087-1089, 1193-1198), so they pin results to ~5e-7 relative.
 
 Usage:  python tests/golden/make_golden.py [/path/to/molds/test]
@@ -17,9 +17,11 @@ import re
 import sys
 
 CASES = [f"{m}_{t}" for m in ("ch4", "c2h6", "ch3f", "ch3cl") for t in ("mndo", "am1", "pm3")]
+# the dispersion-corrected theories and the vdW option
+CASES += ["c2h6_am1d", "c2h6_pm3d", "c2h6_pm3_vdw"]
 # SCF blocks printed before a frequency run: the first SCF of each pins PM3 for
 # O (with the H-O core-core rule) and for C=C.
-EXTRA = ["h2o_pm3_freq_num_proj_s1", "c2h4_pm3_freq_num_proj"]
+EXTRA = ["h2o_pm3_freq_num_proj_s1", "c2h4_pm3_freq_num_proj", "c2h6-nh3-cluster_pm3d_freq"]
 
 
 def parse_dat(text, natoms):
@@ -44,6 +46,9 @@ def parse_dat(text, natoms):
         dip.append([float(m.group(i)) for i in (1, 2, 3)])
     out = {"trace": trace, "mo_energies": mo, "energy": e, "core_repulsion": ec,
            "mulliken": q, "dipole": dip}
+    vdw = re.search(r"Empirical van der Waals correction:\t(\S+)", body)
+    if vdw:
+        out["vdw_energy"] = float(vdw.group(1))
     if hof:
         out["heat_of_formation"] = float(hof.group(1))
     return out

@@ -118,7 +118,8 @@ def test_reference_fixtures_fp64(ctx, case):
     ref = O.scf(mol, p)
     params = M.SCFParams(max_iter=p.max_iter, rms_density=p.rms_density, damping_thresh=p.damping_thresh,
                          damping_weight=p.damping_weight, diis_num_error_vect=p.diis_num_error_vect,
-                         diis_start_error=p.diis_start_error, diis_end_error=p.diis_end_error)
+                         diis_start_error=p.diis_start_error, diis_end_error=p.diis_end_error,
+                         vdw=p.vdw, vdw_s6=p.vdw_s6, vdw_d=p.vdw_d)
     es = M.ElectronicStructure(mol.theory, params, context=ctx)
     es.SetMolecule(M.Molecule(mol.Z, mol.xyz))
     es.DoSCF(True)
@@ -128,6 +129,7 @@ def test_reference_fixtures_fp64(ctx, case):
     assert np.max(np.abs(es.GetEnergiesMO() - ref.eps)) < 1e-7
     D = es.GetDipoleMoments()
     assert np.max(np.abs(D - ref.dipole)) < DIP_TOL
+    assert abs(es.GetVdWCorrectionEnergy() - ref.vdw_energy) < 1e-12
     # the printed values of the reference itself (7 significant digits)
     assert abs(es.GetElectronicEnergy(0) - case["energy"]) <= 1e-6 * abs(case["energy"])
     for mine, theirs in zip(D.ravel(), np.array(case["dipole"]).ravel()):

@@ -88,6 +88,16 @@ def test_dipole_moments(case):
         assert close(mine, theirs, rel=PRINT_REL, abs_=1e-9), (mine, theirs)
 
 
+def test_vdw_energy(case):
+    """Empirical dispersion energy (Cndo2.cpp:464-513, printed at :1118-1122)
+    of the AM1-D / PM3-D cases and of PM3 with vdW yes; 0 elsewhere."""
+    c, mol, r = case
+    if "vdw_energy" in c:
+        assert close(r.vdw_energy, c["vdw_energy"], abs_=1e-12), (r.vdw_energy, c["vdw_energy"])
+    else:
+        assert r.vdw_energy == 0.0
+
+
 def test_aos_match(case):
     c, mol, r = case
     assert O.num_aos(mol) == c["n_ao"]
