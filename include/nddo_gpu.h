@@ -27,8 +27,12 @@ extern "C" {
 typedef struct nddo_ctx nddo_ctx;
 
 /* AM1-D / PM3-D: MolDS's dispersion-corrected sets (THEORY am1-d / pm3-d;
- * src/am1/Am1D.cpp, src/pm3/Pm3D.cpp), H, C, N, O and S only. */
-enum { NDDO_THEORY_MNDO = 0, NDDO_THEORY_AM1 = 1, NDDO_THEORY_PM3 = 2, NDDO_THEORY_AM1D = 3, NDDO_THEORY_PM3D = 4 };
+ * src/am1/Am1D.cpp, src/pm3/Pm3D.cpp) and PDDG/PM3 (THEORY pm3/pddg;
+ * src/pm3/Pm3Pddg.cpp), H, C, N, O and S only. */
+enum {
+  NDDO_THEORY_MNDO = 0, NDDO_THEORY_AM1 = 1, NDDO_THEORY_PM3 = 2, NDDO_THEORY_AM1D = 3, NDDO_THEORY_PM3D = 4,
+  NDDO_THEORY_PM3PDDG = 5
+};
 enum { NDDO_PRECISION_FP64 = 0, NDDO_PRECISION_MIXED = 1 };
 enum {
   NDDO_OK = 0,

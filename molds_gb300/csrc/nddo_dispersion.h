@@ -1,6 +1,7 @@
 /*
- * AM1-D and PM3-D, MolDS's dispersion-corrected variants, and the empirical
- * van der Waals energy.  Plain C; included by C, C++ and CUDA alike.
+ * The NDDO variants beyond MNDO / AM1 / PM3: AM1-D and PM3-D (MolDS's
+ * dispersion-corrected sets) with the empirical van der Waals energy, and
+ * PDDG/PM3.  Plain C; included by C, C++ and CUDA alike.
  *
  * AM1-D / PM3-D are the AM1 / PM3 parameter sets with U_s, U_p, beta_s,
  * beta_p and the core-core exponent alpha replaced by the values of
@@ -20,7 +21,7 @@
 #define MOLDS_GB300_NDDO_DISPERSION_H
 
 /* parameter slots beyond the three published sets of nddo_elements.h */
-enum { NDDO_AM1D = 3, NDDO_PM3D = 4, NDDO_NUM_THEORY_SLOTS = 5 };
+enum { NDDO_AM1D = 3, NDDO_PM3D = 4, NDDO_PM3PDDG = 5, NDDO_NUM_THEORY_SLOTS = 6 };
 
 #define NDDO_J2AU      (1.0e18 / 4.35974394)   /* src/base/Parameters.cpp:46 */
 #define NDDO_AVOGADRO  6.0221415e23            /* src/base/Parameters.cpp:56 */
@@ -59,6 +60,58 @@ static inline const nddo_dispersion_element* nddo_dispersion_lookup(int atomic_n
   int i;
   for (i = 0; i < NDDO_NUM_DISPERSION_ELEMENTS; ++i)
     if (nddo_dispersion_elements[i].atomic_number == atomic_number) return &nddo_dispersion_elements[i];
+  return 0;
+}
+
+/*
+ * PDDG/PM3 (Repasky, Chandrasekhar, Jorgensen, J. Comput. Chem. 23, 1601
+ * (2002); src/pm3/Pm3Pddg.cpp): its own U, zeta, beta, alpha, multipole
+ * distances D1, D2, additive terms rho0..rho2 and two core-core Gaussians
+ * (the one-centre integrals stay PM3's, src/base/atoms/Atom.cpp:950-1061),
+ * plus the pairwise PDDG term of Pm3Pddg::GetDiatomCoreRepulsionEnergy
+ * (Pm3Pddg.cpp:143-165, 239-245):
+ *   (1 / (n_A + n_B)) sum_{i,j} (n_A Pa_i + n_B Pb_j) exp(-10 A^-2 (R - Da_i - Db_j)^2),
+ * n = valence electrons.  Values of src/base/atoms/<El>atom.cpp (e.g.
+ * Catom.cpp:190-218); H, C, N, O, S only (Pm3Pddg.cpp:134-141).
+ */
+typedef struct {
+  int atomic_number;
+  double u_s, u_p, zeta_s, zeta_p, beta_s, beta_p;   /* [eV], [1/bohr], [eV] */
+  double alpha;                                      /* [1/Angstrom] */
+  double d1, d2;                                     /* [bohr] */
+  double rho[3];                                     /* [bohr] */
+  double gk[2], gl[2], gm[2];                        /* [eV], [1/Angstrom^2], [Angstrom] */
+  double pa[2], da[2];                               /* [eV], [Angstrom] */
+} nddo_pddg_element;
+
+enum { NDDO_NUM_PDDG_ELEMENTS = 5 };
+
+static const nddo_pddg_element nddo_pddg_elements[NDDO_NUM_PDDG_ELEMENTS] = {
+  { 1, -12.893272, 0.0, 0.972786, 0.0, -6.152654, 0.0, 3.381686, 0.0, 0.0, { 0.919616, 0.0, 0.0 },
+    { 1.122244, -1.069737 }, { 4.707790, 5.857995 }, { 1.547099, 1.567893 },
+    { 0.057193, -0.034823 }, { 0.663395, 1.081901 } },
+  { 6, -48.241241, -36.461256, 1.567864, 1.846659, -11.952818, -9.922411, 2.725772, 0.831413, 0.663222,
+    { 1.214657, 0.848467, 0.652785 },
+    { 0.048906, 0.047697 }, { 5.765340, 5.973721 }, { 1.682232, 0.894406 },
+    { -0.000743, 0.000985 }, { 0.836915, 1.585236 } },
+  { 7, -49.454546, -47.757406, 2.035807, 2.324327, -14.117230, -19.938509, 2.849124, 0.654855, 0.526924,
+    { 1.142818, 0.991235, 0.676704 },
+    { 1.513320, -1.511892 }, { 5.904394, 6.030014 }, { 1.728376, 1.734108 },
+    { -0.003160, 0.012501 }, { 1.004172, 1.516336 } },
+  { 8, -87.412505, -72.183070, 3.814565, 2.318011, -44.874553, -24.601939, 3.225309, 0.403741, 0.528360,
+    { 0.863494, 0.936266, 0.624291 },
+    { -1.138455, 1.146007 }, { 6.000043, 5.963494 }, { 1.622362, 1.614788 },
+    { -0.001000, -0.001522 }, { 1.360685, 1.366407 } },
+  { 16, -43.906366, -43.461348, 1.012002, 1.876999, -2.953912, -8.507779, 2.539751, 1.006989, 0.891487,
+    { 1.517625, 0.711672, 0.754336 },
+    { -0.330692, 0.024171 }, { 6.000000, 6.000000 }, { 0.823837, 2.017756 },
+    { 0.120434, -0.002663 }, { 0.672870, 2.032340 } },
+};
+
+static inline const nddo_pddg_element* nddo_pddg_lookup(int atomic_number) {
+  int i;
+  for (i = 0; i < NDDO_NUM_PDDG_ELEMENTS; ++i)
+    if (nddo_pddg_elements[i].atomic_number == atomic_number) return &nddo_pddg_elements[i];
   return 0;
 }
 

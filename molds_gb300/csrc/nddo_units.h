@@ -33,6 +33,8 @@ typedef struct {
   double core_mass;     /* atomic mass [a.u.] - valence electrons: weight of the dipole origin */
   double vdw_c6;        /* dispersion C6 coefficient [a.u.] (0: none)  */
   double vdw_r0;        /* van der Waals radius [bohr]                 */
+  double pddg_pa[2];    /* PDDG/PM3 core-core pre-factors [a.u.] (0 elsewhere) */
+  double pddg_da[2];    /* PDDG/PM3 core-core distances [bohr]         */
   int n_ao;             /* 1 or 4                                      */
   int principal_n;      /* 1, 2 or 3                                   */
   int atomic_number;
@@ -47,8 +49,10 @@ static inline int nddo_fill_atom_params(int theory, int atomic_number, nddo_atom
   if (e < 0 || theory < 0 || theory >= NDDO_NUM_THEORY_SLOTS) return -1;
   const nddo_dispersion_element* dsp = nddo_dispersion_lookup(atomic_number);
   /* AM1-D / PM3-D: the AM1 / PM3 set with the overrides below (H, C, N, O, S) */
-  const int base = theory == NDDO_AM1D ? NDDO_AM1 : (theory == NDDO_PM3D ? NDDO_PM3 : theory);
-  if (base != theory && !dsp) return -1;
+  const nddo_pddg_element* pg = nddo_pddg_lookup(atomic_number);
+  const int base = theory == NDDO_AM1D ? NDDO_AM1 : ((theory == NDDO_PM3D || theory == NDDO_PM3PDDG) ? NDDO_PM3 : theory);
+  if ((theory == NDDO_AM1D || theory == NDDO_PM3D) && !dsp) return -1;
+  if (theory == NDDO_PM3PDDG && !pg) return -1;
   const nddo_element* el = &nddo_elements[e];
   const nddo_theory_params* t = &el->t[base];
   int i;
@@ -77,23 +81,44 @@ static inline int nddo_fill_atom_params(int theory, int atomic_number, nddo_atom
   }
   out->e_atom = t->e_atom * NDDO_EV2AU;
   out->dhf_atom = t->dhf_atom * NDDO_KCAL2AU;
-  {
-    double f = 1.0;
-    int k;
-    for (k = 2; k <= 2 * el->principal_n; ++k) f *= k;
-    out->sto_norm[0] = pow(2.0 * t->zeta_s, el->principal_n + 0.5) / sqrt(f);
-    out->sto_norm[1] = (t->zeta_p > 0.0) ? pow(2.0 * t->zeta_p, el->principal_n + 0.5) / sqrt(f) : 0.0;
-  }
   out->core_mass = nddo_atomic_mass_gmol(atomic_number) * NDDO_GMOLIN2AU - (double)el->core_charge;
   out->vdw_c6 = dsp ? dsp->c6 * NDDO_J2AU * pow(10.0 * NDDO_ANG2AU, 6.0) / NDDO_AVOGADRO : 0.0;
   out->vdw_r0 = dsp ? dsp->r0 * NDDO_ANG2AU : 0.0;
-  if (base != theory) {
+  out->pddg_pa[0] = out->pddg_pa[1] = out->pddg_da[0] = out->pddg_da[1] = 0.0;
+  if (theory == NDDO_PM3PDDG) {
+    out->u[0] = pg->u_s * NDDO_EV2AU;
+    out->u[1] = pg->u_p * NDDO_EV2AU;
+    out->zeta[0] = pg->zeta_s;
+    out->zeta[1] = pg->zeta_p;
+    out->beta[0] = pg->beta_s * NDDO_EV2AU;
+    out->beta[1] = pg->beta_p * NDDO_EV2AU;
+    out->alpha = pg->alpha / NDDO_ANG2AU;
+    out->d[1] = pg->d1;
+    out->d[2] = pg->d2;
+    for (i = 0; i < 3; ++i) out->rho[i] = pg->rho[i];
+    for (i = 0; i < 4; ++i) {
+      out->gk[i] = i < 2 ? pg->gk[i] * NDDO_EV2AU : 0.0;
+      out->gl[i] = i < 2 ? pg->gl[i] / pow(NDDO_ANG2AU, 2.0) : 0.0;
+      out->gm[i] = i < 2 ? pg->gm[i] * NDDO_ANG2AU : 0.0;
+    }
+    for (i = 0; i < 2; ++i) {
+      out->pddg_pa[i] = pg->pa[i] * NDDO_EV2AU;
+      out->pddg_da[i] = pg->da[i] * NDDO_ANG2AU;
+    }
+  } else if (base != theory) {
     const double* o = theory == NDDO_AM1D ? dsp->am1d : dsp->pm3d;
     out->u[0] = o[0] * NDDO_EV2AU;
     out->u[1] = o[1] * NDDO_EV2AU;
     out->beta[0] = o[2] * NDDO_EV2AU;
     out->beta[1] = o[3] * NDDO_EV2AU;
     out->alpha = o[4] / NDDO_ANG2AU;
+  }
+  {
+    double f = 1.0;
+    int k;
+    for (k = 2; k <= 2 * el->principal_n; ++k) f *= k;
+    out->sto_norm[0] = pow(2.0 * out->zeta[0], el->principal_n + 0.5) / sqrt(f);
+    out->sto_norm[1] = (out->zeta[1] > 0.0) ? pow(2.0 * out->zeta[1], el->principal_n + 0.5) / sqrt(f) : 0.0;
   }
   out->n_ao = el->n_ao;
   out->principal_n = el->principal_n;

@@ -74,6 +74,17 @@ __device__ __forceinline__ double core_core(const nddo_atom_params& pa, const nd
     }
     e += pa.core_charge * pb.core_charge * t * NDDO_ANG2AU / R;
   }
+  if (theory == NDDO_PM3PDDG) {
+    // PDDG term (Pm3Pddg.cpp:143-165, 239-245); n = valence electrons = core charge
+    const double na = pa.core_charge, nb = pb.core_charge;
+    double t = 0.0;
+    for (int i = 0; i < 2; ++i)
+      for (int k = 0; k < 2; ++k) {
+        const double x = R - pa.pddg_da[i] - pb.pddg_da[k];
+        t += (na * pa.pddg_pa[i] + nb * pb.pddg_pa[k]) * exp(-10.0 / (NDDO_ANG2AU * NDDO_ANG2AU) * (x * x));
+      }
+    e += t / (na + nb);
+  }
   return e;
 }
 

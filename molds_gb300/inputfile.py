@@ -15,8 +15,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 ANG2AU = 1.0 / 0.5291772             # src/base/Parameters.cpp:48
-THEORIES = {"mndo": 0, "am1": 1, "pm3": 2, "am1-d": 3, "pm3-d": 4}   # src/base/InputParser.cpp:286-292
-THEORY_NAMES = {0: "MNDO", 1: "AM1", 2: "PM3", 3: "AM1-D", 4: "PM3-D"}
+THEORIES = {"mndo": 0, "am1": 1, "pm3": 2, "am1-d": 3, "pm3-d": 4, "pm3/pddg": 5}   # src/base/InputParser.cpp:286-293
+THEORY_NAMES = {0: "MNDO", 1: "AM1", 2: "PM3", 3: "AM1-D", 4: "PM3-D", 5: "PM3/PDDG"}
 SYMBOL_TO_Z = {"h": 1, "c": 6, "n": 7, "o": 8, "f": 9, "s": 16, "cl": 17}
 Z_TO_SYMBOL = {1: "H", 6: "C", 7: "N", 8: "O", 9: "F", 16: "S", 17: "Cl"}
 
@@ -106,7 +106,7 @@ def parse(text: str) -> InputFile:
         if t == "theory":
             name = need(i + 1)
             if name not in THEORIES:
-                raise InputError(f"theory '{name}' is not an NDDO theory (mndo, am1, pm3, am1-d, pm3-d)")
+                raise InputError(f"theory '{name}' is not an NDDO theory (mndo, am1, pm3, am1-d, pm3-d, pm3/pddg)")
             theory = THEORIES[name]
             i += 2
             if need(i) != "theory_end":

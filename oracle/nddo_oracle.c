@@ -17,6 +17,7 @@
  *   Fock elements .......................... src/mndo/Mndo.cpp:422-650, src/cndo/Cndo2.cpp:1526-1636
  *   core-core (MNDO + H-N/H-O rule) ........ src/mndo/Mndo.cpp:223-240, 319-327
  *   AM1/PM3 Gaussian core-core terms ....... src/am1/Am1.cpp:145-170, src/am1/Am1.h:45-47
+ *   PDDG/PM3 core-core term ................ src/pm3/Pm3Pddg.cpp:143-165, 239-245
  *   Cartesian (dipole) matrix, STO-6G ...... src/cndo/Cndo2.cpp:1946-2057, 2068-2130, 2149-2400
  *   Gaussian overlaps (s, p) ............... src/cndo/Cndo2.cpp:4563-4575, 4601-5153
  *
@@ -338,6 +339,16 @@ static double pair_core_core(int theory, const nddo_atom_params* A, const nddo_a
       t += B->gk[i] * exp(-B->gl[i] * pow(R - B->gm[i], 2.0));
     }
     e += A->core_charge * B->core_charge * t * NDDO_ANG2AU / R;
+  }
+  if (theory == NDDO_PM3PDDG) {
+    /* Pm3Pddg::GetDiatomCoreRepulsionEnergy, src/pm3/Pm3Pddg.cpp:143-165, 239-245 */
+    int na = (int)A->core_charge, nb = (int)B->core_charge;
+    double temp = 0.0;
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j)
+        temp += ((double)na * A->pddg_pa[i] + (double)nb * B->pddg_pa[j]) *
+                exp(-10.0 / (NDDO_ANG2AU * NDDO_ANG2AU) * pow(R - A->pddg_da[i] - B->pddg_da[j], 2.0));
+    e += temp / (na + nb);
   }
   return e;
 }

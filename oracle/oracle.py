@@ -44,7 +44,7 @@ SOURCES = [os.path.join(HERE, "nddo_oracle.c")]
 HEADERS = [os.path.join(HERE, "..", "molds_gb300", "csrc", "nddo_units.h"),
            os.path.join(HERE, "..", "molds_gb300", "csrc", "nddo_elements.h")]
 
-THEORIES = {"mndo": 0, "am1": 1, "pm3": 2, "am1-d": 3, "pm3-d": 4}
+THEORIES = {"mndo": 0, "am1": 1, "pm3": 2, "am1-d": 3, "pm3-d": 4, "pm3/pddg": 5}
 SYMBOL_TO_Z = {"h": 1, "c": 6, "n": 7, "o": 8, "f": 9, "s": 16, "cl": 17}
 ANG2AU = 1.0 / 0.5291772          # src/base/Parameters.cpp:48
 KCAL2AU = 0.00159360175           # src/base/Parameters.cpp:47

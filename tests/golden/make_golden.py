@@ -18,10 +18,11 @@ import sys
 
 CASES = [f"{m}_{t}" for m in ("ch4", "c2h6", "ch3f", "ch3cl") for t in ("mndo", "am1", "pm3")]
 # the dispersion-corrected theories and the vdW option
-CASES += ["c2h6_am1d", "c2h6_pm3d", "c2h6_pm3_vdw"]
+CASES += ["c2h6_am1d", "c2h6_pm3d", "c2h6_pm3_vdw", "c2h6_pm3pddg"]
 # SCF blocks printed before a frequency run: the first SCF of each pins PM3 for
 # O (with the H-O core-core rule) and for C=C.
-EXTRA = ["h2o_pm3_freq_num_proj_s1", "c2h4_pm3_freq_num_proj", "c2h6-nh3-cluster_pm3d_freq"]
+EXTRA = ["h2o_pm3_freq_num_proj_s1", "c2h4_pm3_freq_num_proj", "c2h6-nh3-cluster_pm3d_freq",
+         "c2h6-h2o-cluster_pm3pddg_freq"]
 
 
 def parse_dat(text, natoms):
