@@ -77,6 +77,20 @@ GEOMETRY_END
     assert abs(f.molecule.xyz[1, 0] - 1.0 / 0.5291772) < 1e-15
 
 
+@pytest.mark.parametrize("name,theory", [("am1-d", 3), ("pm3-d", 4), ("pm3/pddg", 5)])
+def test_parser_variants_and_vdw_keys(name, theory):
+    """THEORY am1-d / pm3-d / pm3/pddg and the SCF keys vdW, vdW_s6, vdW_d
+    (src/base/InputParser.cpp:286-293, 684-712) reach the C parameter block."""
+    text = f"THEORY\n {name}\nTHEORY_END\nSCF\n vdW yes\n vdW_s6 0.88\n vdW_d 20\nSCF_END\n" \
+           "GEOMETRY\n C 0 0 0\n O 1.2 0 0\nGEOMETRY_END"
+    f = inputfile.parse(text)
+    assert f.theory == theory
+    assert f.scf.vdw and f.scf.vdw_s6 == 0.88 and f.scf.vdw_d == 20.0
+    import molds_gb300 as M
+    c = M.to_c_params(f.scf)
+    assert c.vdw == 1 and c.vdw_s6 == 0.88 and c.vdw_d == 20.0 and c.dipole == 1
+
+
 @pytest.mark.parametrize("bad", ["THEORY\n zindos\nTHEORY_END\nGEOMETRY\n H 0 0 0\n H 1 0 0\nGEOMETRY_END",
                                  "THEORY\n pm3\nTHEORY_END\nGEOMETRY\n Xe 0 0 0\nGEOMETRY_END",
                                  "THEORY\n pm3\nTHEORY_END\nCIS\nCIS_END\nGEOMETRY\n H 0 0 0\nGEOMETRY_END",
