@@ -1,0 +1,84 @@
+"""The C++ host layer (include/nddo_electronic_structure.hpp): MolDS's
+ElectronicStructure call surface over the C ABI, built with g++ against the
+library as a MolDS translation unit would be.
+
+CPU: it compiles, links and reports a missing GPU as a thrown MolDSException
+(exit 3, status NDDO_ERR_CUDA), not a crash.  GPU: SetMolecule + DoSCF through
+it give the oracle's energy, charges and iteration count."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+FIX = json.load(open(os.path.join(HERE, "golden", "reference_fixtures.json")))["cases"]
+
+
+def _program(tmp_path):
+    from molds_gb300 import build
+    build.build()
+    libdir = os.path.join(ROOT, "molds_gb300", "_build")
+    exe = str(tmp_path / "es_main")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(HERE, "cpp", "electronic_structure_main.cpp"), "-o", exe,
+                    "-L", libdir, "-lnddo_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    return exe
+
+
+def _write_molecule(tmp_path, mol):
+    p = tmp_path / "mol.txt"
+    lines = [str(mol.theory)] + [f"{z} {x!r} {y!r} {w!r}" for z, (x, y, w) in zip(mol.Z, mol.xyz)]
+    p.write_text("\n".join(lines) + "\n")
+    return str(p)
+
+
+def _args(p):
+    return [str(p.max_iter), repr(p.rms_density), repr(p.damping_thresh), repr(p.damping_weight),
+            str(p.diis_num_error_vect), repr(p.diis_start_error), repr(p.diis_end_error)]
+
+
+def _parse(out):
+    vals = {}
+    for line in out.splitlines():
+        k, v = line.split(" ", 1)
+        vals.setdefault(k, []).append(v)
+    return vals
+
+
+def test_cpp_host_builds_and_reports_errors_as_exceptions(tmp_path):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present: the GPU test covers this program")
+    except ImportError:
+        pass
+    exe = _program(tmp_path)
+    mol, p = O.parse_input([c for c in FIX if c["name"] == "ch3f_pm3"][0]["input"])
+    r = subprocess.run([exe, _write_molecule(tmp_path, mol)] + _args(p), capture_output=True, text=True)
+    assert r.returncode == 3, (r.returncode, r.stdout, r.stderr)
+    assert r.stdout.startswith("error -2 ")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ch3f_pm3", "c2h6_pm3pddg", "ch3cl_mndo"])
+def test_cpp_host_matches_oracle(tmp_path, name):
+    exe = _program(tmp_path)
+    case = [c for c in FIX if c["name"] == name][0]
+    mol, p = O.parse_input(case["input"])
+    ref = O.scf(mol, p)
+    r = subprocess.run([exe, _write_molecule(tmp_path, mol)] + _args(p), capture_output=True, text=True)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    v = _parse(r.stdout)
+    assert abs(float(v["energy"][0]) - ref.energy) < 1e-8
+    assert abs(float(v["core_repulsion"][0]) - ref.core_repulsion) < 1e-10
+    assert int(v["iterations"][0]) == ref.iterations
+    q = np.array([float(x) for x in v["charge"]])
+    assert np.max(np.abs(q - ref.charges)) < 1e-6
+    assert abs(float(v["homo"][0]) - ref.eps[0]) < 1e-7
+    assert np.max(np.abs(np.array([float(x) for x in v["dipole"]]) - ref.dipole[0])) < 1e-6
+    assert int(v["excited_state_error"][0]) == -1
