@@ -32,14 +32,16 @@ def _program(tmp_path):
 
 def _write_molecule(tmp_path, mol):
     p = tmp_path / "mol.txt"
-    lines = [str(mol.theory)] + [f"{z} {x!r} {y!r} {w!r}" for z, (x, y, w) in zip(mol.Z, mol.xyz)]
+    lines = [str(int(mol.theory))] + [f"{int(z)} {float(x):.17g} {float(y):.17g} {float(w):.17g}"
+                                       for z, (x, y, w) in zip(mol.Z, mol.xyz)]
     p.write_text("\n".join(lines) + "\n")
     return str(p)
 
 
 def _args(p):
-    return [str(p.max_iter), repr(p.rms_density), repr(p.damping_thresh), repr(p.damping_weight),
-            str(p.diis_num_error_vect), repr(p.diis_start_error), repr(p.diis_end_error)]
+    return [str(int(p.max_iter)), f"{float(p.rms_density):.17g}", f"{float(p.damping_thresh):.17g}",
+            f"{float(p.damping_weight):.17g}", str(int(p.diis_num_error_vect)), f"{float(p.diis_start_error):.17g}",
+            f"{float(p.diis_end_error):.17g}"]
 
 
 def _parse(out):
