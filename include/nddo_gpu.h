@@ -34,6 +34,10 @@ enum {
   NDDO_THEORY_PM3PDDG = 5
 };
 enum { NDDO_PRECISION_FP64 = 0, NDDO_PRECISION_MIXED = 1 };
+/* FP64 eigensolver of the SCF (Lapack::Dsyevd's stand-in): AUTO and
+ * HOUSEHOLDER = Householder tridiagonalisation + bisection + inverse
+ * iteration; JACOBI = the warm-started cyclic Jacobi. */
+enum { NDDO_EIGEN_AUTO = 0, NDDO_EIGEN_JACOBI = 1, NDDO_EIGEN_HOUSEHOLDER = 2 };
 enum {
   NDDO_OK = 0,
   NDDO_NOT_CONVERGED = 1,
@@ -61,6 +65,7 @@ typedef struct {
   int vdw;                     /* vdW yes/no: empirical dispersion energy (always on for AM1-D / PM3-D) */
   double vdw_s6;               /* vdW_s6 (default 1.40; AM1-D / PM3-D use 1.40)  */
   double vdw_d;                /* vdW_d  (default 23;  AM1-D / PM3-D use 23)    */
+  int eigensolver;             /* NDDO_EIGEN_* for FP64 eigensolves (default AUTO) */
 } nddo_scf_params;
 
 typedef struct {

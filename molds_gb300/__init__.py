@@ -48,7 +48,7 @@ class ScfParamsC(ctypes.Structure):
                 ("diis_end_error", ctypes.c_double), ("precision", ctypes.c_int),
                 ("fp64_switch_error", ctypes.c_double), ("tensor_cores", ctypes.c_int),
                 ("dipole", ctypes.c_int), ("vdw", ctypes.c_int), ("vdw_s6", ctypes.c_double),
-                ("vdw_d", ctypes.c_double)]
+                ("vdw_d", ctypes.c_double), ("eigensolver", ctypes.c_int)]
 
 
 class ScfResultC(ctypes.Structure):
@@ -167,6 +167,7 @@ def to_c_params(p: SCFParams) -> ScfParamsC:
     c.vdw = 1 if getattr(p, "vdw", False) else 0
     c.vdw_s6 = float(getattr(p, "vdw_s6", 1.40))
     c.vdw_d = float(getattr(p, "vdw_d", 23.0))
+    c.eigensolver = {"auto": 0, "jacobi": 1, "householder": 2}[str(getattr(p, "eigensolver", "auto")).lower()]
     return c
 
 

@@ -104,6 +104,7 @@ nddo::ScfSettings to_settings(const nddo_scf_params* p) {
     s.vdw = p->vdw;
     s.vdw_s6 = p->vdw_s6;
     s.vdw_d = p->vdw_d;
+    s.eigensolver = p->eigensolver;
   }
   return s;
 }
@@ -132,6 +133,7 @@ bool valid_params(const nddo_scf_params* p, std::string* why) {
   if (p->precision != NDDO_PRECISION_FP64 && p->precision != NDDO_PRECISION_MIXED) { *why = "unknown precision"; return false; }
   if (!(p->rms_density > 0.0)) { *why = "rms_density must be > 0"; return false; }
   if (p->vdw && !(p->vdw_s6 >= 0.0 && p->vdw_d > 0.0)) { *why = "vdw_s6 must be >= 0 and vdw_d > 0"; return false; }
+  if (p->eigensolver < NDDO_EIGEN_AUTO || p->eigensolver > NDDO_EIGEN_HOUSEHOLDER) { *why = "unknown eigensolver"; return false; }
   return true;
 }
 
@@ -155,6 +157,7 @@ void nddo_default_params(nddo_scf_params* p) {
   p->vdw = 0;
   p->vdw_s6 = 1.40;
   p->vdw_d = 23.0;
+  p->eigensolver = NDDO_EIGEN_AUTO;
 }
 
 int nddo_create(int device, size_t hbm_budget_bytes, nddo_ctx** out) {

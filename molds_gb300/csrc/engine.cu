@@ -304,6 +304,7 @@ void Batch::allocate(const BatchCapacity& cap) {
   d_G64 = dalloc<double>(mat, &bytes_);
   d_T64 = dalloc<double>(mat, &bytes_);
   for (int i = 0; i < 6; ++i) d_S[i] = dalloc<double>(mat, &bytes_);
+  d_td = dalloc<double>(3 * (size_t)vec, &bytes_);
   d_state = dalloc<MolState>(nm, &bytes_);
   d_charges = dalloc<double>(cap.atoms, &bytes_);
   d_sweeps = dalloc<int>(nm, &bytes_);
@@ -348,9 +349,9 @@ void Batch::allocate(const BatchCapacity& cap) {
   cap_.ws_slots = ws;
   // persistent job tables and lists: one job per molecule per GEMM kind
   job_cap_ = nm;
-  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_};
+  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_, &j_hh_};
   for (JobSet* j : all) { j->d = dalloc<GemmJob>(job_cap_, &bytes_); j->cap = job_cap_; }
-  cuda_check(cudaHostAlloc(&h_jobs_, sizeof(GemmJob) * (size_t)job_cap_ * 13, cudaHostAllocDefault), "cudaHostAlloc jobs");
+  cuda_check(cudaHostAlloc(&h_jobs_, sizeof(GemmJob) * (size_t)job_cap_ * 14, cudaHostAllocDefault), "cudaHostAlloc jobs");
   cuda_check(cudaHostAlloc(&h_lists_, sizeof(int) * (size_t)nm * (kJacobiBuckets + 1), cudaHostAllocDefault),
              "cudaHostAlloc lists");
   for (int b = 0; b < kJacobiBuckets; ++b) d_bucket_lists_.push_back(dalloc<int>(nm, &bytes_));
@@ -438,16 +439,17 @@ Batch::~Batch() {
                   d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs, d_tc_err, d_dip_ws};
   for (void* p : ptrs) if (p) cudaFree(p);
   for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
+  if (d_td) cudaFree(d_td);
 }
 
 void Batch::free_jobs() {
-  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_};
+  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_, &j_hh_};
   for (JobSet* j : all) { if (j->d) cudaFree(j->d); j->d = nullptr; j->n = 0; j->tiles = 0; j->cap = 0; }
 }
 
 void Batch::make_jobset(JobSet* js, const std::vector<GemmJob>& jobs_in) {
   // staging slot of this job set inside the pinned table
-  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_};
+  JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_, &j_hh_};
   int idx = 0;
   while (all[idx] != js) ++idx;
   GemmJob* stage = h_jobs_ + (size_t)idx * job_cap_;
@@ -482,7 +484,7 @@ static GemmJob job(long long a, long long b, long long c, int M, int N, int K, i
 }
 
 void Batch::build_jobs(const std::vector<int>& which) {
-  std::vector<GemmJob> t1, t2, dn, w, kt, yt, mm, d2, z, pp, ns1, ns2, ov;
+  std::vector<GemmJob> t1, t2, dn, w, kt, yt, mm, d2, z, pp, ns1, ns2, ov, hh;
   for (int m : which) {
     const DevMol& d = h_mols[m];
     const int n = d.nao, o = d.nocc, v = n - o;
@@ -492,6 +494,15 @@ void Batch::build_jobs(const std::vector<int>& which) {
     t1.push_back(job(b, b, b, n, n, n, n, n, n, m));            // T = F C^T          (B transposed)
     t2.push_back(job(b, b, b, n, n, n, n, n, n, m));            // G = C T
     dn.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0, 0.0, 1)); // P = 2 C_o^T C_o  (A transposed, symmetric)
+    // Householder path: the density from the smaller eigenvector set, rows
+    // [lo, hi) of C: P = 2 C_o^T C_o, or P = 2 I - 2 C_v^T C_v
+    if (v <= o) {
+      GemmJob j = job(b + (long long)o * n, b + (long long)o * n, b, n, n, v, n, n, n, m, -2.0, 0.0, 1);
+      j.diag = 2.0;
+      hh.push_back(j);
+    } else {
+      hh.push_back(job(b, b, b, n, n, o, n, n, n, m, 2.0, 0.0, 1));
+    }
     if (o > 0 && v > 0) {
       w.push_back(job(b + (long long)o * n, b, b, v, n, n, n, n, n, m));   // U = C_v F  (v x n)
       kt.push_back(job(b, b, b, v, o, n, n, n, o, m));                      // Kt = U C_o^T  (B transposed)
@@ -506,6 +517,14 @@ void Batch::build_jobs(const std::vector<int>& which) {
   make_jobset(&j_w_, w); make_jobset(&j_kt_, kt); make_jobset(&j_yt_, yt); make_jobset(&j_m_, mm);
   make_jobset(&j_d2_, d2); make_jobset(&j_z_, z); make_jobset(&j_p_, pp);
   make_jobset(&j_ns1_, ns1); make_jobset(&j_ns2_, ns2); make_jobset(&j_ov_, ov);
+  make_jobset(&j_hh_, hh);
+  list_max_n_ = 0;
+  hh_max_k_ = 0;
+  for (int m : which) {
+    const DevMol& d = h_mols[m];
+    list_max_n_ = std::max(list_max_n_, d.nao);
+    hh_max_k_ = std::max(hh_max_k_, std::min(d.nocc, d.nao - d.nocc));
+  }
 }
 
 void Batch::upload_list(const std::vector<int>& which) {
@@ -828,8 +847,31 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const
   }
 }
 
+bool Batch::householder(const ScfSettings& s) const {
+  return s.precision == 0 && s.eigensolver != 1 && list_max_n_ <= hh_back_max_n();
+}
+
+void Batch::hh_vectors(int final_pass, int require_active) {
+  const int nl = (int)cur_list_.size();
+  const int max_k = final_pass ? list_max_n_ : hh_max_k_;
+  launches_ += 3;
+  launch_hh_vectors(d_mols, d_list, nl, list_max_n_, max_k, d_state, require_active, final_pass, d_G64, d_td,
+                    vec_total_, d_eps, d_T64, d_S, d_C, stream_);
+}
+
 void Batch::eigen_step(const ScfSettings& s) {
-  if (s.precision == 0) {
+  if (householder(s)) {
+    // FP64 Householder tridiagonalisation (one launch per size bucket, each
+    // with its own shared-memory footprint), then the density's eigenpairs
+    int h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
+    for (size_t b = 0; b < buckets_.size(); ++b) {
+      launches_ += 1;
+      launch_hh_tridiag(d_mols, bucket_dev_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_F, d_G64,
+                        d_td, vec_total_, d_S[4], stream_);
+    }
+    hh_vectors(0, 1);
+    prof_end(h);
+  } else if (s.precision == 0) {
     // size buckets on the cluster Jacobi (a few molecules) form G = C F C^T
     // inside it on the cluster's SMs; the transform GEMMs run only when some
     // bucket uses the one-CTA Jacobi (a molecule's path depends on its bucket
@@ -893,7 +935,12 @@ void Batch::eigen_step(const ScfSettings& s) {
 }
 
 void Batch::density_step(const ScfSettings& s) {
-  if (s.precision == 0) {
+  if (householder(s)) {
+    launches_ += 1;
+    int h = prof_begin(kKDensity, active_work_estimate(kKDensity));
+    launch_gemm(j_hh_.d, j_hh_.n, j_hh_.tiles, d_C, d_C, d_P, true, false, 0.0, d_state, 1, -1, stream_);
+    prof_end(h);
+  } else if (s.precision == 0) {
     launches_ += 1;
     int h = prof_begin(kKDensity, active_work_estimate(kKDensity));
     launch_gemm(j_dens_.d, j_dens_.n, j_dens_.tiles, d_C, d_C, d_P, true, false, 0.0, d_state, 1, -1, stream_);
@@ -989,6 +1036,9 @@ void Batch::finish(const ScfSettings& s, const std::vector<int>& which) {
   upload_list(which);
   const int nl = (int)which.size();
   const int max_atoms = list_max_atoms();
+  // every eigenpair of the last diagonalised Fock matrix: MO energies and
+  // eigenvector rows, as Dsyevd leaves them after the last iteration
+  if (householder(s)) hh_vectors(1, 0);
   launches_ += 2;
   int h = prof_begin(kKEnergy, 0.0);
   launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, max_atoms, d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0,

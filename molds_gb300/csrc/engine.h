@@ -32,6 +32,7 @@ struct ScfSettings {
   int dipole = 1;               // dipole moment after convergence (MolDS DoSCF always computes it)
   int vdw = 0;                  // empirical dispersion energy (SCF block "vdW yes"; always on for AM1-D / PM3-D)
   double vdw_s6 = 1.40, vdw_d = 23.0;
+  int eigensolver = 0;          // FP64 eigensolves: 0 auto (Householder), 1 Jacobi, 2 Householder
 };
 
 // kernel classes timed by the optional per-launch CUDA-event profiler
@@ -153,6 +154,12 @@ class Batch {
   void upload_list(const std::vector<int>& which);
   void eigen_step(const ScfSettings& s);
   void density_step(const ScfSettings& s);
+  // FP64 Householder path (tridiag.cu): used for this list and these settings
+  bool householder(const ScfSettings& s) const;
+  // eigenpairs of the current list from each molecule's last
+  // tridiagonalisation: final_pass = 0 the density's set, 1 every index (MO
+  // energies and vectors)
+  void hh_vectors(int final_pass, int require_active);
 
   Engine* eng_;
   cudaStream_t stream_;
@@ -186,6 +193,8 @@ class Batch {
   float *d_Cf = nullptr, *d_Cnf = nullptr, *d_Ff = nullptr;   // FP32 shadows of the tensor-core chain
   double *d_G64 = nullptr, *d_T64 = nullptr;
   double* d_S[6] = {};
+  double* d_td = nullptr;                // tridiagonal d, e, tau (3 x vec arena)
+  int list_max_n_ = 0, hh_max_k_ = 0;    // largest basis and density-set size of the current list
   float *d_jA32 = nullptr, *d_jV32 = nullptr;
   void* d_bj_ws = nullptr;               // block-Jacobi workspace (bases above kSmallJacobiMaxN)
   int* h_bj_pending = nullptr;           // pinned: molecules still rotating after a block-Jacobi sweep
@@ -214,7 +223,7 @@ class Batch {
   GemmJob* h_jobs_ = nullptr;             // pinned staging of the job tables
   int* h_lists_ = nullptr;                // pinned staging of the molecule / bucket lists
   int job_cap_ = 0;
-  JobSet j_trans1_, j_trans2_, j_dens_, j_w_, j_kt_, j_yt_, j_m_, j_d2_, j_z_, j_p_, j_ns1_, j_ns2_, j_ov_;
+  JobSet j_trans1_, j_trans2_, j_dens_, j_w_, j_kt_, j_yt_, j_m_, j_d2_, j_z_, j_p_, j_ns1_, j_ns2_, j_ov_, j_hh_;
   void free_jobs();
   void make_jobset(JobSet* js, const std::vector<GemmJob>& jobs);
 

@@ -18,6 +18,7 @@ struct GemmJob {
   int tc_tiles_n;   // the same job in 128 x 128 tiles (tensor-core kernel)
   int tc_tile0;
   int pad;
+  double diag;      // added to the diagonal of C (CUDA-core kernel): C = alpha op(A) op(B) + beta C + diag I
 };
 
 int gemm_tiles(int M, int N);
@@ -116,6 +117,21 @@ void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int m
                        int require_active, const double* G, const double* Cin, int use_basis, double* Cout,
                        double* eps, double* Aws, double* Vws, long long ws_stride, int max_sweeps,
                        int* sweeps_out, cudaStream_t s);
+
+// tridiag.cu: FP64 Householder tridiagonalisation + bisection + inverse
+// iteration + back-transformation.  td holds d, e, tau of every molecule at
+// vec0, vec0 + vstride, vec0 + 2 vstride; W (N x N arena) the reflectors.
+int hh_smem_max_n();     // largest basis whose packed matrix fits one CTA's shared memory
+int hh_back_max_n();     // largest basis the back-transformation kernel serves
+void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
+                       int require_active, const double* F, double* W, double* td, long long vstride, double* Aws,
+                       cudaStream_t s);
+// eigenpairs of the SCF pass (final_pass = 0: the smaller of the occupied and
+// virtual sets) or of every index (final_pass = 1) into eps and rows of C;
+// Z and S4[0..3] are N x N scratch arenas
+void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
+                       int require_active, int final_pass, const double* W, const double* td, long long vstride,
+                       double* eps, double* Z, double* const* S4, double* C, cudaStream_t s);
 
 // scf_kernels.cu
 void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C,

@@ -105,7 +105,8 @@ gemm_kernel(const GemmJob* __restrict__ jobs, int njobs, const TA* __restrict__ 
       const int gj = col0 + tx * 4 + j;
       if (gj >= job.N) continue;
       TC* c = Cj + (long long)gi * job.ldc + gj;
-      const double v = job.alpha * (double)acc[i][j];
+      double v = job.alpha * (double)acc[i][j];
+      if (gi == gj) v += job.diag;
       *c = (TC)(job.beta != 0.0 ? v + job.beta * (double)(*c) : v);
       if (job.sym && tm != tn) {   // mirror (beta is zero for symmetric jobs)
         TC* cm = Cj + (long long)gj * job.ldc + gi;

@@ -1,0 +1,596 @@
+// Kernel (d), FP64 path: batched symmetric eigensolver by Householder
+// tridiagonalisation, Sturm bisection, inverse iteration and
+// back-transformation.
+//
+// Stands in for MolDS's Lapack::Dsyevd (src/wrappers/Lapack.cpp:102-160,
+// called at src/cndo/Cndo2.cpp:652-655).  Output convention is the
+// reference's: eigenvalues ascending, eigenvectors as ROWS of C with each
+// row's component sum made >= 0 (Lapack.cpp:141-150).
+//
+// Why this algorithm on GB300: the chip issues FP64 at about two FMAs per
+// clock per SM (1.2 TFLOP/s over 152 SMs), so an FP64 eigensolve is bound by
+// its FP64 operation count, not by memory.  A warm-started cyclic Jacobi costs
+// ~4 N^3 FMAs per sweep (3-4 sweeps per SCF iteration) plus the 2 N^3 of the
+// warm-start transform.  Householder tridiagonalisation costs (2/3) N^3 FMAs,
+// and during the SCF the density needs only the smaller of the occupied and
+// virtual eigenvector sets (k vectors): the back-transformation costs N^2 k
+// FMAs and P = 2 X^T X (or 2 I - 2 X^T X) N^2 k / 2.  All N eigenpairs are
+// formed once, after the last iteration, for the MO energies and vectors.
+//
+// Kernels (each molecule's work depends only on its own data, so results are
+// bitwise independent of the batch):
+//   hh_tridiag_kernel   one CTA per molecule: A = Q T Q^T with the packed lower
+//                       triangle in shared memory (or a global workspace for
+//                       large N); reflector j goes to row j of W, d / e / tau
+//                       to the tridiagonal arena
+//   tri_vectors_kernel  one thread per wanted index: the eigenvalue of T by
+//                       bisection on a division-free Sturm sequence, then two
+//                       steps of inverse iteration with a partial-pivoting LU of
+//                       T - lambda I (as LAPACK dstebz / dstein do)
+//   tri_orth_kernel     one CTA per molecule: classical Gram-Schmidt, applied
+//                       twice, within clusters of close eigenvalues (gap below
+//                       1e-3 ||T||_1, dstein's criterion)
+//   hh_back_kernel      X = Q Z, 32 columns per CTA, reflectors applied in
+//                       reverse order; X written as rows of C (sign-fixed in the
+//                       final pass)
+#include <cuda_runtime.h>
+#include <mutex>
+#include "nddo_batch.cuh"
+#include "kernels.h"
+
+namespace nddo {
+
+constexpr int kHhThreads = 512;
+constexpr int kVecThreads = 128;
+constexpr int kOrthThreads = 256;
+constexpr int kBackCols = 32, kBackWarps = 8;
+
+__device__ __forceinline__ int tri_off(int i) { return (i * (i + 1)) >> 1; }
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Index range [lo, hi) of the eigenpairs a pass needs: the final pass all of
+// them; an SCF iteration only the smaller of the occupied (0..nocc) and
+// virtual (nocc..n) sets (the density is 2 X^T X or 2 I - 2 X^T X).
+__host__ __device__ inline void hh_range(int n, int nocc, int final_pass, int* lo, int* hi) {
+  if (final_pass) { *lo = 0; *hi = n; return; }
+  if (n - nocc <= nocc) { *lo = nocc; *hi = n; }
+  else { *lo = 0; *hi = nocc; }
+}
+
+size_t hh_tridiag_smem_bytes(int n, bool a_in_smem) {
+  size_t d = 3 * (size_t)n + 8;
+  if (a_in_smem) d += (size_t)n * (n + 1) / 2;
+  return d * sizeof(double);
+}
+
+static int g_hh_smem_max_n = -1;
+static std::once_flag g_hh_once;
+
+int hh_smem_max_n() {
+  std::call_once(g_hh_once, [] {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    int n = 8;
+    while (hh_tridiag_smem_bytes(n + 1, true) <= (size_t)optin) ++n;
+    g_hh_smem_max_n = n;
+  });
+  return g_hh_smem_max_n;
+}
+
+// ---------------------------------------------------------------------------
+// Tridiagonalisation (LAPACK dsytd2 'L' semantics, own parallel layout).
+// Step k: x = A[k+1:, k]; H = I - tau u u^T with u = (1, x_1 s, ..., x_{m-1} s)
+// zeroes x below its first entry; p = tau A22 u, w = p - (tau/2)(p.u) u,
+// A22 <- A22 - u w^T - w u^T (lower triangle only).
+// ---------------------------------------------------------------------------
+template <bool kSmem>
+__global__ void __launch_bounds__(kHhThreads)
+hh_tridiag_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
+                  int require_active, const double* __restrict__ F, double* __restrict__ W, double* __restrict__ td,
+                  long long vstride, double* __restrict__ Aws) {
+  extern __shared__ __align__(16) double hsm[];
+  const int mi = list[blockIdx.x];
+  if (require_active && st[mi].status != kActive) return;
+  const DevMol mol = mols[mi];
+  const int n = mol.nao;
+  const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nth >> 5;
+  double* A = kSmem ? hsm : Aws + mol.mat0;
+  double* v = kSmem ? hsm + (long long)n * (n + 1) / 2 : hsm;
+  double* p = v + n;
+  double* w = p + n;
+  double* sc = w + n;   // [0] tau of the current step
+  const double* Fm = F + mol.mat0;
+  double* Wm = W + mol.mat0;
+  double* dd = td + mol.vec0;
+  double* ee = dd + vstride;
+  double* tt = ee + vstride;
+
+  for (int i = warp; i < n; i += nwarps)
+    for (int j = lane; j <= i; j += 32) A[tri_off(i) + j] = Fm[(long long)i * n + j];
+  __syncthreads();
+
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m = n - 1 - k;   // trailing size
+    const int r0 = k + 1;      // first trailing row / column
+    if (warp == 0) {
+      double s = 0.0;
+      for (int i = 1 + lane; i < m; i += 32) {
+        const double x = A[tri_off(r0 + i) + k];
+        s = fma(x, x, s);
+      }
+      s = warp_sum_d(s);
+      const double alpha = A[tri_off(r0) + k];
+      double tau = 0.0, beta = alpha, scal = 0.0;
+      if (s != 0.0) {
+        const double nrm = sqrt(fma(alpha, alpha, s));
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tau = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+      }
+      for (int i = lane; i < m; i += 32) {
+        const double vi = i == 0 ? 1.0 : A[tri_off(r0 + i) + k] * scal;
+        v[i] = vi;
+        Wm[(long long)k * n + r0 + i] = vi;
+      }
+      if (lane == 0) {
+        dd[k] = A[tri_off(k) + k];
+        ee[k] = beta;
+        tt[k] = tau;
+        sc[k & 1] = tau;   // two slots: a warp may still read this step's value when warp 0 starts the next
+      }
+    }
+    __syncthreads();
+    const double tau = sc[k & 1];
+    if (tau == 0.0) continue;   // uniform: H = I, nothing to update
+    // p = tau A22 v: a group of g lanes per row (g a power of two, g * rows <= threads)
+    int gsh = 0;
+    while (gsh < 5 && (m << (gsh + 1)) <= nth) ++gsh;
+    const int g = 1 << gsh, ngrp = nth >> gsh, grp = tid >> gsh, gl = tid & (g - 1);
+    for (int i0 = 0; i0 < m; i0 += ngrp) {
+      const int i = i0 + grp;
+      double s = 0.0;
+      if (i < m) {
+        const int R = r0 + i;
+        const int oR = tri_off(R) + r0;
+        for (int j = gl; j < m; j += g) {
+          const double a = j <= i ? A[oR + j] : A[tri_off(r0 + j) + R];
+          s = fma(a, v[j], s);
+        }
+      }
+      for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (i < m && gl == 0) p[i] = tau * s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double s = 0.0;
+      for (int i = lane; i < m; i += 32) s = fma(p[i], v[i], s);
+      s = warp_sum_d(s);
+      const double c = 0.5 * tau * s;
+      for (int i = lane; i < m; i += 32) w[i] = fma(-c, v[i], p[i]);
+    }
+    __syncthreads();
+    // A22 -= v w^T + w v^T on the lower triangle; rows i and m-1-i share a warp
+    const int npair = (m + 1) >> 1;
+    for (int q = warp; q < npair; q += nwarps) {
+      const int i1 = q, i2 = m - 1 - q;
+      const int len1 = i1 + 1, len = i2 == i1 ? len1 : len1 + i2 + 1;
+      for (int t = lane; t < len; t += 32) {
+        const bool first = t < len1;
+        const int i = first ? i1 : i2;
+        const int j = first ? t : t - len1;
+        double* a = A + tri_off(r0 + i) + r0 + j;
+        *a = fma(-v[i], w[j], fma(-w[i], v[j], *a));
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    if (n >= 2) {
+      dd[n - 2] = A[tri_off(n - 2) + n - 2];
+      ee[n - 2] = A[tri_off(n - 1) + n - 2];
+      tt[n - 2] = 0.0;
+    }
+    dd[n - 1] = A[tri_off(n - 1) + n - 1];
+    ee[n - 1] = 0.0;
+    tt[n - 1] = 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tridiagonal eigenpairs.
+// ---------------------------------------------------------------------------
+
+// Number of eigenvalues of T below x: sign changes of the leading principal
+// minors P_0 = 1, P_1 = d_0 - x, P_{i+1} = (d_i - x) P_i - e_{i-1}^2 P_{i-1}
+// (a zero minor takes the sign opposite to its predecessor).  No divisions;
+// the pair (P_i, P_{i+1}) is rescaled by a power of two when it leaves
+// [2^-256, 2^256].  Three FP64 operations per step; signs and exponents are
+// read with integer operations.
+__device__ __forceinline__ int sturm_count(const double* __restrict__ d, const double* __restrict__ e2, int n,
+                                           double x) {
+  double p0 = 1.0, p1 = d[0] - x;
+  long long b = __double_as_longlong(p1);
+  int s_prev = ((b << 1) == 0) ? 1 : (int)((unsigned long long)b >> 63);
+  int cnt = s_prev;
+  for (int i = 1; i < n; ++i) {
+    const double p2 = fma(d[i] - x, p1, -(e2[i - 1] * p0));
+    b = __double_as_longlong(p2);
+    const int s = ((b << 1) == 0) ? (s_prev ^ 1) : (int)((unsigned long long)b >> 63);
+    cnt += s != s_prev;
+    s_prev = s;
+    p0 = p1;
+    p1 = p2;
+    const int e1 = (int)((__double_as_longlong(p0) >> 52) & 0x7ff);
+    const int e0 = (int)((b >> 52) & 0x7ff);
+    const int em = e0 > e1 ? e0 : e1;
+    if (em != 0 && (em > 1023 + 256 || em < 1023 - 256)) {
+      const double scale = __longlong_as_double((long long)(2046 - em) << 52);
+      p0 *= scale;
+      p1 *= scale;
+    }
+  }
+  return cnt;
+}
+
+// uniform pseudo-random value in [-0.5, 0.5): the start vector of inverse iteration
+__device__ __forceinline__ double start_entry(unsigned int idx, unsigned int i) {
+  unsigned long long z = ((unsigned long long)idx << 32) ^ (unsigned long long)(i * 0x9E3779B9u) ^ 0x2545F4914F6CDD1DULL;
+  z ^= z >> 33; z *= 0xff51afd7ed558ccdULL;
+  z ^= z >> 33; z *= 0xc4ceb9fe1a85ec53ULL;
+  z ^= z >> 33;
+  const double one_two = __longlong_as_double((long long)(0x3FF0000000000000ULL | (z >> 12)));
+  return one_two - 1.5;
+}
+
+// One solve (T - lam I) x = b with the stored factors (forward elimination
+// with the row interchanges, then back substitution); b is overwritten by x.
+// Layout of every per-vector array: element i of vector c at i * k + c.
+__device__ __forceinline__ void tri_solve(int n, int k, double* __restrict__ x, const double* __restrict__ fl,
+                                          const double* __restrict__ fu1i, const double* __restrict__ fu2,
+                                          const double* __restrict__ fpiv, const double* __restrict__ e) {
+  double cb = x[0];
+  for (int i = 0; i + 1 < n; ++i) {
+    const long long o = (long long)i * k;
+    const double bn = x[o + k];
+    const double l = fl[o];
+    if (fpiv[o] != 0.0) { x[o] = bn; cb = fma(-l, bn, cb); }
+    else { x[o] = cb; cb = fma(-l, cb, bn); }
+  }
+  x[(long long)(n - 1) * k] = cb;
+  double x2 = 0.0, x1 = cb * fu1i[(long long)(n - 1) * k];
+  x[(long long)(n - 1) * k] = x1;
+  for (int i = n - 2; i >= 0; --i) {
+    const long long o = (long long)i * k;
+    const double u3 = fpiv[o] != 0.0 ? e[i + 1] : 0.0;
+    const double xi = fma(-u3, x2, fma(-fu2[o], x1, x[o])) * fu1i[o];
+    x[o] = xi;
+    x2 = x1;
+    x1 = xi;
+  }
+}
+
+// grid: (list entry, chunk of kVecThreads indices); one thread per wanted index
+__global__ void __launch_bounds__(kVecThreads)
+tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
+                   int require_active, int final_pass, const double* __restrict__ td, long long vstride,
+                   double* __restrict__ eps, double* __restrict__ Z, double* __restrict__ S0, double* __restrict__ S1,
+                   double* __restrict__ S2, double* __restrict__ S3) {
+  extern __shared__ __align__(16) double vsm[];
+  const int mi = list[blockIdx.x];
+  if (require_active && st[mi].status != kActive) return;
+  const DevMol mol = mols[mi];
+  const int n = mol.nao;
+  int lo, hi;
+  hh_range(n, mol.nocc, final_pass, &lo, &hi);
+  const int k = hi - lo;
+  const int c0 = blockIdx.y * kVecThreads;
+  if (c0 >= k) return;
+  double* d = vsm;
+  double* e = d + n;
+  double* e2 = e + n;
+  double* red = e2 + n;   // 2 * (kVecThreads / 32)
+  const double* tdd = td + mol.vec0;
+  const double* tde = tdd + vstride;
+  const int tid = threadIdx.x;
+  // Gershgorin interval and the 1-norm of T
+  double gl = 1e300, gu = -1e300;
+  for (int i = tid; i < n; i += kVecThreads) {
+    const double di = tdd[i];
+    const double ei = i + 1 < n ? tde[i] : 0.0;
+    const double em = i > 0 ? tde[i - 1] : 0.0;
+    d[i] = di;
+    e[i] = ei;
+    e2[i] = ei * ei;
+    const double r = fabs(ei) + fabs(em);
+    gl = fmin(gl, di - r);
+    gu = fmax(gu, di + r);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    gl = fmin(gl, __shfl_xor_sync(0xffffffffu, gl, o));
+    gu = fmax(gu, __shfl_xor_sync(0xffffffffu, gu, o));
+  }
+  if ((tid & 31) == 0) { red[2 * (tid >> 5)] = gl; red[2 * (tid >> 5) + 1] = gu; }
+  __syncthreads();
+  gl = red[0];
+  gu = red[1];
+  for (int w = 1; w < kVecThreads / 32; ++w) { gl = fmin(gl, red[2 * w]); gu = fmax(gu, red[2 * w + 1]); }
+  const double ulp = 2.220446049250313e-16;
+  const double tnorm = fmax(fabs(gl), fabs(gu));
+  const double pad = 2.0 * ulp * tnorm * n + 1e-300;
+  gl -= pad;
+  gu += pad;
+  const double tiny = ulp * tnorm + 1e-300;   // replaces an exactly zero pivot
+
+  const int c = c0 + tid;
+  if (c >= k) return;
+  const int idx = lo + c;
+  // bisection: count(lo_) <= idx < count(hi_)
+  double a = gl, bnd = gu;
+  for (int it = 0; it < 80; ++it) {
+    const double mid = 0.5 * (a + bnd);
+    if (bnd - a <= 2.0 * ulp * fmax(fabs(a), fabs(bnd)) + ulp * tnorm) break;
+    if (sturm_count(d, e2, n, mid) > idx) bnd = mid; else a = mid;
+  }
+  const double lam = 0.5 * (a + bnd);
+  eps[mol.vec0 + idx] = lam;
+
+  // inverse iteration: factor T - lam I = P L U once, solve twice
+  double* x = Z + mol.mat0 + c;
+  double* fl = S0 + mol.mat0 + c;
+  double* fu1i = S1 + mol.mat0 + c;
+  double* fu2 = S2 + mol.mat0 + c;
+  double* fpiv = S3 + mol.mat0 + c;
+  {
+    double cc = d[0] - lam, s1 = n > 1 ? e[0] : 0.0;
+    for (int i = 0; i + 1 < n; ++i) {
+      const long long o = (long long)i * k;
+      const double ei = e[i];
+      const double a1 = d[i + 1] - lam;
+      const double e1 = i + 2 < n ? e[i + 1] : 0.0;
+      if (fabs(ei) > fabs(cc)) {
+        const double r = 1.0 / ei;
+        const double l = cc * r;
+        fl[o] = l; fu1i[o] = r; fu2[o] = a1; fpiv[o] = 1.0;
+        cc = fma(-l, a1, s1);
+        s1 = -l * e1;
+      } else {
+        if (cc == 0.0) cc = tiny;
+        const double r = 1.0 / cc;
+        const double l = ei * r;
+        fl[o] = l; fu1i[o] = r; fu2[o] = s1; fpiv[o] = 0.0;
+        cc = fma(-l, s1, a1);
+        s1 = e1;
+      }
+    }
+    if (cc == 0.0) cc = tiny;
+    fu1i[(long long)(n - 1) * k] = 1.0 / cc;
+  }
+  for (int i = 0; i < n; ++i) x[(long long)i * k] = start_entry((unsigned)idx, (unsigned)i);
+  for (int step = 0; step < 2; ++step) {
+    tri_solve(n, k, x, fl, fu1i, fu2, fpiv, e);
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) { const double xi = x[(long long)i * k]; s = fma(xi, xi, s); }
+    const double r = s > 0.0 ? rsqrt(s) : 0.0;
+    for (int i = 0; i < n; ++i) x[(long long)i * k] *= r;
+  }
+}
+
+// Re-orthogonalisation inside clusters of close eigenvalues: for each vector j
+// of a cluster, z_j <- z_j - sum_{l<j} <z_l, z_j> z_l twice (classical
+// Gram-Schmidt applied twice), then normalised.  One CTA per molecule.
+__global__ void __launch_bounds__(kOrthThreads)
+tri_orth_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
+                int require_active, int final_pass, const double* __restrict__ td, long long vstride,
+                const double* __restrict__ eps, double* __restrict__ Z) {
+  __shared__ double dots[1024];
+  __shared__ double red[kOrthThreads / 32];
+  __shared__ double onenrm_s;
+  const int mi = list[blockIdx.x];
+  if (require_active && st[mi].status != kActive) return;
+  const DevMol mol = mols[mi];
+  const int n = mol.nao;
+  int lo, hi;
+  hh_range(n, mol.nocc, final_pass, &lo, &hi);
+  const int k = hi - lo;
+  if (k < 2) return;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nwarps = kOrthThreads / 32;
+  const double* tdd = td + mol.vec0;
+  const double* tde = tdd + vstride;
+  double nr = 0.0;
+  for (int i = tid; i < n; i += kOrthThreads) {
+    const double r = fabs(tdd[i]) + (i + 1 < n ? fabs(tde[i]) : 0.0) + (i > 0 ? fabs(tde[i - 1]) : 0.0);
+    nr = fmax(nr, r);
+  }
+  for (int o = 16; o > 0; o >>= 1) nr = fmax(nr, __shfl_xor_sync(0xffffffffu, nr, o));
+  if (lane == 0) red[warp] = nr;
+  __syncthreads();
+  if (tid == 0) {
+    double m = 0.0;
+    for (int w = 0; w < nwarps; ++w) m = fmax(m, red[w]);
+    onenrm_s = m;
+  }
+  __syncthreads();
+  const double ortol = 1e-3 * onenrm_s;
+  const double* ev = eps + mol.vec0 + lo;
+  double* Zm = Z + mol.mat0;
+  int c0 = 0;
+  while (c0 < k) {
+    int c1 = c0 + 1;
+    while (c1 < k && ev[c1] - ev[c1 - 1] < ortol) ++c1;
+    if (c1 - c0 >= 2) {
+      for (int j = c0 + 1; j < c1; ++j) {
+        const int nprev = j - c0;
+        for (int pass = 0; pass < 2; ++pass) {
+          // dots with the earlier vectors of the cluster (warp per vector)
+          for (int l0 = 0; l0 < nprev; l0 += 1024) {
+            const int cnt = min(1024, nprev - l0);
+            for (int q = warp; q < cnt; q += nwarps) {
+              const int l = c0 + l0 + q;
+              double s = 0.0;
+              for (int i = lane; i < n; i += 32) s = fma(Zm[(long long)i * k + l], Zm[(long long)i * k + j], s);
+              s = warp_sum_d(s);
+              if (lane == 0) dots[q] = s;
+            }
+            __syncthreads();
+            for (int i = tid; i < n; i += kOrthThreads) {
+              double zj = Zm[(long long)i * k + j];
+              for (int q = 0; q < cnt; ++q) zj = fma(-dots[q], Zm[(long long)i * k + c0 + l0 + q], zj);
+              Zm[(long long)i * k + j] = zj;
+            }
+            __syncthreads();
+          }
+        }
+        double s = 0.0;
+        for (int i = tid; i < n; i += kOrthThreads) { const double z = Zm[(long long)i * k + j]; s = fma(z, z, s); }
+        s = warp_sum_d(s);
+        if (lane == 0) red[warp] = s;
+        __syncthreads();
+        double tot = 0.0;
+        for (int w = 0; w < nwarps; ++w) tot += red[w];
+        const double r = tot > 0.0 ? rsqrt(tot) : 0.0;
+        for (int i = tid; i < n; i += kOrthThreads) Zm[(long long)i * k + j] *= r;
+        __syncthreads();
+      }
+    }
+    c0 = c1;
+  }
+}
+
+// X = Q Z with Q = H_0 H_1 ... H_{n-3}: H_{n-3} is applied first.  CTA = 32
+// columns (lanes) x 8 row slices (warps, rows i = warp mod 8); the columns sit
+// in shared memory (pitch 33).  Output: row lo + c of C; in the final pass
+// each row's component sum is made >= 0.
+__global__ void __launch_bounds__(kBackCols * kBackWarps)
+hh_back_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
+               int require_active, int final_pass, const double* __restrict__ W, const double* __restrict__ td,
+               long long vstride, const double* __restrict__ Z, double* __restrict__ C) {
+  extern __shared__ __align__(16) double bsm[];
+  const int mi = list[blockIdx.x];
+  if (require_active && st[mi].status != kActive) return;
+  const DevMol mol = mols[mi];
+  const int n = mol.nao;
+  int lo, hi;
+  hh_range(n, mol.nocc, final_pass, &lo, &hi);
+  const int k = hi - lo;
+  const int cb = blockIdx.y * kBackCols;
+  if (cb >= k) return;
+  constexpr int kP = kBackCols + 1;
+  double* zs = bsm;                       // n x kP
+  double* red = zs + (long long)n * kP;   // kBackWarps x kBackCols
+  double* dotv = red + kBackWarps * kBackCols;
+  double* taus = dotv + kBackCols;        // n
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const double* Zm = Z + mol.mat0;
+  const double* Wm = W + mol.mat0;
+  const double* tt = td + mol.vec0 + 2 * vstride;
+  const int c = cb + lane;
+  for (int i = warp; i < n; i += kBackWarps) zs[i * kP + lane] = c < k ? Zm[(long long)i * k + c] : 0.0;
+  for (int i = tid; i < n; i += kBackCols * kBackWarps) taus[i] = tt[i];
+  __syncthreads();
+  for (int j = n - 3; j >= 0; --j) {
+    const double tau = taus[j];
+    if (tau == 0.0) continue;
+    const double* u = Wm + (long long)j * n;
+    // row slices are fixed (row i belongs to warp i mod 8), so a warp only
+    // reads rows it updated itself at the previous reflector
+    const int i0 = j + 1 + ((warp - (j + 1)) & (kBackWarps - 1));
+    double part = 0.0;
+    for (int i = i0; i < n; i += kBackWarps) part = fma(u[i], zs[i * kP + lane], part);
+    red[warp * kBackCols + lane] = part;
+    __syncthreads();
+    if (warp == 0) {
+      double s = red[lane];
+#pragma unroll
+      for (int q = 1; q < kBackWarps; ++q) s += red[q * kBackCols + lane];
+      dotv[lane] = tau * s;
+    }
+    __syncthreads();
+    const double dt = dotv[lane];
+    for (int i = i0; i < n; i += kBackWarps) {
+      double* z = zs + i * kP + lane;
+      *z = fma(-dt, u[i], *z);
+    }
+  }
+  __syncthreads();
+  // rows of C: warp per row, lanes over the components
+  double* Cm = C + mol.mat0;
+  for (int q = warp; q < kBackCols; q += kBackWarps) {
+    const int cc = cb + q;
+    if (cc >= k) break;
+    double sgn = 1.0;
+    if (final_pass) {
+      double s = 0.0;
+      for (int i = lane; i < n; i += 32) s += zs[i * kP + q];
+      s = warp_sum_d(s);
+      sgn = s < 0.0 ? -1.0 : 1.0;
+    }
+    double* row = Cm + (long long)(lo + cc) * n;
+    for (int i = lane; i < n; i += 32) row[i] = sgn * zs[i * kP + q];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static std::once_flag g_hh_attr_once;
+
+static void hh_set_attributes() {
+  std::call_once(g_hh_attr_once, [] {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncSetAttribute(hh_tridiag_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncSetAttribute(hh_tridiag_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncSetAttribute(hh_back_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncSetAttribute(tri_vectors_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  });
+}
+
+size_t hh_back_smem_bytes(int n) {
+  return ((size_t)n * (kBackCols + 1) + kBackWarps * kBackCols + kBackCols + n) * sizeof(double);
+}
+
+int hh_back_max_n() {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  int n = 8;
+  while (hh_back_smem_bytes(n + 1) <= (size_t)optin) ++n;
+  return n;
+}
+
+void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
+                       int require_active, const double* F, double* W, double* td, long long vstride, double* Aws,
+                       cudaStream_t s) {
+  if (nlist <= 0) return;
+  hh_set_attributes();
+  const bool smem = max_n <= hh_smem_max_n();
+  const size_t sh = hh_tridiag_smem_bytes(max_n, smem);
+  if (smem)
+    hh_tridiag_kernel<true><<<nlist, kHhThreads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws);
+  else
+    hh_tridiag_kernel<false><<<nlist, kHhThreads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws);
+}
+
+void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
+                       int require_active, int final_pass, const double* W, const double* td, long long vstride,
+                       double* eps, double* Z, double* const* S4, double* C, cudaStream_t s) {
+  if (nlist <= 0 || max_k <= 0) return;
+  hh_set_attributes();
+  const size_t vsh = (3 * (size_t)max_n + 2 * (kVecThreads / 32)) * sizeof(double);
+  dim3 gv(nlist, (max_k + kVecThreads - 1) / kVecThreads);
+  tri_vectors_kernel<<<gv, kVecThreads, vsh, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z,
+                                                  S4[0], S4[1], S4[2], S4[3]);
+  tri_orth_kernel<<<nlist, kOrthThreads, 0, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z);
+  dim3 gb(nlist, (max_k + kBackCols - 1) / kBackCols);
+  hh_back_kernel<<<gb, kBackCols * kBackWarps, hh_back_smem_bytes(max_n), s>>>(mols, list, st, require_active,
+                                                                              final_pass, W, td, vstride, Z, C);
+}
+
+}  // namespace nddo

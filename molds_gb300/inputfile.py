@@ -42,6 +42,7 @@ class SCFParams:
     vdw_s6: float = 1.40             # vdW_s6 (src/base/Parameters.cpp:141)
     vdw_d: float = 23.0              # vdW_d (src/base/Parameters.cpp:142)
     dipole: bool = True              # dipole moment after convergence, as DoSCF (not a MolDS key)
+    eigensolver: str = "auto"        # FP64 eigensolves: "auto" / "householder" or "jacobi" (not a MolDS key)
 
 
 @dataclass
