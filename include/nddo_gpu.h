@@ -28,7 +28,8 @@ typedef struct nddo_ctx nddo_ctx;
 
 /* AM1-D / PM3-D: MolDS's dispersion-corrected sets (THEORY am1-d / pm3-d;
  * src/am1/Am1D.cpp, src/pm3/Pm3D.cpp) and PDDG/PM3 (THEORY pm3/pddg;
- * src/pm3/Pm3Pddg.cpp), H, C, N, O and S only. */
+ * src/pm3/Pm3Pddg.cpp).  AM1-D and PDDG/PM3: H, C, N, O and S; PM3-D: H, C,
+ * N, O, F, S, Cl. */
 enum {
   NDDO_THEORY_MNDO = 0, NDDO_THEORY_AM1 = 1, NDDO_THEORY_PM3 = 2, NDDO_THEORY_AM1D = 3, NDDO_THEORY_PM3D = 4,
   NDDO_THEORY_PM3PDDG = 5
@@ -238,8 +239,10 @@ int nddo_measure_fma_peak(nddo_ctx* ctx, int precision, double* tflops);
  * = default stream); err/err_len receive the message of a failure.
  * Limit: n_atoms <= 512; larger molecules are rejected with NDDO_ERR_BUDGET.
  * The first call on a device sets that device up (resolves the array's address
- * and uploads constant tables): make it before any stream capture.  Calls
- * share the one array, so calls that overlap on the GPU race; serialise them. */
+ * and uploads constant tables).  No call may be made on a stream that is being
+ * captured (each call copies from host memory and synchronises); such a call
+ * returns NDDO_ERR_ARGUMENT.  Calls share the one array, so calls that overlap
+ * on the GPU race; serialise them. */
 int nddo_pair_integrals_noalloc(int device, int theory, int n_atoms, const int* atomic_numbers,
                                 const double* xyz_bohr, double* d_pair_blocks, size_t pair_block_capacity,
                                 double* d_core_hamiltonian, double* core_repulsion, void* stream,

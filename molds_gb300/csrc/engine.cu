@@ -575,7 +575,8 @@ int Batch::list_max_atoms() const {
 const char* kernel_class_name(int k) {
   static const char* names[kKNumClasses] = {"pair_integrals", "core_hamiltonian", "fock_build", "basis_orthonormalise",
                                             "warm_start_transform", "jacobi_eigensolver", "density", "fp64_refinement",
-                                            "diis", "energy", "dipole"};
+                                            "diis", "energy", "dipole", "tridiagonalisation",
+                                            "tridiagonal_eigenvectors"};
   return (k >= 0 && k < kKNumClasses) ? names[k] : "?";
 }
 
@@ -652,6 +653,10 @@ double Batch::active_work_estimate(int cls) const {
     const double n = d.nao, o = d.nocc, v = n - o;
     switch (cls) {
       case kKJacobi: w += 10.0 / 3.0 * n * n * n; break;
+      // the tridiagonalisation share of the (10/3) N^3 eigensolver convention
+      case kKTridiag: w += 4.0 / 3.0 * n * n * n; break;
+      // back-transformation of the k = min(o, v) density vectors (2 N^2 k flops)
+      case kKEigvec: w += 2.0 * n * n * std::min(o, v); break;
       case kKTransform: w += 4.0 * n * n * n; break;
       case kKOrtho: w += 4.0 * n * n * n; break;
       case kKDensity: w += 2.0 * n * n * o; break;
@@ -848,28 +853,31 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const
 }
 
 bool Batch::householder(const ScfSettings& s) const {
-  return s.precision == 0 && s.eigensolver != 1 && list_max_n_ <= hh_back_max_n();
+  return s.eigensolver != 1 && list_max_n_ <= hh_back_max_n();
 }
 
-void Batch::hh_vectors(int final_pass, int require_active) {
+void Batch::hh_vectors(const ScfSettings& s, int final_pass, int require_active) {
   const int nl = (int)cur_list_.size();
   const int max_k = final_pass ? list_max_n_ : hh_max_k_;
-  launches_ += 3;
-  launch_hh_vectors(d_mols, d_list, nl, list_max_n_, max_k, d_state, require_active, final_pass, d_G64, d_td,
-                    vec_total_, d_eps, d_T64, d_S, d_C, stream_);
+  const int mixed = s.precision == 1 ? 1 : 0;
+  launches_ += (mixed && !final_pass) ? 4 : 3;
+  launch_hh_vectors(d_mols, d_list, nl, list_max_n_, max_k, d_state, require_active, final_pass, mixed, d_G64, d_td,
+                    vec_total_, d_eps, d_T64, d_S, d_C, d_Cf, stream_);
 }
 
 void Batch::eigen_step(const ScfSettings& s) {
   if (householder(s)) {
     // FP64 Householder tridiagonalisation (one launch per size bucket, each
     // with its own shared-memory footprint), then the density's eigenpairs
-    int h = prof_begin(kKJacobi, active_work_estimate(kKJacobi));
+    int h = prof_begin(kKTridiag, active_work_estimate(kKTridiag));
     for (size_t b = 0; b < buckets_.size(); ++b) {
       launches_ += 1;
       launch_hh_tridiag(d_mols, bucket_dev_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_F, d_G64,
                         d_td, vec_total_, d_S[4], stream_);
     }
-    hh_vectors(0, 1);
+    prof_end(h);
+    h = prof_begin(kKEigvec, active_work_estimate(kKEigvec));
+    hh_vectors(s, 0, 1);
     prof_end(h);
   } else if (s.precision == 0) {
     // size buckets on the cluster Jacobi (a few molecules) form G = C F C^T
@@ -936,9 +944,17 @@ void Batch::eigen_step(const ScfSettings& s) {
 
 void Batch::density_step(const ScfSettings& s) {
   if (householder(s)) {
-    launches_ += 1;
+    // P = 2 X^T X or 2 I - 2 X^T X from the density's eigenvector rows: FP64
+    // on the CUDA cores; in the FP32 phase of the mixed path from the FP32
+    // rows on the tensor cores (3xTF32, FP32 accumulation)
+    const bool mixed = s.precision == 1;
     int h = prof_begin(kKDensity, active_work_estimate(kKDensity));
-    launch_gemm(j_hh_.d, j_hh_.n, j_hh_.tiles, d_C, d_C, d_P, true, false, 0.0, d_state, 1, -1, stream_);
+    launches_ += 1;
+    launch_gemm(j_hh_.d, j_hh_.n, j_hh_.tiles, d_C, d_C, d_P, true, false, 0.0, d_state, 1, mixed ? 1 : -1, stream_);
+    if (mixed) {
+      launches_ += 1;
+      launch_tc_gemm(j_hh_.d, j_hh_.n, j_hh_.tc_tiles, d_Cf, d_Cf, d_P, true, false, d_state, 1, 0, d_tc_err, stream_);
+    }
     prof_end(h);
   } else if (s.precision == 0) {
     launches_ += 1;
@@ -1038,7 +1054,7 @@ void Batch::finish(const ScfSettings& s, const std::vector<int>& which) {
   const int max_atoms = list_max_atoms();
   // every eigenpair of the last diagonalised Fock matrix: MO energies and
   // eigenvector rows, as Dsyevd leaves them after the last iteration
-  if (householder(s)) hh_vectors(1, 0);
+  if (householder(s)) hh_vectors(s, 1, 0);
   launches_ += 2;
   int h = prof_begin(kKEnergy, 0.0);
   launch_fock_kernel(d_atoms, d_pairs, d_mols, d_list, nl, max_atoms, d_blocks, d_H, d_P, d_F, d_Pold, d_state, 0,

@@ -38,7 +38,7 @@ struct ScfSettings {
 // kernel classes timed by the optional per-launch CUDA-event profiler
 enum KernelClass {
   kKPair = 0, kKHcore, kKFock, kKOrtho, kKTransform, kKJacobi, kKDensity, kKRefine, kKDiis, kKEnergy, kKDipole,
-  kKNumClasses
+  kKTridiag, kKEigvec, kKNumClasses
 };
 const char* kernel_class_name(int k);
 
@@ -159,7 +159,7 @@ class Batch {
   // eigenpairs of the current list from each molecule's last
   // tridiagonalisation: final_pass = 0 the density's set, 1 every index (MO
   // energies and vectors)
-  void hh_vectors(int final_pass, int require_active);
+  void hh_vectors(const ScfSettings& s, int final_pass, int require_active);
 
   Engine* eng_;
   cudaStream_t stream_;

@@ -1,5 +1,6 @@
 // Grouped batch: concurrent molecule groups on their own streams (engine.h).
 #include <algorithm>
+#include <cstdlib>
 #include <exception>
 #include <stdexcept>
 #include <thread>
@@ -9,7 +10,12 @@
 namespace nddo {
 
 int GroupedBatch::default_groups(int n_mol) {
-  // groups of at least 48 molecules, at most four streams
+  // groups of at least 48 molecules, at most four streams; MOLDS_GB300_GROUPS
+  // overrides the count (tuning sweeps)
+  if (const char* e = std::getenv("MOLDS_GB300_GROUPS")) {
+    const int g = std::atoi(e);
+    if (g >= 1) return std::min(g, std::max(1, n_mol));
+  }
   return std::max(1, std::min(4, n_mol / 48));
 }
 

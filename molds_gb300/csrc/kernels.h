@@ -37,6 +37,8 @@ void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, 
                     bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
 void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C, bool ta,
                     bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
+void launch_tc_gemm(const GemmJob* jobs, int njobs, int ntiles, const float* A, const float* B, double* C, bool ta,
+                    bool tb, const MolState* st, int require_active, int require_phase, int* err, cudaStream_t s);
 // block Jacobi (block_jacobi.cu) for bases above the one-CTA Jacobi's limit
 constexpr int kSmallJacobiMaxN = 194;
 // FP64 lists of at most this many molecules with a basis of at least
@@ -129,9 +131,12 @@ void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n
 // eigenpairs of the SCF pass (final_pass = 0: the smaller of the occupied and
 // virtual sets) or of every index (final_pass = 1) into eps and rows of C;
 // Z and S4[0..3] are N x N scratch arenas
+// mixed = 1: molecules in the FP32 phase get FP32 vectors in the rows of C32
+// (the FP64 phase and the final pass write C)
 void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
-                       int require_active, int final_pass, const double* W, const double* td, long long vstride,
-                       double* eps, double* Z, double* const* S4, double* C, cudaStream_t s);
+                       int require_active, int final_pass, int mixed, const double* W, const double* td,
+                       long long vstride, double* eps, double* Z, double* const* S4, double* C, float* C32,
+                       cudaStream_t s);
 
 // scf_kernels.cu
 void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C,

@@ -8,7 +8,11 @@
  * src/base/atoms/<El>atom.cpp (e.g. Catom.cpp:155-159 and 219-223), and the
  * dispersion energy always on with s6 = 1.40, d = 23
  * (src/base/InputParser.cpp:1657-1664, src/base/Parameters.cpp:60-61).  MolDS
- * defines them for H, C, N, O and S only.
+ * gives H, C, N, O and S their own AM1-D / PM3-D values; its F and Cl PM3-D
+ * sets are PM3's (Fatom.cpp:213-217, Clatom.cpp:231-235), and their AM1-D
+ * alpha is never assigned (Fatom.cpp:153, Clatom.cpp:171), so AM1-D is served
+ * for H, C, N, O, S and PM3-D for all seven elements.  Every element carries
+ * the C6 coefficient and radius of the vdW option.
  *
  * Dispersion energy (Grimme's damped C6 / R^6 form, src/cndo/Cndo2.cpp:464-513):
  *   E = -s6 sum_{A<B} C6_AB f(R_AB) / R_AB^6,  C6_AB = 2 C6_A C6_B / (C6_A + C6_B),
@@ -34,26 +38,35 @@ typedef struct {
   double r0;        /* [Angstrom] */
   double am1d[5];   /* U_s, U_p, beta_s, beta_p [eV], alpha [1/Angstrom] */
   double pm3d[5];
+  int has_am1d;     /* 0: no AM1-D set (F, Cl: the reference never assigns their AM1-D alpha) */
 } nddo_dispersion_element;
 
-enum { NDDO_NUM_DISPERSION_ELEMENTS = 5 };
+enum { NDDO_NUM_DISPERSION_ELEMENTS = 7 };
 
 static const nddo_dispersion_element nddo_dispersion_elements[NDDO_NUM_DISPERSION_ELEMENTS] = {
   { 1, 0.16, 1.110,
     { -11.223791, 0.0, -6.376265, 0.0, 3.577756 },
-    { -13.054076, 0.0, -5.628901, 0.0, 3.417532 } },
+    { -13.054076, 0.0, -5.628901, 0.0, 3.417532 }, 1 },
   { 6, 1.65, 1.610,
     { -52.183798, -39.368413, -15.682341, -7.804762, 2.625506 },
-    { -47.275431, -36.268916, -11.941466, -9.819760, 2.721152 } },
+    { -47.275431, -36.268916, -11.941466, -9.819760, 2.721152 }, 1 },
   { 7, 1.11, 1.550,
     { -71.997845, -57.401718, -20.092408, -18.470679, 2.968737 },
-    { -49.348460, -47.543768, -14.068411, -20.039292, 3.060404 } },
+    { -49.348460, -47.543768, -14.068411, -20.039292, 3.060404 }, 1 },
   { 8, 0.70, 1.490,
     { -97.610588, -78.589700, -29.502481, -29.495380, 4.633699 },
-    { -86.960302, -71.926845, -45.234302, -24.788037, 3.387806 } },
+    { -86.960302, -71.926845, -45.234302, -24.788037, 3.387806 }, 1 },
   { 16, 10.3, 1.870,
     { -57.235044, -48.307513, -3.311308, -7.256468, 2.309315 },
-    { -50.249536, -43.968965, -8.397415, -7.594232, 2.234331 } },
+    { -50.249536, -43.968965, -8.397415, -7.594232, 2.234331 }, 1 },
+  /* F and Cl: C6 and radius for the vdW option; their PM3-D set is PM3's
+   * (Fatom.cpp:213-217, Clatom.cpp:231-235) */
+  { 9, 0.57, 1.430,
+    { 0, 0, 0, 0, 0 },
+    { -110.435303, -105.685047, -48.405939, -27.744660, 3.358921 }, 0 },
+  { 17, 8.00, 1.820,
+    { 0, 0, 0, 0, 0 },
+    { -100.626747, -53.614396, -27.528560, -11.593922, 2.517296 }, 0 },
 };
 
 static inline const nddo_dispersion_element* nddo_dispersion_lookup(int atomic_number) {

@@ -48,10 +48,11 @@ static inline int nddo_fill_atom_params(int theory, int atomic_number, nddo_atom
   int e = nddo_element_index(atomic_number);
   if (e < 0 || theory < 0 || theory >= NDDO_NUM_THEORY_SLOTS) return -1;
   const nddo_dispersion_element* dsp = nddo_dispersion_lookup(atomic_number);
-  /* AM1-D / PM3-D: the AM1 / PM3 set with the overrides below (H, C, N, O, S) */
+  /* AM1-D / PM3-D: the AM1 / PM3 set with the overrides of nddo_dispersion.h */
   const nddo_pddg_element* pg = nddo_pddg_lookup(atomic_number);
   const int base = theory == NDDO_AM1D ? NDDO_AM1 : ((theory == NDDO_PM3D || theory == NDDO_PM3PDDG) ? NDDO_PM3 : theory);
   if ((theory == NDDO_AM1D || theory == NDDO_PM3D) && !dsp) return -1;
+  if (theory == NDDO_AM1D && !dsp->has_am1d) return -1;
   if (theory == NDDO_PM3PDDG && !pg) return -1;
   const nddo_element* el = &nddo_elements[e];
   const nddo_theory_params* t = &el->t[base];

@@ -15,7 +15,10 @@
 //
 // The first call on a device sets it up: it resolves the array's device
 // address with cudaGetSymbolAddress (with that device current) and uploads
-// the constant tables.  Make that first call before any stream capture.
+// the constant tables.  No call may be made on a stream that is being
+// captured: every call copies its inputs from host memory and ends with a
+// stream synchronisation, so a call on a capturing stream is rejected with
+// NDDO_ERR_ARGUMENT.
 // Every call shares the one array and leaves the last call's contents in it:
 // calls that overlap on the GPU (different streams, or different host threads)
 // race and must be serialised by the caller.
@@ -117,6 +120,10 @@ int setup_device(int device, cudaStream_t s, unsigned char** out, char* err, siz
   static const int zs[NDDO_NUM_ELEMENTS] = {1, 6, 7, 8, 9, 16, 17};
   for (int t = 0; t < NDDO_NUM_THEORY_SLOTS; ++t)
     for (int k = 0; k < NDDO_NUM_ELEMENTS; ++k) nddo_fill_atom_params(t, zs[k], &params[t * NDDO_NUM_ELEMENTS + k]);
+  // The element parameters live in the library's __constant__ table, which
+  // the engine (nddo_create / nddo_set_molecule) fills with the same default
+  // parameter sets; both paths assume those defaults, so this upload writes
+  // the values an engine on this device already holds.
   if (e == cudaSuccess) {
     upload_params(params, s);
     e = cudaGetLastError();
@@ -188,6 +195,17 @@ extern "C" int nddo_pair_integrals_noalloc(int device, int theory, int n_atoms, 
   cudaError_t ce = cudaSetDevice(device);
   if (ce != cudaSuccess) return set_error(err, err_len, NDDO_ERR_CUDA, cudaGetErrorString(ce));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    ce = cudaStreamIsCapturing(s, &cap);
+    if (ce != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+      cudaSetDevice(prev);
+      return set_error(err, err_len, ce != cudaSuccess ? NDDO_ERR_CUDA : NDDO_ERR_ARGUMENT,
+                       ce != cudaSuccess ? cudaGetErrorString(ce)
+                                         : "the stream is being captured: this call copies from host memory and "
+                                           "synchronises, so it cannot be recorded into a graph");
+    }
+  }
   unsigned char* base = nullptr;
   int rc = setup_device(device, s, &base, err, err_len);
   if (rc == 0) {
@@ -218,9 +236,10 @@ extern "C" int nddo_pair_integrals_noalloc(int device, int theory, int n_atoms, 
       const int grid = (int)((np + 255) / 256 < 1024 ? (np + 255) / 256 : 1024);
       noalloc_pairs_kernel<<<grid, 256, 0, s>>>(d_atoms, n_atoms, d_rowoff, d_pairs);
       ce = cudaGetLastError();
-      if (ce == cudaSuccess)
+      if (ce == cudaSuccess) {
         launch_pair_kernel(d_atoms, d_pairs, np, d_mol, d_eri, d_ovt, d_pair_blocks, d_core_hamiltonian, d_ecore, s);
-      ce = cudaGetLastError();
+        ce = cudaGetLastError();
+      }
     }
     if (ce == cudaSuccess) {
       launch_hcore_kernel(d_atoms, d_pairs, d_mol, d_list, 1, d_pair_blocks, d_ecore, d_core_hamiltonian, d_state, s);

@@ -208,7 +208,8 @@ tc_gemm_kernel(const GemmJob* __restrict__ jobs, int njobs, const TA* __restrict
           const float a = (float)job.alpha * S[i * kTcOutLd + j];
           *c = (TC)(job.beta != 0.0 ? a + (float)job.beta * (float)(*c) : a);
         } else {
-          const double a = job.alpha * (double)S[i * kTcOutLd + j];
+          double a = job.alpha * (double)S[i * kTcOutLd + j];
+          if (gi == gj) a += job.diag;
           *c = (TC)(job.beta != 0.0 ? a + job.beta * (double)(*c) : a);
         }
       }
@@ -253,6 +254,7 @@ TC_LAUNCH(double, double, float)
 TC_LAUNCH(float, double, double)
 TC_LAUNCH(double, float, float)
 TC_LAUNCH(double, double, double)
+TC_LAUNCH(float, float, double)
 #undef TC_LAUNCH
 
 }  // namespace nddo

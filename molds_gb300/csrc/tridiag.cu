@@ -41,7 +41,7 @@
 namespace nddo {
 
 constexpr int kHhThreads = 512;
-constexpr int kVecThreads = 128;
+constexpr int kVecThreads = 64;
 constexpr int kOrthThreads = 256;
 constexpr int kBackCols = 32, kBackWarps = 8;
 
@@ -212,28 +212,112 @@ hh_tridiag_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list,
 // the pair (P_i, P_{i+1}) is rescaled by a power of two when it leaves
 // [2^-256, 2^256].  Three FP64 operations per step; signs and exponents are
 // read with integer operations.
+__device__ __forceinline__ void sturm_step(double d, double e2, double x, double& p0, double& p1, int& s_prev,
+                                           int& cnt) {
+  const double p2 = fma(d - x, p1, -(e2 * p0));
+  const long long b = __double_as_longlong(p2);
+  const int s = ((b << 1) == 0) ? (s_prev ^ 1) : (int)((unsigned long long)b >> 63);
+  cnt += s != s_prev;
+  s_prev = s;
+  p0 = p1;
+  p1 = p2;
+}
+
+__device__ __forceinline__ void sturm_rescale(double& p0, double& p1) {
+  const int e1 = (int)((__double_as_longlong(p0) >> 52) & 0x7ff);
+  const int e0 = (int)((__double_as_longlong(p1) >> 52) & 0x7ff);
+  const int em = e0 > e1 ? e0 : e1;
+  if (em != 0 && (em > 1023 + 256 || em < 1023 - 256)) {
+    const double scale = __longlong_as_double((long long)(2046 - em) << 52);
+    p0 *= scale;
+    p1 *= scale;
+  }
+}
+
 __device__ __forceinline__ int sturm_count(const double* __restrict__ d, const double* __restrict__ e2, int n,
                                            double x) {
   double p0 = 1.0, p1 = d[0] - x;
-  long long b = __double_as_longlong(p1);
+  const long long b = __double_as_longlong(p1);
   int s_prev = ((b << 1) == 0) ? 1 : (int)((unsigned long long)b >> 63);
   int cnt = s_prev;
-  for (int i = 1; i < n; ++i) {
-    const double p2 = fma(d[i] - x, p1, -(e2[i - 1] * p0));
-    b = __double_as_longlong(p2);
-    const int s = ((b << 1) == 0) ? (s_prev ^ 1) : (int)((unsigned long long)b >> 63);
-    cnt += s != s_prev;
-    s_prev = s;
-    p0 = p1;
-    p1 = p2;
-    const int e1 = (int)((__double_as_longlong(p0) >> 52) & 0x7ff);
-    const int e0 = (int)((b >> 52) & 0x7ff);
-    const int em = e0 > e1 ? e0 : e1;
-    if (em != 0 && (em > 1023 + 256 || em < 1023 - 256)) {
-      const double scale = __longlong_as_double((long long)(2046 - em) << 52);
-      p0 *= scale;
-      p1 *= scale;
+  int i = 1;
+  // four steps between range checks: a step changes |P| by at most a factor
+  // of ~(|d| + 2|e| + |x|)^2, far inside the 2^+-256 margin
+  for (; i + 4 <= n; i += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) sturm_step(d[i + u], e2[i + u - 1], x, p0, p1, s_prev, cnt);
+    sturm_rescale(p0, p1);
+  }
+  for (; i < n; ++i) {
+    sturm_step(d[i], e2[i - 1], x, p0, p1, s_prev, cnt);
+    sturm_rescale(p0, p1);
+  }
+  return cnt;
+}
+
+// Half of a Sturm count for a lane pair (a twisted factorisation of T - x I
+// at index r = n/2 - 1).  side 0 runs the leading minors P_1 .. P_{r+1} and
+// counts the sign changes of P_0 .. P_r; side 1 runs the trailing minors
+// Q_i = det(T[i.., i..] - x I), Q_{n-1} .. Q_{r+1}, and counts the changes of
+// Q_n = 1 .. Q_{r+1}.  The pivot at the twist, gamma_r = det(T - x I) /
+// (P_r Q_{r+1}) with det = Q_{r+1} P_{r+1} - e_r^2 P_r Q_{r+2}, adds one
+// when negative (or zero).  Both lanes do n/2 steps, so the pair halves the
+// latency of a count at the same FP64 work.
+// Output: (v0, v1) = (P_r, P_{r+1}) on side 0, (Q_{r+2}, Q_{r+1}) on side 1;
+// sg = sign bit of P_r / Q_{r+1} as counted (a zero takes the sign opposite to
+// its predecessor).
+__device__ __forceinline__ int sturm_half(const double* __restrict__ d, const double* __restrict__ e2, int n, int r,
+                                          int side, double x, double* v0, double* v1, int* sg) {
+  double p0 = 1.0, p1;
+  int s_prev = 0, cnt = 0;
+  if (side == 0) {
+    p1 = d[0] - x;
+    long long b = __double_as_longlong(p1);
+    int s1 = ((b << 1) == 0) ? 1 : (int)((unsigned long long)b >> 63);
+    if (r >= 1) { cnt = s1; s_prev = s1; }
+    // P_2 .. P_r counted, then P_{r+1} uncounted
+    int i = 1;
+    for (; i + 4 <= r; i += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) sturm_step(d[i + u], e2[i + u - 1], x, p0, p1, s_prev, cnt);
+      sturm_rescale(p0, p1);
     }
+    for (; i < r; ++i) {
+      sturm_step(d[i], e2[i - 1], x, p0, p1, s_prev, cnt);
+      sturm_rescale(p0, p1);
+    }
+    // now p1 = P_r (r >= 1) with sign s_prev; for r == 0, p1 = P_1, p0 = P_0
+    if (r >= 1) {
+      int dummy = 0, sdummy = s_prev;
+      const double pr = p1;
+      sturm_step(d[r], e2[r - 1], x, p0, p1, sdummy, dummy);   // p1 = P_{r+1}, p0 = P_r
+      *v0 = pr;
+      *v1 = p1;
+      *sg = s_prev;
+    } else {
+      *v0 = 1.0;   // P_0
+      *v1 = p1;    // P_1
+      *sg = 0;
+    }
+  } else {
+    p1 = d[n - 1] - x;   // Q_{n-1}
+    long long b = __double_as_longlong(p1);
+    s_prev = ((b << 1) == 0) ? 1 : (int)((unsigned long long)b >> 63);
+    cnt = s_prev;
+    // Q_i = (d_i - x) Q_{i+1} - e_i^2 Q_{i+2}, i = n-2 down to r+1
+    int i = n - 2;
+    for (; i - 4 >= r; i -= 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) sturm_step(d[i - u], e2[i - u], x, p0, p1, s_prev, cnt);
+      sturm_rescale(p0, p1);
+    }
+    for (; i > r; --i) {
+      sturm_step(d[i], e2[i], x, p0, p1, s_prev, cnt);
+      sturm_rescale(p0, p1);
+    }
+    *v0 = p0;   // Q_{r+2}
+    *v1 = p1;   // Q_{r+1}
+    *sg = s_prev;
   }
   return cnt;
 }
@@ -275,7 +359,10 @@ __device__ __forceinline__ void tri_solve(int n, int k, double* __restrict__ x, 
   }
 }
 
-// grid: (list entry, chunk of kVecThreads indices); one thread per wanted index
+// grid: (list entry, chunk of kVecPerCta indices); a lane pair per wanted
+// index in the bisection, the pair's first lane for the inverse iteration
+constexpr int kVecPerCta = kVecThreads / 2;
+
 __global__ void __launch_bounds__(kVecThreads)
 tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
                    int require_active, int final_pass, const double* __restrict__ td, long long vstride,
@@ -289,7 +376,7 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   int lo, hi;
   hh_range(n, mol.nocc, final_pass, &lo, &hi);
   const int k = hi - lo;
-  const int c0 = blockIdx.y * kVecThreads;
+  const int c0 = blockIdx.y * kVecPerCta;
   if (c0 >= k) return;
   double* d = vsm;
   double* e = d + n;
@@ -327,20 +414,49 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   gu += pad;
   const double tiny = ulp * tnorm + 1e-300;   // replaces an exactly zero pivot
 
-  const int c = c0 + tid;
-  if (c >= k) return;
-  const int idx = lo + c;
-  // bisection: count(lo_) <= idx < count(hi_)
+  const int side = tid & 1;
+  const int c = c0 + (tid >> 1);
+  const bool valid = c < k;
+  const int idx = lo + (valid ? c : 0);
+  // bisection: count(a) <= idx < count(bnd).  The final pass resolves the
+  // eigenvalue to round-off (MO energies).  An SCF pass stops at 1e-10 ||T||
+  // and takes three inverse-iteration steps instead of two: an eigenvalue
+  // outside the vector's cluster is at least 1e-3 ||T|| away, so the error
+  // left in the vector is below (1e-7)^3.
+  const double abstol = final_pass ? ulp * tnorm : 1e-10 * tnorm;
   double a = gl, bnd = gu;
-  for (int it = 0; it < 80; ++it) {
-    const double mid = 0.5 * (a + bnd);
-    if (bnd - a <= 2.0 * ulp * fmax(fabs(a), fabs(bnd)) + ulp * tnorm) break;
-    if (sturm_count(d, e2, n, mid) > idx) bnd = mid; else a = mid;
+  if (n == 1) {
+    a = bnd = d[0];
+  } else {
+    const int r = n / 2 - 1;
+    const double e2r = e2[r];
+    for (int it = 0; it < 80; ++it) {
+      const bool done = !valid || bnd - a <= 2.0 * ulp * fmax(fabs(a), fabs(bnd)) + abstol;
+      if (__all_sync(0xffffffffu, done)) break;
+      const double mid = 0.5 * (a + bnd);
+      double v0, v1;
+      int sg;
+      const int cp = sturm_half(d, e2, n, r, side, mid, &v0, &v1, &sg);
+      const int co = __shfl_xor_sync(0xffffffffu, cp, 1);
+      const double w0 = __shfl_xor_sync(0xffffffffu, v0, 1);
+      const double w1 = __shfl_xor_sync(0xffffffffu, v1, 1);
+      const int so = __shfl_xor_sync(0xffffffffu, sg, 1);
+      const double Pr = side ? w0 : v0, Pr1 = side ? w1 : v1, Qr2 = side ? v0 : w0, Qr1 = side ? v1 : w1;
+      const int sP = side ? so : sg, sQ = side ? sg : so;
+      const double det = fma(Qr1, Pr1, -(e2r * Pr * Qr2));
+      const long long bd = __double_as_longlong(det);
+      const int gneg = ((bd << 1) == 0) ? 1 : ((int)((unsigned long long)bd >> 63) ^ sP ^ sQ);
+      const int total = cp + co + gneg;
+      if (!done) {
+        if (total > idx) bnd = mid; else a = mid;
+      }
+    }
   }
+  if (!valid || side) return;
   const double lam = 0.5 * (a + bnd);
   eps[mol.vec0 + idx] = lam;
 
-  // inverse iteration: factor T - lam I = P L U once, solve twice
+  // inverse iteration: factor T - lam I = P L U once, solve 2 or 3 times
   double* x = Z + mol.mat0 + c;
   double* fl = S0 + mol.mat0 + c;
   double* fu1i = S1 + mol.mat0 + c;
@@ -372,7 +488,8 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
     fu1i[(long long)(n - 1) * k] = 1.0 / cc;
   }
   for (int i = 0; i < n; ++i) x[(long long)i * k] = start_entry((unsigned)idx, (unsigned)i);
-  for (int step = 0; step < 2; ++step) {
+  const int nsteps = final_pass ? 2 : 3;
+  for (int step = 0; step < nsteps; ++step) {
     tri_solve(n, k, x, fl, fu1i, fu2, fpiv, e);
     double s = 0.0;
     for (int i = 0; i < n; ++i) { const double xi = x[(long long)i * k]; s = fma(xi, xi, s); }
@@ -463,16 +580,21 @@ tri_orth_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, c
 }
 
 // X = Q Z with Q = H_0 H_1 ... H_{n-3}: H_{n-3} is applied first.  CTA = 32
-// columns (lanes) x 8 row slices (warps, rows i = warp mod 8); the columns sit
-// in shared memory (pitch 33).  Output: row lo + c of C; in the final pass
-// each row's component sum is made >= 0.
+// columns (lanes) x 8 row slices (warps, row i belongs to warp i mod 8); the
+// columns sit in shared memory (pitch 33).  Output: row lo + c of C; in the
+// final pass each row's component sum is made >= 0.  T = double: the FP64
+// path; T = float: the FP32 phase of the mixed-precision path (reflectors and
+// vectors rounded to FP32 as they are staged, FP32 arithmetic, rows of the
+// FP32 shadow C32).  require_phase >= 0 serves only molecules in that phase.
+template <typename T>
 __global__ void __launch_bounds__(kBackCols * kBackWarps)
 hh_back_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
-               int require_active, int final_pass, const double* __restrict__ W, const double* __restrict__ td,
-               long long vstride, const double* __restrict__ Z, double* __restrict__ C) {
+               int require_active, int require_phase, int final_pass, const double* __restrict__ W,
+               const double* __restrict__ td, long long vstride, const double* __restrict__ Z, T* __restrict__ C) {
   extern __shared__ __align__(16) double bsm[];
   const int mi = list[blockIdx.x];
   if (require_active && st[mi].status != kActive) return;
+  if (require_phase >= 0 && st[mi].phase != require_phase) return;
   const DevMol mol = mols[mi];
   const int n = mol.nao;
   int lo, hi;
@@ -481,56 +603,68 @@ hh_back_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, co
   const int cb = blockIdx.y * kBackCols;
   if (cb >= k) return;
   constexpr int kP = kBackCols + 1;
-  double* zs = bsm;                       // n x kP
-  double* red = zs + (long long)n * kP;   // kBackWarps x kBackCols
-  double* dotv = red + kBackWarps * kBackCols;
-  double* taus = dotv + kBackCols;        // n
+  T* zs = reinterpret_cast<T*>(bsm);                                   // n x kP
+  T* red = zs + (long long)n * kP;                                     // kBackWarps x kBackCols
+  T* dotv = red + kBackWarps * kBackCols;                              // kBackCols
+  T* taus = dotv + kBackCols;                                          // n
+  T* urow = taus + n;                                                  // 2 n (FP32: staged reflectors)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const double* Zm = Z + mol.mat0;
   const double* Wm = W + mol.mat0;
   const double* tt = td + mol.vec0 + 2 * vstride;
   const int c = cb + lane;
-  for (int i = warp; i < n; i += kBackWarps) zs[i * kP + lane] = c < k ? Zm[(long long)i * k + c] : 0.0;
-  for (int i = tid; i < n; i += kBackCols * kBackWarps) taus[i] = tt[i];
+  for (int i = warp; i < n; i += kBackWarps) zs[i * kP + lane] = c < k ? (T)Zm[(long long)i * k + c] : (T)0;
+  for (int i = tid; i < n; i += kBackCols * kBackWarps) taus[i] = (T)tt[i];
   __syncthreads();
   for (int j = n - 3; j >= 0; --j) {
-    const double tau = taus[j];
-    if (tau == 0.0) continue;
-    const double* u = Wm + (long long)j * n;
+    const T tau = taus[j];
+    if (tau == (T)0) continue;
+    const double* ug = Wm + (long long)j * n;
+    const T* u;
+    if (sizeof(T) == 4) {
+      // two staging rows: a warp still updating with reflector j + 1 reads the other one
+      T* ur = urow + (j & 1) * n;
+      for (int i = j + 1 + tid; i < n; i += kBackCols * kBackWarps) ur[i] = (T)ug[i];
+      __syncthreads();
+      u = ur;
+    } else {
+      u = reinterpret_cast<const T*>(ug);
+    }
     // row slices are fixed (row i belongs to warp i mod 8), so a warp only
     // reads rows it updated itself at the previous reflector
     const int i0 = j + 1 + ((warp - (j + 1)) & (kBackWarps - 1));
-    double part = 0.0;
+    T part = 0;
     for (int i = i0; i < n; i += kBackWarps) part = fma(u[i], zs[i * kP + lane], part);
     red[warp * kBackCols + lane] = part;
     __syncthreads();
     if (warp == 0) {
-      double s = red[lane];
+      T sum = red[lane];
 #pragma unroll
-      for (int q = 1; q < kBackWarps; ++q) s += red[q * kBackCols + lane];
-      dotv[lane] = tau * s;
+      for (int q = 1; q < kBackWarps; ++q) sum += red[q * kBackCols + lane];
+      dotv[lane] = tau * sum;
     }
     __syncthreads();
-    const double dt = dotv[lane];
+    const T dt = dotv[lane];
     for (int i = i0; i < n; i += kBackWarps) {
-      double* z = zs + i * kP + lane;
+      T* z = zs + i * kP + lane;
       *z = fma(-dt, u[i], *z);
     }
   }
   __syncthreads();
   // rows of C: warp per row, lanes over the components
-  double* Cm = C + mol.mat0;
+  T* Cm = C + mol.mat0;
   for (int q = warp; q < kBackCols; q += kBackWarps) {
     const int cc = cb + q;
     if (cc >= k) break;
-    double sgn = 1.0;
+    T sgn = 1;
     if (final_pass) {
-      double s = 0.0;
+      T s = 0;
       for (int i = lane; i < n; i += 32) s += zs[i * kP + q];
-      s = warp_sum_d(s);
-      sgn = s < 0.0 ? -1.0 : 1.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      sgn = s < (T)0 ? (T)-1 : (T)1;
     }
-    double* row = Cm + (long long)(lo + cc) * n;
+    T* row = Cm + (long long)(lo + cc) * n;
     for (int i = lane; i < n; i += 32) row[i] = sgn * zs[i * kP + q];
   }
 }
@@ -547,13 +681,14 @@ static void hh_set_attributes() {
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncSetAttribute(hh_tridiag_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaFuncSetAttribute(hh_tridiag_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-    cudaFuncSetAttribute(hh_back_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncSetAttribute(hh_back_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncSetAttribute(hh_back_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaFuncSetAttribute(tri_vectors_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   });
 }
 
 size_t hh_back_smem_bytes(int n) {
-  return ((size_t)n * (kBackCols + 1) + kBackWarps * kBackCols + kBackCols + n) * sizeof(double);
+  return ((size_t)n * (kBackCols + 1) + kBackWarps * kBackCols + kBackCols + 3 * n) * sizeof(double);
 }
 
 int hh_back_max_n() {
@@ -579,18 +714,24 @@ void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n
 }
 
 void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
-                       int require_active, int final_pass, const double* W, const double* td, long long vstride,
-                       double* eps, double* Z, double* const* S4, double* C, cudaStream_t s) {
+                       int require_active, int final_pass, int mixed, const double* W, const double* td,
+                       long long vstride, double* eps, double* Z, double* const* S4, double* C, float* C32,
+                       cudaStream_t s) {
   if (nlist <= 0 || max_k <= 0) return;
   hh_set_attributes();
   const size_t vsh = (3 * (size_t)max_n + 2 * (kVecThreads / 32)) * sizeof(double);
-  dim3 gv(nlist, (max_k + kVecThreads - 1) / kVecThreads);
+  dim3 gv(nlist, (max_k + kVecPerCta - 1) / kVecPerCta);
   tri_vectors_kernel<<<gv, kVecThreads, vsh, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z,
                                                   S4[0], S4[1], S4[2], S4[3]);
   tri_orth_kernel<<<nlist, kOrthThreads, 0, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z);
   dim3 gb(nlist, (max_k + kBackCols - 1) / kBackCols);
-  hh_back_kernel<<<gb, kBackCols * kBackWarps, hh_back_smem_bytes(max_n), s>>>(mols, list, st, require_active,
-                                                                              final_pass, W, td, vstride, Z, C);
+  // mixed precision: FP32 back-transformation for molecules still in the FP32 phase
+  const int fp64_phase = (mixed && !final_pass) ? 1 : -1;
+  hh_back_kernel<double><<<gb, kBackCols * kBackWarps, hh_back_smem_bytes(max_n), s>>>(
+      mols, list, st, require_active, fp64_phase, final_pass, W, td, vstride, Z, C);
+  if (fp64_phase == 1)
+    hh_back_kernel<float><<<gb, kBackCols * kBackWarps, hh_back_smem_bytes(max_n), s>>>(
+        mols, list, st, require_active, 0, final_pass, W, td, vstride, Z, C32);
 }
 
 }  // namespace nddo

@@ -31,7 +31,66 @@
 #include <math.h>
 #include <string.h>
 #include <stdlib.h>
-#include "../molds_gb300/csrc/nddo_units.h"
+
+/* Per-atom parameters in atomic units.  The oracle does not include the
+ * product's parameter tables: oracle/parameters.py builds each record from
+ * tests/golden/reference_parameters.json (the values MolDS's
+ * SetAtomicParameters assigns, read from the reference sources as text) and
+ * installs it with oracle_set_atom; the unit constant and the STO-6G tables
+ * come from the same file. */
+typedef struct {
+  double core_charge;
+  double u[2], zeta[2], beta[2], alpha;
+  double gss, gsp, gpp, gp2, hsp, hpp;
+  double d[3], rho[3];
+  double gk[4], gl[4], gm[4];
+  double e_atom, dhf_atom, core_mass, vdw_c6, vdw_r0;
+  double pddg_pa[2], pddg_da[2];
+  int n_ao, principal_n, atomic_number;
+} oracle_atom;
+
+enum { ORACLE_MNDO = 0, ORACLE_PM3PDDG = 5, ORACLE_SLOTS = 6, ORACLE_MAXZ = 18, ORACLE_REC = 44 };
+static oracle_atom g_tab[ORACLE_SLOTS][ORACLE_MAXZ];
+static int g_have[ORACLE_SLOTS][ORACLE_MAXZ];
+static double g_ang2au = 0.0;                       /* Parameters::angstrom2AU */
+static double g_sto_exp[3][2][6], g_sto_coef[3][2][6];
+
+/* rec: the ORACLE_REC doubles of oracle/parameters.py RECORD */
+int oracle_set_atom(int theory, int Z, const double* rec) {
+  if (theory < 0 || theory >= ORACLE_SLOTS || Z < 1 || Z >= ORACLE_MAXZ) return -1;
+  oracle_atom* a = &g_tab[theory][Z];
+  int k = 0;
+  a->core_charge = rec[k++];
+  a->u[0] = rec[k++]; a->u[1] = rec[k++];
+  a->zeta[0] = rec[k++]; a->zeta[1] = rec[k++];
+  a->beta[0] = rec[k++]; a->beta[1] = rec[k++];
+  a->alpha = rec[k++];
+  a->gss = rec[k++]; a->gsp = rec[k++]; a->gpp = rec[k++]; a->gp2 = rec[k++]; a->hsp = rec[k++]; a->hpp = rec[k++];
+  for (int i = 0; i < 3; ++i) a->d[i] = rec[k++];
+  for (int i = 0; i < 3; ++i) a->rho[i] = rec[k++];
+  for (int i = 0; i < 4; ++i) a->gk[i] = rec[k++];
+  for (int i = 0; i < 4; ++i) a->gl[i] = rec[k++];
+  for (int i = 0; i < 4; ++i) a->gm[i] = rec[k++];
+  a->e_atom = rec[k++]; a->dhf_atom = rec[k++]; a->core_mass = rec[k++];
+  a->vdw_c6 = rec[k++]; a->vdw_r0 = rec[k++];
+  a->pddg_pa[0] = rec[k++]; a->pddg_pa[1] = rec[k++]; a->pddg_da[0] = rec[k++]; a->pddg_da[1] = rec[k++];
+  a->n_ao = (int)rec[k++]; a->principal_n = (int)rec[k++]; a->atomic_number = (int)rec[k++];
+  g_have[theory][Z] = 1;
+  return k == ORACLE_REC ? 0 : -1;
+}
+
+/* ex, co: [shell K, L, M][s, p][6] */
+void oracle_set_constants(double angstrom2au, const double* ex, const double* co) {
+  g_ang2au = angstrom2au;
+  memcpy(g_sto_exp, ex, sizeof(g_sto_exp));
+  memcpy(g_sto_coef, co, sizeof(g_sto_coef));
+}
+
+static int oracle_fill(int theory, int Z, oracle_atom* out) {
+  if (theory < 0 || theory >= ORACLE_SLOTS || Z < 1 || Z >= ORACLE_MAXZ || !g_have[theory][Z]) return -1;
+  *out = g_tab[theory][Z];
+  return 0;
+}
 
 enum { ORB_S = 0, ORB_PY = 1, ORB_PZ = 2, ORB_PX = 3 };
 
@@ -247,7 +306,7 @@ static int decompose(int mu, int nu, int* out) {
 }
 
 static double local_eri(int mu, int nu, int la, int si, double R,
-                        const nddo_atom_params* A, const nddo_atom_params* B) {
+                        const oracle_atom* A, const oracle_atom* B) {
   int ma[2], mb[2];
   int na = decompose(mu, nu, ma), nb = decompose(la, si, mb);
   if (na == 1 && nb == 1 && ma[0] == QXY && mb[0] == QXY) {
@@ -271,8 +330,8 @@ static double local_eri(int mu, int nu, int la, int si, double R,
 static const int kind_of_local[4] = {0, 2, 1, 2};  /* s, py (pi), pz (sigma), px (pi) */
 
 /* space-frame overlap block S[mu][nu] (mu on A, nu on B) */
-static void pair_overlap(const nddo_atom_params* A, const double* ra,
-                         const nddo_atom_params* B, const double* rb, double S[4][4]) {
+static void pair_overlap(const oracle_atom* A, const double* ra,
+                         const oracle_atom* B, const double* rb, double S[4][4]) {
   double T[4][4], L[4][4];
   double x = rb[0] - ra[0], y = rb[1] - ra[1], z = rb[2] - ra[2];
   double R = sqrt(x * x + y * y + z * z);
@@ -296,8 +355,8 @@ static void pair_overlap(const nddo_atom_params* A, const double* ra,
 }
 
 /* space-frame (mu nu|la si) block, mu,nu on A and la,si on B; 256 doubles */
-static void pair_eri(const nddo_atom_params* A, const double* ra,
-                     const nddo_atom_params* B, const double* rb, double W[4][4][4][4]) {
+static void pair_eri(const oracle_atom* A, const double* ra,
+                     const oracle_atom* B, const double* rb, double W[4][4][4][4]) {
   double T[4][4], L[4][4][4][4], tmp[4][4][4][4];
   double x = rb[0] - ra[0], y = rb[1] - ra[1], z = rb[2] - ra[2];
   double R = sqrt(x * x + y * y + z * z);
@@ -320,34 +379,34 @@ static void pair_eri(const nddo_atom_params* A, const double* ra,
     W[a][b][c][d] = (a < nA && b < nA && c < nB && d < nB) ? s : 0.0; }
 }
 
-static int is_n_or_o(const nddo_atom_params* p) { return p->atomic_number == 7 || p->atomic_number == 8; }
+static int is_n_or_o(const oracle_atom* p) { return p->atomic_number == 7 || p->atomic_number == 8; }
 
 /* E_AB; sssS = (s_A s_A | s_B s_B) */
-static double pair_core_core(int theory, const nddo_atom_params* A, const nddo_atom_params* B, double R, double ssss) {
+static double pair_core_core(int theory, const oracle_atom* A, const oracle_atom* B, double R, double ssss) {
   double f;
   if (A->atomic_number == 1 && is_n_or_o(B))
-    f = 1.0 + (R / NDDO_ANG2AU) * exp(-B->alpha * R) + exp(-A->alpha * R);
+    f = 1.0 + (R / g_ang2au) * exp(-B->alpha * R) + exp(-A->alpha * R);
   else if (B->atomic_number == 1 && is_n_or_o(A))
-    f = 1.0 + (R / NDDO_ANG2AU) * exp(-A->alpha * R) + exp(-B->alpha * R);
+    f = 1.0 + (R / g_ang2au) * exp(-A->alpha * R) + exp(-B->alpha * R);
   else
     f = 1.0 + exp(-A->alpha * R) + exp(-B->alpha * R);
   double e = A->core_charge * B->core_charge * ssss * f;
-  if (theory != NDDO_MNDO) {
+  if (theory != ORACLE_MNDO) {
     double t = 0.0;
     for (int i = 0; i < 4; ++i) {
       t += A->gk[i] * exp(-A->gl[i] * pow(R - A->gm[i], 2.0));
       t += B->gk[i] * exp(-B->gl[i] * pow(R - B->gm[i], 2.0));
     }
-    e += A->core_charge * B->core_charge * t * NDDO_ANG2AU / R;
+    e += A->core_charge * B->core_charge * t * g_ang2au / R;
   }
-  if (theory == NDDO_PM3PDDG) {
+  if (theory == ORACLE_PM3PDDG) {
     /* Pm3Pddg::GetDiatomCoreRepulsionEnergy, src/pm3/Pm3Pddg.cpp:143-165, 239-245 */
     int na = (int)A->core_charge, nb = (int)B->core_charge;
     double temp = 0.0;
     for (int i = 0; i < 2; ++i)
       for (int j = 0; j < 2; ++j)
         temp += ((double)na * A->pddg_pa[i] + (double)nb * B->pddg_pa[j]) *
-                exp(-10.0 / (NDDO_ANG2AU * NDDO_ANG2AU) * pow(R - A->pddg_da[i] - B->pddg_da[j], 2.0));
+                exp(-10.0 / (g_ang2au * g_ang2au) * pow(R - A->pddg_da[i] - B->pddg_da[j], 2.0));
     e += temp / (na + nb);
   }
   return e;
@@ -357,10 +416,10 @@ static double pair_core_core(int theory, const nddo_atom_params* A, const nddo_a
 /* Exported API (ctypes)                                                    */
 /* ------------------------------------------------------------------------ */
 
-static int fill_params(int theory, int natoms, const int* Z, nddo_atom_params* P, int* first) {
+static int fill_params(int theory, int natoms, const int* Z, oracle_atom* P, int* first) {
   int n = 0;
   for (int a = 0; a < natoms; ++a) {
-    if (nddo_fill_atom_params(theory, Z[a], &P[a]) != 0) return -1;
+    if (oracle_fill(theory, Z[a], &P[a]) != 0) return -1;
     first[a] = n;
     n += P[a].n_ao;
   }
@@ -370,8 +429,8 @@ static int fill_params(int theory, int natoms, const int* Z, nddo_atom_params* P
 int oracle_num_aos(int theory, int natoms, const int* Z) {
   int n = 0;
   for (int a = 0; a < natoms; ++a) {
-    nddo_atom_params p;
-    if (nddo_fill_atom_params(theory, Z[a], &p) != 0) return -1;
+    oracle_atom p;
+    if (oracle_fill(theory, Z[a], &p) != 0) return -1;
     n += p.n_ao;
   }
   return n;
@@ -382,7 +441,7 @@ int oracle_num_aos(int theory, int natoms, const int* Z) {
  * core-core energy.  Returns N or a negative error. */
 int oracle_integrals(int theory, int natoms, const int* Z, const double* xyz,
                      double* S, double* eri, double* ecore) {
-  nddo_atom_params* P = (nddo_atom_params*)malloc(sizeof(nddo_atom_params) * (natoms > 0 ? natoms : 1));
+  oracle_atom* P = (oracle_atom*)malloc(sizeof(oracle_atom) * (natoms > 0 ? natoms : 1));
   int* first = (int*)malloc(sizeof(int) * (natoms > 0 ? natoms : 1));
   int N = fill_params(theory, natoms, Z, P, first);
   if (N < 0) { free(P); free(first); return -1; }
@@ -411,12 +470,12 @@ int oracle_integrals(int theory, int natoms, const int* Z, const double* xyz,
   return N;
 }
 
-static double coulomb1(const nddo_atom_params* p, int m, int n) {
+static double coulomb1(const oracle_atom* p, int m, int n) {
   if (m == 0 && n == 0) return p->gss;
   if (m == 0 || n == 0) return p->gsp;
   return (m == n) ? p->gpp : p->gp2;
 }
-static double exchange1(const nddo_atom_params* p, int m, int n) {
+static double exchange1(const oracle_atom* p, int m, int n) {
   if (m == n) return coulomb1(p, m, n);
   if (m == 0 || n == 0) return p->hsp;
   return p->hpp;
@@ -426,7 +485,7 @@ static double exchange1(const nddo_atom_params* p, int m, int n) {
  * Fock (U on the diagonal, 1/2(beta_mu + beta_nu) S_mu,nu between atoms). */
 int oracle_fock(int theory, int natoms, const int* Z, const double* S, const double* eri,
                 const double* Pd, int guess, double* F) {
-  nddo_atom_params* P = (nddo_atom_params*)malloc(sizeof(nddo_atom_params) * (natoms > 0 ? natoms : 1));
+  oracle_atom* P = (oracle_atom*)malloc(sizeof(oracle_atom) * (natoms > 0 ? natoms : 1));
   int* first = (int*)malloc(sizeof(int) * (natoms > 0 ? natoms : 1));
   int N = fill_params(theory, natoms, Z, P, first);
   if (N < 0) { free(P); free(first); return -1; }
@@ -492,8 +551,8 @@ int oracle_fock(int theory, int natoms, const int* Z, const double* S, const dou
  * E_atom and dHf_atom (MNDO).  out has 4 doubles per atom. */
 int oracle_atom_info(int theory, int natoms, const int* Z, double* out) {
   for (int a = 0; a < natoms; ++a) {
-    nddo_atom_params p;
-    if (nddo_fill_atom_params(theory, Z[a], &p) != 0) return -1;
+    oracle_atom p;
+    if (oracle_fill(theory, Z[a], &p) != 0) return -1;
     out[4 * a + 0] = p.core_charge;
     out[4 * a + 1] = p.n_ao;
     out[4 * a + 2] = p.e_atom;
@@ -565,7 +624,7 @@ static double gto_cartesian(int ia, double a, const double* ra, int ib, double b
 /* X[3][N][N]: every AO pair, same atom included, each element summed over the
  * 6 x 6 primitive pairs (Cndo2.cpp:1946-2057, 2068-2130).  Returns N. */
 int oracle_cartesian(int theory, int natoms, const int* Z, const double* xyz, double* X) {
-  nddo_atom_params* P = (nddo_atom_params*)malloc(sizeof(nddo_atom_params) * (natoms > 0 ? natoms : 1));
+  oracle_atom* P = (oracle_atom*)malloc(sizeof(oracle_atom) * (natoms > 0 ? natoms : 1));
   int* first = (int*)malloc(sizeof(int) * (natoms > 0 ? natoms : 1));
   int N = fill_params(theory, natoms, Z, P, first);
   if (N < 0) { free(P); free(first); return -1; }
@@ -583,9 +642,9 @@ int oracle_cartesian(int theory, int natoms, const int* Z, const double* xyz, do
           double acc[3] = {0.0, 0.0, 0.0};
           for (int i = 0; i < 6; ++i)
             for (int j = 0; j < 6; ++j) {
-              const double c = nddo_sto6g_coef[shA][la][i] * nddo_sto6g_coef[shB][lb][j];
-              const double a = (zA * zA) * nddo_sto6g_exp[shA][la][i];
-              const double b = (zB * zB) * nddo_sto6g_exp[shB][lb][j];
+              const double c = g_sto_coef[shA][la][i] * g_sto_coef[shB][lb][j];
+              const double a = (zA * zA) * g_sto_exp[shA][la][i];
+              const double b = (zB * zB) * g_sto_exp[shB][lb][j];
               const double sasb = gto_sasb(a, b, R);
               for (int k = 0; k < 3; ++k)
                 acc[k] += c * gto_cartesian(axis_of_orb[mu], a, ra, axis_of_orb[nu], b, rb, k, sasb);
@@ -602,8 +661,8 @@ int oracle_cartesian(int theory, int natoms, const int* Z, const double* xyz, do
  * (src/base/atoms/Atom.h:34). */
 int oracle_core_masses(int theory, int natoms, const int* Z, double* out) {
   for (int a = 0; a < natoms; ++a) {
-    nddo_atom_params p;
-    if (nddo_fill_atom_params(theory, Z[a], &p) != 0) return -1;
+    oracle_atom p;
+    if (oracle_fill(theory, Z[a], &p) != 0) return -1;
     out[a] = p.core_mass;
   }
   return 0;
@@ -613,8 +672,8 @@ int oracle_core_masses(int theory, int natoms, const int* Z, double* out) {
  * (src/base/atoms/<El>atom.cpp, e.g. Catom.cpp:60-63); 2 doubles per atom. */
 int oracle_vdw_params(int theory, int natoms, const int* Z, double* out) {
   for (int a = 0; a < natoms; ++a) {
-    nddo_atom_params p;
-    if (nddo_fill_atom_params(theory, Z[a], &p) != 0) return -1;
+    oracle_atom p;
+    if (oracle_fill(theory, Z[a], &p) != 0) return -1;
     out[2 * a] = p.vdw_c6;
     out[2 * a + 1] = p.vdw_r0;
   }

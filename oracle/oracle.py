@@ -37,23 +37,26 @@ from dataclasses import dataclass, field
 import numpy as np
 import scipy.linalg
 
+try:
+    from . import parameters as P
+except ImportError:          # loaded as a top-level module
+    import parameters as P
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 SOURCES = [os.path.join(HERE, "nddo_oracle.c")]
-HEADERS = [os.path.join(HERE, "..", "molds_gb300", "csrc", "nddo_units.h"),
-           os.path.join(HERE, "..", "molds_gb300", "csrc", "nddo_elements.h")]
 
 THEORIES = {"mndo": 0, "am1": 1, "pm3": 2, "am1-d": 3, "pm3-d": 4, "pm3/pddg": 5}
 SYMBOL_TO_Z = {"h": 1, "c": 6, "n": 7, "o": 8, "f": 9, "s": 16, "cl": 17}
-ANG2AU = 1.0 / 0.5291772          # src/base/Parameters.cpp:48
-KCAL2AU = 0.00159360175           # src/base/Parameters.cpp:47
+ANG2AU = P.constants()["angstrom2AU"]        # src/base/Parameters.cpp:48
+KCAL2AU = P.constants()["kcalMolin2AU"]      # src/base/Parameters.cpp:47
 
 
 def build(force: bool = False) -> str:
     """Compile the C restatement into oracle/_build/liboracle.so."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    newest = max(os.path.getmtime(p) for p in SOURCES + HEADERS)
+    newest = max(os.path.getmtime(p) for p in SOURCES)
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
         return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
@@ -86,6 +89,18 @@ def lib():
                                                    ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                                    ctypes.c_double]
             L.oracle_sto_overlap_local.restype = ctypes.c_double
+            L.oracle_set_atom.argtypes = [ctypes.c_int, ctypes.c_int, dp]
+            L.oracle_set_atom.restype = ctypes.c_int
+            L.oracle_set_constants.argtypes = [ctypes.c_double, dp, dp]
+            # every parameter set of the reference's element files (tests/golden/reference_parameters.json)
+            ex, co = P.sto6g_tables()
+            L.oracle_set_constants(ANG2AU, _dp(np.ascontiguousarray(ex, dtype=np.float64)),
+                                   _dp(np.ascontiguousarray(co, dtype=np.float64)))
+            for theory in range(6):
+                for z in P.Z_TO_SYMBOL:
+                    rec = P.record_array(theory, z)
+                    if rec is not None and L.oracle_set_atom(theory, z, _dp(np.asarray(rec, dtype=np.float64))) != 0:
+                        raise RuntimeError(f"oracle parameter record of Z={z} theory={theory} rejected")
             _lib = L
     return _lib
 

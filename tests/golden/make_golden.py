@@ -9,7 +9,7 @@ electronic and core dipole moments (x, y, z in a.u.), the empirical van der
 Waals energy where the run has one and, for MNDO, the heat of formation.  MolDS prints these with %e (7 significant digits,
 src/cndo/Cndo2.cpp:1087-1089, 1193-1198), so they pin results to ~5e-7 relative.
 
-Usage:  python tests/golden/make_golden.py [/path/to/molds/test]
+Usage:  python tests/golden/make_golden.py <path to the MolDS test directory>
 """
 import json
 import os
@@ -56,7 +56,9 @@ def parse_dat(text, natoms):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <MolDS test directory>")
+    src = sys.argv[1]
     fixtures = []
     for name in CASES + EXTRA:
         inp = open(os.path.join(src, name + ".in")).read()
