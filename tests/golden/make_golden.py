@@ -23,6 +23,9 @@ CASES += ["c2h6_am1d", "c2h6_pm3d", "c2h6_pm3_vdw", "c2h6_pm3pddg"]
 # O (with the H-O core-core rule) and for C=C.
 EXTRA = ["h2o_pm3_freq_num_proj_s1", "c2h4_pm3_freq_num_proj", "c2h6-nh3-cluster_pm3d_freq",
          "c2h6-h2o-cluster_pm3pddg_freq"]
+# water dimers: the first SCF of an Ehrenfest run (AM1-D, which keeps AM1's O
+# zeta, D / rho, G / H and Gaussians) and of a geometry optimisation (PM3-D)
+EXTRA += ["h2o-dimer_am1d_ehrenfest", "h2o-dimer_pm3d_opt_bfgs_space_fixed"]
 
 
 def parse_dat(text, natoms):
