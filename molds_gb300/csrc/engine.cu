@@ -34,9 +34,9 @@ static T* dalloc(size_t count, size_t* total) {
 // ---------------------------------------------------------------------------
 __global__ void init_state_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, int n,
                                   MolState* __restrict__ st, double* __restrict__ C, double* __restrict__ P,
-                                  int requires_guess, int reset_density, double* __restrict__ hist_dens,
-                                  double* __restrict__ hist_err, int diis_m, long long mat_total,
-                                  int* __restrict__ sweeps) {
+                                  double* __restrict__ eps, int requires_guess, int reset_density,
+                                  double* __restrict__ hist_dens, double* __restrict__ hist_err, int diis_m,
+                                  long long mat_total, int* __restrict__ sweeps) {
   const int m = list[blockIdx.x];
   const DevMol mol = mols[m];
   const long long n2 = (long long)mol.nao * mol.nao;
@@ -51,6 +51,10 @@ __global__ void init_state_kernel(const DevMol* __restrict__ mols, const int* __
   }
   // a run from the previous density (requires_guess = 0) also keeps the
   // previous eigenvectors as the eigensolver's warm-start basis
+  // a cold start also forgets the eigenvalues of the last solve, which the
+  // FP64 eigensolver would otherwise take as starting points
+  if (reset_density)
+    for (int i = threadIdx.x; i < mol.nao; i += blockDim.x) eps[mol.vec0 + i] = __longlong_as_double(0x7ff8000000000000LL);
   if (reset_density)
     for (long long i = threadIdx.x; i < n2; i += blockDim.x) {
       const long long r = i / mol.nao, c = i % mol.nao;
@@ -794,7 +798,7 @@ void Batch::begin(const ScfSettings& s, const std::vector<int>& which, bool requ
   for (int m : which) active_host_[m] = 1;
   launches_ += 1;
   init_state_kernel<<<(unsigned)which.size(), 256, 0, stream_>>>(d_mols, d_list, (int)which.size(), d_state, d_C,
-                                                                 d_P, requires_guess ? 1 : 0, requires_guess ? 1 : 0,
+                                                                 d_P, d_eps, requires_guess ? 1 : 0, requires_guess ? 1 : 0,
                                                                  d_hist_dens, d_hist_err, diis_m_, mat_total_, d_sweeps);
   cuda_check(cudaGetLastError(), "init_state");
 }

@@ -41,7 +41,7 @@
 namespace nddo {
 
 constexpr int kHhThreads = 512;
-constexpr int kVecThreads = 64;
+constexpr int kVecThreads = 32;   // one warp: 16 lane pairs, 16 eigenpairs per CTA
 constexpr int kOrthThreads = 256;
 constexpr int kBackCols = 32, kBackWarps = 8;
 
@@ -206,120 +206,147 @@ hh_tridiag_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list,
 // Tridiagonal eigenpairs.
 // ---------------------------------------------------------------------------
 
-// Number of eigenvalues of T below x: sign changes of the leading principal
-// minors P_0 = 1, P_1 = d_0 - x, P_{i+1} = (d_i - x) P_i - e_{i-1}^2 P_{i-1}
-// (a zero minor takes the sign opposite to its predecessor).  No divisions;
-// the pair (P_i, P_{i+1}) is rescaled by a power of two when it leaves
-// [2^-256, 2^256].  Three FP64 operations per step; signs and exponents are
-// read with integer operations.
-__device__ __forceinline__ void sturm_step(double d, double e2, double x, double& p0, double& p1, int& s_prev,
-                                           int& cnt) {
-  const double p2 = fma(d - x, p1, -(e2 * p0));
-  const long long b = __double_as_longlong(p2);
-  const int s = ((b << 1) == 0) ? (s_prev ^ 1) : (int)((unsigned long long)b >> 63);
-  cnt += s != s_prev;
-  s_prev = s;
-  p0 = p1;
-  p1 = p2;
-}
-
-__device__ __forceinline__ void sturm_rescale(double& p0, double& p1) {
-  const int e1 = (int)((__double_as_longlong(p0) >> 52) & 0x7ff);
-  const int e0 = (int)((__double_as_longlong(p1) >> 52) & 0x7ff);
-  const int em = e0 > e1 ? e0 : e1;
-  if (em != 0 && (em > 1023 + 256 || em < 1023 - 256)) {
-    const double scale = __longlong_as_double((long long)(2046 - em) << 52);
-    p0 *= scale;
-    p1 *= scale;
+// Sturm counts and the characteristic polynomial, by a lane pair.
+//
+// The count of eigenvalues of T below x is the number of sign changes of the
+// leading principal minors P_0 = 1, P_1 = d_0 - x,
+// P_{i+1} = (d_i - x) P_i - e_{i-1}^2 P_{i-1} (a zero minor takes the sign
+// opposite to its predecessor); no divisions, and the pair (P_i, P_{i+1}) is
+// rescaled by a power of two when it leaves [2^-256, 2^256].  A lane pair
+// splits it as a twisted factorisation of T - x I at r = n/2 - 1: side 0 runs
+// P_1 .. P_{r+1} and counts the changes of P_0 .. P_r; side 1 runs the
+// trailing minors Q_i = det(T[i.., i..] - x I), Q_{n-1} .. Q_{r+1}, and counts
+// the changes of Q_n = 1 .. Q_{r+1}; the pivot at the twist,
+// gamma_r = det(T - x I) / (P_r Q_{r+1}) with
+// det = Q_{r+1} P_{r+1} - e_r^2 P_r Q_{r+2}, adds one when negative (or zero).
+// Both lanes do n/2 steps: half the latency of a count at the same FP64 work.
+// With kDeriv the first and second x-derivatives run alongside (same
+// recurrence: P'_{i+1} = (d_i - x) P'_i - P_i - e^2 P'_{i-1},
+// P''_{i+1} = (d_i - x) P''_i - 2 P'_i - e^2 P''_{i-1}) and are rescaled with
+// the minors, so det, det' and det'' share one scale factor.
+template <bool kDeriv>
+struct MinorPair {
+  double p0, p1, q0, q1, r0, r1;   // value, first and second derivative of (P_{i-1}, P_i)
+  __device__ __forceinline__ void step(double d, double e2, double x, int& s_prev, int& cnt, bool count) {
+    const double t = d - x;
+    const double p2 = fma(t, p1, -(e2 * p0));
+    if (kDeriv) {
+      const double q2 = fma(t, q1, -fma(e2, q0, p1));
+      const double r2 = fma(t, r1, -fma(e2, r0, 2.0 * q1));
+      q0 = q1; q1 = q2;
+      r0 = r1; r1 = r2;
+    }
+    if (count) {
+      const long long b = __double_as_longlong(p2);
+      const int s = ((b << 1) == 0) ? (s_prev ^ 1) : (int)((unsigned long long)b >> 63);
+      cnt += s != s_prev;
+      s_prev = s;
+    }
+    p0 = p1;
+    p1 = p2;
   }
-}
-
-__device__ __forceinline__ int sturm_count(const double* __restrict__ d, const double* __restrict__ e2, int n,
-                                           double x) {
-  double p0 = 1.0, p1 = d[0] - x;
-  const long long b = __double_as_longlong(p1);
-  int s_prev = ((b << 1) == 0) ? 1 : (int)((unsigned long long)b >> 63);
-  int cnt = s_prev;
-  int i = 1;
-  // four steps between range checks: a step changes |P| by at most a factor
-  // of ~(|d| + 2|e| + |x|)^2, far inside the 2^+-256 margin
-  for (; i + 4 <= n; i += 4) {
-#pragma unroll
-    for (int u = 0; u < 4; ++u) sturm_step(d[i + u], e2[i + u - 1], x, p0, p1, s_prev, cnt);
-    sturm_rescale(p0, p1);
+  __device__ __forceinline__ void rescale() {
+    const int e1 = (int)((__double_as_longlong(p0) >> 52) & 0x7ff);
+    const int e0 = (int)((__double_as_longlong(p1) >> 52) & 0x7ff);
+    const int em = e0 > e1 ? e0 : e1;
+    if (em != 0 && (em > 1023 + 256 || em < 1023 - 256)) {
+      const double scale = __longlong_as_double((long long)(2046 - em) << 52);
+      p0 *= scale;
+      p1 *= scale;
+      if (kDeriv) { q0 *= scale; q1 *= scale; r0 *= scale; r1 *= scale; }
+    }
   }
-  for (; i < n; ++i) {
-    sturm_step(d[i], e2[i - 1], x, p0, p1, s_prev, cnt);
-    sturm_rescale(p0, p1);
-  }
-  return cnt;
-}
+};
 
-// Half of a Sturm count for a lane pair (a twisted factorisation of T - x I
-// at index r = n/2 - 1).  side 0 runs the leading minors P_1 .. P_{r+1} and
-// counts the sign changes of P_0 .. P_r; side 1 runs the trailing minors
-// Q_i = det(T[i.., i..] - x I), Q_{n-1} .. Q_{r+1}, and counts the changes of
-// Q_n = 1 .. Q_{r+1}.  The pivot at the twist, gamma_r = det(T - x I) /
-// (P_r Q_{r+1}) with det = Q_{r+1} P_{r+1} - e_r^2 P_r Q_{r+2}, adds one
-// when negative (or zero).  Both lanes do n/2 steps, so the pair halves the
-// latency of a count at the same FP64 work.
-// Output: (v0, v1) = (P_r, P_{r+1}) on side 0, (Q_{r+2}, Q_{r+1}) on side 1;
-// sg = sign bit of P_r / Q_{r+1} as counted (a zero takes the sign opposite to
-// its predecessor).
+// One lane's half.  v[0..1] = (P_r, P_{r+1}) on side 0, (Q_{r+2}, Q_{r+1}) on
+// side 1, their derivatives in v[2..3] and v[4..5]; sg = sign bit of P_r /
+// Q_{r+1} as counted.
+template <bool kDeriv>
 __device__ __forceinline__ int sturm_half(const double* __restrict__ d, const double* __restrict__ e2, int n, int r,
-                                          int side, double x, double* v0, double* v1, int* sg) {
-  double p0 = 1.0, p1;
+                                          int side, double x, double* v, int* sg) {
+  MinorPair<kDeriv> m;
+  m.p0 = 1.0; m.q0 = 0.0; m.q1 = -1.0; m.r0 = 0.0; m.r1 = 0.0;
   int s_prev = 0, cnt = 0;
   if (side == 0) {
-    p1 = d[0] - x;
-    long long b = __double_as_longlong(p1);
-    int s1 = ((b << 1) == 0) ? 1 : (int)((unsigned long long)b >> 63);
+    m.p1 = d[0] - x;
+    const long long b = __double_as_longlong(m.p1);
+    const int s1 = ((b << 1) == 0) ? 1 : (int)((unsigned long long)b >> 63);
     if (r >= 1) { cnt = s1; s_prev = s1; }
-    // P_2 .. P_r counted, then P_{r+1} uncounted
+    // P_2 .. P_r counted (four steps between range checks: a step changes |P|
+    // by a factor far inside the 2^+-256 margin), then P_{r+1} uncounted
     int i = 1;
     for (; i + 4 <= r; i += 4) {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) sturm_step(d[i + u], e2[i + u - 1], x, p0, p1, s_prev, cnt);
-      sturm_rescale(p0, p1);
+      for (int u = 0; u < 4; ++u) m.step(d[i + u], e2[i + u - 1], x, s_prev, cnt, true);
+      m.rescale();
     }
     for (; i < r; ++i) {
-      sturm_step(d[i], e2[i - 1], x, p0, p1, s_prev, cnt);
-      sturm_rescale(p0, p1);
+      m.step(d[i], e2[i - 1], x, s_prev, cnt, true);
+      m.rescale();
     }
-    // now p1 = P_r (r >= 1) with sign s_prev; for r == 0, p1 = P_1, p0 = P_0
     if (r >= 1) {
-      int dummy = 0, sdummy = s_prev;
-      const double pr = p1;
-      sturm_step(d[r], e2[r - 1], x, p0, p1, sdummy, dummy);   // p1 = P_{r+1}, p0 = P_r
-      *v0 = pr;
-      *v1 = p1;
-      *sg = s_prev;
+      const int sr = s_prev;
+      m.step(d[r], e2[r - 1], x, s_prev, cnt, false);   // (p0, p1) = (P_r, P_{r+1})
+      *sg = sr;
     } else {
-      *v0 = 1.0;   // P_0
-      *v1 = p1;    // P_1
-      *sg = 0;
+      *sg = 0;   // (P_0, P_1)
     }
   } else {
-    p1 = d[n - 1] - x;   // Q_{n-1}
-    long long b = __double_as_longlong(p1);
+    m.p1 = d[n - 1] - x;   // Q_{n-1}
+    const long long b = __double_as_longlong(m.p1);
     s_prev = ((b << 1) == 0) ? 1 : (int)((unsigned long long)b >> 63);
     cnt = s_prev;
     // Q_i = (d_i - x) Q_{i+1} - e_i^2 Q_{i+2}, i = n-2 down to r+1
     int i = n - 2;
     for (; i - 4 >= r; i -= 4) {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) sturm_step(d[i - u], e2[i - u], x, p0, p1, s_prev, cnt);
-      sturm_rescale(p0, p1);
+      for (int u = 0; u < 4; ++u) m.step(d[i - u], e2[i - u], x, s_prev, cnt, true);
+      m.rescale();
     }
     for (; i > r; --i) {
-      sturm_step(d[i], e2[i], x, p0, p1, s_prev, cnt);
-      sturm_rescale(p0, p1);
+      m.step(d[i], e2[i], x, s_prev, cnt, true);
+      m.rescale();
     }
-    *v0 = p0;   // Q_{r+2}
-    *v1 = p1;   // Q_{r+1}
     *sg = s_prev;
   }
+  v[0] = m.p0; v[1] = m.p1;
+  if (kDeriv) { v[2] = m.q0; v[3] = m.q1; v[4] = m.r0; v[5] = m.r1; }
   return cnt;
+}
+
+// One evaluation at x by a lane pair (both lanes return the same values): the
+// count of eigenvalues below x and, with kDeriv, det(T - x I) with its first
+// two derivatives, scaled by one common power of two.
+struct TriEval {
+  int count;
+  double f, f1, f2;
+};
+
+template <bool kDeriv>
+__device__ __forceinline__ TriEval pair_eval(const double* __restrict__ d, const double* __restrict__ e2, int n,
+                                             int r, int side, double e2r, double x) {
+  double v[6], w[6];
+  int sg;
+  const int cp = sturm_half<kDeriv>(d, e2, n, r, side, x, v, &sg);
+  const int co = __shfl_xor_sync(0xffffffffu, cp, 1);
+  const int so = __shfl_xor_sync(0xffffffffu, sg, 1);
+#pragma unroll
+  for (int k = 0; k < (kDeriv ? 6 : 2); ++k) w[k] = __shfl_xor_sync(0xffffffffu, v[k], 1);
+  const double* P = side ? w : v;   // (P_r, P_{r+1}) and derivatives
+  const double* Q = side ? v : w;   // (Q_{r+2}, Q_{r+1}) and derivatives
+  const int sP = side ? so : sg, sQ = side ? sg : so;
+  TriEval out;
+  out.f = fma(Q[1], P[1], -(e2r * P[0] * Q[0]));
+  const long long bd = __double_as_longlong(out.f);
+  const int gneg = ((bd << 1) == 0) ? 1 : ((int)((unsigned long long)bd >> 63) ^ sP ^ sQ);
+  out.count = cp + co + gneg;
+  out.f1 = out.f2 = 0.0;
+  if (kDeriv) {
+    out.f1 = fma(Q[3], P[1], Q[1] * P[3]) - e2r * fma(P[2], Q[0], P[0] * Q[2]);
+    out.f2 = fma(Q[5], P[1], fma(2.0 * Q[3], P[3], Q[1] * P[5])) -
+             e2r * fma(P[4], Q[0], fma(2.0 * P[2], Q[2], P[0] * Q[4]));
+  }
+  return out;
 }
 
 // uniform pseudo-random value in [-0.5, 0.5): the start vector of inverse iteration
@@ -332,42 +359,88 @@ __device__ __forceinline__ double start_entry(unsigned int idx, unsigned int i) 
   return one_two - 1.5;
 }
 
-// One solve (T - lam I) x = b with the stored factors (forward elimination
-// with the row interchanges, then back substitution); b is overwritten by x.
-// Layout of every per-vector array: element i of vector c at i * k + c.
-__device__ __forceinline__ void tri_solve(int n, int k, double* __restrict__ x, const double* __restrict__ fl,
-                                          const double* __restrict__ fu1i, const double* __restrict__ fu2,
-                                          const double* __restrict__ fpiv, const double* __restrict__ e) {
-  double cb = x[0];
+// One solve (T - lam I) y = b with the stored factors (forward elimination
+// with the row interchanges, then back substitution), in place in x (element
+// i at x[i * ld]).  b is the pseudo-random start vector (start) or scale * x;
+// returns sum y_i^2, so the normalisation costs no extra pass.
+template <typename PivT>
+__device__ __forceinline__ double tri_solve(int n, int ld, double* __restrict__ x, const double* __restrict__ fl,
+                                            const double* __restrict__ fu1i, const double* __restrict__ fu2,
+                                            const PivT* __restrict__ piv, const double* __restrict__ e, bool start,
+                                            double scale, unsigned idx) {
+  double cb = start ? start_entry(idx, 0) : scale * x[0];
   for (int i = 0; i + 1 < n; ++i) {
-    const long long o = (long long)i * k;
-    const double bn = x[o + k];
+    const long long o = (long long)i * ld;
+    const double bn = start ? start_entry(idx, (unsigned)(i + 1)) : scale * x[o + ld];
     const double l = fl[o];
-    if (fpiv[o] != 0.0) { x[o] = bn; cb = fma(-l, bn, cb); }
+    if (piv[o]) { x[o] = bn; cb = fma(-l, bn, cb); }
     else { x[o] = cb; cb = fma(-l, cb, bn); }
   }
-  x[(long long)(n - 1) * k] = cb;
-  double x2 = 0.0, x1 = cb * fu1i[(long long)(n - 1) * k];
-  x[(long long)(n - 1) * k] = x1;
+  const long long on = (long long)(n - 1) * ld;
+  double x2 = 0.0, x1 = cb * fu1i[on];
+  x[on] = x1;
+  double ss = x1 * x1;
   for (int i = n - 2; i >= 0; --i) {
-    const long long o = (long long)i * k;
-    const double u3 = fpiv[o] != 0.0 ? e[i + 1] : 0.0;
+    const long long o = (long long)i * ld;
+    const double u3 = piv[o] ? e[i + 1] : 0.0;
     const double xi = fma(-u3, x2, fma(-fu2[o], x1, x[o])) * fu1i[o];
     x[o] = xi;
+    ss = fma(xi, xi, ss);
     x2 = x1;
     x1 = xi;
   }
+  return ss;
+}
+
+// Inverse iteration for eigenvalue lam: T - lam I = P L U with partial
+// pivoting (as LAPACK dlagtf), then two solves from a pseudo-random start;
+// the normalised vector goes to out[i * out_ld].  The factors and the vector
+// live at stride ld in shared memory or in the global scratch arenas.
+template <typename PivT>
+__device__ __forceinline__ void inverse_iteration(int n, int ld, const double* __restrict__ d,
+                                                  const double* __restrict__ e, double lam, double tiny, unsigned idx,
+                                                  double* __restrict__ fl, double* __restrict__ fu1i,
+                                                  double* __restrict__ fu2, PivT* __restrict__ piv,
+                                                  double* __restrict__ x, double* __restrict__ out, long long out_ld) {
+  double cc = d[0] - lam, s1 = n > 1 ? e[0] : 0.0;
+  for (int i = 0; i + 1 < n; ++i) {
+    const long long o = (long long)i * ld;
+    const double ei = e[i];
+    const double a1 = d[i + 1] - lam;
+    const double e1 = i + 2 < n ? e[i + 1] : 0.0;
+    if (fabs(ei) > fabs(cc)) {
+      const double r = 1.0 / ei;
+      const double l = cc * r;
+      fl[o] = l; fu1i[o] = r; fu2[o] = a1; piv[o] = (PivT)1;
+      cc = fma(-l, a1, s1);
+      s1 = -l * e1;
+    } else {
+      if (cc == 0.0) cc = tiny;
+      const double r = 1.0 / cc;
+      const double l = ei * r;
+      fl[o] = l; fu1i[o] = r; fu2[o] = s1; piv[o] = (PivT)0;
+      cc = fma(-l, s1, a1);
+      s1 = e1;
+    }
+  }
+  if (cc == 0.0) cc = tiny;
+  fu1i[(long long)(n - 1) * ld] = 1.0 / cc;
+  const double s1s = tri_solve(n, ld, x, fl, fu1i, fu2, piv, e, true, 1.0, idx);
+  const double r1 = s1s > 0.0 ? rsqrt(s1s) : 0.0;
+  const double s2s = tri_solve(n, ld, x, fl, fu1i, fu2, piv, e, false, r1, idx);
+  const double r2 = s2s > 0.0 ? rsqrt(s2s) : 0.0;
+  for (int i = 0; i < n; ++i) out[(long long)i * out_ld] = x[(long long)i * ld] * r2;
 }
 
 // grid: (list entry, chunk of kVecPerCta indices); a lane pair per wanted
-// index in the bisection, the pair's first lane for the inverse iteration
+// index for its eigenvalue, the pair's first lane for its inverse iteration
 constexpr int kVecPerCta = kVecThreads / 2;
 
 __global__ void __launch_bounds__(kVecThreads)
 tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
                    int require_active, int final_pass, const double* __restrict__ td, long long vstride,
                    double* __restrict__ eps, double* __restrict__ Z, double* __restrict__ S0, double* __restrict__ S1,
-                   double* __restrict__ S2, double* __restrict__ S3) {
+                   double* __restrict__ S2, double* __restrict__ S3, int vec_smem) {
   extern __shared__ __align__(16) double vsm[];
   const int mi = list[blockIdx.x];
   if (require_active && st[mi].status != kActive) return;
@@ -418,83 +491,93 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   const int c = c0 + (tid >> 1);
   const bool valid = c < k;
   const int idx = lo + (valid ? c : 0);
-  // bisection: count(a) <= idx < count(bnd).  The final pass resolves the
-  // eigenvalue to round-off (MO energies).  An SCF pass stops at 1e-10 ||T||
-  // and takes three inverse-iteration steps instead of two: an eigenvalue
-  // outside the vector's cluster is at least 1e-3 ||T|| away, so the error
-  // left in the vector is below (1e-7)^3.
-  const double abstol = final_pass ? ulp * tnorm : 1e-10 * tnorm;
-  double a = gl, bnd = gu;
+  // Eigenvalue idx of T to round-off:
+  //  0. warm start: the eigenvalue of the same index from the previous pass of
+  //     this SCF (eps holds it; a cold start stores NaN there).  When the count
+  //     shows no other eigenvalue between it and eigenvalue idx (count = idx
+  //     or idx + 1), step 2 starts from it directly;
+  //  1. otherwise bisection on the count until [a, b] holds eigenvalue idx
+  //     alone (count(a) = idx, count(b) = idx + 1), or is below the tolerance
+  //     (a cluster: the midpoint is the eigenvalue);
+  //  2. Laguerre's iteration on p(x) = det(T - x I), of degree n with real
+  //     roots only: G = p'/p, H = G^2 - p''/p,
+  //     x <- x - n / (G +- sqrt((n - 1)(n H - G^2))), the sign chosen to move
+  //     towards eigenvalue idx (down when count(x) > idx).  For a real-rooted
+  //     polynomial that step never passes the nearest root on its side and
+  //     converges cubically; each point's exact count still narrows [a, b],
+  //     and a step that would leave [a, b] bisects instead.
+  const double tol = 2.0 * ulp * tnorm;
+  double a = gl, bnd = gu, lam = 0.0;
   if (n == 1) {
-    a = bnd = d[0];
+    lam = d[0];
   } else {
     const int r = n / 2 - 1;
     const double e2r = e2[r];
+    int ca = 0, cb = n;
+    {
+      const double x0 = valid ? eps[mol.vec0 + idx] : 0.0;
+      const bool warm = valid && x0 > gl && x0 < gu;   // false for NaN
+      if (__any_sync(0xffffffffu, warm)) {
+        const TriEval ev = pair_eval<false>(d, e2, n, r, side, e2r, warm ? x0 : 0.5 * (gl + gu));
+        if (warm) {
+          if (ev.count == idx + 1) { bnd = x0; cb = idx + 1; ca = idx; }
+          else if (ev.count == idx) { a = x0; ca = idx; cb = idx + 1; }
+        }
+      }
+    }
     for (int it = 0; it < 80; ++it) {
-      const bool done = !valid || bnd - a <= 2.0 * ulp * fmax(fabs(a), fabs(bnd)) + abstol;
+      const bool done = !valid || (ca == idx && cb == idx + 1) || bnd - a <= 2.0 * ulp * fmax(fabs(a), fabs(bnd)) + tol;
       if (__all_sync(0xffffffffu, done)) break;
       const double mid = 0.5 * (a + bnd);
-      double v0, v1;
-      int sg;
-      const int cp = sturm_half(d, e2, n, r, side, mid, &v0, &v1, &sg);
-      const int co = __shfl_xor_sync(0xffffffffu, cp, 1);
-      const double w0 = __shfl_xor_sync(0xffffffffu, v0, 1);
-      const double w1 = __shfl_xor_sync(0xffffffffu, v1, 1);
-      const int so = __shfl_xor_sync(0xffffffffu, sg, 1);
-      const double Pr = side ? w0 : v0, Pr1 = side ? w1 : v1, Qr2 = side ? v0 : w0, Qr1 = side ? v1 : w1;
-      const int sP = side ? so : sg, sQ = side ? sg : so;
-      const double det = fma(Qr1, Pr1, -(e2r * Pr * Qr2));
-      const long long bd = __double_as_longlong(det);
-      const int gneg = ((bd << 1) == 0) ? 1 : ((int)((unsigned long long)bd >> 63) ^ sP ^ sQ);
-      const int total = cp + co + gneg;
+      const TriEval ev = pair_eval<false>(d, e2, n, r, side, e2r, mid);
       if (!done) {
-        if (total > idx) bnd = mid; else a = mid;
+        if (ev.count > idx) { bnd = mid; cb = ev.count; }
+        else { a = mid; ca = ev.count; }
+      }
+    }
+    // Laguerre starts from the warm-start end, or inside the isolating bracket
+    lam = (a > gl && bnd == gu) ? a : ((bnd < gu && a == gl) ? bnd : 0.5 * (a + bnd));
+    bool conv = !valid || !(ca == idx && cb == idx + 1);
+    const double dn = (double)n;
+    for (int it = 0; it < 24; ++it) {
+      if (__all_sync(0xffffffffu, conv)) break;
+      const TriEval ev = pair_eval<true>(d, e2, n, r, side, e2r, lam);
+      if (!conv) {
+        double xn;
+        if (ev.f == 0.0) {
+          xn = lam;
+          conv = true;
+        } else {
+          const bool above = ev.count > idx;   // lam lies above eigenvalue idx
+          if (above) bnd = lam; else a = lam;
+          const double G = ev.f1 / ev.f;
+          const double H = fma(G, G, -ev.f2 / ev.f);
+          const double disc = sqrt(fmax((dn - 1.0) * fma(dn, H, -G * G), 0.0));
+          const double den = above ? G + disc : G - disc;
+          xn = lam - dn / den;
+          if (!(xn >= a && xn <= bnd)) xn = 0.5 * (a + bnd);
+          if (fabs(xn - lam) <= 2.0 * ulp * fabs(lam) + 1e-300 || bnd - a <= tol) conv = true;
+        }
+        lam = xn;
       }
     }
   }
   if (!valid || side) return;
-  const double lam = 0.5 * (a + bnd);
   eps[mol.vec0 + idx] = lam;
-
-  // inverse iteration: factor T - lam I = P L U once, solve 2 or 3 times
-  double* x = Z + mol.mat0 + c;
-  double* fl = S0 + mol.mat0 + c;
-  double* fu1i = S1 + mol.mat0 + c;
-  double* fu2 = S2 + mol.mat0 + c;
-  double* fpiv = S3 + mol.mat0 + c;
-  {
-    double cc = d[0] - lam, s1 = n > 1 ? e[0] : 0.0;
-    for (int i = 0; i + 1 < n; ++i) {
-      const long long o = (long long)i * k;
-      const double ei = e[i];
-      const double a1 = d[i + 1] - lam;
-      const double e1 = i + 2 < n ? e[i + 1] : 0.0;
-      if (fabs(ei) > fabs(cc)) {
-        const double r = 1.0 / ei;
-        const double l = cc * r;
-        fl[o] = l; fu1i[o] = r; fu2[o] = a1; fpiv[o] = 1.0;
-        cc = fma(-l, a1, s1);
-        s1 = -l * e1;
-      } else {
-        if (cc == 0.0) cc = tiny;
-        const double r = 1.0 / cc;
-        const double l = ei * r;
-        fl[o] = l; fu1i[o] = r; fu2[o] = s1; fpiv[o] = 0.0;
-        cc = fma(-l, s1, a1);
-        s1 = e1;
-      }
-    }
-    if (cc == 0.0) cc = tiny;
-    fu1i[(long long)(n - 1) * k] = 1.0 / cc;
-  }
-  for (int i = 0; i < n; ++i) x[(long long)i * k] = start_entry((unsigned)idx, (unsigned)i);
-  const int nsteps = final_pass ? 2 : 3;
-  for (int step = 0; step < nsteps; ++step) {
-    tri_solve(n, k, x, fl, fu1i, fu2, fpiv, e);
-    double s = 0.0;
-    for (int i = 0; i < n; ++i) { const double xi = x[(long long)i * k]; s = fma(xi, xi, s); }
-    const double r = s > 0.0 ? rsqrt(s) : 0.0;
-    for (int i = 0; i < n; ++i) x[(long long)i * k] *= r;
+  const int cl = tid >> 1;   // this pair's slot in the CTA
+  if (vec_smem) {
+    // factors and vector in shared memory, element i of slot cl at i * kVecPerCta + cl
+    double* fl = red + 2 * (kVecThreads / 32);
+    double* fu1i = fl + (long long)n * kVecPerCta;
+    double* fu2 = fu1i + (long long)n * kVecPerCta;
+    double* xs = fu2 + (long long)n * kVecPerCta;
+    unsigned char* piv = reinterpret_cast<unsigned char*>(xs + (long long)n * kVecPerCta);
+    inverse_iteration(n, kVecPerCta, d, e, lam, tiny, (unsigned)idx, fl + cl, fu1i + cl, fu2 + cl, piv + cl, xs + cl,
+                      Z + mol.mat0 + c, k);
+  } else {
+    double* x = Z + mol.mat0 + c;
+    inverse_iteration(n, k, d, e, lam, tiny, (unsigned)idx, S0 + mol.mat0 + c, S1 + mol.mat0 + c, S2 + mol.mat0 + c,
+                      S3 + mol.mat0 + c, x, x, k);
   }
 }
 
@@ -658,10 +741,13 @@ hh_back_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, co
     if (cc >= k) break;
     T sgn = 1;
     if (final_pass) {
+      // component sum in index order, as Lapack::Dsyevd's phase fix does
+      // (src/wrappers/Lapack.cpp:139-150): a row whose sum is zero up to
+      // round-off gets the sign that order of summation gives
       T s = 0;
-      for (int i = lane; i < n; i += 32) s += zs[i * kP + q];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0)
+        for (int i = 0; i < n; ++i) s += zs[i * kP + q];
+      s = __shfl_sync(0xffffffffu, s, 0);
       sgn = s < (T)0 ? (T)-1 : (T)1;
     }
     T* row = Cm + (long long)(lo + cc) * n;
@@ -685,6 +771,25 @@ static void hh_set_attributes() {
     cudaFuncSetAttribute(hh_back_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaFuncSetAttribute(tri_vectors_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   });
+}
+
+// tri_vectors_kernel: d, e, e^2 and the reduction slots; with vec_smem also
+// the factors, vector and pivot flags of its kVecPerCta inverse iterations
+size_t tri_vectors_smem_bytes(int n, bool vec_smem) {
+  size_t b = (3 * (size_t)n + 2 * (kVecThreads / 32)) * sizeof(double);
+  if (vec_smem) b += (size_t)n * kVecPerCta * (4 * sizeof(double) + 1);
+  return b;
+}
+
+static int hh_optin_smem() {
+  static int optin = -1;
+  if (optin < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    optin = v;
+  }
+  return optin;
 }
 
 size_t hh_back_smem_bytes(int n) {
@@ -719,10 +824,11 @@ void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n
                        cudaStream_t s) {
   if (nlist <= 0 || max_k <= 0) return;
   hh_set_attributes();
-  const size_t vsh = (3 * (size_t)max_n + 2 * (kVecThreads / 32)) * sizeof(double);
+  const bool vec_smem = tri_vectors_smem_bytes(max_n, true) <= (size_t)hh_optin_smem();
+  const size_t vsh = tri_vectors_smem_bytes(max_n, vec_smem);
   dim3 gv(nlist, (max_k + kVecPerCta - 1) / kVecPerCta);
   tri_vectors_kernel<<<gv, kVecThreads, vsh, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z,
-                                                  S4[0], S4[1], S4[2], S4[3]);
+                                                  S4[0], S4[1], S4[2], S4[3], vec_smem ? 1 : 0);
   tri_orth_kernel<<<nlist, kOrthThreads, 0, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z);
   dim3 gb(nlist, (max_k + kBackCols - 1) / kBackCols);
   // mixed precision: FP32 back-transformation for molecules still in the FP32 phase

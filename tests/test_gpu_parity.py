@@ -155,9 +155,10 @@ def test_density_and_eigenvectors_fp64(ctx):
     assert np.max(np.abs(P - ref.P)) < 1e-8
     C = es.GetFockMatrix()
     eps = es.GetEnergiesMO()
-    # rows are orthonormal eigenvectors with component sum >= 0 (Lapack.cpp:141-150)
+    # rows are orthonormal eigenvectors with component sum >= 0 (Lapack.cpp:141-150;
+    # a row whose sum vanishes by symmetry may carry either sign at round-off level)
     assert np.max(np.abs(C @ C.T - np.eye(len(eps)))) < 1e-10
-    assert np.all(C.sum(axis=1) >= 0)
+    assert np.all(C.sum(axis=1) >= -1e-12)
 
 
 def test_octane_pm3_fp64(ctx):
@@ -175,7 +176,7 @@ def test_octane_pm3_fp64(ctx):
     assert np.max(np.abs(es.GetOrbitalElectronPopulation() - ref.P)) < 1e-8
     C = es.GetFockMatrix()
     assert np.max(np.abs(C @ C.T - np.eye(C.shape[0]))) < 1e-10
-    assert np.all(C.sum(axis=1) >= 0)
+    assert np.all(C.sum(axis=1) >= -1e-12)
     assert np.max(np.abs(es.GetDipoleMoments() - ref.dipole)) < DIP_TOL
 
 
