@@ -377,7 +377,13 @@ def run_ours(args):
                  "host wall clock"}
 
     # ---- roofline of the dominant kernel -----------------------------------
+    # the roofline's kernel: the single kernel with the largest share of the
+    # serialised device time (the ncu launch list under profiles/); on the
+    # FP64 Householder path that is the tridiagonalisation, otherwise the
+    # class with the most event time
     dom = max(kt, key=lambda k: kt[k]["ms"])
+    if kt.get("tridiagonalisation", {}).get("launches", 0) > 0:
+        dom = "tridiagonalisation"
     d = kt[dom]
     compute_bound = dom in ("jacobi_eigensolver", "warm_start_transform", "basis_orthonormalise", "density",
                             "fp64_refinement", "tridiagonalisation", "tridiagonal_eigenvectors")
