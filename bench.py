@@ -483,23 +483,37 @@ def _cpu_worker_pm3(args):
 
 
 def run_alkanes(args):
-    """All molecules in one device-resident batch; a step = integrals + SCF +
-    energies of all of them.  Mixed precision (FP32 eigen phase, FP64 after the
-    DIIS error drops below 1e-4); each molecule's |dE| and max|dP| against the
-    FP64 GPU path of the same batch."""
+    """All molecules of this rank in one device-resident batch; a step =
+    integrals + SCF + energies of all of them.  The uneven workload's precision
+    ramp is `--precision mixed` (FP32 back-transformation and density until the
+    DIIS error drops below 1e-4, FP64 eigensolve throughout); each molecule's
+    |dE| and max|dP| against the FP64 GPU path of the same batch.  Under
+    torchrun the molecules are split over the ranks by predicted cost
+    (molds_gb300/sharding.py)."""
     import numpy as np
     from molds_gb300.inputfile import Molecule
+    from molds_gb300 import sharding
+    from molds_gb300 import workloads as W
     os.environ.update(OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
+    rank, world, local, dist = dist_setup()
+    # every rank computes the same cost-based assignment (N^3 per molecule,
+    # longest first onto the least-loaded rank) and builds its own share
+    n_all = np.array([6 * W.alkane_carbons(3_000_000 + j) + 2 for j in range(args.alkanes)])
+    shards = sharding.shard_by_cost(sharding.predicted_cost(n_all), world)
+    mine = shards[rank]
     cores = host_cores()
     t0 = time.perf_counter()
     with mp.get_context("spawn").Pool(cores) as pool:      # before any CUDA call
-        gen = pool.map(_gen_alkane, range(args.alkanes), chunksize=16)
+        gen = pool.map(_gen_alkane, mine, chunksize=16)
     t_gen = time.perf_counter() - t0
     mols = [Molecule(Z, xyz) for Z, xyz in gen]
     import molds_gb300 as M
     from molds_gb300 import build
     build.build()
-    ctx = M.Context(0)
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+    ctx = M.Context(local)
     nao = np.array([int(sum(4 if z > 1 else 1 for z in m.Z)) for m in mols])
     steps = args.steps if args.steps != 10 else 2
     warm = args.warmup if args.warmup != 3 else 1
@@ -512,11 +526,13 @@ def run_alkanes(args):
     clocks.start()
     batch.profile(True)
     l0 = batch.launch_count()
+    barrier_sync(dist)
     batch.timer(0)
     for _ in range(steps):
         batch.run(params)
     batch.timer(1)
-    ms = batch.timer(2) / steps
+    ms = max_over_ranks(batch.timer(2) / steps, dist)
+    barrier_sync(dist)
     clk = clocks.stop()
     launches = (batch.launch_count() - l0) // steps
     kt = batch.kernel_times()
@@ -533,11 +549,17 @@ def run_alkanes(args):
     samp = rng.choice(both, size=min(256, both.size), replace=False) if both.size else []
     dp = np.array([float(np.max(np.abs(batch.density(i, nao[i]) - ref.density(i, nao[i])))) for i in samp])
     its = np.array([r["iterations"] for r in res])
-    value = conv.sum() / (ms * 1e-3)
+    n_conv = int(conv.sum())
+    if dist is not None:                     # converged solves of the whole job over the slowest rank's time
+        import torch
+        t = torch.tensor([n_conv], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t)
+        n_conv = int(t.item())
+    value = n_conv / (ms * 1e-3)
     # CPU baseline: the oracle on a bounded sample, all host cores
     cpu = None
     if not args.no_cpu_baseline:
-        sample = mols[:args.cpu_sample]
+        sample = mols[:min(args.cpu_sample, 32)]
         t1 = time.perf_counter()
         with mp.get_context("spawn").Pool(cores) as pool:
             out = pool.map(_cpu_worker_pm3, [(m.Z, m.xyz) for m in sample], chunksize=1)
@@ -549,7 +571,7 @@ def run_alkanes(args):
                "max_abs_dE_gpu_vs_cpu_Eh": max((abs(o[0] - res[i]["energy"]) for i, o in enumerate(out)
                                                 if o[2] and res[i]["status"] == M.STATUS_CONVERGED), default=None)}
     line = {"metric": "converged SCF solves/s, uneven batch of random alkanes with the precision ramp",
-            "value": value, "unit": "solves/s", "n_gpus": 1, "steps": steps, "warmup": warm, "ms_per_step": ms,
+            "value": value, "unit": "solves/s", "n_gpus": world, "steps": steps, "warmup": warm, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32+fp64" if args.precision == "mixed" else "f64",
             "data": f"synthetic: {args.alkanes} seeded random alkanes (seed 3e6 + j), generated in {t_gen:.1f} s",
@@ -563,12 +585,24 @@ def run_alkanes(args):
                             "iterations_median": float(np.median(its)), "iterations_max": int(its.max())},
             "accuracy": {"molecules_compared": int(both.size),
                          "max_abs_dE_vs_fp64_gpu_Eh": float(de.max()) if de.size else None,
-                         "p99_abs_dE_Eh": float(np.percentile(de, 99)) if de.size else None,
-                         "max_abs_dP_sample": float(dp.max()) if dp.size else None, "dP_sample": int(dp.size)},
+                         "abs_dE_percentiles_Eh": {str(q): float(np.percentile(de, q)) for q in (50, 90, 99, 100)}
+                         if de.size else None,
+                         "abs_dE_histogram_log10_Eh": {f"<=1e{e}": int(np.sum(de <= 10.0 ** e))
+                                                       for e in (-14, -12, -10, -8, -6)} if de.size else None,
+                         "max_abs_dP_sample": float(dp.max()) if dp.size else None,
+                         "abs_dP_percentiles": {str(q): float(np.percentile(dp, q)) for q in (50, 90, 99, 100)}
+                         if dp.size else None, "dP_sample": int(dp.size)},
+            "sharding": {"ranks": world, "molecules_this_rank": len(mine),
+                         "predicted_cost_imbalance": float(sharding.shard_loads(sharding.predicted_cost(n_all), shards).max()
+                                                           / max(1e-30, sharding.predicted_cost(n_all).sum() / world))},
             "cpu_baseline": cpu, "clocks": clk}
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     batch.close()
     ref.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
 
 
 # ---------------------------------------------------------------------------

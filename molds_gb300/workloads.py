@@ -162,6 +162,13 @@ def _generator():
     return _gen_lib
 
 
+def alkane_carbons(seed: int, n_range=(3, 60)) -> int:
+    """The carbon count random_alkane(seed) draws (uniform in n_range), without
+    building the molecule: the basis size N = 6 n + 2 is what a cost-based
+    sharder needs."""
+    return int(np.random.default_rng(seed).integers(n_range[0], n_range[1] + 1))
+
+
 def random_alkane(seed: int, n: int | None = None, n_range=(3, 60), min_dist=1.8, min_dist_h=1.0,
                   attempts=48, budget=200000, max_trees=400) -> Molecule:
     """A random saturated acyclic alkane CnH(2n+2).
@@ -181,9 +188,8 @@ def random_alkane(seed: int, n: int | None = None, n_range=(3, 60), min_dist=1.8
     `budget` draws is redrawn.  The growth runs in C (csrc/alkane_gen.c); n is
     drawn here from the seed."""
     import ctypes
-    rng = np.random.default_rng(seed)
     if n is None:
-        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        n = alkane_carbons(seed, n_range)
     total = 3 * n + 2
     Z = np.zeros(total, dtype=np.int32)
     xyz = np.zeros((total, 3))
