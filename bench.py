@@ -299,6 +299,23 @@ def run_ours(args):
     kt = batch.kernel_times()
     batch.profile(False)
     res, charges = batch.results()
+
+    # ---- the same steps as the library runs them without the profiler:
+    # each SCF iteration replayed from a captured CUDA graph --------------
+    g0, gl0 = batch.graph_launch_count(), batch.launch_count()
+    batch.run(params)                          # captures
+    barrier_sync(dist)
+    batch.timer(0)
+    for _ in range(args.steps):
+        batch.run(params)
+    batch.timer(1)
+    ms_graph = max_over_ranks(batch.timer(2), dist) / args.steps
+    barrier_sync(dist)
+    graphs = {"value": aggregate_throughput(world, args.nmol, ms_graph), "unit": "solves/s", "ms_per_step": ms_graph,
+              "graph_launches_per_step": (batch.graph_launch_count() - g0) / (args.steps + 1),
+              "kernels_per_step": (batch.launch_count() - gl0) / (args.steps + 1),
+              "note": "profiler off: every SCF iteration of a molecule group is one replay of a captured CUDA graph; "
+                      "the headline value above is measured with per-launch CUDA events (no graphs)"}
     ms_max = max_over_ranks(ms, dist)
     per_step_ms = ms_max / args.steps
     value = aggregate_throughput(world, args.nmol, per_step_ms)
@@ -453,6 +470,7 @@ def run_ours(args):
                 "cpu_baseline": cpu,
                 "clocks": clk,
                 "accuracy": acc,
+                "graphs": graphs,
                 "mixed": mixed}
         print(json.dumps(line), flush=True)
     batch.close()

@@ -177,8 +177,13 @@ const char* nddo_kernel_class_name(int k);
 /* CUDA events on the batch's stream: op 0 records the start, op 1 the stop,
  * op 2 synchronises and writes the elapsed milliseconds to *ms. */
 int nddo_batch_timer(nddo_batch* b, int op, double* ms);
-/* Number of CUDA kernels this batch has launched so far. */
+/* Number of CUDA kernels this batch has launched so far (kernels replayed
+ * from a captured graph included). */
 long long nddo_batch_launch_count(const nddo_batch* b);
+/* Number of CUDA-graph launches so far: each SCF iteration of a molecule group
+ * is captured once and replayed (MolDS has no counterpart; its SCF loop,
+ * Cndo2::DoSCF src/cndo/Cndo2.cpp:585-729, calls its routines directly). */
+long long nddo_batch_graph_launch_count(const nddo_batch* b);
 /* Jacobi sweeps summed over the molecules of the last run (eigensolver work). */
 long long nddo_batch_jacobi_sweeps(nddo_batch* b);
 

@@ -107,6 +107,7 @@ SIGNATURES = {
     "nddo_batch_timer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _DP]),
     "nddo_measure_fma_peak": (ctypes.c_int, [_CTX, ctypes.c_int, _DP]),
     "nddo_batch_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "nddo_batch_graph_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
     "nddo_batch_jacobi_sweeps": (ctypes.c_longlong, [ctypes.c_void_p]),
     "nddo_server_create": (ctypes.c_int, [_CTX, ctypes.POINTER(ScfParamsC), ctypes.c_size_t, ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_void_p)]),
@@ -412,6 +413,10 @@ class ResidentBatch:
 
     def launch_count(self) -> int:
         return int(self.ctx.lib.nddo_batch_launch_count(self.h))
+
+    def graph_launch_count(self) -> int:
+        """CUDA-graph replays (one per SCF iteration of a molecule group)."""
+        return int(self.ctx.lib.nddo_batch_graph_launch_count(self.h))
 
     def timer(self, op):
         ms = ctypes.c_double()

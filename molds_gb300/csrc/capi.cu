@@ -526,6 +526,7 @@ int nddo_batch_get_matrix(nddo_batch* h, int which, int m, double* out) {
 size_t nddo_batch_device_bytes(const nddo_batch* h) { return h ? h->b->device_bytes() : 0; }
 
 long long nddo_batch_launch_count(const nddo_batch* h) { return h ? h->b->launches() : -1; }
+long long nddo_batch_graph_launch_count(const nddo_batch* h) { return h ? h->b->graph_launches() : -1; }
 
 long long nddo_batch_jacobi_sweeps(nddo_batch* h) {
   if (!h) return -1;

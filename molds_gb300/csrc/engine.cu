@@ -8,6 +8,7 @@
 // Each step is one launch over all active molecules of the batch; a converged
 // molecule drops out of every later launch by its own state flag.
 #include "engine.h"
+#include "tuning.h"
 
 #include <algorithm>
 #include <cmath>
@@ -350,6 +351,10 @@ void Batch::allocate(const BatchCapacity& cap) {
     bytes_ += b;
   }
   cuda_check(cudaHostAlloc(&h_bj_pending, sizeof(int), cudaHostAllocDefault), "cudaHostAlloc");
+  cuda_check(cudaHostAlloc(&h_block_count_, 2 * sizeof(int), cudaHostAllocDefault), "cudaHostAlloc");
+  cuda_check(cudaHostAlloc(&h_block_active_, 2 * (size_t)nm, cudaHostAllocDefault), "cudaHostAlloc");
+  for (int k = 0; k < 2; ++k)
+    cuda_check(cudaEventCreateWithFlags(&block_ev_[k], cudaEventDisableTiming), "cudaEventCreate");
   cap_.ws_slots = ws;
   // persistent job tables and lists: one job per molecule per GEMM kind
   job_cap_ = nm;
@@ -430,6 +435,10 @@ void Batch::release(int slot) {
 }
 
 Batch::~Batch() {
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  for (cudaEvent_t e : block_ev_) if (e) cudaEventDestroy(e);
+  if (h_block_count_) cudaFreeHost(h_block_count_);
+  if (h_block_active_) cudaFreeHost(h_block_active_);
   free_jobs();
   for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   for (int* p : d_bucket_lists_) cudaFree(p);
@@ -537,6 +546,9 @@ void Batch::upload_list(const std::vector<int>& which) {
   // the pinned staging buffers may still feed copies of the previous list
   cuda_check(cudaStreamSynchronize(stream_), "list staging");
   cur_list_ = which;
+  // every launch shape of an iteration (grids, shared memory, job tables)
+  // follows from this rebuild: a captured graph is only valid for this layout
+  ++layout_version_;
   const int nm = cap_.slots;
   std::copy(which.begin(), which.end(), h_lists_);
   if (!which.empty())
@@ -1019,6 +1031,52 @@ void Batch::iterate(const ScfSettings& s, const std::vector<int>& which) {
   cuda_check(cudaGetLastError(), "diis_kernel");
 }
 
+bool same_launches(const ScfSettings& a, const ScfSettings& b) {
+  return a.max_iter == b.max_iter && a.rms_density == b.rms_density && a.damping_thresh == b.damping_thresh &&
+         a.damping_weight == b.damping_weight && a.diis_num_error_vect == b.diis_num_error_vect &&
+         a.diis_start_error == b.diis_start_error && a.diis_end_error == b.diis_end_error &&
+         a.precision == b.precision && a.switch_error == b.switch_error && a.max_sweeps == b.max_sweeps &&
+         a.keep_trace == b.keep_trace && a.tensor_cores == b.tensor_cores && a.eigensolver == b.eigensolver;
+}
+
+// The launches of one SCF iteration depend only on the molecule list and the
+// settings, and every kernel reads the per-molecule state from device memory,
+// so an iteration captured once can be replayed: one graph launch instead of
+// a dozen kernel launches.  Not while profiling (per-launch events) nor on the
+// block Jacobi, which reads a host flag between its sweeps.
+void Batch::iterate_graph(const ScfSettings& s, const std::vector<int>& which) {
+  upload_list(which);   // outside any capture: may synchronise when the list changes
+  if (!s.graphs || prof_on_ || !householder(s)) {
+    iterate(s, which);
+    return;
+  }
+  if (!graph_exec_ || !same_launches(graph_settings_, s) || graph_layout_ != layout_version_) {
+    if (graph_exec_) { cudaGraphExecDestroy(graph_exec_); graph_exec_ = nullptr; }
+    hh_prepare();
+    const long long before = launches_;
+    cudaGraph_t g = nullptr;
+    cuda_check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
+    try {
+      iterate(s, which);
+    } catch (...) {
+      cudaStreamEndCapture(stream_, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    cuda_check(cudaStreamEndCapture(stream_, &g), "end capture");
+    const cudaError_t e = cudaGraphInstantiate(&graph_exec_, g, 0);
+    cudaGraphDestroy(g);
+    cuda_check(e, "graph instantiate");
+    graph_kernels_ = launches_ - before;
+    launches_ = before;
+    graph_settings_ = s;
+    graph_layout_ = layout_version_;
+  }
+  cuda_check(cudaGraphLaunch(graph_exec_, stream_), "graph launch");
+  launches_ += graph_kernels_;
+  ++graph_launches_;
+}
+
 int Batch::count_active(const std::vector<int>& which) {
   upload_list(which);
   launches_ += 1;
@@ -1082,14 +1140,27 @@ void Batch::scf(const ScfSettings& s, bool requires_guess) {
   std::vector<int> all(h_mols.size());
   for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
   begin(s, all, requires_guess);
-  // One molecule: its iterations are short, so the host enqueues three before
-  // it waits for the convergence count.  Every kernel of an iteration skips
-  // molecules that are no longer active, so iterations enqueued past
-  // convergence change nothing.
-  const int every = all.size() == 1 ? 3 : 1;
-  for (int it = 0; it < s.max_iter; ++it) {
-    iterate(s, all);
-    if (((it + 1) % every == 0 || it + 1 == s.max_iter) && count_active(all) == 0) break;
+  // Iterations are enqueued in blocks (three for one molecule, whose
+  // iterations are short, two otherwise).  After each block the count of
+  // still-active molecules is copied to pinned memory behind an event, and
+  // the host reads a block's count only after it has enqueued the next block,
+  // so the device never waits for the host.  Every kernel of an iteration
+  // skips molecules that are no longer active, so the iterations enqueued past
+  // convergence change nothing (and cost only their empty launches).
+  const int block = all.size() == 1 ? 3 : tuned_check_block();
+  int it = 0, nblock = 0;
+  while (it < s.max_iter) {
+    for (int b = 0; b < block && it < s.max_iter; ++b, ++it) iterate_graph(s, all);
+    const int slot = nblock & 1;
+    count_active_async(all, h_block_count_ + slot, h_block_active_ + (size_t)slot * cap_.slots, block_ev_[slot]);
+    ++nblock;
+    if (nblock >= 2) {
+      const int prev = (nblock - 2) & 1;
+      cuda_check(cudaEventSynchronize(block_ev_[prev]), "block count");
+      if (prof_on_) std::copy(h_block_active_ + (size_t)prev * cap_.slots,
+                              h_block_active_ + (size_t)prev * cap_.slots + h_mols.size(), active_host_.begin());
+      if (h_block_count_[prev] == 0) break;
+    }
   }
   finish(s, all);
   int tc_err = 0;

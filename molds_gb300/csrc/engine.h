@@ -33,7 +33,13 @@ struct ScfSettings {
   int vdw = 0;                  // empirical dispersion energy (SCF block "vdW yes"; always on for AM1-D / PM3-D)
   double vdw_s6 = 1.40, vdw_d = 23.0;
   int eigensolver = 0;          // FP64 eigensolves: 0 auto (Householder), 1 Jacobi, 2 Householder
+  int graphs = 1;               // replay each SCF iteration from a captured CUDA graph (Householder path,
+                                // profiling off)
 };
+
+// settings that change the launches of an SCF iteration (a captured graph is
+// replayed only while they are unchanged)
+bool same_launches(const ScfSettings& a, const ScfSettings& b);
 
 // kernel classes timed by the optional per-launch CUDA-event profiler
 enum KernelClass {
@@ -118,6 +124,10 @@ class Batch {
   void finish(const ScfSettings& s, const std::vector<int>& which);
   // Number of still-active molecules among `which` (synchronises).
   int count_active(const std::vector<int>& which);
+  // One SCF iteration, replayed from a captured CUDA graph when the settings
+  // allow it (iterate() otherwise)
+  void iterate_graph(const ScfSettings& s, const std::vector<int>& which);
+  long long graph_launches() const { return graph_launches_; }
 
   // results (synchronise and copy out)
   void results(std::vector<MolResult>* out);
@@ -227,6 +237,18 @@ class Batch {
   void free_jobs();
   void make_jobset(JobSet* js, const std::vector<GemmJob>& jobs);
 
+  // captured SCF iteration
+  cudaGraphExec_t graph_exec_ = nullptr;
+  ScfSettings graph_settings_;
+  long long graph_layout_ = -1;           // layout_version_ the graph was captured for
+  long long layout_version_ = 0;          // bumped whenever the job tables and size buckets are rebuilt
+  long long graph_kernels_ = 0;           // kernels in one replay
+  long long graph_launches_ = 0;          // replays so far
+  // pipelined convergence checks: pinned counts and their events (two blocks in flight)
+  int* h_block_count_ = nullptr;
+  char* h_block_active_ = nullptr;
+  cudaEvent_t block_ev_[2] = {nullptr, nullptr};
+
   // profiler
   long long launches_ = 0;   // kernels launched by this batch so far
   bool prof_on_ = false;
@@ -268,6 +290,7 @@ class GroupedBatch {
   void set_coordinates(const double* xyz);
   size_t device_bytes() const;
   long long launches() const;
+  long long graph_launches() const;
   long long jacobi_sweeps() const;
   void set_profiling(bool on);
   void profile_reset();

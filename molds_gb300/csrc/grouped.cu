@@ -6,17 +6,18 @@
 #include <thread>
 
 #include "engine.h"
+#include "tuning.h"
 
 namespace nddo {
 
 int GroupedBatch::default_groups(int n_mol) {
-  // groups of at least 48 molecules, at most four streams; MOLDS_GB300_GROUPS
-  // overrides the count (tuning sweeps)
+  // concurrent molecule groups by batch size, from the autotuner's table;
+  // MOLDS_GB300_GROUPS overrides the count (sweeps)
   if (const char* e = std::getenv("MOLDS_GB300_GROUPS")) {
     const int g = std::atoi(e);
     if (g >= 1) return std::min(g, std::max(1, n_mol));
   }
-  return std::max(1, std::min(4, n_mol / 48));
+  return tuned_groups(n_mol);
 }
 
 GroupedBatch::GroupedBatch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m, int groups) {
@@ -123,6 +124,12 @@ size_t GroupedBatch::device_bytes() const {
 long long GroupedBatch::launches() const {
   long long t = 0;
   for (const auto& b : g_) t += b->launches();
+  return t;
+}
+
+long long GroupedBatch::graph_launches() const {
+  long long t = 0;
+  for (const auto& b : g_) t += b->graph_launches();
   return t;
 }
 

@@ -125,6 +125,7 @@ void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int m
 // vec0, vec0 + vstride, vec0 + 2 vstride; W (N x N arena) the reflectors.
 int hh_smem_max_n();     // largest basis whose packed matrix fits one CTA's shared memory
 int hh_back_max_n();     // largest basis the back-transformation kernel serves
+void hh_prepare();       // one-time kernel attributes and device limits (before any stream capture)
 void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                        int require_active, const double* F, double* W, double* td, long long vstride, double* Aws,
                        cudaStream_t s);

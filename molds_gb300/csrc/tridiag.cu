@@ -37,10 +37,11 @@
 #include <mutex>
 #include "nddo_batch.cuh"
 #include "kernels.h"
+#include "tuning.h"
 
 namespace nddo {
 
-constexpr int kHhThreads = 512;
+constexpr int kHhMaxThreads = 1024;   // the CTA size comes from the tuning table (256, 512 or 1024)
 constexpr int kVecThreads = 32;   // one warp: 16 lane pairs, 16 eigenpairs per CTA
 constexpr int kOrthThreads = 256;
 constexpr int kBackCols = 32, kBackWarps = 8;
@@ -90,7 +91,7 @@ int hh_smem_max_n() {
 // A22 <- A22 - u w^T - w u^T (lower triangle only).
 // ---------------------------------------------------------------------------
 template <bool kSmem>
-__global__ void __launch_bounds__(kHhThreads)
+__global__ void __launch_bounds__(kHhMaxThreads)
 hh_tridiag_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
                   int require_active, const double* __restrict__ F, double* __restrict__ W, double* __restrict__ td,
                   long long vstride, double* __restrict__ Aws) {
@@ -782,13 +783,13 @@ size_t tri_vectors_smem_bytes(int n, bool vec_smem) {
 }
 
 static int hh_optin_smem() {
-  static int optin = -1;
-  if (optin < 0) {
-    int dev = 0, v = 0;
+  static int optin = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    optin = v;
-  }
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  });
   return optin;
 }
 
@@ -797,12 +798,20 @@ size_t hh_back_smem_bytes(int n) {
 }
 
 int hh_back_max_n() {
-  int dev = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  int n = 8;
-  while (hh_back_smem_bytes(n + 1) <= (size_t)optin) ++n;
-  return n;
+  static int nmax = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int n = 8;
+    while (hh_back_smem_bytes(n + 1) <= (size_t)hh_optin_smem()) ++n;
+    nmax = n;
+  });
+  return nmax;
+}
+
+void hh_prepare() {
+  hh_set_attributes();
+  hh_smem_max_n();
+  hh_back_max_n();
 }
 
 void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
@@ -812,10 +821,11 @@ void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n
   hh_set_attributes();
   const bool smem = max_n <= hh_smem_max_n();
   const size_t sh = hh_tridiag_smem_bytes(max_n, smem);
+  const int threads = tuned_tridiag_threads(max_n);
   if (smem)
-    hh_tridiag_kernel<true><<<nlist, kHhThreads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws);
+    hh_tridiag_kernel<true><<<nlist, threads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws);
   else
-    hh_tridiag_kernel<false><<<nlist, kHhThreads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws);
+    hh_tridiag_kernel<false><<<nlist, threads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws);
 }
 
 void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,

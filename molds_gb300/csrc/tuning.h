@@ -1,0 +1,10 @@
+// Launch shapes chosen by the autotuner (tuning.cpp reads molds_gb300/tuning.txt).
+#pragma once
+
+namespace nddo {
+
+int tuned_groups(int n_mol);            // concurrent molecule groups of a fixed batch
+int tuned_tridiag_threads(int n);       // threads of a tridiagonalisation CTA for basis n
+int tuned_check_block();                // SCF iterations enqueued per convergence check
+
+}  // namespace nddo
