@@ -125,7 +125,9 @@ int nddo_get_dipole(nddo_ctx* ctx, double* out9);
  * MolDS's cartesianMatrix (Cndo2::CalcCartesianMatrixByGTOExpansion,
  * src/cndo/Cndo2.cpp:1946-2130).  Needs only a molecule. */
 int nddo_get_cartesian_matrix(nddo_ctx* ctx, double* out_3nn);
-/* Per-iteration log of Cndo2::SatisfyConvergenceCriterion (Cndo2.cpp:1505-1510). */
+/* Per-iteration log of Cndo2::SatisfyConvergenceCriterion (Cndo2.cpp:1505-1510).
+ * Returns the number of entries written (>= 0; compare it with max_entries,
+ * not with the status codes) or a negative NDDO_ERR_* code. */
 int nddo_get_trace(nddo_ctx* ctx, int max_entries, double* rms, double* diis_error, int* diis_on, int* damp_on);
 /* Packed space-frame (mu nu|la si) blocks of all atom pairs a < b, row-major
  * pair order; 10x10 (sp-sp), 10x1, 1x10 or 1x1 doubles per pair.  With

@@ -322,7 +322,10 @@ class ElectronicStructure:
         n = self.result.iterations
         rms, de = np.zeros(n), np.zeros(n)
         on, dm = np.zeros(n, dtype=np.int32), np.zeros(n, dtype=np.int32)
-        k = self.ctx.check(self.ctx.lib.nddo_get_trace(self.ctx.h, n, _dp(rms), _dp(de), _ip(on), _ip(dm)))
+        # the return value is the entry count (>= 0), or a negative error code
+        k = self.ctx.lib.nddo_get_trace(self.ctx.h, n, _dp(rms), _dp(de), _ip(on), _ip(dm))
+        if k < 0:
+            self.ctx.check(k)
         return [(i, float(rms[i]), float(de[i]), bool(on[i]), bool(dm[i])) for i in range(k)]
 
 

@@ -203,6 +203,16 @@ MolLayout layout_molecule(const MoleculeInput& in) {
 inline long long round32(long long x) { return (x + 31) / 32 * 32; }
 }  // namespace
 
+int molecule_nao(const MoleculeInput& in) {
+  int ao = 0;
+  for (int z : in.Z) {
+    const int e = nddo_element_index(z);
+    if (e >= 0) ao += nddo_elements[e].n_ao;
+  }
+  return ao;
+}
+
+
 size_t Batch::bytes_per_mat_element(int diis_m) {
   // H F P P_old C G64 T64 + six refinement buffers (FP64), G32 T32 + three tensor-core
   // shadows (FP32), DIIS history
@@ -310,6 +320,9 @@ void Batch::allocate(const BatchCapacity& cap) {
   d_T64 = dalloc<double>(mat, &bytes_);
   for (int i = 0; i < 6; ++i) d_S[i] = dalloc<double>(mat, &bytes_);
   d_td = dalloc<double>(3 * (size_t)vec, &bytes_);
+  d_hh_small_ = dalloc<int>(nm, &bytes_);
+  d_hh_large_ = dalloc<int>(nm, &bytes_);
+  d_gridbar_ = dalloc<unsigned>(4, &bytes_);
   d_state = dalloc<MolState>(nm, &bytes_);
   d_charges = dalloc<double>(cap.atoms, &bytes_);
   d_sweeps = dalloc<int>(nm, &bytes_);
@@ -361,7 +374,7 @@ void Batch::allocate(const BatchCapacity& cap) {
   JobSet* all[] = {&j_trans1_, &j_trans2_, &j_dens_, &j_w_, &j_kt_, &j_yt_, &j_m_, &j_d2_, &j_z_, &j_p_, &j_ns1_, &j_ns2_, &j_ov_, &j_hh_};
   for (JobSet* j : all) { j->d = dalloc<GemmJob>(job_cap_, &bytes_); j->cap = job_cap_; }
   cuda_check(cudaHostAlloc(&h_jobs_, sizeof(GemmJob) * (size_t)job_cap_ * 14, cudaHostAllocDefault), "cudaHostAlloc jobs");
-  cuda_check(cudaHostAlloc(&h_lists_, sizeof(int) * (size_t)nm * (kJacobiBuckets + 1), cudaHostAllocDefault),
+  cuda_check(cudaHostAlloc(&h_lists_, sizeof(int) * (size_t)nm * (kJacobiBuckets + 3), cudaHostAllocDefault),
              "cudaHostAlloc lists");
   for (int b = 0; b < kJacobiBuckets; ++b) d_bucket_lists_.push_back(dalloc<int>(nm, &bytes_));
   cuda_check(cudaStreamSynchronize(stream_), "allocate");
@@ -533,10 +546,22 @@ void Batch::build_jobs(const std::vector<int>& which) {
   make_jobset(&j_hh_, hh);
   list_max_n_ = 0;
   hh_max_k_ = 0;
+  hh_small_.clear();
+  hh_large_.clear();
+  hh_small_max_n_ = hh_small_max_k_ = 0;
+  const int per_molecule = hh_back_max_n();
   for (int m : which) {
     const DevMol& d = h_mols[m];
+    const int kd = std::min(d.nocc, d.nao - d.nocc);
     list_max_n_ = std::max(list_max_n_, d.nao);
-    hh_max_k_ = std::max(hh_max_k_, std::min(d.nocc, d.nao - d.nocc));
+    hh_max_k_ = std::max(hh_max_k_, kd);
+    if (d.nao <= per_molecule) {
+      hh_small_.push_back(m);
+      hh_small_max_n_ = std::max(hh_small_max_n_, d.nao);
+      hh_small_max_k_ = std::max(hh_small_max_k_, kd);
+    } else {
+      hh_large_.push_back(m);
+    }
   }
 }
 
@@ -554,20 +579,38 @@ void Batch::upload_list(const std::vector<int>& which) {
   if (!which.empty())
     cuda_check(cudaMemcpyAsync(d_list, h_lists_, which.size() * sizeof(int), cudaMemcpyHostToDevice, stream_), "upload list");
   build_jobs(which);
+  {
+    // the Householder path's two lists (staged behind the bucket lists)
+    int* stage = h_lists_ + (size_t)(kJacobiBuckets + 1) * nm;
+    std::copy(hh_small_.begin(), hh_small_.end(), stage);
+    std::copy(hh_large_.begin(), hh_large_.end(), stage + nm);
+    if (!hh_small_.empty())
+      cuda_check(cudaMemcpyAsync(d_hh_small_, stage, hh_small_.size() * sizeof(int), cudaMemcpyHostToDevice, stream_),
+                 "upload list");
+    if (!hh_large_.empty())
+      cuda_check(cudaMemcpyAsync(d_hh_large_, stage + nm, hh_large_.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                 stream_),
+                 "upload list");
+  }
   // Jacobi size buckets: smaller molecules get a smaller shared-memory
   // footprint; the first edge keeps bases below the cluster Jacobi's minimum
   // apart from the ones it serves, so a molecule's kernel follows its own size
   buckets_.clear();
   bucket_max_n_.clear();
+  bucket_hh_max_n_.clear();
   bucket_dev_.clear();
   const int edges[kJacobiBuckets] = {kClusterJacobiMinN - 1, 64, 96, 128, 160, 194, 256, 338, 1 << 30};
   int lo = 0, bi = 0;
   for (int hi : edges) {
     std::vector<int> b;
-    int mx = 0;
+    int mx = 0, mx_hh = 0;
     for (int m : which) {
       const int n = h_mols[m].nao;
-      if (n > lo && n <= hi) { b.push_back(m); mx = std::max(mx, n); }
+      if (n > lo && n <= hi) {
+        b.push_back(m);
+        mx = std::max(mx, n);
+        if (n <= hh_back_max_n()) mx_hh = std::max(mx_hh, n);
+      }
     }
     lo = hi;
     const int slot = bi++;
@@ -578,6 +621,7 @@ void Batch::upload_list(const std::vector<int>& which) {
                "upload bucket");
     buckets_.push_back(b);
     bucket_max_n_.push_back(mx);
+    bucket_hh_max_n_.push_back(mx_hh);
     bucket_dev_.push_back(d_bucket_lists_[slot]);
   }
 }
@@ -869,16 +913,23 @@ void Batch::run_jacobi(bool fp32, const ScfSettings& s, const double* Cin, const
 }
 
 bool Batch::householder(const ScfSettings& s) const {
-  return s.eigensolver != 1 && list_max_n_ <= hh_back_max_n();
+  return s.eigensolver != 1 && list_max_n_ <= hh_grid_max_n();
 }
 
 void Batch::hh_vectors(const ScfSettings& s, int final_pass, int require_active) {
-  const int nl = (int)cur_list_.size();
-  const int max_k = final_pass ? list_max_n_ : hh_max_k_;
   const int mixed = s.precision == 1 ? 1 : 0;
-  launches_ += (mixed && !final_pass) ? 4 : 3;
-  launch_hh_vectors(d_mols, d_list, nl, list_max_n_, max_k, d_state, require_active, final_pass, mixed, d_G64, d_td,
-                    vec_total_, d_eps, d_T64, d_S, d_C, d_Cf, stream_);
+  if (!hh_small_.empty()) {
+    const int max_k = final_pass ? hh_small_max_n_ : hh_small_max_k_;
+    launches_ += (mixed && !final_pass) ? 4 : 3;
+    launch_hh_vectors(d_mols, d_hh_small_, (int)hh_small_.size(), hh_small_max_n_, max_k, d_state, require_active,
+                      final_pass, mixed, d_G64, d_td, vec_total_, d_eps, d_T64, d_S, d_C, d_Cf, stream_);
+  }
+  for (size_t i = 0; i < hh_large_.size(); ++i) {
+    const DevMol& d = h_mols[hh_large_[i]];
+    launches_ += (mixed && !final_pass) ? 4 : 3;
+    launch_hh_grid_vectors(d_mols, d_hh_large_ + i, d.nao, d.nocc, d_state, require_active, final_pass, mixed, d_G64,
+                           d_td, vec_total_, d_eps, d_T64, d_S, d_S[5], d_gridbar_, d_C, d_Cf, stream_);
+  }
 }
 
 void Batch::eigen_step(const ScfSettings& s) {
@@ -887,9 +938,16 @@ void Batch::eigen_step(const ScfSettings& s) {
     // with its own shared-memory footprint), then the density's eigenpairs
     int h = prof_begin(kKTridiag, active_work_estimate(kKTridiag));
     for (size_t b = 0; b < buckets_.size(); ++b) {
+      if (bucket_hh_max_n_[b] == 0) continue;
       launches_ += 1;
-      launch_hh_tridiag(d_mols, bucket_dev_[b], (int)buckets_[b].size(), bucket_max_n_[b], d_state, 1, d_F, d_G64,
-                        d_td, vec_total_, d_S[4], stream_);
+      launch_hh_tridiag(d_mols, bucket_dev_[b], (int)buckets_[b].size(), bucket_hh_max_n_[b], d_state, 1, d_F, d_G64,
+                        d_td, vec_total_, d_S[4], hh_back_max_n(), stream_);
+    }
+    // bases above the per-molecule kernels: one molecule at a time on every SM
+    for (size_t i = 0; i < hh_large_.size(); ++i) {
+      launches_ += 1;
+      launch_hh_grid_tridiag(d_mols, d_hh_large_ + i, d_state, 1, d_F, d_G64, d_td, vec_total_, d_S[4], d_S[5],
+                             d_gridbar_, stream_);
     }
     prof_end(h);
     h = prof_begin(kKEigvec, active_work_estimate(kKEigvec));
@@ -1042,11 +1100,13 @@ bool same_launches(const ScfSettings& a, const ScfSettings& b) {
 // The launches of one SCF iteration depend only on the molecule list and the
 // settings, and every kernel reads the per-molecule state from device memory,
 // so an iteration captured once can be replayed: one graph launch instead of
-// a dozen kernel launches.  Not while profiling (per-launch events) nor on the
-// block Jacobi, which reads a host flag between its sweeps.
+// a dozen kernel launches.  Not while profiling (per-launch events), nor on the
+// block Jacobi, which reads a host flag between its sweeps, nor for lists with
+// a molecule on the whole-GPU eigensolver (its cooperative launches run long
+// enough that a launch costs nothing, and are not captured).
 void Batch::iterate_graph(const ScfSettings& s, const std::vector<int>& which) {
   upload_list(which);   // outside any capture: may synchronise when the list changes
-  if (!s.graphs || prof_on_ || !householder(s)) {
+  if (!s.graphs || prof_on_ || !householder(s) || !hh_large_.empty()) {
     iterate(s, which);
     return;
   }

@@ -205,6 +205,15 @@ class Batch {
   double* d_S[6] = {};
   double* d_td = nullptr;                // tridiagonal d, e, tau (3 x vec arena)
   int list_max_n_ = 0, hh_max_k_ = 0;    // largest basis and density-set size of the current list
+  // Householder path: molecules up to hh_back_max_n() on the per-molecule
+  // kernels (hh_small_, with their largest basis and density-set size), the
+  // larger ones one at a time on the whole-GPU kernels (hh_large_)
+  std::vector<int> hh_small_, hh_large_;
+  int* d_hh_small_ = nullptr;
+  int* d_hh_large_ = nullptr;
+  int hh_small_max_n_ = 0, hh_small_max_k_ = 0;
+  std::vector<int> bucket_hh_max_n_;     // per size bucket: largest basis on the per-molecule kernels
+  unsigned* d_gridbar_ = nullptr;        // grid-barrier words of the cooperative launches
   float *d_jA32 = nullptr, *d_jV32 = nullptr;
   void* d_bj_ws = nullptr;               // block-Jacobi workspace (bases above kSmallJacobiMaxN)
   int* h_bj_pending = nullptr;           // pinned: molecules still rotating after a block-Jacobi sweep
@@ -325,5 +334,8 @@ class Engine {
 
 // throws std::runtime_error with the CUDA error text
 void cuda_check(cudaError_t e, const char* what);
+
+// basis functions of a molecule (unknown elements count zero; layout rejects them)
+int molecule_nao(const MoleculeInput& in);
 
 }  // namespace nddo

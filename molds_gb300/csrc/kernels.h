@@ -126,9 +126,15 @@ void launch_jacobi_f64(const DevMol* mols, const int* mol_list, int nlist, int m
 int hh_smem_max_n();     // largest basis whose packed matrix fits one CTA's shared memory
 int hh_back_max_n();     // largest basis the back-transformation kernel serves
 void hh_prepare();       // one-time kernel attributes and device limits (before any stream capture)
+// molecules above max_n_served are skipped (the whole-GPU path serves them)
 void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                        int require_active, const double* F, double* W, double* td, long long vstride, double* Aws,
-                       cudaStream_t s);
+                       int max_n_served, cudaStream_t s);
+// eigenvalues (bisection + Laguerre) and inverse-iteration vectors of T into
+// eps and the columns of Z (N x k per molecule)
+void launch_tri_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
+                        int require_active, int final_pass, const double* td, long long vstride, double* eps,
+                        double* Z, double* const* S4, cudaStream_t s);
 // eigenpairs of the SCF pass (final_pass = 0: the smaller of the occupied and
 // virtual sets) or of every index (final_pass = 1) into eps and rows of C;
 // Z and S4[0..3] are N x N scratch arenas
@@ -138,6 +144,19 @@ void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n
                        int require_active, int final_pass, int mixed, const double* W, const double* td,
                        long long vstride, double* eps, double* Z, double* const* S4, double* C, float* C32,
                        cudaStream_t s);
+
+// tridiag_grid.cu: the same eigensolver for one large molecule on every SM
+// (cooperative launches; bar = 4 words of grid-barrier state, scratch = the
+// molecule's N x N arena of another scratch matrix).  A grid barrier that
+// waits longer than about two seconds marks the molecule failed.
+int hh_grid_max_n();     // largest basis the whole-GPU path serves
+void launch_hh_grid_tridiag(const DevMol* mols, const int* one, MolState* st, int require_active, const double* F,
+                            double* W, double* td, long long vstride, double* Aws, double* scratch, unsigned* bar,
+                            cudaStream_t s);
+void launch_hh_grid_vectors(const DevMol* mols, const int* one, int n, int nocc, MolState* st, int require_active,
+                            int final_pass, int mixed, const double* W, const double* td, long long vstride,
+                            double* eps, double* Z, double* const* S4, double* scratch, unsigned* bar, double* C,
+                            float* C32, cudaStream_t s);
 
 // scf_kernels.cu
 void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C,

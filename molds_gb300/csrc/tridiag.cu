@@ -38,6 +38,7 @@
 #include "nddo_batch.cuh"
 #include "kernels.h"
 #include "tuning.h"
+#include "tridiag.cuh"
 
 namespace nddo {
 
@@ -45,23 +46,6 @@ constexpr int kHhMaxThreads = 1024;   // the CTA size comes from the tuning tabl
 constexpr int kVecThreads = 32;   // one warp: 16 lane pairs, 16 eigenpairs per CTA
 constexpr int kOrthThreads = 256;
 constexpr int kBackCols = 32, kBackWarps = 8;
-
-__device__ __forceinline__ int tri_off(int i) { return (i * (i + 1)) >> 1; }
-
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Index range [lo, hi) of the eigenpairs a pass needs: the final pass all of
-// them; an SCF iteration only the smaller of the occupied (0..nocc) and
-// virtual (nocc..n) sets (the density is 2 X^T X or 2 I - 2 X^T X).
-__host__ __device__ inline void hh_range(int n, int nocc, int final_pass, int* lo, int* hi) {
-  if (final_pass) { *lo = 0; *hi = n; return; }
-  if (n - nocc <= nocc) { *lo = nocc; *hi = n; }
-  else { *lo = 0; *hi = nocc; }
-}
 
 size_t hh_tridiag_smem_bytes(int n, bool a_in_smem) {
   size_t d = 3 * (size_t)n + 8;
@@ -94,12 +78,13 @@ template <bool kSmem>
 __global__ void __launch_bounds__(kHhMaxThreads)
 hh_tridiag_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
                   int require_active, const double* __restrict__ F, double* __restrict__ W, double* __restrict__ td,
-                  long long vstride, double* __restrict__ Aws) {
+                  long long vstride, double* __restrict__ Aws, int max_n_served) {
   extern __shared__ __align__(16) double hsm[];
   const int mi = list[blockIdx.x];
   if (require_active && st[mi].status != kActive) return;
   const DevMol mol = mols[mi];
   const int n = mol.nao;
+  if (n > max_n_served) return;   // served by the whole-GPU kernel (tridiag_grid.cu)
   const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nth >> 5;
   double* A = kSmem ? hsm : Aws + mol.mat0;
   double* v = kSmem ? hsm + (long long)n * (n + 1) / 2 : hsm;
@@ -492,11 +477,12 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   const int c = c0 + (tid >> 1);
   const bool valid = c < k;
   const int idx = lo + (valid ? c : 0);
-  // Eigenvalue idx of T to round-off:
+  // Eigenvalue idx of T to round-off.  [a, b] always carries the true counts
+  // of its ends (count(a) <= idx < count(b)).
   //  0. warm start: the eigenvalue of the same index from the previous pass of
-  //     this SCF (eps holds it; a cold start stores NaN there).  When the count
-  //     shows no other eigenvalue between it and eigenvalue idx (count = idx
-  //     or idx + 1), step 2 starts from it directly;
+  //     this SCF (eps holds it; a cold start stores NaN there).  Its count
+  //     narrows [a, b]; when the count is idx or idx + 1 (no other eigenvalue
+  //     between it and eigenvalue idx), step 2 starts from it directly;
   //  1. otherwise bisection on the count until [a, b] holds eigenvalue idx
   //     alone (count(a) = idx, count(b) = idx + 1), or is below the tolerance
   //     (a cluster: the midpoint is the eigenvalue);
@@ -505,8 +491,14 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   //     x <- x - n / (G +- sqrt((n - 1)(n H - G^2))), the sign chosen to move
   //     towards eigenvalue idx (down when count(x) > idx).  For a real-rooted
   //     polynomial that step never passes the nearest root on its side and
-  //     converges cubically; each point's exact count still narrows [a, b],
-  //     and a step that would leave [a, b] bisects instead.
+  //     converges cubically, so it is taken only from a point whose count is
+  //     idx or idx + 1 (the nearest root on the chosen side is then eigenvalue
+  //     idx).  Each point's count narrows [a, b]; a point with another count,
+  //     a step that would leave [a, b], and a step that is not at most half
+  //     the previous one bisect [a, b] instead.  (A cluster of m close
+  //     eigenvalues beyond the wanted one, seen from a distance large against
+  //     its width, acts like an m-fold root: Laguerre then converges only
+  //     linearly, each step covering about m^-1/2 of the distance.)
   const double tol = 2.0 * ulp * tnorm;
   double a = gl, bnd = gu, lam = 0.0;
   if (n == 1) {
@@ -515,19 +507,22 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
     const int r = n / 2 - 1;
     const double e2r = e2[r];
     int ca = 0, cb = n;
+    bool adj = false;   // lam is a warm start with count idx or idx + 1
     {
       const double x0 = valid ? eps[mol.vec0 + idx] : 0.0;
       const bool warm = valid && x0 > gl && x0 < gu;   // false for NaN
       if (__any_sync(0xffffffffu, warm)) {
         const TriEval ev = pair_eval<false>(d, e2, n, r, side, e2r, warm ? x0 : 0.5 * (gl + gu));
         if (warm) {
-          if (ev.count == idx + 1) { bnd = x0; cb = idx + 1; ca = idx; }
-          else if (ev.count == idx) { a = x0; ca = idx; cb = idx + 1; }
+          if (ev.count > idx) { bnd = x0; cb = ev.count; }
+          else { a = x0; ca = ev.count; }
+          if (ev.count == idx || ev.count == idx + 1) { adj = true; lam = x0; }
         }
       }
     }
     for (int it = 0; it < 80; ++it) {
-      const bool done = !valid || (ca == idx && cb == idx + 1) || bnd - a <= 2.0 * ulp * fmax(fabs(a), fabs(bnd)) + tol;
+      const bool done = !valid || adj || (ca == idx && cb == idx + 1) ||
+                        bnd - a <= 2.0 * ulp * fmax(fabs(a), fabs(bnd)) + tol;
       if (__all_sync(0xffffffffu, done)) break;
       const double mid = 0.5 * (a + bnd);
       const TriEval ev = pair_eval<false>(d, e2, n, r, side, e2r, mid);
@@ -536,28 +531,38 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
         else { a = mid; ca = ev.count; }
       }
     }
-    // Laguerre starts from the warm-start end, or inside the isolating bracket
-    lam = (a > gl && bnd == gu) ? a : ((bnd < gu && a == gl) ? bnd : 0.5 * (a + bnd));
-    bool conv = !valid || !(ca == idx && cb == idx + 1);
+    const bool isolated = ca == idx && cb == idx + 1;
+    if (!adj) lam = 0.5 * (a + bnd);
+    bool conv = !valid || !(adj || isolated);
     const double dn = (double)n;
-    for (int it = 0; it < 24; ++it) {
+    double prev_step = 1e300;
+    for (int it = 0; it < 64; ++it) {
       if (__all_sync(0xffffffffu, conv)) break;
       const TriEval ev = pair_eval<true>(d, e2, n, r, side, e2r, lam);
       if (!conv) {
-        double xn;
+        double xn = lam;
         if (ev.f == 0.0) {
-          xn = lam;
           conv = true;
         } else {
           const bool above = ev.count > idx;   // lam lies above eigenvalue idx
-          if (above) bnd = lam; else a = lam;
-          const double G = ev.f1 / ev.f;
-          const double H = fma(G, G, -ev.f2 / ev.f);
-          const double disc = sqrt(fmax((dn - 1.0) * fma(dn, H, -G * G), 0.0));
-          const double den = above ? G + disc : G - disc;
-          xn = lam - dn / den;
-          if (!(xn >= a && xn <= bnd)) xn = 0.5 * (a + bnd);
-          if (fabs(xn - lam) <= 2.0 * ulp * fabs(lam) + 1e-300 || bnd - a <= tol) conv = true;
+          if (above) { bnd = lam; cb = ev.count; }
+          else { a = lam; ca = ev.count; }
+          bool take = false, done = false;
+          double step = 0.0, xl = 0.0;
+          if (ev.count == idx || ev.count == idx + 1) {
+            const double G = ev.f1 / ev.f;
+            const double H = fma(G, G, -ev.f2 / ev.f);
+            const double disc = sqrt(fmax((dn - 1.0) * fma(dn, H, -G * G), 0.0));
+            const double den = above ? G + disc : G - disc;
+            xl = lam - dn / den;
+            const bool inside = xl >= a && xl <= bnd;
+            step = fabs(xl - lam);
+            done = inside && step <= 2.0 * ulp * fabs(lam) + 1e-300;
+            take = inside && (done || step <= 0.5 * prev_step);
+          }
+          if (take) { xn = xl; prev_step = step; }
+          else { xn = 0.5 * (a + bnd); prev_step = 1e300; }
+          if (done || bnd - a <= tol) conv = true;
         }
         lam = xn;
       }
@@ -816,22 +821,23 @@ void hh_prepare() {
 
 void launch_hh_tridiag(const DevMol* mols, const int* list, int nlist, int max_n, const MolState* st,
                        int require_active, const double* F, double* W, double* td, long long vstride, double* Aws,
-                       cudaStream_t s) {
-  if (nlist <= 0) return;
+                       int max_n_served, cudaStream_t s) {
+  if (nlist <= 0 || max_n <= 0) return;
   hh_set_attributes();
   const bool smem = max_n <= hh_smem_max_n();
   const size_t sh = hh_tridiag_smem_bytes(max_n, smem);
   const int threads = tuned_tridiag_threads(max_n);
   if (smem)
-    hh_tridiag_kernel<true><<<nlist, threads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws);
+    hh_tridiag_kernel<true><<<nlist, threads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws,
+                                                       max_n_served);
   else
-    hh_tridiag_kernel<false><<<nlist, threads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws);
+    hh_tridiag_kernel<false><<<nlist, threads, sh, s>>>(mols, list, st, require_active, F, W, td, vstride, Aws,
+                                                        max_n_served);
 }
 
-void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
-                       int require_active, int final_pass, int mixed, const double* W, const double* td,
-                       long long vstride, double* eps, double* Z, double* const* S4, double* C, float* C32,
-                       cudaStream_t s) {
+void launch_tri_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
+                        int require_active, int final_pass, const double* td, long long vstride, double* eps,
+                        double* Z, double* const* S4, cudaStream_t s) {
   if (nlist <= 0 || max_k <= 0) return;
   hh_set_attributes();
   const bool vec_smem = tri_vectors_smem_bytes(max_n, true) <= (size_t)hh_optin_smem();
@@ -839,6 +845,14 @@ void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n
   dim3 gv(nlist, (max_k + kVecPerCta - 1) / kVecPerCta);
   tri_vectors_kernel<<<gv, kVecThreads, vsh, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z,
                                                   S4[0], S4[1], S4[2], S4[3], vec_smem ? 1 : 0);
+}
+
+void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
+                       int require_active, int final_pass, int mixed, const double* W, const double* td,
+                       long long vstride, double* eps, double* Z, double* const* S4, double* C, float* C32,
+                       cudaStream_t s) {
+  if (nlist <= 0 || max_k <= 0) return;
+  launch_tri_vectors(mols, list, nlist, max_n, max_k, st, require_active, final_pass, td, vstride, eps, Z, S4, s);
   tri_orth_kernel<<<nlist, kOrthThreads, 0, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z);
   dim3 gb(nlist, (max_k + kBackCols - 1) / kBackCols);
   // mixed precision: FP32 back-transformation for molecules still in the FP32 phase
