@@ -34,6 +34,7 @@
 //                       reverse order; X written as rows of C (sign-fixed in the
 //                       final pass)
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <mutex>
 #include "nddo_batch.cuh"
 #include "kernels.h"
@@ -354,26 +355,57 @@ __device__ __forceinline__ double tri_solve(int n, int ld, double* __restrict__ 
                                             const double* __restrict__ fu1i, const double* __restrict__ fu2,
                                             const PivT* __restrict__ piv, const double* __restrict__ e, bool start,
                                             double scale, unsigned idx) {
+  // Both sweeps load their inputs four elements ahead (the loads do not
+  // depend on the carried values; with the factors in global memory the
+  // latency would otherwise be paid once per element).
   double cb = start ? start_entry(idx, 0) : scale * x[0];
-  for (int i = 0; i + 1 < n; ++i) {
-    const long long o = (long long)i * ld;
-    const double bn = start ? start_entry(idx, (unsigned)(i + 1)) : scale * x[o + ld];
-    const double l = fl[o];
-    if (piv[o]) { x[o] = bn; cb = fma(-l, bn, cb); }
-    else { x[o] = cb; cb = fma(-l, cb, bn); }
+  for (int i0 = 0; i0 + 1 < n; i0 += 4) {
+    double bn[4], l[4];
+    bool pv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      const long long o = (long long)i * ld;
+      const bool in = i + 1 < n;
+      bn[u] = !in ? 0.0 : (start ? start_entry(idx, (unsigned)(i + 1)) : scale * x[o + ld]);
+      l[u] = in ? fl[o] : 0.0;
+      pv[u] = in && piv[o];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      if (i + 1 >= n) break;
+      const long long o = (long long)i * ld;
+      if (pv[u]) { x[o] = bn[u]; cb = fma(-l[u], bn[u], cb); }
+      else { x[o] = cb; cb = fma(-l[u], cb, bn[u]); }
+    }
   }
   const long long on = (long long)(n - 1) * ld;
   double x2 = 0.0, x1 = cb * fu1i[on];
   x[on] = x1;
   double ss = x1 * x1;
-  for (int i = n - 2; i >= 0; --i) {
-    const long long o = (long long)i * ld;
-    const double u3 = piv[o] ? e[i + 1] : 0.0;
-    const double xi = fma(-u3, x2, fma(-fu2[o], x1, x[o])) * fu1i[o];
-    x[o] = xi;
-    ss = fma(xi, xi, ss);
-    x2 = x1;
-    x1 = xi;
+  for (int i0 = n - 2; i0 >= 0; i0 -= 4) {
+    double xo[4], f2[4], f1[4], u3[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 - u;
+      const long long o = (long long)i * ld;
+      const bool in = i >= 0;
+      xo[u] = in ? x[o] : 0.0;
+      f2[u] = in ? fu2[o] : 0.0;
+      f1[u] = in ? fu1i[o] : 0.0;
+      u3[u] = (in && piv[o]) ? e[i + 1] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 - u;
+      if (i < 0) break;
+      const double xi = fma(-u3[u], x2, fma(-f2[u], x1, xo[u])) * f1[u];
+      x[(long long)i * ld] = xi;
+      ss = fma(xi, xi, ss);
+      x2 = x1;
+      x1 = xi;
+    }
   }
   return ss;
 }
@@ -418,7 +450,7 @@ __device__ __forceinline__ void inverse_iteration(int n, int ld, const double* _
   for (int i = 0; i < n; ++i) out[(long long)i * out_ld] = x[(long long)i * ld] * r2;
 }
 
-// grid: (list entry, chunk of kVecPerCta indices); a lane pair per wanted
+// grid: (list entry, chunk of `pairs` <= kVecPerCta indices); a lane pair per wanted
 // index for its eigenvalue, the pair's first lane for its inverse iteration
 constexpr int kVecPerCta = kVecThreads / 2;
 
@@ -426,7 +458,7 @@ __global__ void __launch_bounds__(kVecThreads)
 tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
                    int require_active, int final_pass, const double* __restrict__ td, long long vstride,
                    double* __restrict__ eps, double* __restrict__ Z, double* __restrict__ S0, double* __restrict__ S1,
-                   double* __restrict__ S2, double* __restrict__ S3, int vec_smem) {
+                   double* __restrict__ S2, double* __restrict__ S3, int vec_smem, int pairs) {
   extern __shared__ __align__(16) double vsm[];
   const int mi = list[blockIdx.x];
   if (require_active && st[mi].status != kActive) return;
@@ -435,7 +467,7 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   int lo, hi;
   hh_range(n, mol.nocc, final_pass, &lo, &hi);
   const int k = hi - lo;
-  const int c0 = blockIdx.y * kVecPerCta;
+  const int c0 = blockIdx.y * pairs;
   if (c0 >= k) return;
   double* d = vsm;
   double* e = d + n;
@@ -475,7 +507,7 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
 
   const int side = tid & 1;
   const int c = c0 + (tid >> 1);
-  const bool valid = c < k;
+  const bool valid = (tid >> 1) < pairs && c < k;
   const int idx = lo + (valid ? c : 0);
   // Eigenvalue idx of T to round-off.  [a, b] always carries the true counts
   // of its ends (count(a) <= idx < count(b)).
@@ -842,9 +874,10 @@ void launch_tri_vectors(const DevMol* mols, const int* list, int nlist, int max_
   hh_set_attributes();
   const bool vec_smem = tri_vectors_smem_bytes(max_n, true) <= (size_t)hh_optin_smem();
   const size_t vsh = tri_vectors_smem_bytes(max_n, vec_smem);
-  dim3 gv(nlist, (max_k + kVecPerCta - 1) / kVecPerCta);
+  const int pairs = std::max(1, std::min(kVecPerCta, tuned_vec_pairs(max_n)));
+  dim3 gv(nlist, (max_k + pairs - 1) / pairs);
   tri_vectors_kernel<<<gv, kVecThreads, vsh, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z,
-                                                  S4[0], S4[1], S4[2], S4[3], vec_smem ? 1 : 0);
+                                                  S4[0], S4[1], S4[2], S4[3], vec_smem ? 1 : 0, pairs);
 }
 
 void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,

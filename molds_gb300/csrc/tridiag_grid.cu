@@ -283,6 +283,46 @@ hh_tridiag_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ 
 // ---------------------------------------------------------------------------
 // Re-orthogonalisation inside clusters, over the grid.
 // ---------------------------------------------------------------------------
+
+// Partial products part[s][l - l_beg][j] = sum over the rows of split s of
+// Z[i][l] Z[i][b0 + j], for l in [l_beg, l_end) and j < nb: the work items
+// (32-wide tile of l, split of the rows) are spread over the CTAs; each CTA
+// stages 32 rows of both column sets in shared memory per step and every
+// thread accumulates two outputs (j = lane, l and l + 16).
+__device__ void tile_products(const double* __restrict__ Zm, int n, int k, int l_beg, int l_end, int b0, int nb,
+                              int S, double* __restrict__ part, double (*sa)[33], double (*sb)[33]) {
+  const int L = l_end - l_beg, nlt = (L + 31) >> 5, items = nlt * S, R = (n + S - 1) / S;
+  const int t = threadIdx.x, j = t & 31, l = t >> 5;
+  for (int it = blockIdx.x; it < items; it += gridDim.x) {
+    const int lt = it % nlt, sp = it / nlt;
+    const int l0 = l_beg + 32 * lt, nl = min(32, l_end - l0);
+    const int r0 = sp * R, r1 = min(n, r0 + R);
+    double acc0 = 0.0, acc1 = 0.0;
+    for (int rc = r0; rc < r1; rc += 32) {
+      __syncthreads();
+      for (int e = t; e < 2048; e += kGridThreads) {
+        const int half = e >> 10, rr = (e >> 5) & 31, cc = e & 31, i = rc + rr;
+        double v = 0.0;
+        if (i < r1) {
+          if (half == 0) { if (cc < nl) v = __ldcg(Zm + (long long)i * k + l0 + cc); }
+          else if (cc < nb) v = __ldcg(Zm + (long long)i * k + b0 + cc);
+        }
+        if (half == 0) sa[rr][cc] = v; else sb[rr][cc] = v;
+      }
+      __syncthreads();
+#pragma unroll 8
+      for (int rr = 0; rr < 32; ++rr) {
+        const double zb = sb[rr][j];
+        acc0 = fma(sa[rr][l], zb, acc0);
+        acc1 = fma(sa[rr][l + 16], zb, acc1);
+      }
+    }
+    double* P = part + ((long long)sp * (nlt * 32) + 32 * lt) * 32;
+    __stcg(P + l * 32 + j, acc0);
+    __stcg(P + (l + 16) * 32 + j, acc1);
+  }
+}
+
 __global__ void __launch_bounds__(kGridThreads, 1)
 tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one, MolState* __restrict__ st,
                      int require_active, int final_pass, const double* __restrict__ td, long long vstride,
@@ -291,7 +331,8 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
   extern __shared__ __align__(16) double osm[];
   __shared__ int flag;
   __shared__ double red[kGridWarps];
-  __shared__ double Ms[32][33], Li[32][33];
+  __shared__ double sa[32][33], sb[32][33];
+  __shared__ double rs[32];
   const int mi = one[0];
   if (require_active && st[mi].status != kActive) return;
   const DevMol mol = mols[mi];
@@ -301,13 +342,14 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
   const int k = hi - lo;
   if (k < 2) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int G = gridDim.x, cta = blockIdx.x, gw = cta * kGridWarps + warp, TW = G * kGridWarps;
+  const int G = gridDim.x, cta = blockIdx.x;
   double* gs = osm;                                            // kOrthChunk x 32 coefficients
   int* cs = reinterpret_cast<int*>(gs + kOrthChunk * 32);      // cluster [cs, ce) of each column
   int* ce = cs + k;
   double* Zm = Z + mol.mat0;
-  double* Gm = scratch + mol.mat0;                             // (k x 32) projection coefficients
-  double* Mg = Gm + (long long)k * 32;                         // 32 x 32 Gram matrix
+  double* Gf = scratch + mol.mat0;                             // (k x 32) projection coefficients
+  double* Mg = Gf + (long long)k * 32;                         // 32 x 32 Gram matrix
+  double* part = Mg + 1024;                                    // partial products of the row splits
   const double* tdd = td + mol.vec0;
   const double* tde = tdd + vstride;
   const double* ev = eps + mol.vec0 + lo;
@@ -333,7 +375,7 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
   }
   __syncthreads();
   GridBarrier gb{bar, 0u};
-  const int rounds = (n + 4 * TW - 1) / (4 * TW);   // rows per warp, four at a time
+  const int rstep = G * kGridWarps;
 
   for (int b0 = 0; b0 < k; b0 += 32) {
     const int nb = min(32, k - b0);
@@ -344,45 +386,24 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
     if (!any) continue;
     const int L = b0 - cmin;
     const int jc = b0 + lane;
-    const bool jin = lane < nb && ce[b0 + min(lane, nb - 1)] - cs[b0 + min(lane, nb - 1)] >= 2;
-    const int jcs = lane < nb ? cs[b0 + lane] : b0;
 
     // two projections against the earlier vectors of each column's cluster
     for (int pass = 0; pass < 2 && L > 0; ++pass) {
-      // coefficients <z_l, z_j>: a warp per group of gsz earlier vectors
-      // (gsz grows with L only while every warp of the grid stays busy)
-      int gsz = 1;
-      while (gsz < 8 && L >= gsz * 2 * TW) gsz <<= 1;
-      const int ngrp = (L + gsz - 1) / gsz;
-      for (int g = gw; g < ngrp; g += TW) {
-        const int l0 = cmin + gsz * g;
-        double acc[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) acc[q] = 0.0;
-        const bool lv = lane < gsz && l0 + lane < b0;
-        for (int i0 = 0; i0 < n; i0 += 4) {
-          double zl[4], zj[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const bool in = i0 + u < n;
-            const double* zr = Zm + (long long)(i0 + u) * k;
-            zl[u] = (in && lv) ? __ldcg(zr + l0 + lane) : 0.0;
-            zj[u] = (in && lane < nb) ? __ldcg(zr + jc) : 0.0;
-          }
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-              if (q < gsz) acc[q] = fma(__shfl_sync(0xffffffffu, zl[u], q), zj[u], acc[q]);
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int l = l0 + q;
-          if (q < gsz && l < b0) __stcg(Gm + (long long)(l - cmin) * 32 + lane, (jin && l >= jcs) ? acc[q] : 0.0);
-        }
+      const int nlt = (L + 31) >> 5;
+      const int S = max(1, min(32, G / nlt));
+      tile_products(Zm, n, k, cmin, b0, b0, nb, S, part, sa, sb);
+      if (!gb.sync(&flag)) { grid_fail(st, mi); return; }
+      // coefficients: the sum over the splits, kept only within each column's cluster
+      for (int e = cta * kGridThreads + tid; e < L * 32; e += G * kGridThreads) {
+        const int l = cmin + (e >> 5), jj = e & 31;
+        double v = 0.0;
+        for (int sp = 0; sp < S; ++sp) v += __ldcg(part + (long long)sp * (nlt * 32) * 32 + e);
+        const bool keep = jj < nb && ce[b0 + jj] - cs[b0 + jj] >= 2 && l >= cs[b0 + jj];
+        __stcg(Gf + e, keep ? v : 0.0);
       }
       if (!gb.sync(&flag)) { grid_fail(st, mi); return; }
-      // z_j -= sum_l G[l][j] z_l on the warp's rows
+      // z_j -= sum_l G[l][j] z_l on the warp's rows (four rows per round)
+      const int rounds = (n + 4 * rstep - 1) / (4 * rstep);
       for (int t0 = 0; t0 < rounds; ++t0) {
         int rows[4];
         double acc[4];
@@ -395,7 +416,7 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
         for (int c0 = 0; c0 < L; c0 += kOrthChunk) {
           const int cn = min(kOrthChunk, L - c0);
           __syncthreads();
-          for (int e = tid; e < cn * 32; e += kGridThreads) gs[e] = __ldcg(Gm + (long long)c0 * 32 + e);
+          for (int e = tid; e < cn * 32; e += kGridThreads) gs[e] = __ldcg(Gf + (long long)c0 * 32 + e);
           __syncthreads();
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
@@ -418,54 +439,50 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
 
     // two Cholesky-QR passes inside the block (cluster members only)
     for (int pass = 0; pass < 2; ++pass) {
-      for (int e = gw; e < nb * nb; e += TW) {
-        const int a = e / nb, c = e - a * nb;
-        if (a > c) continue;
-        const int ca = b0 + a, cc = b0 + c;
-        const bool in = ce[ca] - cs[ca] >= 2 && cs[ca] == cs[cc];
-        double s = 0.0;
-        if (in)
-          for (int i = lane; i < n; i += 32) s = fma(__ldcg(Zm + (long long)i * k + ca), __ldcg(Zm + (long long)i * k + cc), s);
-        s = warp_sum_d(s);
-        if (lane == 0) __stcg(Mg + a * 32 + c, in ? s : (a == c ? 1.0 : 0.0));
+      const int S = max(1, min(G, n >> 3));
+      tile_products(Zm, n, k, b0, b0 + nb, b0, nb, S, part, sa, sb);
+      if (!gb.sync(&flag)) { grid_fail(st, mi); return; }
+      for (int e = cta * kGridThreads + tid; e < 1024; e += G * kGridThreads) {
+        const int a = e >> 5, c = e & 31;
+        double v = 0.0;
+        for (int sp = 0; sp < S; ++sp) v += __ldcg(part + (long long)sp * 1024 + e);
+        const bool in = a < nb && c < nb && ce[b0 + a] - cs[b0 + a] >= 2 && cs[b0 + a] == cs[b0 + c];
+        __stcg(Mg + e, in ? v : (a == c ? 1.0 : 0.0));
       }
       if (!gb.sync(&flag)) { grid_fail(st, mi); return; }
-      // M = L L^T (right-looking, unscaled), then L^-1, in every CTA
-      for (int e = tid; e < 1024; e += kGridThreads) {
-        const int a = e >> 5, c = e & 31;
-        double v = (a == c) ? 1.0 : 0.0;
-        if (a < nb && c < nb) v = a <= c ? __ldcg(Mg + a * 32 + c) : __ldcg(Mg + c * 32 + a);
-        Ms[a][c] = v;
-      }
-      for (int c = 0; c < 32; ++c) {
-        __syncthreads();
-        const double inv = 1.0 / fmax(Ms[c][c], 1e-300);
-        for (int e = tid; e < 1024; e += kGridThreads) {
-          const int a = e >> 5, q = e & 31;
-          if (a > c && q > c && q <= a) Ms[a][q] = fma(-Ms[a][c] * inv, Ms[q][c], Ms[a][q]);
-        }
-      }
+      // every CTA: M = L L^T (one warp, right-looking and unscaled: after the
+      // loop L[a][q] = Ms[a][q] / sqrt(Ms[q][q])), then L^-1
+      for (int e = tid; e < 1024; e += kGridThreads) sa[e >> 5][e & 31] = __ldcg(Mg + e);
       __syncthreads();
-      if (tid < 32) {
-        // column tid of L^-1 by forward substitution (L[a][b] = Ms[a][b] / sqrt(Ms[b][b]))
-        const int c = tid;
-        for (int a = 0; a < c; ++a) Li[a][c] = 0.0;
-        Li[c][c] = rsqrt(fmax(Ms[c][c], 1e-300));
+      if (warp == 0) {
+        for (int c = 0; c < 32; ++c) {
+          const double piv = fmax(sa[c][c], 1e-300);
+          __syncwarp();
+          if (lane > c) {
+            const double f = sa[lane][c] / piv;
+            for (int q = c + 1; q <= lane; ++q) sa[lane][q] = fma(-f, sa[q][c], sa[lane][q]);
+          }
+          __syncwarp();
+        }
+        rs[lane] = rsqrt(fmax(sa[lane][lane], 1e-300));
+        __syncwarp();
+        const int c = lane;   // column c of L^-1, by forward substitution
+        for (int a = 0; a < c; ++a) sb[a][c] = 0.0;
+        sb[c][c] = rs[c];
         for (int a = c + 1; a < 32; ++a) {
           double s = 0.0;
-          for (int q = c; q < a; ++q) s = fma(Ms[a][q] * rsqrt(fmax(Ms[q][q], 1e-300)), Li[q][c], s);
-          Li[a][c] = -s / sqrt(fmax(Ms[a][a], 1e-300));
+          for (int q = c; q < a; ++q) s = fma(sa[a][q] * rs[q], sb[q][c], s);
+          sb[a][c] = -s * rs[a];
         }
       }
       __syncthreads();
-      for (int t0 = 0; t0 < rounds * 4; ++t0) {
-        const int i = cta + G * (warp + kGridWarps * t0);
-        if (i >= n) break;
+      for (int i = cta + G * warp; i < n; i += rstep) {
         const double z = lane < nb ? __ldcg(Zm + (long long)i * k + jc) : 0.0;
         double y = 0.0;
+#pragma unroll
         for (int q = 0; q < 32; ++q) {
           const double zq = __shfl_sync(0xffffffffu, z, q);
-          if (q <= lane) y = fma(Li[lane][q], zq, y);
+          if (q <= lane) y = fma(sb[lane][q], zq, y);
         }
         if (lane < nb) __stcg(Zm + (long long)i * k + jc, y);
       }
@@ -477,7 +494,12 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
 // ---------------------------------------------------------------------------
 // X = Q Z with kCols columns per CTA (lanes: column lane % kCols, row slice
 // lane / kCols; S = 8 * 32 / kCols row slices, row i in slice i mod S).
+// Reflector j is staged in shared memory while every thread holds its share
+// of reflector j - 1 in registers (loaded during the work on j), so the
+// reflector rows cost one coalesced global read each.
 // ---------------------------------------------------------------------------
+constexpr int kBackPre = 24;   // reflector entries per thread held in registers: N <= 24 * 256
+
 template <typename T, int kCols>
 __global__ void __launch_bounds__(kWideWarps * 32)
 hh_back_wide_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one, const MolState* __restrict__ st,
@@ -485,7 +507,7 @@ hh_back_wide_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one
                     const double* __restrict__ td, long long vstride, const double* __restrict__ Z,
                     T* __restrict__ C) {
   extern __shared__ __align__(16) double bwm[];
-  constexpr int kSpw = 32 / kCols, kS = kWideWarps * kSpw;
+  constexpr int kSpw = 32 / kCols, kS = kWideWarps * kSpw, kT = kWideWarps * 32;
   const int mi = one[0];
   if (require_active && st[mi].status != kActive) return;
   if (require_phase >= 0 && st[mi].phase != require_phase) return;
@@ -499,7 +521,7 @@ hh_back_wide_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one
   T* zs = reinterpret_cast<T*>(bwm);          // n x kCols
   T* red = zs + (long long)n * kCols;          // kWideWarps x kCols
   T* dotv = red + kWideWarps * kCols;          // kCols
-  T* urow = dotv + kCols;                      // 2 n (FP32: staged reflectors)
+  T* us = dotv + kCols;                        // the staged reflector (n)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int c = lane % kCols, slice = warp * kSpw + lane / kCols;
   const double* Zm = Z + mol.mat0;
@@ -507,41 +529,52 @@ hh_back_wide_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one
   const double* tt = td + mol.vec0 + 2 * vstride;
   const int col = cb + c;
   for (int i = slice; i < n; i += kS) zs[i * kCols + c] = col < k ? (T)Zm[(long long)i * k + col] : (T)0;
+  if (n >= 3)
+    for (int i = n - 2 + tid; i < n; i += kT) us[i] = (T)Wm[(long long)(n - 3) * n + i];
   __syncthreads();
   for (int j = n - 3; j >= 0; --j) {
+    // reflector j - 1 (entries j .. n-1) into registers
+    double pre[kBackPre];
+    if (j > 0) {
+      const double* ug = Wm + (long long)(j - 1) * n;
+#pragma unroll
+      for (int q = 0; q < kBackPre; ++q) {
+        const int i = j + tid + q * kT;
+        pre[q] = i < n ? ug[i] : 0.0;
+      }
+    }
     const T tau = (T)tt[j];
-    if (tau == (T)0) continue;
-    const double* ug = Wm + (long long)j * n;
-    const T* u;
-    if (sizeof(T) == 4) {
-      T* ur = urow + (j & 1) * n;
-      for (int i = j + 1 + tid; i < n; i += kWideWarps * 32) ur[i] = (T)ug[i];
+    if (tau != (T)0) {
+      const int i0 = j + 1 + ((slice - (j + 1)) & (kS - 1));
+      T part = 0;
+      for (int i = i0; i < n; i += kS) part = fma(us[i], zs[i * kCols + c], part);
+#pragma unroll
+      for (int o = kCols; o < 32; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      if (lane < kCols) red[warp * kCols + lane] = part;
       __syncthreads();
-      u = ur;
-    } else {
-      u = reinterpret_cast<const T*>(ug);
-    }
-    const int i0 = j + 1 + ((slice - (j + 1)) & (kS - 1));
-    T part = 0;
-    for (int i = i0; i < n; i += kS) part = fma(u[i], zs[i * kCols + c], part);
+      if (tid < kCols) {
+        T sum = red[tid];
 #pragma unroll
-    for (int o = kCols; o < 32; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if (lane < kCols) red[warp * kCols + lane] = part;
-    __syncthreads();
-    if (tid < kCols) {
-      T sum = red[tid];
+        for (int q = 1; q < kWideWarps; ++q) sum += red[q * kCols + tid];
+        dotv[tid] = tau * sum;
+      }
+      __syncthreads();
+      const T dt = dotv[c];
+      for (int i = i0; i < n; i += kS) {
+        T* z = zs + i * kCols + c;
+        *z = fma(-dt, us[i], *z);
+      }
+    }
+    __syncthreads();   // every thread is done with reflector j
+    if (j > 0) {
 #pragma unroll
-      for (int q = 1; q < kWideWarps; ++q) sum += red[q * kCols + tid];
-      dotv[tid] = tau * sum;
+      for (int q = 0; q < kBackPre; ++q) {
+        const int i = j + tid + q * kT;
+        if (i < n) us[i] = (T)pre[q];
+      }
     }
     __syncthreads();
-    const T dt = dotv[c];
-    for (int i = i0; i < n; i += kS) {
-      T* z = zs + i * kCols + c;
-      *z = fma(-dt, u[i], *z);
-    }
   }
-  __syncthreads();
   T* Cm = C + mol.mat0;
   for (int q = warp; q < kCols; q += kWideWarps) {
     const int cc = cb + q;
@@ -593,7 +626,7 @@ size_t tridiag_grid_smem(int n) { return 3 * (size_t)n * sizeof(double); }
 size_t orth_grid_smem(int k) { return (size_t)kOrthChunk * 32 * sizeof(double) + 2 * (size_t)k * sizeof(int); }
 template <typename T>
 size_t back_wide_smem(int n, int cols) {
-  return ((size_t)n * cols + kWideWarps * cols + cols + (sizeof(T) == 4 ? 2 * (size_t)n : 0)) * sizeof(T);
+  return ((size_t)n * cols + kWideWarps * cols + cols + (size_t)n) * sizeof(T);
 }
 template <typename T>
 int back_wide_cols(int n) {
@@ -650,7 +683,7 @@ int hh_grid_max_n() {
     const size_t lim = (size_t)(optin_smem() - kStaticSmem);
     int n = 8;
     while (tridiag_grid_smem(n + 1) <= lim && orth_grid_smem(n + 1) <= lim && back_wide_cols<double>(n + 1) > 0 &&
-           back_wide_cols<float>(n + 1) > 0)
+           back_wide_cols<float>(n + 1) > 0 && n + 1 <= kBackPre * kWideWarps * 32)
       ++n;
     nmax = n;
   });

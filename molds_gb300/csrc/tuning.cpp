@@ -5,6 +5,8 @@
 //                                 concurrent molecule groups
 //   tridiag_threads <n> <t>       bases up to n: t threads per tridiagonalisation CTA
 //   check_block <b>               SCF iterations enqueued per convergence check
+//   vec_pairs <n> <p>             bases up to n: p eigenpairs (lane pairs) per CTA of
+//                                 the tridiagonal eigenvector kernel (1..16)
 // MOLDS_GB300_TUNING names another table (the autotuner's candidates);
 // missing entries keep the built-in defaults.
 #include <dlfcn.h>
@@ -26,6 +28,7 @@ namespace {
 struct Table {
   std::vector<std::pair<int, int>> groups{{48, 1}, {96, 2}, {144, 3}, {192, 4}};
   std::vector<std::pair<int, int>> tridiag_threads{{1 << 30, 512}};
+  std::vector<std::pair<int, int>> vec_pairs{{1 << 30, 16}};
   int check_block = 2;
 };
 
@@ -51,7 +54,7 @@ void load() {
   std::ifstream f(env ? std::string(env) : default_path());
   if (!f) return;
   Table t;
-  bool groups = false, threads = false;
+  bool groups = false, threads = false, pairs = false;
   std::string line;
   while (std::getline(f, line)) {
     if (line.empty() || line[0] == '#') continue;
@@ -72,10 +75,17 @@ void load() {
       if (!threads) t.tridiag_threads.clear();
       threads = true;
       t.tridiag_threads.emplace_back(a, b);
+    } else if (key == "vec_pairs" && a >= 1 && b >= 1 && b <= 16) {
+      if (!pairs) t.vec_pairs.clear();
+      pairs = true;
+      t.vec_pairs.emplace_back(a, b);
     }
   }
   std::sort(t.groups.begin(), t.groups.end());
   std::sort(t.tridiag_threads.begin(), t.tridiag_threads.end());
+  std::sort(t.vec_pairs.begin(), t.vec_pairs.end());
+  if (t.vec_pairs.empty() || t.vec_pairs.back().first < (1 << 30))
+    t.vec_pairs.emplace_back(1 << 30, t.vec_pairs.empty() ? 16 : t.vec_pairs.back().second);
   if (t.tridiag_threads.empty() || t.tridiag_threads.back().first < (1 << 30))
     t.tridiag_threads.emplace_back(1 << 30, t.tridiag_threads.empty() ? 512 : t.tridiag_threads.back().second);
   g_table = t;
@@ -102,5 +112,11 @@ int tuned_tridiag_threads(int n) {
 }
 
 int tuned_check_block() { return table().check_block; }
+
+int tuned_vec_pairs(int n) {
+  for (const auto& e : table().vec_pairs)
+    if (n <= e.first) return e.second;
+  return 16;
+}
 
 }  // namespace nddo
