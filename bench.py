@@ -742,8 +742,12 @@ def run_md(args):
 # ---------------------------------------------------------------------------
 def run_water512(args):
     """One SCF of a 512-water cluster (8x8x8 jittered lattice, seed 4) under
-    MNDO through the plain ElectronicStructure path (block Jacobi for
-    N = 3072), with the RMS / DIIS-error trace."""
+    MNDO through the plain ElectronicStructure path (N = 3072: the whole-GPU
+    Householder eigensolver), FP64 and then mixed precision, with the RMS /
+    DIIS-error trace.  The reference's algorithm does not converge on this
+    cluster with the benchmark's SCF block (density DIIS falls into an
+    occupation-swapping 2-cycle, in the oracle as here), so the line reports
+    seconds per SCF iteration over --max-iter iterations."""
     import numpy as np
     import molds_gb300 as M
     from molds_gb300 import build, workloads as W
@@ -754,7 +758,8 @@ def run_water512(args):
     out = {}
     clocks = Clocks(0)
     clocks.start()
-    for prec in ([args.precision] if args.precision == "fp64" else ["mixed"]):
+    precs = [args.precision] + (["mixed"] if args.precision == "fp64" and not args.no_mixed else [])
+    for prec in precs:
         es = M.ElectronicStructure("mndo", M.SCFParams(**scf, precision=prec), context=ctx)
         t0 = time.perf_counter()
         es.SetMolecule(mol)
@@ -776,7 +781,7 @@ def run_water512(args):
     line = {"metric": "large single SCF: (H2O)512 MNDO, seconds per SCF iteration", "value": first["s_per_iteration"],
             "unit": "s/iteration", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * first["scf_s"],
             "higher_is_better": False, "scaling": "replicas only", "vs_baseline": None,
-            "dtype": "fp32+fp64" if "mixed" in out else "f64",
+            "dtype": "f64" if precs[0] == "fp64" else "fp32+fp64",
             "data": "synthetic: (H2O)512 on a jittered 8x8x8 lattice, seed 4",
             "config": {"workload": "(H2O)512 MNDO, 1536 atoms, 3072 basis functions, 2048 occupied", "scf": scf},
             "runs": out, "clocks": clk}

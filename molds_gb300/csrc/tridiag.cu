@@ -355,57 +355,26 @@ __device__ __forceinline__ double tri_solve(int n, int ld, double* __restrict__ 
                                             const double* __restrict__ fu1i, const double* __restrict__ fu2,
                                             const PivT* __restrict__ piv, const double* __restrict__ e, bool start,
                                             double scale, unsigned idx) {
-  // Both sweeps load their inputs four elements ahead (the loads do not
-  // depend on the carried values; with the factors in global memory the
-  // latency would otherwise be paid once per element).
   double cb = start ? start_entry(idx, 0) : scale * x[0];
-  for (int i0 = 0; i0 + 1 < n; i0 += 4) {
-    double bn[4], l[4];
-    bool pv[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + u;
-      const long long o = (long long)i * ld;
-      const bool in = i + 1 < n;
-      bn[u] = !in ? 0.0 : (start ? start_entry(idx, (unsigned)(i + 1)) : scale * x[o + ld]);
-      l[u] = in ? fl[o] : 0.0;
-      pv[u] = in && piv[o];
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + u;
-      if (i + 1 >= n) break;
-      const long long o = (long long)i * ld;
-      if (pv[u]) { x[o] = bn[u]; cb = fma(-l[u], bn[u], cb); }
-      else { x[o] = cb; cb = fma(-l[u], cb, bn[u]); }
-    }
+  for (int i = 0; i + 1 < n; ++i) {
+    const long long o = (long long)i * ld;
+    const double bn = start ? start_entry(idx, (unsigned)(i + 1)) : scale * x[o + ld];
+    const double l = fl[o];
+    if (piv[o]) { x[o] = bn; cb = fma(-l, bn, cb); }
+    else { x[o] = cb; cb = fma(-l, cb, bn); }
   }
   const long long on = (long long)(n - 1) * ld;
   double x2 = 0.0, x1 = cb * fu1i[on];
   x[on] = x1;
   double ss = x1 * x1;
-  for (int i0 = n - 2; i0 >= 0; i0 -= 4) {
-    double xo[4], f2[4], f1[4], u3[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 - u;
-      const long long o = (long long)i * ld;
-      const bool in = i >= 0;
-      xo[u] = in ? x[o] : 0.0;
-      f2[u] = in ? fu2[o] : 0.0;
-      f1[u] = in ? fu1i[o] : 0.0;
-      u3[u] = (in && piv[o]) ? e[i + 1] : 0.0;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 - u;
-      if (i < 0) break;
-      const double xi = fma(-u3[u], x2, fma(-f2[u], x1, xo[u])) * f1[u];
-      x[(long long)i * ld] = xi;
-      ss = fma(xi, xi, ss);
-      x2 = x1;
-      x1 = xi;
-    }
+  for (int i = n - 2; i >= 0; --i) {
+    const long long o = (long long)i * ld;
+    const double u3 = piv[o] ? e[i + 1] : 0.0;
+    const double xi = fma(-u3, x2, fma(-fu2[o], x1, x[o])) * fu1i[o];
+    x[o] = xi;
+    ss = fma(xi, xi, ss);
+    x2 = x1;
+    x1 = xi;
   }
   return ss;
 }
@@ -526,8 +495,8 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   //     converges cubically, so it is taken only from a point whose count is
   //     idx or idx + 1 (the nearest root on the chosen side is then eigenvalue
   //     idx).  Each point's count narrows [a, b]; a point with another count,
-  //     a step that would leave [a, b], and a step that is not at most half
-  //     the previous one bisect [a, b] instead.  (A cluster of m close
+  //     a step that would leave [a, b], and a step above round-off level that
+  //     is not at most half the previous one bisect [a, b] instead.  (A cluster of m close
   //     eigenvalues beyond the wanted one, seen from a distance large against
   //     its width, acts like an m-fold root: Laguerre then converges only
   //     linearly, each step covering about m^-1/2 of the distance.)
@@ -590,7 +559,8 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
             const bool inside = xl >= a && xl <= bnd;
             step = fabs(xl - lam);
             done = inside && step <= 2.0 * ulp * fabs(lam) + 1e-300;
-            take = inside && (done || step <= 0.5 * prev_step);
+            // steps at round-off level never trigger the bisection
+            take = inside && (done || step <= 0.5 * prev_step || step <= 64.0 * ulp * fabs(lam) + 1e-300);
           }
           if (take) { xn = xl; prev_step = step; }
           else { xn = 0.5 * (a + bnd); prev_step = 1e300; }
