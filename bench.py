@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
+                    help="default: mixed for the uneven alkanes (their precision ramp), fp64 otherwise")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision measurement")
     ap.add_argument("--nmol", type=int, default=N_MOL)
     ap.add_argument("--dipole", default="on", choices=["on", "off"],
@@ -67,7 +68,10 @@ def parse():
     ap.add_argument("--alkanes", type=int, default=4096, help="alkanes: molecules in the uneven batch")
     ap.add_argument("--repeats", type=int, default=200, help="octane: timed solves")
     ap.add_argument("--max-iter", type=int, default=500, help="water512: SCF iteration cap")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.precision is None:
+        a.precision = "mixed" if a.workload == "alkanes" else "fp64"
+    return a
 
 
 def workload(rank: int, nmol: int):
