@@ -322,7 +322,11 @@ void Batch::allocate(const BatchCapacity& cap) {
   d_td = dalloc<double>(3 * (size_t)vec, &bytes_);
   d_hh_small_ = dalloc<int>(nm, &bytes_);
   d_hh_large_ = dalloc<int>(nm, &bytes_);
-  d_gridbar_ = dalloc<unsigned>(4, &bytes_);
+  grid_ctas_ = hh_grid_ctas();
+  d_gridmap_ = dalloc<int>(3 * ((size_t)nm + grid_ctas_), &bytes_);
+  cuda_check(cudaHostAlloc(&h_gridmap_, sizeof(int) * 3 * ((size_t)nm + grid_ctas_), cudaHostAllocDefault),
+             "cudaHostAlloc");
+  d_gridbar_ = dalloc<unsigned>(4 * (size_t)grid_ctas_, &bytes_);
   d_state = dalloc<MolState>(nm, &bytes_);
   d_charges = dalloc<double>(cap.atoms, &bytes_);
   d_sweeps = dalloc<int>(nm, &bytes_);
@@ -466,6 +470,9 @@ Batch::~Batch() {
   for (void* p : ptrs) if (p) cudaFree(p);
   for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
   if (d_td) cudaFree(d_td);
+  void* hh[] = {d_hh_small_, d_hh_large_, d_gridmap_, d_gridbar_};
+  for (void* p : hh) if (p) cudaFree(p);
+  if (h_gridmap_) cudaFreeHost(h_gridmap_);
 }
 
 void Batch::free_jobs() {
@@ -548,20 +555,48 @@ void Batch::build_jobs(const std::vector<int>& which) {
   hh_max_k_ = 0;
   hh_small_.clear();
   hh_large_.clear();
-  hh_small_max_n_ = hh_small_max_k_ = 0;
+  hh_small_max_n_ = hh_small_max_k_ = hh_large_max_n_ = hh_large_max_k_ = 0;
+  // Householder path: bases above the per-molecule kernels' limit always go to
+  // the whole-GPU kernels; so do bases of at least kGridShareMinN while at
+  // most a quarter as many of them as SMs are in the list (each then gets
+  // four or more SMs instead of one)
   const int per_molecule = hh_back_max_n();
+  int n_big = 0;
+  for (int m : which) n_big += h_mols[m].nao >= kGridShareMinN;
+  const bool share = 4 * n_big <= grid_ctas_;
   for (int m : which) {
     const DevMol& d = h_mols[m];
     const int kd = std::min(d.nocc, d.nao - d.nocc);
     list_max_n_ = std::max(list_max_n_, d.nao);
     hh_max_k_ = std::max(hh_max_k_, kd);
-    if (d.nao <= per_molecule) {
+    if (d.nao <= per_molecule && !(share && d.nao >= kGridShareMinN)) {
       hh_small_.push_back(m);
       hh_small_max_n_ = std::max(hh_small_max_n_, d.nao);
       hh_small_max_k_ = std::max(hh_small_max_k_, kd);
     } else {
       hh_large_.push_back(m);
+      hh_large_max_n_ = std::max(hh_large_max_n_, d.nao);
+      hh_large_max_k_ = std::max(hh_large_max_k_, kd);
     }
+  }
+  // chunks of at most grid_ctas_ molecules and their CTA maps
+  grid_chunks_.clear();
+  int off = 0;
+  for (int f = 0; f < (int)hh_large_.size(); f += grid_ctas_) {
+    GridChunk c;
+    c.first = f;
+    c.count = std::min(grid_ctas_, (int)hh_large_.size() - f);
+    std::vector<int> ns(c.count);
+    c.max_k = 0;
+    for (int i = 0; i < c.count; ++i) {
+      const DevMol& d = h_mols[hh_large_[f + i]];
+      ns[i] = d.nao;
+      c.max_k = std::max(c.max_k, std::min(d.nocc, d.nao - d.nocc));
+    }
+    c.map_off = off;
+    c.nctas = hh_grid_assign(ns.data(), c.count, grid_ctas_, h_gridmap_ + off);
+    off += 3 * c.nctas;
+    grid_chunks_.push_back(c);
   }
 }
 
@@ -587,10 +622,15 @@ void Batch::upload_list(const std::vector<int>& which) {
     if (!hh_small_.empty())
       cuda_check(cudaMemcpyAsync(d_hh_small_, stage, hh_small_.size() * sizeof(int), cudaMemcpyHostToDevice, stream_),
                  "upload list");
-    if (!hh_large_.empty())
+    if (!hh_large_.empty()) {
       cuda_check(cudaMemcpyAsync(d_hh_large_, stage + nm, hh_large_.size() * sizeof(int), cudaMemcpyHostToDevice,
                                  stream_),
                  "upload list");
+      const GridChunk& last = grid_chunks_.back();
+      cuda_check(cudaMemcpyAsync(d_gridmap_, h_gridmap_, sizeof(int) * (last.map_off + 3 * last.nctas),
+                                 cudaMemcpyHostToDevice, stream_),
+                 "upload grid map");
+    }
   }
   // Jacobi size buckets: smaller molecules get a smaller shared-memory
   // footprint; the first edge keeps bases below the cluster Jacobi's minimum
@@ -924,11 +964,21 @@ void Batch::hh_vectors(const ScfSettings& s, int final_pass, int require_active)
     launch_hh_vectors(d_mols, d_hh_small_, (int)hh_small_.size(), hh_small_max_n_, max_k, d_state, require_active,
                       final_pass, mixed, d_G64, d_td, vec_total_, d_eps, d_T64, d_S, d_C, d_Cf, stream_);
   }
-  for (size_t i = 0; i < hh_large_.size(); ++i) {
-    const DevMol& d = h_mols[hh_large_[i]];
-    launches_ += (mixed && !final_pass) ? 4 : 3;
-    launch_hh_grid_vectors(d_mols, d_hh_large_ + i, d.nao, d.nocc, d_state, require_active, final_pass, mixed, d_G64,
-                           d_td, vec_total_, d_eps, d_T64, d_S, d_S[5], d_gridbar_, d_C, d_Cf, stream_);
+  if (!hh_large_.empty()) {
+    const int nl = (int)hh_large_.size();
+    const int max_k = final_pass ? hh_large_max_n_ : hh_large_max_k_;
+    launches_ += 1;
+    launch_tri_vectors(d_mols, d_hh_large_, nl, hh_large_max_n_, max_k, d_state, require_active, final_pass, d_td,
+                       vec_total_, d_eps, d_T64, d_S, stream_);
+    for (const GridChunk& c : grid_chunks_) {
+      launches_ += 1;
+      launch_hh_grid_orth(d_mols, d_hh_large_ + c.first, d_gridmap_ + c.map_off, c.nctas, c.count,
+                          final_pass ? hh_large_max_n_ : c.max_k, d_state, require_active, final_pass, d_td,
+                          vec_total_, d_eps, d_T64, d_S[5], d_gridbar_, stream_);
+    }
+    launches_ += (mixed && !final_pass) ? 2 : 1;
+    launch_hh_grid_back(d_mols, d_hh_large_, nl, hh_large_max_n_, max_k, d_state, require_active, final_pass, mixed,
+                        d_G64, d_td, vec_total_, d_T64, d_C, d_Cf, stream_);
   }
 }
 
@@ -943,11 +993,11 @@ void Batch::eigen_step(const ScfSettings& s) {
       launch_hh_tridiag(d_mols, bucket_dev_[b], (int)buckets_[b].size(), bucket_hh_max_n_[b], d_state, 1, d_F, d_G64,
                         d_td, vec_total_, d_S[4], hh_back_max_n(), stream_);
     }
-    // bases above the per-molecule kernels: one molecule at a time on every SM
-    for (size_t i = 0; i < hh_large_.size(); ++i) {
+    // the whole-GPU path: each chunk's molecules share one cooperative launch
+    for (const GridChunk& c : grid_chunks_) {
       launches_ += 1;
-      launch_hh_grid_tridiag(d_mols, d_hh_large_ + i, d_state, 1, d_F, d_G64, d_td, vec_total_, d_S[4], d_S[5],
-                             d_gridbar_, stream_);
+      launch_hh_grid_tridiag(d_mols, d_hh_large_ + c.first, d_gridmap_ + c.map_off, c.nctas, c.count, d_state, 1,
+                             d_F, d_G64, d_td, vec_total_, d_S[4], d_S[5], d_gridbar_, stream_);
     }
     prof_end(h);
     h = prof_begin(kKEigvec, active_work_estimate(kKEigvec));

@@ -212,8 +212,16 @@ class Batch {
   int* d_hh_small_ = nullptr;
   int* d_hh_large_ = nullptr;
   int hh_small_max_n_ = 0, hh_small_max_k_ = 0;
+  int hh_large_max_n_ = 0, hh_large_max_k_ = 0;
   std::vector<int> bucket_hh_max_n_;     // per size bucket: largest basis on the per-molecule kernels
-  unsigned* d_gridbar_ = nullptr;        // grid-barrier words of the cooperative launches
+  // whole-GPU path: the large molecules in chunks of at most one per SM, each
+  // chunk one cooperative launch whose CTAs are split over its molecules
+  struct GridChunk { int first, count, nctas, map_off, max_k; };
+  std::vector<GridChunk> grid_chunks_;
+  int grid_ctas_ = 0;                    // CTAs of a cooperative launch (the SM count)
+  int* d_gridmap_ = nullptr;             // per CTA: list entry, CTA in the sub-grid, sub-grid size
+  int* h_gridmap_ = nullptr;             // pinned staging of d_gridmap_
+  unsigned* d_gridbar_ = nullptr;        // barrier words, 4 per molecule of a chunk
   float *d_jA32 = nullptr, *d_jV32 = nullptr;
   void* d_bj_ws = nullptr;               // block-Jacobi workspace (bases above kSmallJacobiMaxN)
   int* h_bj_pending = nullptr;           // pinned: molecules still rotating after a block-Jacobi sweep

@@ -26,11 +26,11 @@ GroupedBatch::GroupedBatch(Engine* eng, const std::vector<MoleculeInput>& mols, 
   n_ = (int)mols.size();
   device_ = eng->device();
   groups = std::max(1, std::min(groups, n_));
-  // a molecule on the whole-GPU eigensolver takes every SM in its cooperative
-  // launches: two groups with such molecules must not wait for each other's
-  // SMs, so such batches run as one group
+  // molecules that may run on the whole-GPU eigensolver take every SM in its
+  // cooperative launches: two groups with such molecules must not wait for
+  // each other's SMs, so such batches run as one group
   for (const MoleculeInput& m : mols)
-    if (molecule_nao(m) > hh_back_max_n()) { groups = 1; break; }
+    if (molecule_nao(m) >= kGridShareMinN) { groups = 1; break; }
   // contiguous groups of near-equal molecule count, in input order
   int atom = 0, mol = 0;
   for (int g = 0; g < groups; ++g) {

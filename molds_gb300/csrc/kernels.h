@@ -145,18 +145,33 @@ void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n
                        long long vstride, double* eps, double* Z, double* const* S4, double* C, float* C32,
                        cudaStream_t s);
 
-// tridiag_grid.cu: the same eigensolver for one large molecule on every SM
-// (cooperative launches; bar = 4 words of grid-barrier state, scratch = the
-// molecule's N x N arena of another scratch matrix).  A grid barrier that
-// waits longer than about two seconds marks the molecule failed.
+// tridiag_grid.cu: the same eigensolver for large molecules on many SMs each.
+// A cooperative launch of nctas CTAs (one per SM) serves nlist <= nctas
+// molecules of list; map3 holds per CTA (entry of list, CTA index within the
+// molecule's sub-grid, sub-grid size), from hh_grid_assign; bars = 4 words of
+// barrier state per entry.  scratch = another N x N scratch arena.  A
+// sub-grid barrier that waits longer than about two seconds marks the
+// molecule failed.
 int hh_grid_max_n();     // largest basis the whole-GPU path serves
-void launch_hh_grid_tridiag(const DevMol* mols, const int* one, MolState* st, int require_active, const double* F,
-                            double* W, double* td, long long vstride, double* Aws, double* scratch, unsigned* bar,
-                            cudaStream_t s);
-void launch_hh_grid_vectors(const DevMol* mols, const int* one, int n, int nocc, MolState* st, int require_active,
-                            int final_pass, int mixed, const double* W, const double* td, long long vstride,
-                            double* eps, double* Z, double* const* S4, double* scratch, unsigned* bar, double* C,
-                            float* C32, cudaStream_t s);
+// Bases from this size on share the whole-GPU kernels when few of them are in
+// a list (Batch::build_jobs).  Above the serving middle lane's largest basis
+// (400), so that only one serving lane issues cooperative launches.
+constexpr int kGridShareMinN = 401;
+int hh_grid_ctas();      // CTAs of one cooperative launch (the SM count)
+// CTA split of G CTAs over count molecules of bases n[] (N^3 shares, at least
+// one each): writes 3 ints per CTA into map3, returns the CTAs used (0 if
+// count > G)
+int hh_grid_assign(const int* n, int count, int G, int* map3);
+void launch_hh_grid_tridiag(const DevMol* mols, const int* list, const int* map3, int nctas, int nlist, MolState* st,
+                            int require_active, const double* F, double* W, double* td, long long vstride,
+                            double* Aws, double* scratch, unsigned* bars, cudaStream_t s);
+void launch_hh_grid_orth(const DevMol* mols, const int* list, const int* map3, int nctas, int nlist, int max_k,
+                         MolState* st, int require_active, int final_pass, const double* td, long long vstride,
+                         double* eps, double* Z, double* scratch, unsigned* bars, cudaStream_t s);
+// X = Q Z for every molecule of list (grid: molecules x column groups)
+void launch_hh_grid_back(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
+                         int require_active, int final_pass, int mixed, const double* W, const double* td,
+                         long long vstride, const double* Z, double* C, float* C32, cudaStream_t s);
 
 // scf_kernels.cu
 void launch_gemm(const GemmJob* jobs, int njobs, int ntiles, const double* A, const double* B, double* C,

@@ -12,7 +12,7 @@ namespace {
 // (at most 3.2 N^2 doubles, an all-heavy molecule), pair records, energies and
 // index lists (at most N^2 / 2 pairs), atoms and charges (at most N^2 / 16).
 constexpr double kBlocksPerMat = 3.2, kPairsPerMat = 0.5, kAtomsPerMat = 1.0 / 16.0;
-constexpr int kSmallLaneMaxN = 194;   // FP32 Jacobi fully in shared memory
+constexpr int kSmallLaneMaxN = 194;   // tridiagonalisation in shared memory
 constexpr int kMidLaneMaxN = 400;
 
 BatchCapacity lane_capacity(size_t bytes, int max_n, int min_n, int diis_m, int ws_slots) {
@@ -42,7 +42,10 @@ Server::Server(Engine* eng, const ScfSettings& s, size_t hbm_budget, int max_bas
   s_.keep_trace = 0;
   t0_ = std::chrono::steady_clock::now();
   const int m = s_.diis_num_error_vect;
-  // lanes by basis size: one-CTA Jacobi (<= 194), block Jacobi up to 400, larger
+  // lanes by basis size: the per-molecule eigensolver with its matrix in shared
+  // memory (<= 194), in a global workspace up to 400, and the larger ones
+  // (whole-GPU eigensolver kernels when few are resident; the only lane that
+  // issues cooperative launches)
   struct Spec { int lo, hi; double share; int min_n, ws; };
   std::vector<Spec> specs;
   if (max_basis <= kSmallLaneMaxN) specs.push_back({0, max_basis, 1.0, 2, 1});

@@ -1,5 +1,7 @@
-// Kernel (d), FP64 path for one large molecule: the Householder eigensolver
-// of tridiag.cu spread over every SM (cooperative launches, one CTA per SM).
+// Kernel (d), FP64 path for large molecules: the Householder eigensolver of
+// tridiag.cu spread over many SMs per molecule.  One cooperative launch (one
+// CTA per SM) serves up to one molecule per SM: each molecule gets a sub-grid
+// of CTAs in proportion to N^3, with its own barrier words.
 //
 // Stands in for MolDS's Lapack::Dsyevd (src/wrappers/Lapack.cpp:102-160) on
 // the bases that do not fit one SM: a one-CTA tridiagonalisation of N = 3072
@@ -28,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <mutex>
+#include <vector>
 #include "nddo_batch.cuh"
 #include "kernels.h"
 #include "tridiag.cuh"
@@ -48,13 +51,14 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   return v;
 }
 
-// Grid-wide barrier of a cooperative launch.  bar[0] counts arrivals, bar[1]
-// is the generation, bar[2] the error flag: a wait longer than
-// kGridWaitCycles sets it, and every CTA leaves at its next barrier.  The host
-// zeroes bar before each launch.
+// Barrier over the CTAs of one molecule's sub-grid of a cooperative launch.
+// bar[0] counts arrivals, bar[1] is the generation, bar[2] the error flag: a
+// wait longer than kGridWaitCycles sets it, and every CTA of the sub-grid
+// leaves at its next barrier.  The host zeroes the words before each launch.
 struct GridBarrier {
   unsigned* bar;
   unsigned gen;
+  unsigned nblocks;   // CTAs of this molecule's sub-grid
   __device__ bool sync(int* flag) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -63,7 +67,7 @@ struct GridBarrier {
         ok = 0;
       } else {
         __threadfence();
-        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+        if (atomicAdd(bar, 1u) == nblocks - 1) {
           atomicExch(bar, 0u);
           __threadfence();
           atomicExch(bar + 1, gen + 1);
@@ -131,19 +135,20 @@ __device__ __forceinline__ void grid_fail(MolState* st, int mi) {
 }
 
 __global__ void __launch_bounds__(kGridThreads, 1)
-hh_tridiag_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one, MolState* __restrict__ st,
-                       int require_active, const double* __restrict__ F, double* __restrict__ W,
-                       double* __restrict__ td, long long vstride, double* __restrict__ Aws,
-                       double* __restrict__ scratch, unsigned* __restrict__ bar) {
+hh_tridiag_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const int3* __restrict__ map,
+                       MolState* __restrict__ st, int require_active, const double* __restrict__ F,
+                       double* __restrict__ W, double* __restrict__ td, long long vstride, double* __restrict__ Aws,
+                       double* __restrict__ scratch, unsigned* __restrict__ bars) {
   extern __shared__ __align__(16) double gsm[];
   __shared__ int flag;
   __shared__ double red[kGridWarps], wred[kGridWarps], hs[4];
-  const int mi = one[0];
+  const int3 slot = map[blockIdx.x];   // (list entry, CTA within the molecule's sub-grid, sub-grid size)
+  const int mi = list[slot.x];
   if (require_active && st[mi].status != kActive) return;
   const DevMol mol = mols[mi];
   const int n = mol.nao;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int G = gridDim.x, cta = blockIdx.x, rstep = G * kGridWarps;
+  const int G = slot.z, cta = slot.y, rstep = G * kGridWarps;
   const double* Fm = F + mol.mat0;
   double* A = Aws + mol.mat0;
   double* Wm = W + mol.mat0;
@@ -164,7 +169,7 @@ hh_tridiag_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ 
     }
     return;
   }
-  GridBarrier gb{bar, 0u};
+  GridBarrier gb{bars + 4 * slot.x, 0u, (unsigned)G};
 
   // column 0 (= row 0) and reflector 0
   for (int j = 1 + tid; j < n; j += kGridThreads) vk[j] = Fm[j];
@@ -290,10 +295,10 @@ hh_tridiag_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ 
 // stages 32 rows of both column sets in shared memory per step and every
 // thread accumulates two outputs (j = lane, l and l + 16).
 __device__ void tile_products(const double* __restrict__ Zm, int n, int k, int l_beg, int l_end, int b0, int nb,
-                              int S, double* __restrict__ part, double (*sa)[33], double (*sb)[33]) {
+                              int S, double* __restrict__ part, double (*sa)[33], double (*sb)[33], int cta, int G) {
   const int L = l_end - l_beg, nlt = (L + 31) >> 5, items = nlt * S, R = (n + S - 1) / S;
   const int t = threadIdx.x, j = t & 31, l = t >> 5;
-  for (int it = blockIdx.x; it < items; it += gridDim.x) {
+  for (int it = cta; it < items; it += G) {
     const int lt = it % nlt, sp = it / nlt;
     const int l0 = l_beg + 32 * lt, nl = min(32, l_end - l0);
     const int r0 = sp * R, r1 = min(n, r0 + R);
@@ -324,16 +329,17 @@ __device__ void tile_products(const double* __restrict__ Zm, int n, int k, int l
 }
 
 __global__ void __launch_bounds__(kGridThreads, 1)
-tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one, MolState* __restrict__ st,
-                     int require_active, int final_pass, const double* __restrict__ td, long long vstride,
-                     const double* __restrict__ eps, double* __restrict__ Z, double* __restrict__ scratch,
-                     unsigned* __restrict__ bar) {
+tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const int3* __restrict__ map,
+                     MolState* __restrict__ st, int require_active, int final_pass, const double* __restrict__ td,
+                     long long vstride, const double* __restrict__ eps, double* __restrict__ Z,
+                     double* __restrict__ scratch, unsigned* __restrict__ bars) {
   extern __shared__ __align__(16) double osm[];
   __shared__ int flag;
   __shared__ double red[kGridWarps];
   __shared__ double sa[32][33], sb[32][33];
   __shared__ double rs[32];
-  const int mi = one[0];
+  const int3 slot = map[blockIdx.x];
+  const int mi = list[slot.x];
   if (require_active && st[mi].status != kActive) return;
   const DevMol mol = mols[mi];
   const int n = mol.nao;
@@ -342,7 +348,7 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
   const int k = hi - lo;
   if (k < 2) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int G = gridDim.x, cta = blockIdx.x;
+  const int G = slot.z, cta = slot.y;
   double* gs = osm;                                            // kOrthChunk x 32 coefficients
   int* cs = reinterpret_cast<int*>(gs + kOrthChunk * 32);      // cluster [cs, ce) of each column
   int* ce = cs + k;
@@ -350,6 +356,9 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
   double* Gf = scratch + mol.mat0;                             // (k x 32) projection coefficients
   double* Mg = Gf + (long long)k * 32;                         // 32 x 32 Gram matrix
   double* part = Mg + 1024;                                    // partial products of the row splits
+  // the molecule's scratch matrix holds N x N doubles: the splits are capped
+  // so that the partial products fit behind the coefficients
+  const long long part_cap = (long long)n * n - (long long)k * 32 - 1024;
   const double* tdd = td + mol.vec0;
   const double* tde = tdd + vstride;
   const double* ev = eps + mol.vec0 + lo;
@@ -374,7 +383,7 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
       }
   }
   __syncthreads();
-  GridBarrier gb{bar, 0u};
+  GridBarrier gb{bars + 4 * slot.x, 0u, (unsigned)G};
   const int rstep = G * kGridWarps;
 
   for (int b0 = 0; b0 < k; b0 += 32) {
@@ -390,8 +399,8 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
     // two projections against the earlier vectors of each column's cluster
     for (int pass = 0; pass < 2 && L > 0; ++pass) {
       const int nlt = (L + 31) >> 5;
-      const int S = max(1, min(32, G / nlt));
-      tile_products(Zm, n, k, cmin, b0, b0, nb, S, part, sa, sb);
+      const int S = max(1, min(min(32, G / nlt), (int)(part_cap / (nlt * 1024))));
+      tile_products(Zm, n, k, cmin, b0, b0, nb, S, part, sa, sb, cta, G);
       if (!gb.sync(&flag)) { grid_fail(st, mi); return; }
       // coefficients: the sum over the splits, kept only within each column's cluster
       for (int e = cta * kGridThreads + tid; e < L * 32; e += G * kGridThreads) {
@@ -439,8 +448,8 @@ tri_orth_grid_kernel(const DevMol* __restrict__ mols, const int* __restrict__ on
 
     // two Cholesky-QR passes inside the block (cluster members only)
     for (int pass = 0; pass < 2; ++pass) {
-      const int S = max(1, min(G, n >> 3));
-      tile_products(Zm, n, k, b0, b0 + nb, b0, nb, S, part, sa, sb);
+      const int S = max(1, min(min(G, n >> 3), (int)(part_cap / 1024)));
+      tile_products(Zm, n, k, b0, b0 + nb, b0, nb, S, part, sa, sb, cta, G);
       if (!gb.sync(&flag)) { grid_fail(st, mi); return; }
       for (int e = cta * kGridThreads + tid; e < 1024; e += G * kGridThreads) {
         const int a = e >> 5, c = e & 31;
@@ -502,13 +511,13 @@ constexpr int kBackPre = 24;   // reflector entries per thread held in registers
 
 template <typename T, int kCols>
 __global__ void __launch_bounds__(kWideWarps * 32)
-hh_back_wide_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one, const MolState* __restrict__ st,
+hh_back_wide_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
                     int require_active, int require_phase, int final_pass, const double* __restrict__ W,
                     const double* __restrict__ td, long long vstride, const double* __restrict__ Z,
                     T* __restrict__ C) {
   extern __shared__ __align__(16) double bwm[];
   constexpr int kSpw = 32 / kCols, kS = kWideWarps * kSpw, kT = kWideWarps * 32;
-  const int mi = one[0];
+  const int mi = list[blockIdx.x];
   if (require_active && st[mi].status != kActive) return;
   if (require_phase >= 0 && st[mi].phase != require_phase) return;
   const DevMol mol = mols[mi];
@@ -516,7 +525,7 @@ hh_back_wide_kernel(const DevMol* __restrict__ mols, const int* __restrict__ one
   int lo, hi;
   hh_range(n, mol.nocc, final_pass, &lo, &hi);
   const int k = hi - lo;
-  const int cb = blockIdx.x * kCols;
+  const int cb = blockIdx.y * kCols;
   if (cb >= k) return;
   T* zs = reinterpret_cast<T*>(bwm);          // n x kCols
   T* red = zs + (long long)n * kCols;          // kWideWarps x kCols
@@ -650,27 +659,26 @@ void set_attributes() {
   });
 }
 
-void cooperative(const void* fn, size_t smem, void** args, cudaStream_t s, unsigned* bar) {
-  cuda_check(cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), s), "grid barrier reset");
-  cuda_check(cudaLaunchCooperativeKernel(fn, dim3(num_sms()), dim3(kGridThreads), args, smem, s),
-             "cooperative launch");
+void cooperative(const void* fn, int nctas, int nlist, size_t smem, void** args, cudaStream_t s, unsigned* bars) {
+  cuda_check(cudaMemsetAsync(bars, 0, 4 * sizeof(unsigned) * (size_t)nlist, s), "grid barrier reset");
+  cuda_check(cudaLaunchCooperativeKernel(fn, dim3(nctas), dim3(kGridThreads), args, smem, s), "cooperative launch");
 }
 
 template <typename T>
-void launch_back_wide(const DevMol* mols, const int* one, int n, int k, const MolState* st, int require_active,
-                      int require_phase, int final_pass, const double* W, const double* td, long long vstride,
-                      const double* Z, T* C, cudaStream_t s) {
-  const int cols = back_wide_cols<T>(n);
-  const size_t sh = back_wide_smem<T>(n, cols);
-  const dim3 g((k + cols - 1) / cols);
+void launch_back_wide(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
+                      int require_active, int require_phase, int final_pass, const double* W, const double* td,
+                      long long vstride, const double* Z, T* C, cudaStream_t s) {
+  const int cols = back_wide_cols<T>(max_n);
+  const size_t sh = back_wide_smem<T>(max_n, cols);
+  const dim3 g(nlist, (max_k + cols - 1) / cols);
   if (cols == 16)
-    hh_back_wide_kernel<T, 16><<<g, kWideWarps * 32, sh, s>>>(mols, one, st, require_active, require_phase,
+    hh_back_wide_kernel<T, 16><<<g, kWideWarps * 32, sh, s>>>(mols, list, st, require_active, require_phase,
                                                                final_pass, W, td, vstride, Z, C);
   else if (cols == 8)
-    hh_back_wide_kernel<T, 8><<<g, kWideWarps * 32, sh, s>>>(mols, one, st, require_active, require_phase,
+    hh_back_wide_kernel<T, 8><<<g, kWideWarps * 32, sh, s>>>(mols, list, st, require_active, require_phase,
                                                               final_pass, W, td, vstride, Z, C);
   else
-    hh_back_wide_kernel<T, 4><<<g, kWideWarps * 32, sh, s>>>(mols, one, st, require_active, require_phase,
+    hh_back_wide_kernel<T, 4><<<g, kWideWarps * 32, sh, s>>>(mols, list, st, require_active, require_phase,
                                                               final_pass, W, td, vstride, Z, C);
 }
 
@@ -690,38 +698,78 @@ int hh_grid_max_n() {
   return nmax;
 }
 
-void launch_hh_grid_tridiag(const DevMol* mols, const int* one, MolState* st, int require_active, const double* F,
-                            double* W, double* td, long long vstride, double* Aws, double* scratch, unsigned* bar,
-                            cudaStream_t s) {
-  set_attributes();
-  // the dynamic shared memory of the largest basis served (the kernel reads
-  // its own n on the device)
-  const size_t sh = tridiag_grid_smem(hh_grid_max_n());
-  void* args[] = {(void*)&mols, (void*)&one, (void*)&st, (void*)&require_active, (void*)&F, (void*)&W,
-                  (void*)&td, (void*)&vstride, (void*)&Aws, (void*)&scratch, (void*)&bar};
-  cooperative((const void*)hh_tridiag_grid_kernel, sh, args, s, bar);
+int hh_grid_ctas() { return num_sms(); }
+
+int hh_grid_assign(const int* n, int count, int G, int* map3) {
+  if (count < 1 || count > G) return 0;
+  // CTAs in proportion to N^3 (the tridiagonalisation's work), at least one each
+  std::vector<double> c(count);
+  std::vector<int> a(count);
+  double tot = 0.0;
+  for (int i = 0; i < count; ++i) { c[i] = (double)n[i] * n[i] * n[i]; tot += c[i]; }
+  int used = 0;
+  for (int i = 0; i < count; ++i) { a[i] = std::max(1, (int)(G * c[i] / tot)); used += a[i]; }
+  while (used > G) {   // only possible through the minimum of one
+    int best = -1;
+    for (int i = 0; i < count; ++i)
+      if (a[i] > 1 && (best < 0 || a[i] > a[best])) best = i;
+    --a[best];
+    --used;
+  }
+  while (used < G) {
+    int best = 0;
+    for (int i = 1; i < count; ++i)
+      if (c[i] / a[i] > c[best] / a[best]) best = i;
+    ++a[best];
+    ++used;
+  }
+  int q = 0;
+  for (int i = 0; i < count; ++i)
+    for (int j = 0; j < a[i]; ++j, ++q) {
+      map3[3 * q] = i;
+      map3[3 * q + 1] = j;
+      map3[3 * q + 2] = a[i];
+    }
+  return q;
 }
 
-void launch_hh_grid_vectors(const DevMol* mols, const int* one, int n, int nocc, MolState* st, int require_active,
-                            int final_pass, int mixed, const double* W, const double* td, long long vstride,
-                            double* eps, double* Z, double* const* S4, double* scratch, unsigned* bar, double* C,
-                            float* C32, cudaStream_t s) {
+void launch_hh_grid_tridiag(const DevMol* mols, const int* list, const int* map3, int nctas, int nlist, MolState* st,
+                            int require_active, const double* F, double* W, double* td, long long vstride,
+                            double* Aws, double* scratch, unsigned* bars, cudaStream_t s) {
+  if (nlist <= 0) return;
   set_attributes();
-  int lo, hi;
-  hh_range(n, nocc, final_pass, &lo, &hi);
-  const int k = hi - lo;
-  if (k <= 0) return;
-  launch_tri_vectors(mols, one, 1, n, k, st, require_active, final_pass, td, vstride, eps, Z, S4, s);
-  {
-    const size_t sh = orth_grid_smem(k);
-    void* args[] = {(void*)&mols, (void*)&one, (void*)&st, (void*)&require_active, (void*)&final_pass, (void*)&td,
-                    (void*)&vstride, (void*)&eps, (void*)&Z, (void*)&scratch, (void*)&bar};
-    cooperative((const void*)tri_orth_grid_kernel, sh, args, s, bar);
-  }
+  // the dynamic shared memory of the largest basis served (each CTA reads
+  // its molecule's n on the device)
+  const size_t sh = tridiag_grid_smem(hh_grid_max_n());
+  const int3* map = reinterpret_cast<const int3*>(map3);
+  void* args[] = {(void*)&mols, (void*)&list, (void*)&map, (void*)&st, (void*)&require_active, (void*)&F,
+                  (void*)&W, (void*)&td, (void*)&vstride, (void*)&Aws, (void*)&scratch, (void*)&bars};
+  cooperative((const void*)hh_tridiag_grid_kernel, nctas, nlist, sh, args, s, bars);
+}
+
+void launch_hh_grid_orth(const DevMol* mols, const int* list, const int* map3, int nctas, int nlist, int max_k,
+                         MolState* st, int require_active, int final_pass, const double* td, long long vstride,
+                         double* eps, double* Z, double* scratch, unsigned* bars, cudaStream_t s) {
+  if (nlist <= 0 || max_k < 2) return;
+  set_attributes();
+  const size_t sh = orth_grid_smem(max_k);
+  const int3* map = reinterpret_cast<const int3*>(map3);
+  void* args[] = {(void*)&mols, (void*)&list, (void*)&map, (void*)&st, (void*)&require_active, (void*)&final_pass,
+                  (void*)&td, (void*)&vstride, (void*)&eps, (void*)&Z, (void*)&scratch, (void*)&bars};
+  cooperative((const void*)tri_orth_grid_kernel, nctas, nlist, sh, args, s, bars);
+}
+
+void launch_hh_grid_back(const DevMol* mols, const int* list, int nlist, int max_n, int max_k, const MolState* st,
+                         int require_active, int final_pass, int mixed, const double* W, const double* td,
+                         long long vstride, const double* Z, double* C, float* C32, cudaStream_t s) {
+  if (nlist <= 0 || max_k <= 0) return;
+  set_attributes();
   const int fp64_phase = (mixed && !final_pass) ? 1 : -1;
-  launch_back_wide<double>(mols, one, n, k, st, require_active, fp64_phase, final_pass, W, td, vstride, Z, C, s);
+  launch_back_wide<double>(mols, list, nlist, max_n, max_k, st, require_active, fp64_phase, final_pass, W, td,
+                           vstride, Z, C, s);
   if (fp64_phase == 1)
-    launch_back_wide<float>(mols, one, n, k, st, require_active, 0, final_pass, W, td, vstride, Z, C32, s);
+    launch_back_wide<float>(mols, list, nlist, max_n, max_k, st, require_active, 0, final_pass, W, td, vstride, Z,
+                            C32, s);
 }
 
 }  // namespace nddo

@@ -1,6 +1,7 @@
-"""The FP64 eigensolver at the large basis sizes of the benchmarks, and the
-large single molecule ((H2O)512 MNDO, N = 3072), against the oracle through
-the public API.
+"""The FP64 eigensolver at the large basis sizes of the benchmarks, the
+whole-GPU kernels shared by several large molecules, and the large single
+molecule ((H2O)512 MNDO, N = 3072), against the oracle through the public
+API.
 
 Eigenpairs: one SCF iteration from the guess, so the final pass diagonalises
 the guess Fock matrix, which the oracle builds independently; the MO energies
@@ -96,3 +97,30 @@ def test_water512_mndo_trace(ctx):
         assert abs(rms - rrms) <= 1e-6 * rrms + 1e-12, (i, rms, rrms)
         assert abs(derr - rderr) <= 1e-6 * abs(rderr) + 1e-10, (i, derr, rderr)
         assert on == ron and dmp == rdmp, i
+
+
+def test_large_molecules_share_the_gpu(ctx):
+    """Alkanes above 400 basis functions in one batch with a small molecule:
+    the large ones split the SMs of each cooperative launch between them (N^3
+    shares, own barriers), the small one runs on the per-molecule kernels.
+    Every molecule against the oracle (energy, charges, iterations); one that
+    the reference's density DIIS does not converge must not converge here
+    either (both capped at 60 iterations)."""
+    scf = {**SCF, "max_iter": 60}
+    picks = [(3100004, 72), (3100000, 70), (3100005, 68)]   # N = 434 (converges), 422, 410
+    mols = [W.random_alkane(seed, n=n) for seed, n in picks] + [W.octane()]
+    res, charges = M.batch_scf("pm3", mols, M.SCFParams(**scf), context=ctx)
+    checked = 0
+    for m, r, q in zip(mols, res, charges):
+        try:
+            ref = O.scf(O.make_molecule("pm3", m.Z, m.xyz), O.SCFParams(**scf))
+        except O.NotConverged:
+            assert r["status"] != M.STATUS_CONVERGED
+            continue
+        checked += 1
+        assert r["status"] == M.STATUS_CONVERGED
+        assert abs(r["energy"] - ref.energy) < 1e-8
+        assert np.max(np.abs(q - ref.charges)) < 1e-6
+        assert r["iterations"] == ref.iterations
+    assert checked >= 2
+
