@@ -3,7 +3,7 @@
  * MolDS's ElectronicStructure (src/base/ElectronicStructure.h:23-53):
  * GetTheoryType, SetMolecule, DoSCF(requiresGuess), GetFockMatrix (eigenvector
  * rows), GetEnergiesMO, GetElectronicEnergy(0), GetCoreRepulsionEnergy,
- * GetVdWCorrectionEnergy.  Errors are thrown as MolDSException, a
+ * GetVdWCorrectionEnergy, OutputSCFResults.  Errors are thrown as MolDSException, a
  * std::domain_error like MolDS's (src/base/MolDSException.h:26-41), carrying
  * the C ABI's status code.  Header-only; link with -lnddo_gb300.
  *
@@ -118,6 +118,18 @@ class ElectronicStructure {
   // total, electronic, core dipole (x, y, z each) [a.u.]
   double const* GetDipoleMoments() const { Need(); return result_.dipole; }
   int GetTotalNumberAOs() const { return n_; }
+  // The SCF section of MolDS's output for the last DoSCF (the text
+  // Cndo2::DoSCF prints between its banners, src/cndo/Cndo2.cpp:585-729,
+  // with OutputSCFResults :1299-1303).
+  std::string OutputSCFResults() const {
+    Need();
+    std::size_t need = 0;
+    Check(nddo_scf_output_text(ctx_, nullptr, 0, &need));
+    std::string text(need, '\0');
+    Check(nddo_scf_output_text(ctx_, &text[0], need, &need));
+    text.resize(need > 0 ? need - 1 : 0);
+    return text;
+  }
 
  private:
   void Check(int rc) const {

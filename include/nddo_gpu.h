@@ -125,6 +125,28 @@ int nddo_get_dipole(nddo_ctx* ctx, double* out9);
  * MolDS's cartesianMatrix (Cndo2::CalcCartesianMatrixByGTOExpansion,
  * src/cndo/Cndo2.cpp:1946-2130).  Needs only a molecule. */
 int nddo_get_cartesian_matrix(nddo_ctx* ctx, double* out_3nn);
+/* The SCF section of MolDS's output for the last nddo_scf, as Cndo2::DoSCF
+ * prints it between its banners (src/cndo/Cndo2.cpp:585-729): the iteration
+ * log (:1505-1510), then OutputSCFResults (:1299-1303: MO energies, energies,
+ * dipoles, Mulliken charges; MNDO adds the heat of formation,
+ * src/mndo/Mndo.cpp:412-420) and the elapsed time; a non-converged SCF ends
+ * after the iteration log, where MolDS throws.  Writes at most cap - 1 chars
+ * and a terminating NUL into out (may be NULL); *needed = full length + 1. */
+int nddo_scf_output_text(nddo_ctx* ctx, char* out, size_t cap, size_t* needed);
+/* The same text from explicit values (no GPU needed): per iteration rms,
+ * diis_error, diis_on, damp_on (iterations entries); dipole = 9 doubles
+ * (total, electronic, core; x y z) or NULL for no dipole block;
+ * sum_pairs = n_sum_pairs (first, last) atom index pairs. */
+int nddo_format_scf_text(int theory, int n_atoms, const int* Z, int n_ao, int n_occ, int iterations,
+                         const double* rms, const double* diis_error, const int* diis_on, const int* damp_on,
+                         int converged, const double* eps, double energy, double core_repulsion, int vdw,
+                         double vdw_energy, const double* dipole, const double* charges, double heat_of_formation,
+                         int n_sum_pairs, const int* sum_pairs, double seconds, char* out, size_t cap,
+                         size_t* needed);
+/* The SCF option sum_charges (InputParser.cpp:694-700,
+ * Parameters::AddSumChargesIndexPairsSCF): n_pairs (first, last) atom index
+ * pairs whose Mulliken charges the output text sums (Cndo2.cpp:1203-1220). */
+int nddo_set_sum_charges(nddo_ctx* ctx, int n_pairs, const int* pairs);
 /* Per-iteration log of Cndo2::SatisfyConvergenceCriterion (Cndo2.cpp:1505-1510).
  * Returns the number of entries written (>= 0; compare it with max_entries,
  * not with the status codes) or a negative NDDO_ERR_* code. */

@@ -88,6 +88,13 @@ SIGNATURES = {
     "nddo_get_dipole": (ctypes.c_int, [_CTX, _DP]),
     "nddo_get_cartesian_matrix": (ctypes.c_int, [_CTX, _DP]),
     "nddo_get_trace": (ctypes.c_int, [_CTX, ctypes.c_int, _DP, _DP, _IP, _IP]),
+    "nddo_scf_output_text": (ctypes.c_int, [_CTX, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "nddo_format_scf_text": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _IP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            _DP, _DP, _IP, _IP, ctypes.c_int, _DP, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_int, ctypes.c_double, _DP, _DP, ctypes.c_double, ctypes.c_int,
+                                            _IP, ctypes.c_double, ctypes.c_char_p, ctypes.c_size_t,
+                                            ctypes.POINTER(ctypes.c_size_t)]),
+    "nddo_set_sum_charges": (ctypes.c_int, [_CTX, ctypes.c_int, _IP]),
     "nddo_get_pair_blocks": (ctypes.c_int, [_CTX, _DP, ctypes.POINTER(ctypes.c_size_t)]),
     "nddo_batch_scf": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, ctypes.POINTER(ScfParamsC),
                                       ctypes.POINTER(ScfResultC), _DP]),
@@ -256,7 +263,10 @@ class ElectronicStructure:
         self.molecule = Molecule(self.molecule.Z, x)
 
     def DoSCF(self, requiresGuess: bool = True, params: SCFParams | None = None):
-        p = to_c_params(params or self.params)
+        sp = params or self.params
+        pairs = np.ascontiguousarray(np.array(sp.sum_charges, dtype=np.int32).reshape(-1, 2))
+        self.ctx.check(self.ctx.lib.nddo_set_sum_charges(self.ctx.h, len(pairs), _ip(pairs) if len(pairs) else None))
+        p = to_c_params(sp)
         r = ScfResultC()
         rc = self.ctx.lib.nddo_scf(self.ctx.h, ctypes.byref(p), 1 if requiresGuess else 0, ctypes.byref(r))
         self.result = r
@@ -318,6 +328,16 @@ class ElectronicStructure:
         self.ctx.check(self.ctx.lib.nddo_get_pair_blocks(self.ctx.h, _dp(out), ctypes.byref(cnt)))
         return out
 
+    def OutputSCFResults(self) -> str:
+        """The SCF section of MolDS's output for the last DoSCF (the text
+        Cndo2::DoSCF prints between its banners, src/cndo/Cndo2.cpp:585-729,
+        with OutputSCFResults :1299-1303)."""
+        need = ctypes.c_size_t()
+        self.ctx.check(self.ctx.lib.nddo_scf_output_text(self.ctx.h, None, 0, ctypes.byref(need)))
+        buf = ctypes.create_string_buffer(need.value)
+        self.ctx.check(self.ctx.lib.nddo_scf_output_text(self.ctx.h, buf, need.value, ctypes.byref(need)))
+        return buf.value.decode()
+
     def GetTrace(self):
         n = self.result.iterations
         rms, de = np.zeros(n), np.zeros(n)
@@ -327,6 +347,34 @@ class ElectronicStructure:
         if k < 0:
             self.ctx.check(k)
         return [(i, float(rms[i]), float(de[i]), bool(on[i]), bool(dm[i])) for i in range(k)]
+
+
+def format_scf_text(theory, Z, eps, nocc, trace, energy, core_repulsion, charges, dipole=None, vdw=False,
+                    vdw_energy=0.0, heat_of_formation=0.0, converged=True, seconds=0.0, sum_charges=()) -> str:
+    """MolDS's SCF output section from explicit values (nddo_format_scf_text;
+    no GPU needed).  trace: [(iteration, rms, diis_error, diis_on, damping_on)]."""
+    L = load_library()
+    th = THEORIES[theory.lower()] if isinstance(theory, str) else int(theory)
+    Z = np.ascontiguousarray(Z, dtype=np.int32)
+    eps = np.ascontiguousarray(eps, dtype=np.float64)
+    q = np.ascontiguousarray(charges, dtype=np.float64)
+    rms = np.ascontiguousarray([t[1] for t in trace], dtype=np.float64)
+    de = np.ascontiguousarray([t[2] for t in trace], dtype=np.float64)
+    on = np.ascontiguousarray([int(t[3]) for t in trace], dtype=np.int32)
+    dm = np.ascontiguousarray([int(t[4]) for t in trace], dtype=np.int32)
+    dip = None if dipole is None else np.ascontiguousarray(np.ravel(dipole), dtype=np.float64)
+    sp = np.ascontiguousarray(np.ravel(np.array(sum_charges, dtype=np.int32).reshape(-1, 2)), dtype=np.int32)
+    args = (th, int(Z.size), _ip(Z), int(eps.size), int(nocc), len(trace), _dp(rms), _dp(de), _ip(on), _ip(dm),
+            int(bool(converged)), _dp(eps), float(energy), float(core_repulsion), int(bool(vdw)), float(vdw_energy),
+            None if dip is None else _dp(dip), _dp(q), float(heat_of_formation), int(sp.size // 2),
+            _ip(sp) if sp.size else None, float(seconds))
+    need = ctypes.c_size_t()
+    rc = L.nddo_format_scf_text(*args, None, 0, ctypes.byref(need))
+    if rc != 0:
+        raise NddoError(rc, "nddo_format_scf_text: invalid arguments")
+    buf = ctypes.create_string_buffer(need.value)
+    L.nddo_format_scf_text(*args, buf, need.value, ctypes.byref(need))
+    return buf.value.decode()
 
 
 class ElectronicStructureFactory:

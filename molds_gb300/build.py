@@ -19,7 +19,7 @@ LIB = os.path.join(BUILD, "libnddo_gb300.so")
 # host-only helper library: the alkane geometry generator of the workloads
 HOST_LIB = os.path.join(BUILD, "libworkloads.so")
 HOST_SOURCES = ["alkane_gen.c"]
-SOURCES = ["nddo_tables.cpp", "pair_fock.cu", "jacobi.cu", "tridiag.cu", "tridiag_grid.cu", "scf_kernels.cu", "engine.cu", "capi.cu", "noalloc.cu", "server.cu", "block_jacobi.cu", "tc_gemm.cu", "grouped.cu", "tuning.cpp"]
+SOURCES = ["nddo_tables.cpp", "pair_fock.cu", "jacobi.cu", "tridiag.cu", "tridiag_grid.cu", "scf_kernels.cu", "engine.cu", "capi.cu", "noalloc.cu", "server.cu", "block_jacobi.cu", "tc_gemm.cu", "grouped.cu", "tuning.cpp", "scf_text.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -2,6 +2,7 @@
 #include "../../include/nddo_gpu.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -10,6 +11,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "scf_text.h"
 #include "server.h"
 
 struct nddo_batch {
@@ -81,6 +83,10 @@ struct nddo_ctx {
   std::unique_ptr<nddo::Batch> mol;      // current molecule (SetMolecule / DoSCF API)
   nddo::ScfSettings last_settings;
   bool has_scf = false;
+  std::vector<int> Z;                    // elements of the current molecule (the output text)
+  int theory = 0;
+  double scf_seconds = 0.0;              // host wall time of the last nddo_scf
+  std::vector<int> sum_pairs;            // SCF option sum_charges (first, last atom index pairs)
   size_t budget = 0;
   std::string err;
 };
@@ -236,6 +242,8 @@ int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* Z, cons
       ctx->mol = std::move(b);
     }
     ctx->mol->integrals(std::vector<int>{0});
+    ctx->Z.assign(Z, Z + n_atoms);
+    ctx->theory = theory;
     return (int)NDDO_OK;
   });
 }
@@ -255,9 +263,11 @@ int nddo_scf(nddo_ctx* ctx, const nddo_scf_params* params, int requires_guess, n
       return fail(ctx, NDDO_ERR_ARGUMENT, "diis_num_error_vect other than 5 requires nddo_batch_scf");
     }
     if (!requires_guess && !ctx->has_scf) requires_guess = 1;
+    const auto t0 = std::chrono::steady_clock::now();
     ctx->mol->scf(s, requires_guess != 0);
     std::vector<nddo::MolResult> r;
     ctx->mol->results(&r);
+    ctx->scf_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     ctx->last_settings = s;
     ctx->has_scf = true;
     if (result) {
@@ -332,6 +342,121 @@ int nddo_get_core_hamiltonian(nddo_ctx* ctx, double* out) {
     ctx->mol->copy_matrix(0, 0, out);
     return (int)NDDO_OK;
   });
+}
+
+namespace {
+int copy_text(const std::string& text, char* out, size_t cap, size_t* needed) {
+  if (needed) *needed = text.size() + 1;
+  if (out && cap > 0) {
+    const size_t n = std::min(cap - 1, text.size());
+    std::memcpy(out, text.data(), n);
+    out[n] = '\0';
+  }
+  return (int)NDDO_OK;
+}
+}  // namespace
+
+int nddo_scf_output_text(nddo_ctx* ctx, char* out, size_t cap, size_t* needed) {
+  return guarded(ctx, [&]() {
+    if (!ctx->mol || !ctx->has_scf) return fail(ctx, NDDO_ERR_STATE, "no SCF result");
+    std::vector<nddo::TraceEntry> tr;
+    ctx->mol->copy_trace(0, &tr);
+    std::vector<nddo::MolResult> r;
+    ctx->mol->results(&r);
+    const int its = std::min<int>((int)tr.size(), r[0].iterations);
+    std::vector<double> rms(its), derr(its);
+    std::vector<int> on(its), damp(its);
+    for (int i = 0; i < its; ++i) {
+      rms[i] = tr[i].rms;
+      derr[i] = tr[i].diis_err;
+      on[i] = tr[i].diis_on;
+      damp[i] = tr[i].damp_on;
+    }
+    const int n = ctx->mol->nao(0);
+    std::vector<double> eps(n), q(ctx->Z.size());
+    ctx->mol->copy_eps(0, eps.data());
+    ctx->mol->copy_charges(0, q.data());
+    int nelec = 0;
+    for (int z : ctx->Z) {
+      const int e = nddo_element_index(z);
+      nelec += e < 0 ? 0 : nddo_elements[e].core_charge;
+    }
+    nddo::ScfText t;
+    t.theory = ctx->theory;
+    t.n_atoms = (int)ctx->Z.size();
+    t.Z = ctx->Z.data();
+    t.n_ao = n;
+    t.nocc = nelec / 2;
+    t.iterations = its;
+    t.rms = rms.data();
+    t.diis_error = derr.data();
+    t.diis_on = on.data();
+    t.damp_on = damp.data();
+    t.converged = r[0].status == nddo::kConverged;
+    t.eps = eps.data();
+    t.energy = r[0].energy;
+    t.core_repulsion = r[0].core_repulsion;
+    t.vdw = ctx->last_settings.vdw || ctx->theory == NDDO_THEORY_AM1D || ctx->theory == NDDO_THEORY_PM3D;
+    t.vdw_energy = r[0].vdw_energy;
+    t.dipole = ctx->last_settings.dipole ? r[0].dipole : nullptr;
+    t.charges = q.data();
+    t.heat_of_formation = r[0].heat_of_formation;
+    t.seconds = ctx->scf_seconds;
+    t.n_sum = (int)ctx->sum_pairs.size() / 2;
+    t.sum_pairs = ctx->sum_pairs.data();
+    return copy_text(nddo::format_scf_text(t), out, cap, needed);
+  });
+}
+
+int nddo_set_sum_charges(nddo_ctx* ctx, int n_pairs, const int* pairs) {
+  return guarded(ctx, [&]() {
+    if (n_pairs < 0 || (n_pairs > 0 && !pairs)) return fail(ctx, NDDO_ERR_ARGUMENT, "invalid sum_charges pairs");
+    for (int i = 0; i < n_pairs; ++i)
+      if (pairs[2 * i] < 0 || pairs[2 * i + 1] < pairs[2 * i])
+        return fail(ctx, NDDO_ERR_ARGUMENT, "sum_charges needs 0 <= first <= last");
+    ctx->sum_pairs.assign(pairs, pairs + 2 * (size_t)n_pairs);
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_format_scf_text(int theory, int n_atoms, const int* Z, int n_ao, int n_occ, int iterations,
+                         const double* rms, const double* diis_error, const int* diis_on, const int* damp_on,
+                         int converged, const double* eps, double energy, double core_repulsion, int vdw,
+                         double vdw_energy, const double* dipole, const double* charges, double heat_of_formation,
+                         int n_sum_pairs, const int* sum_pairs, double seconds, char* out, size_t cap,
+                         size_t* needed) {
+  try {
+    if (n_sum_pairs < 0 || (n_sum_pairs > 0 && !sum_pairs)) return NDDO_ERR_ARGUMENT;
+    if (n_atoms < 1 || !Z || n_ao < 1 || iterations < 0 || (iterations > 0 && (!rms || !diis_error || !diis_on || !damp_on)) ||
+        (converged && (!eps || !charges)))
+      return NDDO_ERR_ARGUMENT;
+    nddo::ScfText t;
+    t.theory = theory;
+    t.n_atoms = n_atoms;
+    t.Z = Z;
+    t.n_ao = n_ao;
+    t.nocc = n_occ;
+    t.iterations = iterations;
+    t.rms = rms;
+    t.diis_error = diis_error;
+    t.diis_on = diis_on;
+    t.damp_on = damp_on;
+    t.converged = converged;
+    t.eps = eps;
+    t.energy = energy;
+    t.core_repulsion = core_repulsion;
+    t.vdw = vdw;
+    t.vdw_energy = vdw_energy;
+    t.dipole = dipole;
+    t.charges = charges;
+    t.heat_of_formation = heat_of_formation;
+    t.seconds = seconds;
+    t.n_sum = n_sum_pairs;
+    t.sum_pairs = sum_pairs;
+    return copy_text(nddo::format_scf_text(t), out, cap, needed);
+  } catch (...) {
+    return NDDO_ERR_ARGUMENT;
+  }
 }
 
 int nddo_get_trace(nddo_ctx* ctx, int max_entries, double* rms, double* derr, int* on, int* damp) {

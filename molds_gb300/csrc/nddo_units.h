@@ -16,6 +16,7 @@
 #define NDDO_EV2AU   0.03674903
 #define NDDO_ANG2AU  (1.0 / 0.5291772)
 #define NDDO_KCAL2AU 0.00159360175
+#define NDDO_DEBYE2AU 0.393430191
 
 /* Everything a pair or Fock kernel needs about one atom, in atomic units. */
 typedef struct {

@@ -43,6 +43,7 @@ class SCFParams:
     vdw_d: float = 23.0              # vdW_d (src/base/Parameters.cpp:142)
     dipole: bool = True              # dipole moment after convergence, as DoSCF (not a MolDS key)
     eigensolver: str = "auto"        # FP64 eigensolves: "auto" / "householder" or "jacobi" (not a MolDS key)
+    sum_charges: tuple = ()          # sum_charges first last (src/base/InputParser.cpp:694-700): ((first, last), ...)
 
 
 @dataclass
@@ -123,6 +124,13 @@ def parse(text: str) -> InputFile:
                 elif key == "vdw":                 # src/base/InputParser.cpp:684-693
                     scf.vdw = need(i + 1) == "yes"
                     i += 2
+                elif key == "sum_charges":         # src/base/InputParser.cpp:694-700
+                    try:
+                        pair = (int(need(i + 1)), int(need(i + 2)))
+                    except ValueError as e:
+                        raise InputError("sum_charges needs two atom indices") from e
+                    scf.sum_charges = tuple(scf.sum_charges) + (pair,)
+                    i += 3
                 elif key in ("mpi", "scalapack"):
                     i += 2
                 else:

@@ -59,6 +59,8 @@ int main(int argc, char** argv) {
     } catch (const molds_gb300::MolDSException& e) {
       std::printf("excited_state_error %d\n", e.Code());
     }
+    // MolDS's SCF section, last: everything after the marker line is the text
+    std::printf("scf_text\n%s", es.OutputSCFResults().c_str());
     return 0;
   } catch (const molds_gb300::MolDSException& e) {
     std::printf("error %d %s\n", e.Code(), e.what());

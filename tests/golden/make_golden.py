@@ -28,6 +28,15 @@ EXTRA = ["h2o_pm3_freq_num_proj_s1", "c2h4_pm3_freq_num_proj", "c2h6-nh3-cluster
 EXTRA += ["h2o-dimer_am1d_ehrenfest", "h2o-dimer_pm3d_opt_bfgs_space_fixed"]
 
 
+def scf_text(text):
+    """The first SCF section as printed: from its start banner to its done
+    banner (inclusive)."""
+    m = re.search(r"\*{10}  START: [^\n]*-SCF  \*{10}\n", text)
+    b = text.find("**********  DONE: ", m.start())
+    b = text.find("\n", b)
+    return text[m.start():b + 1]
+
+
 def parse_dat(text, natoms):
     """Values of the first SCF block (frequency runs print several)."""
     start = text.find("-SCF  **********")
@@ -49,7 +58,7 @@ def parse_dat(text, natoms):
         m = re.search(label + r"\t+(\S+)\t(\S+)\t(\S+)", body)
         dip.append([float(m.group(i)) for i in (1, 2, 3)])
     out = {"trace": trace, "mo_energies": mo, "energy": e, "core_repulsion": ec,
-           "mulliken": q, "dipole": dip}
+           "mulliken": q, "dipole": dip, "scf_text": scf_text(text)}
     vdw = re.search(r"Empirical van der Waals correction:\t(\S+)", body)
     if vdw:
         out["vdw_energy"] = float(vdw.group(1))

@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from scf_text_compare import compare_scf_text
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -46,6 +47,8 @@ def _args(p):
 
 def _parse(out):
     vals = {}
+    out, _, text = out.partition("scf_text\n")
+    vals["scf_text"] = [text]
     for line in out.splitlines():
         k, v = line.split(" ", 1)
         vals.setdefault(k, []).append(v)
@@ -84,3 +87,5 @@ def test_cpp_host_matches_oracle(tmp_path, name):
     assert abs(float(v["homo"][0]) - ref.eps[0]) < 1e-7
     assert np.max(np.abs(np.array([float(x) for x in v["dipole"]]) - ref.dipole[0])) < 1e-6
     assert int(v["excited_state_error"][0]) == -1
+    # MolDS's SCF output text, against the reference's own output file
+    assert not compare_scf_text(v["scf_text"][0], case["scf_text"], skip_iterations=p.rms_density < 1e-12)

@@ -8,7 +8,9 @@ Bars (from the reference's own correctness targets):
     times a bohr; the STO-6G Cartesian matrix: 1e-11 relative to its largest
     element
 """
+import ctypes
 import json
+import re
 import os
 
 import numpy as np
@@ -17,6 +19,7 @@ import pytest
 import molds_gb300 as M
 from molds_gb300 import workloads as W
 from oracle import oracle as O
+from scf_text_compare import compare_scf_text
 
 pytestmark = pytest.mark.gpu
 
@@ -142,6 +145,15 @@ def test_reference_fixtures_fp64(ctx, case):
             assert on == ron
     if mol.theory == 0:
         assert abs(es.GetHeatsFormation() - ref.heat_of_formation) < E_TOL_FP64
+    # MolDS's SCF output text from the GPU results, against the reference's own
+    # output file (the SCF section of the .dat, line by line)
+    scf_block = re.search(r"(?is)^\s*scf\s*$(.*?)^\s*scf_end", case["input"], re.M).group(1)
+    sums = [(int(a), int(b)) for a, b in re.findall(r"(?i)sum_charges\s+(\d+)\s+(\d+)", scf_block)]
+    if sums:
+        es.ctx.check(es.ctx.lib.nddo_set_sum_charges(es.ctx.h, len(sums), np.ascontiguousarray(
+            np.array(sums, dtype=np.int32).ravel()).ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+    bad = compare_scf_text(es.OutputSCFResults(), case["scf_text"], skip_iterations=p.rms_density < 1e-12)
+    assert not bad, "\n".join(bad[:10])
 
 
 def test_density_and_eigenvectors_fp64(ctx):
