@@ -118,6 +118,14 @@ class ElectronicStructure {
   // total, electronic, core dipole (x, y, z each) [a.u.]
   double const* GetDipoleMoments() const { Need(); return result_.dipole; }
   int GetTotalNumberAOs() const { return n_; }
+  // Forces -dE/dR on the atoms [Hartree/bohr], n_atoms x 3 row-major, of the
+  // last converged SCF (MolDS GetForce after CalcForce, src/mndo/Mndo.cpp:2711-2986).
+  std::vector<double> GetForce() const {
+    Need();
+    std::vector<double> f(3 * molecule_->atomicNumbers.size());
+    Check(nddo_get_forces(ctx_, f.data()));
+    return f;
+  }
   // The SCF section of MolDS's output for the last DoSCF (the text
   // Cndo2::DoSCF prints between its banners, src/cndo/Cndo2.cpp:585-729,
   // with OutputSCFResults :1299-1303).

@@ -143,6 +143,13 @@ int nddo_format_scf_text(int theory, int n_atoms, const int* Z, int n_ao, int n_
                          double vdw_energy, const double* dipole, const double* charges, double heat_of_formation,
                          int n_sum_pairs, const int* sum_pairs, double seconds, char* out, size_t cap,
                          size_t* needed);
+/* Forces on the atoms (-dE/dR, Hartree/bohr, n_atoms x 3 row-major) of the
+ * last converged SCF, ground state: Mndo::CalcForce
+ * (src/mndo/Mndo.cpp:2711-2986) as read by ElectronicStructure::GetForce.
+ * Analytic: the pair terms of the energy (two-centre integrals, electron-core
+ * attractions, resonance, core-core, dispersion) differentiated exactly with
+ * the converged density held fixed. */
+int nddo_get_forces(nddo_ctx* ctx, double* out_natoms_x3);
 /* The SCF option sum_charges (InputParser.cpp:694-700,
  * Parameters::AddSumChargesIndexPairsSCF): n_pairs (first, last) atom index
  * pairs whose Mulliken charges the output text sums (Cndo2.cpp:1203-1220). */
@@ -188,6 +195,11 @@ int nddo_batch_results(nddo_batch* b, nddo_scf_result* results, double* charges)
 /* Density P (which 0) or eigenvector rows C (which 1) of molecule m of the
  * batch after nddo_batch_run: n_ao(m) x n_ao(m) doubles, row-major. */
 int nddo_batch_get_matrix(nddo_batch* b, int which, int m, double* out);
+/* Forces (Hartree/bohr, n_atoms x 3) of molecule m of a resident batch after
+ * nddo_batch_run / nddo_batch_run_ex (as nddo_get_forces): the force callers
+ * of MolDS's MD / RPMD drivers for the batch's molecules (src/md/MD.cpp:108-113,
+ * src/rpmd/RPMD.cpp). */
+int nddo_batch_get_forces(nddo_batch* h, int m, double* out_natoms_x3);
 size_t nddo_batch_device_bytes(const nddo_batch* b);
 void nddo_batch_destroy(nddo_batch* b);
 /* Per-kernel-class CUDA-event timing on the launching stream: after enabling,

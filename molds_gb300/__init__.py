@@ -95,6 +95,8 @@ SIGNATURES = {
                                             _IP, ctypes.c_double, ctypes.c_char_p, ctypes.c_size_t,
                                             ctypes.POINTER(ctypes.c_size_t)]),
     "nddo_set_sum_charges": (ctypes.c_int, [_CTX, ctypes.c_int, _IP]),
+    "nddo_get_forces": (ctypes.c_int, [_CTX, _DP]),
+    "nddo_batch_get_forces": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _DP]),
     "nddo_get_pair_blocks": (ctypes.c_int, [_CTX, _DP, ctypes.POINTER(ctypes.c_size_t)]),
     "nddo_batch_scf": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, ctypes.POINTER(ScfParamsC),
                                       ctypes.POINTER(ScfResultC), _DP]),
@@ -328,6 +330,12 @@ class ElectronicStructure:
         self.ctx.check(self.ctx.lib.nddo_get_pair_blocks(self.ctx.h, _dp(out), ctypes.byref(cnt)))
         return out
 
+    def GetForce(self) -> np.ndarray:
+        """Forces -dE/dR on the atoms (n_atoms, 3) [Hartree/bohr] of the last
+        converged SCF (Mndo::CalcForce, src/mndo/Mndo.cpp:2711-2986; ground
+        state), analytic."""
+        return self._vec(self.ctx.lib.nddo_get_forces, 3 * self.molecule.natoms).reshape(-1, 3)
+
     def OutputSCFResults(self) -> str:
         """The SCF section of MolDS's output for the last DoSCF (the text
         Cndo2::DoSCF prints between its banners, src/cndo/Cndo2.cpp:585-729,
@@ -453,6 +461,12 @@ class ResidentBatch:
 
     def device_bytes(self) -> int:
         return int(self.ctx.lib.nddo_batch_device_bytes(self.h))
+
+    def forces(self, m: int) -> np.ndarray:
+        """Analytic forces (n_atoms, 3) [Hartree/bohr] of molecule m after run()."""
+        out = np.zeros((int(self.nat[m]), 3))
+        self.ctx.check(self.ctx.lib.nddo_batch_get_forces(self.h, m, _dp(out)))
+        return out
 
     def density(self, m: int, nao: int) -> np.ndarray:
         out = np.zeros((nao, nao))

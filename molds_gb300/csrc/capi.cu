@@ -20,6 +20,7 @@ struct nddo_batch {
   std::vector<int> n_atoms;
   bool dipole = false;          // the last nddo_batch_run computed dipole moments
   bool ran = false;             // a run completed: every molecule has a density to start from
+  nddo::ScfSettings last;       // settings of the last run (the forces' dispersion term)
 };
 
 namespace {
@@ -408,6 +409,18 @@ int nddo_scf_output_text(nddo_ctx* ctx, char* out, size_t cap, size_t* needed) {
   });
 }
 
+int nddo_get_forces(nddo_ctx* ctx, double* out) {
+  return guarded(ctx, [&]() {
+    if (!ctx->mol || !ctx->has_scf) return fail(ctx, NDDO_ERR_STATE, "no SCF result");
+    if (!out) return fail(ctx, NDDO_ERR_ARGUMENT, "null output buffer");
+    std::vector<nddo::MolResult> r;
+    ctx->mol->results(&r);
+    if (r[0].status != nddo::kConverged) return fail(ctx, NDDO_ERR_STATE, "forces need a converged SCF");
+    ctx->mol->forces(ctx->last_settings, 0, out);
+    return (int)NDDO_OK;
+  });
+}
+
 int nddo_set_sum_charges(nddo_ctx* ctx, int n_pairs, const int* pairs) {
   return guarded(ctx, [&]() {
     if (n_pairs < 0 || (n_pairs > 0 && !pairs)) return fail(ctx, NDDO_ERR_ARGUMENT, "invalid sum_charges pairs");
@@ -596,6 +609,7 @@ int nddo_batch_run_ex(nddo_batch* h, const nddo_scf_params* params, int requires
     h->b->run(s, guess);
     h->ran = true;
     h->dipole = s.dipole != 0;
+    h->last = s;
     return (int)NDDO_OK;
   });
 }
@@ -644,6 +658,19 @@ int nddo_batch_get_matrix(nddo_batch* h, int which, int m, double* out) {
     if (!out || m < 0 || m >= h->b->size() || (which != 0 && which != 1))
       return fail(h->ctx, NDDO_ERR_ARGUMENT, "bad matrix request");
     h->b->copy_matrix(which == 0 ? 2 : 3, m, out);
+    return (int)NDDO_OK;
+  });
+}
+
+int nddo_batch_get_forces(nddo_batch* h, int m, double* out) {
+  if (!h) return NDDO_ERR_ARGUMENT;
+  return guarded(h->ctx, [&]() -> int {
+    if (!out || m < 0 || m >= h->b->size()) return fail(h->ctx, NDDO_ERR_ARGUMENT, "bad forces request");
+    if (!h->ran) return fail(h->ctx, NDDO_ERR_STATE, "no SCF result");
+    std::vector<nddo::MolResult> r;
+    h->b->results(&r);
+    if (r[m].status != nddo::kConverged) return fail(h->ctx, NDDO_ERR_STATE, "forces need a converged SCF");
+    h->b->forces(h->last, m, out);
     return (int)NDDO_OK;
   });
 }

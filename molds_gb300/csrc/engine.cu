@@ -470,7 +470,7 @@ Batch::~Batch() {
   for (void* p : ptrs) if (p) cudaFree(p);
   for (int i = 0; i < 6; ++i) if (d_S[i]) cudaFree(d_S[i]);
   if (d_td) cudaFree(d_td);
-  void* hh[] = {d_hh_small_, d_hh_large_, d_gridmap_, d_gridbar_};
+  void* hh[] = {d_hh_small_, d_hh_large_, d_gridmap_, d_gridbar_, d_pgrad_, d_forces_};
   for (void* p : hh) if (p) cudaFree(p);
   if (h_gridmap_) cudaFreeHost(h_gridmap_);
 }
@@ -1328,6 +1328,32 @@ void Batch::copy_charges(int m, double* host) const {
   const DevMol& d = h_mols[m];
   cuda_check(cudaMemcpyAsync(host, d_charges + d.atom0, d.natoms * sizeof(double), cudaMemcpyDeviceToHost, stream_), "copy charges");
   cuda_check(cudaStreamSynchronize(stream_), "copy charges");
+}
+
+void Batch::forces(const ScfSettings& s, int m, double* host) {
+  const DevMol& d = h_mols[m];
+  if (3LL * d.npairs > pgrad_cap_) {
+    if (d_pgrad_) cudaFree(d_pgrad_);
+    d_pgrad_ = nullptr;
+    pgrad_cap_ = std::max(3LL * d.npairs, 3LL);
+    cuda_check(cudaMalloc(&d_pgrad_, pgrad_cap_ * sizeof(double)), "cudaMalloc pair gradients");
+  }
+  if (3LL * d.natoms > forces_cap_) {
+    if (d_forces_) cudaFree(d_forces_);
+    d_forces_ = nullptr;
+    forces_cap_ = 3LL * d.natoms;
+    cuda_check(cudaMalloc(&d_forces_, forces_cap_ * sizeof(double)), "cudaMalloc forces");
+  }
+  VdwParams vdw;
+  vdw.on = s.vdw;
+  vdw.s6 = s.vdw_s6;
+  vdw.d = s.vdw_d;
+  launch_forces(d_atoms, d_pairs, d_mols, m, d.pair0, d.npairs, d.natoms, eng_->eri(), eng_->ovt(), d_P, vdw,
+                d_pgrad_, d_forces_, stream_);
+  cuda_check(cudaGetLastError(), "forces");
+  cuda_check(cudaMemcpyAsync(host, d_forces_, 3 * (size_t)d.natoms * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+             "copy forces");
+  cuda_check(cudaStreamSynchronize(stream_), "forces");
 }
 
 void Batch::copy_blocks(int m, double* host, size_t* count) const {

@@ -134,6 +134,8 @@ class Batch {
   void copy_matrix(int which_matrix, int m, double* host) const;   // 0 H, 1 F, 2 P, 3 C
   void copy_eps(int m, double* host) const;
   void copy_charges(int m, double* host) const;
+  // analytic forces (Hartree/bohr, natoms x 3) of molecule m's converged SCF
+  void forces(const ScfSettings& s, int m, double* host);
   void copy_blocks(int m, double* host, size_t* count) const;
   void copy_trace(int m, std::vector<TraceEntry>* out) const;
   // STO-6G Cartesian matrix <mu| r_k |nu> of molecule m, 3 x N x N doubles (synchronises)
@@ -222,6 +224,9 @@ class Batch {
   int* d_gridmap_ = nullptr;             // per CTA: list entry, CTA in the sub-grid, sub-grid size
   int* h_gridmap_ = nullptr;             // pinned staging of d_gridmap_
   unsigned* d_gridbar_ = nullptr;        // barrier words, 4 per molecule of a chunk
+  double* d_pgrad_ = nullptr;            // pair gradients of forces() (grown on demand)
+  double* d_forces_ = nullptr;
+  long long pgrad_cap_ = 0, forces_cap_ = 0;
   float *d_jA32 = nullptr, *d_jV32 = nullptr;
   void* d_bj_ws = nullptr;               // block-Jacobi workspace (bases above kSmallJacobiMaxN)
   int* h_bj_pending = nullptr;           // pinned: molecules still rotating after a block-Jacobi sweep
@@ -304,6 +309,7 @@ class GroupedBatch {
   void copy_charges(int m, double* host) const;
   void copy_matrix(int which_matrix, int m, double* host) const;
   void cartesian_matrix(int m, double* host) const;
+  void forces(const ScfSettings& s, int m, double* host);   // analytic forces of molecule m (natoms x 3)
   void set_coordinates(const double* xyz);
   size_t device_bytes() const;
   long long launches() const;

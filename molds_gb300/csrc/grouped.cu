@@ -105,6 +105,13 @@ void GroupedBatch::copy_charges(int m, double* host) const {
   b.copy_charges(l, host);
 }
 
+void GroupedBatch::forces(const ScfSettings& s, int m, double* host) {
+  int l = 0;
+  const Batch& b = locate(m, &l);
+  for (auto& g : g_)
+    if (g.get() == &b) { g->forces(s, l, host); return; }
+}
+
 void GroupedBatch::copy_matrix(int which, int m, double* host) const {
   int l = 0;
   const Batch& b = locate(m, &l);

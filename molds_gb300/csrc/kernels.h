@@ -86,6 +86,11 @@ struct VdwParams {
   int on;
   double s6, d;
 };
+// analytic forces (Hartree/bohr) of molecule m from its converged density P:
+// pair gradients into grad (3 per pair), then forces (3 per atom)
+void launch_forces(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, int m, long long pair0,
+                   long long npairs, int natoms, const EriTable* eri, const OverlapTable* ovt, const double* P,
+                   VdwParams vdw, double* grad, double* forces, cudaStream_t s);
 void launch_energy_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
                           int nlist, const double* P, const double* F, const double* H, MolState* st,
                           double* charges, VdwParams vdw, cudaStream_t s);

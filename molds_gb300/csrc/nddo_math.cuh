@@ -157,8 +157,8 @@ __host__ __device__ inline void aux_a_all(T p, int kmax, T* a) {
 // damps errors by |q|/k per step.  For |q| > 4: the upward recurrence
 // B_k = (k B_{k-1} + (-1)^k e^q - e^-q) / q from B_0 = (e^q - e^-q) / q, whose
 // error growth k/|q| per step stays below 11!/4^11 overall.  inv[j] = 1/j.
-template <typename T>
-__host__ __device__ inline void aux_b_all(T q, int kmax, T* b, const T* inv) {
+template <typename T, typename IT>
+__host__ __device__ inline void aux_b_all(T q, int kmax, T* b, const IT* inv) {
   const T ep = exp(q), em = exp(-q);
   if (fabs(q) <= (T)4) {
     T term = 1, sum = 0;

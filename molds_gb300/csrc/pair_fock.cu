@@ -28,6 +28,7 @@
 #include <cmath>
 #include "nddo_batch.cuh"
 #include "kernels.h"
+#include "nddo_dual.cuh"
 
 namespace nddo {
 
@@ -54,9 +55,10 @@ constexpr int kPairWarps = 4;
 
 // E_AB of MNDO (Mndo.cpp:223-240, 319-327) plus the AM1/PM3 Gaussians
 // (Am1.cpp:145-170); ssss = (s_A s_A | s_B s_B).
-__device__ __forceinline__ double core_core(const nddo_atom_params& pa, const nddo_atom_params& pb, double R,
-                                            double ssss, int theory) {
-  double f;
+template <typename T>
+__device__ __forceinline__ T core_core(const nddo_atom_params& pa, const nddo_atom_params& pb, T R, T ssss,
+                                       int theory) {
+  T f;
   const bool a_no = (pa.atomic_number == 7 || pa.atomic_number == 8);
   const bool b_no = (pb.atomic_number == 7 || pb.atomic_number == 8);
   if (pa.atomic_number == 1 && b_no)
@@ -65,22 +67,22 @@ __device__ __forceinline__ double core_core(const nddo_atom_params& pa, const nd
     f = 1.0 + (R / NDDO_ANG2AU) * exp(-pa.alpha * R) + exp(-pb.alpha * R);
   else
     f = 1.0 + exp(-pa.alpha * R) + exp(-pb.alpha * R);
-  double e = pa.core_charge * pb.core_charge * ssss * f;
+  T e = (double)(pa.core_charge * pb.core_charge) * ssss * f;
   if (theory != NDDO_MNDO) {
-    double t = 0.0;
+    T t = 0.0;
     for (int i = 0; i < 4; ++i) {
-      if (pa.gk[i] != 0.0) { const double d = R - pa.gm[i]; t += pa.gk[i] * exp(-pa.gl[i] * (d * d)); }
-      if (pb.gk[i] != 0.0) { const double d = R - pb.gm[i]; t += pb.gk[i] * exp(-pb.gl[i] * (d * d)); }
+      if (pa.gk[i] != 0.0) { const T d = R - pa.gm[i]; t += pa.gk[i] * exp(-pa.gl[i] * (d * d)); }
+      if (pb.gk[i] != 0.0) { const T d = R - pb.gm[i]; t += pb.gk[i] * exp(-pb.gl[i] * (d * d)); }
     }
-    e += pa.core_charge * pb.core_charge * t * NDDO_ANG2AU / R;
+    e += (double)(pa.core_charge * pb.core_charge) * t * NDDO_ANG2AU / R;
   }
   if (theory == NDDO_PM3PDDG) {
     // PDDG term (Pm3Pddg.cpp:143-165, 239-245); n = valence electrons = core charge
     const double na = pa.core_charge, nb = pb.core_charge;
-    double t = 0.0;
+    T t = 0.0;
     for (int i = 0; i < 2; ++i)
       for (int k = 0; k < 2; ++k) {
-        const double x = R - pa.pddg_da[i] - pb.pddg_da[k];
+        const T x = R - pa.pddg_da[i] - pb.pddg_da[k];
         t += (na * pa.pddg_pa[i] + nb * pb.pddg_pa[k]) * exp(-10.0 / (NDDO_ANG2AU * NDDO_ANG2AU) * (x * x));
       }
     e += t / (na + nb);
@@ -90,19 +92,20 @@ __device__ __forceinline__ double core_core(const nddo_atom_params& pa, const nd
 
 // One overlap combination of the pair in the diatomic frame (thread-level):
 // norm * ang * (R/2)^(na+nb+1) * sum_t c_t A_i(p) B_j(q).
-__device__ __forceinline__ double overlap_combo(const OverlapTable* __restrict__ ovt, int na, int nb, int c,
-                                                double za, double zb, double norm, double R) {
+template <typename T>
+__device__ __forceinline__ T overlap_combo(const OverlapTable* __restrict__ ovt, int na, int nb, int c, double za,
+                                           double zb, double norm, T R) {
   const int km = ovt->kmax[na - 1][nb - 1][c];
-  double a[12], b[12];
+  T a[12], b[12];
   aux_a_all(0.5 * R * (za + zb), km, a);
   aux_b_all(0.5 * R * (za - zb), km, b, c_inv);
-  double s = 0.0;
+  T s = 0.0;
   const int nt = ovt->nterms[na - 1][nb - 1][c];
   for (int t = 0; t < nt; ++t)
     s += ovt->tc[na - 1][nb - 1][c][t] * a[ovt->ti[na - 1][nb - 1][c][t]] * b[ovt->tj[na - 1][nb - 1][c][t]];
-  double rp = 1.0;
+  T rp = 1.0;
   for (int i = 0; i < na + nb + 1; ++i) rp *= 0.5 * R;
-  return norm * ovt->ang[c] * rp * s;
+  return (norm * ovt->ang[c]) * rp * s;
 }
 
 __device__ __forceinline__ double slot_value(const EriTable* __restrict__ eri, int slot, double R,
@@ -1086,6 +1089,232 @@ void launch_cartesian_matrix(const DevAtom* atoms, const DevPair* pairs, const D
   const long long items = (long long)natoms + (long long)natoms * (natoms - 1) / 2;
   const int blocks = (int)std::max(1LL, std::min<long long>(4096, (items + kDipThreads - 1) / kDipThreads));
   cartesian_matrix_kernel<<<blocks, kDipThreads, 0, s>>>(atoms, pairs, mols, m, X);
+}
+
+// ---------------------------------------------------------------------------
+// Analytic energy gradient (forces) of a converged SCF, for the molecules of
+// a list (Mndo::CalcForce, src/mndo/Mndo.cpp:2711-2986, ground state).
+//
+// With the density P fixed at convergence (the SCF energy is stationary in
+// the orbitals and NDDO has no basis-overlap terms) the energy depends on the
+// geometry only through the pair terms, each a function of the pair's
+// relative position d = R_B - R_A:
+//   E_AB = sum_PQ C_PQ W_PQ(d) + sum_{mu in A, la in B} P_mu,la (beta_mu + beta_la) S_mu,la(d)
+//          + E_core(d) [+ E_vdW(d)]
+// with W = T2 L T2^T the rotated (mu nu|la si) block, C_PQ = m_P m_Q P_P P_Q
+// - 1/2 X_PQ (Coulomb and exchange, m = 2 for mu != nu, X summed over both
+// orbital orders) plus the electron-core attractions -Z_B (mu nu|s_B s_B) on
+// the (mu nu, ss) column and -Z_A on the (ss, la si) row.  One thread per
+// pair evaluates E_AB in dual numbers seeded with d (the exact derivatives of
+// the same local integrals, rotation and overlaps the pair kernels use), and
+// writes dE_AB/dd; the gradient of atom i is then
+//   g_i = sum_{a < i} dE_ai/dd - sum_{b > i} dE_ib/dd   (fixed order).
+// The local frame here is z along d and x from the coordinate axis least
+// aligned with it (smooth in d near every axis); the rotated integrals do not
+// depend on the azimuth of the frame (the local integrals are cylindrically
+// symmetric), so they equal the pair kernels' values.
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ void smooth_frame(const Dual3& x, const Dual3& y, const Dual3& z, Dual3 Rm[4][4]) {
+  const Dual3 r = sqrt(x * x + y * y + z * z);
+  const Dual3 ez[3] = {x / r, y / r, z / r};
+  int k = 0;
+  for (int i = 1; i < 3; ++i)
+    if (::fabs(ez[i].v) < ::fabs(ez[k].v)) k = i;
+  Dual3 ex[3] = {-ez[k] * ez[0], -ez[k] * ez[1], -ez[k] * ez[2]};
+  ex[k] += 1.0;
+  const Dual3 nx = sqrt(ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2]);
+  for (int i = 0; i < 3; ++i) ex[i] /= nx;
+  const Dual3 ey[3] = {ez[1] * ex[2] - ez[2] * ex[1], ez[2] * ex[0] - ez[0] * ex[2], ez[0] * ex[1] - ez[1] * ex[0]};
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) Rm[i][j] = 0.0;
+  Rm[0][0] = 1.0;
+  // rows: space-frame orbitals s, py, pz, px; columns: local s, y, z, x
+  const int comp[4] = {-1, 1, 2, 0};
+  for (int row = 1; row < 4; ++row) {
+    Rm[row][1] = ey[comp[row]];
+    Rm[row][2] = ez[comp[row]];
+    Rm[row][3] = ex[comp[row]];
+  }
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(64)
+pair_grad_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs, long long pair0,
+                 long long npairs, const DevMol* __restrict__ mols, const EriTable* __restrict__ eri,
+                 const OverlapTable* __restrict__ ovt, const double* __restrict__ P, VdwParams vdw,
+                 double* __restrict__ grad) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npairs) return;
+  const long long p = pair0 + t;
+  const DevPair pr = pairs[p];
+  const DevAtom A = atoms[pr.a], B = atoms[pr.b];
+  const DevMol mol = mols[pr.mol];
+  const nddo_atom_params& pa = c_params[A.pidx];
+  const nddo_atom_params& pb = c_params[B.pidx];
+  const int nA = A.nao, nB = B.nao, dA = nA == 4 ? 10 : 1, dB = nB == 4 ? 10 : 1;
+  const Dual3 dx(B.x - A.x, 1.0, 0.0, 0.0), dy(B.y - A.y, 0.0, 1.0, 0.0), dz(B.z - A.z, 0.0, 0.0, 1.0);
+  const Dual3 R = sqrt(dx * dx + dy * dy + dz * dz);
+  const double* Pm = P + mol.mat0;
+  const long long ld = mol.nao;
+
+  // local integrals (the slots this pair's orbitals need)
+  Dual3 val[kNumSlots];
+  {
+    const Dual3 dAv[3] = {pa.d[0], pa.d[1], pa.d[2]}, dBv[3] = {pb.d[0], pb.d[1], pb.d[2]};
+    const Dual3 rAv[3] = {pa.rho[0], pa.rho[1], pa.rho[2]}, rBv[3] = {pb.rho[0], pb.rho[1], pb.rho[2]};
+    for (int sl = 0; sl < 21; ++sl) {
+      bool need;
+      if (nA == 4 && nB == 4) need = true;
+      else if (nA == 4) need = (sl == 0 || sl == 3 || sl == 4 || sl == 10);
+      else if (nB == 4) need = (sl == 0 || sl == 1 || sl == 2 || sl == 13);
+      else need = (sl == 0);
+      Dual3 v = 0.0;
+      if (need)
+        for (int k = 0; k < eri->nterms[sl]; ++k) v += eval_term(eri->terms[sl][k], R, dAv, dBv, rAv, rBv);
+      val[sl] = v;
+    }
+    val[21] = (nA == 4 && nB == 4) ? 0.5 * (val[5] - val[6]) : Dual3(0.0);
+  }
+  Dual3 Rm[4][4];
+  smooth_frame(dx, dy, dz, Rm);
+
+  // C: the density factors of each (mu nu, la si) integral
+  double C[10][10];
+  {
+    double pA[10], pB[10], mA[10], mB[10];
+    for (int q = 0; q < dA; ++q) {
+      int m, n;
+      unpack_index(q, &m, &n);
+      pA[q] = Pm[(A.ao0 + m) * ld + A.ao0 + n];
+      mA[q] = m == n ? 1.0 : 2.0;
+    }
+    for (int q = 0; q < dB; ++q) {
+      int m, n;
+      unpack_index(q, &m, &n);
+      pB[q] = Pm[(B.ao0 + m) * ld + B.ao0 + n];
+      mB[q] = m == n ? 1.0 : 2.0;
+    }
+    for (int q = 0; q < dA; ++q) {
+      int a, b;
+      unpack_index(q, &a, &b);
+      for (int r = 0; r < dB; ++r) {
+        int c, e;
+        unpack_index(r, &c, &e);
+        // exchange: both orders of (a b) and of (c e)
+        double x = 0.0;
+        for (int o1 = 0; o1 < (a == b ? 1 : 2); ++o1) {
+          const int u = o1 ? b : a, w = o1 ? a : b;
+          for (int o2 = 0; o2 < (c == e ? 1 : 2); ++o2) {
+            const int y = o2 ? e : c, z = o2 ? c : e;
+            x += Pm[(A.ao0 + u) * ld + B.ao0 + y] * Pm[(A.ao0 + w) * ld + B.ao0 + z];
+          }
+        }
+        C[q][r] = mA[q] * mB[r] * pA[q] * pB[r] - 0.5 * x;
+      }
+    }
+    for (int q = 0; q < dA; ++q) C[q][0] += -(double)pb.core_charge * mA[q] * pA[q];
+    for (int r = 0; r < dB; ++r) C[0][r] += -(double)pa.core_charge * mB[r] * pB[r];
+  }
+
+  // two-electron and electron-core part: sum_PQ C_PQ (T2 L T2^T)_PQ
+  Dual3 e_pair = 0.0;
+  {
+    Dual3 T2[10][10];
+    for (int q = 0; q < 10; ++q)
+      for (int r = 0; r < 10; ++r) T2[q][r] = (q < dA || q < dB) ? pair_rotation(Rm, q, r) : Dual3(0.0);
+    // M[P][Q'] = sum_Q L[P][Q] T2[Q'][Q]
+    for (int Pl = 0; Pl < dA; ++Pl) {
+      Dual3 Mrow[10];
+      for (int Qp = 0; Qp < dB; ++Qp) {
+        Dual3 acc = 0.0;
+        for (int Q = 0; Q < dB; ++Q) {
+          const int sl = eri->slot_of[Pl][Q];
+          if (sl >= 0) acc += val[sl] * T2[Qp][Q];
+        }
+        Mrow[Qp] = acc;
+      }
+      // W[P'][Q'] = sum_P T2[P'][P] M[P][Q']: accumulate C[P'][Q'] T2[P'][P] M[P][Q']
+      for (int Pp = 0; Pp < dA; ++Pp) {
+        Dual3 cm = 0.0;
+        for (int Qp = 0; Qp < dB; ++Qp) cm += C[Pp][Qp] * Mrow[Qp];
+        e_pair += T2[Pp][Pl] * cm;
+      }
+    }
+  }
+
+  // resonance: sum P_mu,la (beta_mu + beta_la) S_mu,la
+  {
+    const int na = pa.principal_n, nb = pb.principal_n;
+    Dual3 ov[5];
+    for (int c = 0; c < 5; ++c) {
+      const bool need = (c == 0) || (c == 1 && nB == 4) || (c == 2 && nA == 4) || (c >= 3 && nA == 4 && nB == 4);
+      if (!need) { ov[c] = 0.0; continue; }
+      const double za = c >= 2 ? pa.zeta[1] : pa.zeta[0];
+      const double zb = (c == 1 || c >= 3) ? pb.zeta[1] : pb.zeta[0];
+      const double norm = pa.sto_norm[c >= 2 ? 1 : 0] * pb.sto_norm[(c == 1 || c >= 3) ? 1 : 0];
+      ov[c] = overlap_combo(ovt, na, nb, c, za, zb, norm, R);
+    }
+    Dual3 Ls[4][4];
+    Ls[0][0] = ov[0]; Ls[0][2] = ov[1]; Ls[2][0] = ov[2]; Ls[2][2] = ov[3]; Ls[1][1] = ov[4]; Ls[3][3] = ov[4];
+    for (int mu = 0; mu < nA; ++mu)
+      for (int la = 0; la < nB; ++la) {
+        Dual3 sv = 0.0;
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j)
+            if (i == j || (i == 0 && j == 2) || (i == 2 && j == 0)) sv += Rm[mu][i] * Ls[i][j] * Rm[la][j];
+        const double w = Pm[(A.ao0 + mu) * ld + B.ao0 + la] * (pa.beta[mu == 0 ? 0 : 1] + pb.beta[la == 0 ? 0 : 1]);
+        e_pair += w * sv;
+      }
+  }
+
+  // core-core repulsion (with the AM1 / PM3 Gaussians and the PDDG term)
+  e_pair += core_core(pa, pb, R, val[0], mol.theory);
+
+  // empirical dispersion (energy_kernel's pair term)
+  const bool dtheory = mol.theory == NDDO_AM1D || mol.theory == NDDO_PM3D;
+  if (vdw.on || dtheory) {
+    const double s6 = dtheory ? NDDO_VDW_S6_D : vdw.s6, dd = dtheory ? NDDO_VDW_DAMP_D : vdw.d;
+    const double csum = pa.vdw_c6 + pb.vdw_c6;
+    if (csum > 0.0) {
+      const double c6 = 2.0 * pa.vdw_c6 * pb.vdw_c6 / csum;
+      const Dual3 damp = 1.0 / (1.0 + exp(-1.0 * dd * (R / (pa.vdw_r0 + pb.vdw_r0) - 1.0)));
+      const Dual3 R2 = R * R;
+      e_pair += (-1.0 * s6 * c6) * damp / (R2 * R2 * R2);
+    }
+  }
+  grad[3 * t] = e_pair.d[0];
+  grad[3 * t + 1] = e_pair.d[1];
+  grad[3 * t + 2] = e_pair.d[2];
+}
+
+// forces F_i = -g_i of one molecule's atoms from its pair gradients
+__global__ void force_reduce_kernel(const DevMol* __restrict__ mols, int m, const double* __restrict__ grad,
+                                    double* __restrict__ forces) {
+  const DevMol mol = mols[m];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= mol.natoms) return;
+  double g[3] = {0.0, 0.0, 0.0};
+  for (int a = 0; a < i; ++a) {
+    const long long q = pair_index(a, i, mol.natoms);
+    for (int k = 0; k < 3; ++k) g[k] += grad[3 * q + k];
+  }
+  for (int b = i + 1; b < mol.natoms; ++b) {
+    const long long q = pair_index(i, b, mol.natoms);
+    for (int k = 0; k < 3; ++k) g[k] -= grad[3 * q + k];
+  }
+  for (int k = 0; k < 3; ++k) forces[3 * i + k] = -g[k];
+}
+
+void launch_forces(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, int m, long long pair0,
+                   long long npairs, int natoms, const EriTable* eri, const OverlapTable* ovt, const double* P,
+                   VdwParams vdw, double* grad, double* forces, cudaStream_t s) {
+  if (npairs > 0)
+    pair_grad_kernel<<<(unsigned)((npairs + 63) / 64), 64, 0, s>>>(atoms, pairs, pair0, npairs, mols, eri, ovt, P,
+                                                                      vdw, grad);
+  force_reduce_kernel<<<(natoms + 127) / 128, 128, 0, s>>>(mols, m, grad, forces);
 }
 
 }  // namespace nddo

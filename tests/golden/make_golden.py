@@ -1,4 +1,6 @@
-"""Regenerates tests/golden/reference_fixtures.json from the MolDS test suite.
+"""Regenerates tests/golden/reference_fixtures.json (SCF fixtures) and
+tests/golden/reference_md_fixtures.json (ground-state MD force runs) from the
+MolDS test suite.
 
 Reads the reference's own golden input/output pairs (test/<case>.in and
 test/<case>.dat of the MolDS tree, registered in test/Test_Of_MolDS.rb) and
@@ -67,6 +69,29 @@ def parse_dat(text, natoms):
     return out
 
 
+# ground-state MD runs from rest: the momenta printed after each step follow
+# from the analytic forces (MD::UpdateMomenta / UpdateCoordinates,
+# src/md/MD.cpp:97-149)
+MD_CASES = ["c2h6_mndo_force", "c2h6_am1_force", "c2h6_pm3_force", "c2h6_pm3pddg_force", "c2h6_pm3_vdw_force"]
+
+
+def parse_md(inp, dat, natoms):
+    md = re.search(r"(?is)^\s*md\s*$(.*?)^\s*md_end", inp, re.M).group(1)
+    dt = float(re.search(r"(?i)\bdt\s+(\S+)", md).group(1))
+    steps = int(re.search(r"(?i)total_steps\s+(\d+)", md).group(1))
+    momenta = []
+    for s in range(1, steps + 1):
+        a = dat.find(f"START: MD step {s}\n")
+        b = dat.find(f"DONE: MD step {s}\n", a)
+        block = dat[a:b]
+        # Molecule::OutputMomenta (src/base/Molecule.cpp:555-575) prints
+        # p / momentumUnit2AU under the "[a.u.]" heading and the stored
+        # momentum, in atomic units, under "[u]": keep the second triple
+        rows = re.findall(r"Atom momenta:\t\d+\t\S+\t\S+\t\S+\t\S+\t\t(\S+)\t(\S+)\t(\S+)", block)
+        momenta.append([[float(x) for x in r] for r in rows[:natoms]])
+    return {"dt_fs": dt, "steps": steps, "momenta": momenta}
+
+
 def main():
     if len(sys.argv) != 2:
         sys.exit("usage: python tests/golden/make_golden.py <MolDS test directory>")
@@ -84,6 +109,18 @@ def main():
     with open(os.path.join(here, "reference_fixtures.json"), "w") as f:
         json.dump({"source": "MolDS test/*.in, test/*.dat", "cases": fixtures}, f, indent=1)
     print(f"wrote {len(fixtures)} cases")
+    md = []
+    for name in MD_CASES:
+        inp = open(os.path.join(src, name + ".in")).read()
+        dat = open(os.path.join(src, name + ".dat")).read()
+        natoms = int(re.search(r"Total number of atoms: (\d+)", dat).group(1))
+        rec = {"name": name, "input": inp, "natoms": natoms}
+        rec.update(parse_md(inp, dat, natoms))
+        md.append(rec)
+    with open(os.path.join(here, "reference_md_fixtures.json"), "w") as f:
+        json.dump({"source": "MolDS test/*_force.in, test/*_force.dat (momenta after each MD step)", "cases": md},
+                  f, indent=1)
+    print(f"wrote {len(md)} MD cases")
 
 
 if __name__ == "__main__":
