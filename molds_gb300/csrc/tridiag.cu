@@ -574,13 +574,13 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   eps[mol.vec0 + idx] = lam;
   const int cl = tid >> 1;   // this pair's slot in the CTA
   if (vec_smem) {
-    // factors and vector in shared memory, element i of slot cl at i * kVecPerCta + cl
+    // factors and vector in shared memory, element i of slot cl at i * pairs + cl
     double* fl = red + 2 * (kVecThreads / 32);
-    double* fu1i = fl + (long long)n * kVecPerCta;
-    double* fu2 = fu1i + (long long)n * kVecPerCta;
-    double* xs = fu2 + (long long)n * kVecPerCta;
-    unsigned char* piv = reinterpret_cast<unsigned char*>(xs + (long long)n * kVecPerCta);
-    inverse_iteration(n, kVecPerCta, d, e, lam, tiny, (unsigned)idx, fl + cl, fu1i + cl, fu2 + cl, piv + cl, xs + cl,
+    double* fu1i = fl + (long long)n * pairs;
+    double* fu2 = fu1i + (long long)n * pairs;
+    double* xs = fu2 + (long long)n * pairs;
+    unsigned char* piv = reinterpret_cast<unsigned char*>(xs + (long long)n * pairs);
+    inverse_iteration(n, pairs, d, e, lam, tiny, (unsigned)idx, fl + cl, fu1i + cl, fu2 + cl, piv + cl, xs + cl,
                       Z + mol.mat0 + c, k);
   } else {
     double* x = Z + mol.mat0 + c;
@@ -782,10 +782,10 @@ static void hh_set_attributes() {
 }
 
 // tri_vectors_kernel: d, e, e^2 and the reduction slots; with vec_smem also
-// the factors, vector and pivot flags of its kVecPerCta inverse iterations
-size_t tri_vectors_smem_bytes(int n, bool vec_smem) {
+// the factors, vector and pivot flags of its `pairs` inverse iterations
+size_t tri_vectors_smem_bytes(int n, bool vec_smem, int pairs) {
   size_t b = (3 * (size_t)n + 2 * (kVecThreads / 32)) * sizeof(double);
-  if (vec_smem) b += (size_t)n * kVecPerCta * (4 * sizeof(double) + 1);
+  if (vec_smem) b += (size_t)n * pairs * (4 * sizeof(double) + 1);
   return b;
 }
 
@@ -842,9 +842,9 @@ void launch_tri_vectors(const DevMol* mols, const int* list, int nlist, int max_
                         double* Z, double* const* S4, cudaStream_t s) {
   if (nlist <= 0 || max_k <= 0) return;
   hh_set_attributes();
-  const bool vec_smem = tri_vectors_smem_bytes(max_n, true) <= (size_t)hh_optin_smem();
-  const size_t vsh = tri_vectors_smem_bytes(max_n, vec_smem);
   const int pairs = std::max(1, std::min(kVecPerCta, tuned_vec_pairs(max_n)));
+  const bool vec_smem = tri_vectors_smem_bytes(max_n, true, pairs) <= (size_t)hh_optin_smem();
+  const size_t vsh = tri_vectors_smem_bytes(max_n, vec_smem, pairs);
   dim3 gv(nlist, (max_k + pairs - 1) / pairs);
   tri_vectors_kernel<<<gv, kVecThreads, vsh, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z,
                                                   S4[0], S4[1], S4[2], S4[3], vec_smem ? 1 : 0, pairs);
