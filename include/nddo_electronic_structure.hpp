@@ -44,6 +44,9 @@ class MolDSException : public std::domain_error {
 struct Molecule {
   std::vector<int> atomicNumbers;
   std::vector<double> xyz;   // 3 per atom
+  // environmental point charges (MolDS's EPC block, Molecule::AddEpc):
+  // x, y, z in bohr and the charge, 4 per point charge
+  std::vector<double> epcs;
 };
 
 // SCF block with MolDS's defaults (src/base/Parameters.cpp:133-142).
@@ -77,7 +80,10 @@ class ElectronicStructure {
     const int n = static_cast<int>(molecule->atomicNumbers.size());
     if (molecule->xyz.size() != 3 * molecule->atomicNumbers.size())
       throw MolDSException("coordinate count does not match atom count", NDDO_ERR_ARGUMENT);
-    Check(nddo_set_molecule(ctx_, theory_, n, molecule->atomicNumbers.data(), molecule->xyz.data()));
+    if (molecule->epcs.size() % 4) throw MolDSException("point charges need x, y, z and a charge each", NDDO_ERR_ARGUMENT);
+    const int nEpc = static_cast<int>(molecule->epcs.size() / 4);
+    Check(nddo_set_molecule_epc(ctx_, theory_, n, molecule->atomicNumbers.data(), molecule->xyz.data(), nEpc,
+                                nEpc ? molecule->epcs.data() : nullptr));
     molecule_ = molecule;
     n_ = nddo_num_aos(ctx_);
     hasScf_ = false;
@@ -112,6 +118,8 @@ class ElectronicStructure {
   }
   double GetCoreRepulsionEnergy() const { Need(); return result_.core_repulsion; }
   double GetVdWCorrectionEnergy() const { Need(); return result_.vdw_energy; }
+  // sum over cores and environmental point charges of Z_A q / R, included in the energy
+  double GetCoreEpcCoulombEnergy() const { Need(); return result_.core_epc_coulomb; }
   double GetHeatsFormation() const { Need(); return result_.heat_of_formation; }
   int GetIterations() const { Need(); return result_.iterations; }
   double const* GetMullikenCharges() const { Need(); return charges_.data(); }

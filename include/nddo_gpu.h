@@ -80,6 +80,8 @@ typedef struct {
   double dipole[9];            /* total, electronic, core dipole (x, y, z) [a.u.]; 0 with dipole = 0
                                   (Cndo2::OutputSCFDipole, src/cndo/Cndo2.cpp:1126-1185) */
   double vdw_energy;           /* empirical dispersion energy [Eh], included in energy (0 when off) */
+  double core_epc_coulomb;     /* sum over cores and environmental point charges of Z_A q / R [Eh],
+                                  included in energy (0 without point charges; Cndo2.cpp:418-426) */
 } nddo_scf_result;
 
 /* Defaults of src/base/Parameters.cpp:133-139 (precision = FP64). */
@@ -96,6 +98,17 @@ const char* nddo_last_error(const nddo_ctx* ctx);
  * the electron count (odd -> error, src/cndo/Cndo2.cpp:351-357) and computes
  * the one-time pair integrals, overlap and core-core terms. */
 int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* atomic_numbers, const double* xyz_bohr);
+/* nddo_set_molecule with environmental point charges: MolDS's EPC block
+ * (InputParser::ParseEpcsConfiguration, src/base/InputParser.cpp:626-644,
+ * Molecule::AddEpc) as n_epc rows of x, y, z [bohr] and charge.  Each charge
+ * q adds -q (mu nu|s s) to the one-centre blocks of every non-guess Fock
+ * matrix (Mndo::GetFockDiagElement / GetFockOffDiagElement,
+ * src/mndo/Mndo.cpp:474-484, 546-556; the atom-EPC integrals with rho = 0,
+ * :6602-6613) and sum Z_A q / R to the energy (Mndo.cpp:329-331).
+ * n_epc = 0 is nddo_set_molecule.  nddo_set_coordinates moves the atoms and
+ * keeps the point charges in place. */
+int nddo_set_molecule_epc(nddo_ctx* ctx, int theory, int n_atoms, const int* atomic_numbers, const double* xyz_bohr,
+                          int n_epc, const double* epc_xyzq);
 /* New coordinates for the molecule already set (same atoms, bohr), as the MD /
  * MC / optimiser drivers move MolDS's Molecule in place before calling
  * DoSCF(false) (src/md/MD.cpp:108): the one-time integrals are recomputed and
@@ -134,21 +147,24 @@ int nddo_get_cartesian_matrix(nddo_ctx* ctx, double* out_3nn);
  * and a terminating NUL into out (may be NULL); *needed = full length + 1. */
 int nddo_scf_output_text(nddo_ctx* ctx, char* out, size_t cap, size_t* needed);
 /* The same text from explicit values (no GPU needed): per iteration rms,
- * diis_error, diis_on, damp_on (iterations entries); dipole = 9 doubles
+ * diis_error, diis_on, damp_on (iterations entries); epc != 0 adds the
+ * point-charge lines with core_epc (Cndo2.cpp:1090-1115); dipole = 9 doubles
  * (total, electronic, core; x y z) or NULL for no dipole block;
  * sum_pairs = n_sum_pairs (first, last) atom index pairs. */
 int nddo_format_scf_text(int theory, int n_atoms, const int* Z, int n_ao, int n_occ, int iterations,
                          const double* rms, const double* diis_error, const int* diis_on, const int* damp_on,
                          int converged, const double* eps, double energy, double core_repulsion, int vdw,
-                         double vdw_energy, const double* dipole, const double* charges, double heat_of_formation,
-                         int n_sum_pairs, const int* sum_pairs, double seconds, char* out, size_t cap,
-                         size_t* needed);
+                         double vdw_energy, int epc, double core_epc, const double* dipole, const double* charges,
+                         double heat_of_formation, int n_sum_pairs, const int* sum_pairs, double seconds, char* out,
+                         size_t cap, size_t* needed);
 /* Forces on the atoms (-dE/dR, Hartree/bohr, n_atoms x 3 row-major) of the
  * last converged SCF, ground state: Mndo::CalcForce
  * (src/mndo/Mndo.cpp:2711-2986) as read by ElectronicStructure::GetForce.
  * Analytic: the pair terms of the energy (two-centre integrals, electron-core
  * attractions, resonance, core-core, dispersion) differentiated exactly with
- * the converged density held fixed. */
+ * the converged density held fixed.  As in the reference, environmental
+ * point charges enter only through that density: Mndo::CalcForce has no
+ * atom-EPC term. */
 int nddo_get_forces(nddo_ctx* ctx, double* out_natoms_x3);
 /* The SCF option sum_charges (InputParser.cpp:694-700,
  * Parameters::AddSumChargesIndexPairsSCF): n_pairs (first, last) atom index

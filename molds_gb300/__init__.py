@@ -55,7 +55,8 @@ class ScfResultC(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("energy", ctypes.c_double),
                 ("core_repulsion", ctypes.c_double), ("heat_of_formation", ctypes.c_double),
                 ("final_rms", ctypes.c_double), ("final_diis_error", ctypes.c_double),
-                ("dipole", ctypes.c_double * 9), ("vdw_energy", ctypes.c_double)]
+                ("dipole", ctypes.c_double * 9), ("vdw_energy", ctypes.c_double),
+                ("core_epc_coulomb", ctypes.c_double)]
 
 
 class ServeResultC(ctypes.Structure):
@@ -76,6 +77,7 @@ SIGNATURES = {
     "nddo_destroy": (None, [_CTX]),
     "nddo_last_error": (ctypes.c_char_p, [_CTX]),
     "nddo_set_molecule": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _DP]),
+    "nddo_set_molecule_epc": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _DP, ctypes.c_int, _DP]),
     "nddo_set_coordinates": (ctypes.c_int, [_CTX, _DP]),
     "nddo_num_aos": (ctypes.c_int, [_CTX]),
     "nddo_num_atoms": (ctypes.c_int, [_CTX]),
@@ -91,7 +93,8 @@ SIGNATURES = {
     "nddo_scf_output_text": (ctypes.c_int, [_CTX, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "nddo_format_scf_text": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _IP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             _DP, _DP, _IP, _IP, ctypes.c_int, _DP, ctypes.c_double, ctypes.c_double,
-                                            ctypes.c_int, ctypes.c_double, _DP, _DP, ctypes.c_double, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, _DP, _DP,
+                                            ctypes.c_double, ctypes.c_int,
                                             _IP, ctypes.c_double, ctypes.c_char_p, ctypes.c_size_t,
                                             ctypes.POINTER(ctypes.c_size_t)]),
     "nddo_set_sum_charges": (ctypes.c_int, [_CTX, ctypes.c_int, _IP]),
@@ -251,7 +254,10 @@ class ElectronicStructure:
     def SetMolecule(self, molecule: Molecule):
         Z = np.ascontiguousarray(molecule.Z, dtype=np.int32)
         xyz = np.ascontiguousarray(molecule.xyz, dtype=np.float64).reshape(-1, 3)
-        self.ctx.check(self.ctx.lib.nddo_set_molecule(self.ctx.h, self.theory, int(Z.shape[0]), _ip(Z), _dp(xyz)))
+        epc = getattr(molecule, "epc", None)
+        epc = np.zeros((0, 4)) if epc is None else np.ascontiguousarray(epc, dtype=np.float64).reshape(-1, 4)
+        self.ctx.check(self.ctx.lib.nddo_set_molecule_epc(self.ctx.h, self.theory, int(Z.shape[0]), _ip(Z), _dp(xyz),
+                                                          int(epc.shape[0]), _dp(epc) if epc.size else None))
         self.molecule = molecule
         self.n = self.ctx.lib.nddo_num_aos(self.ctx.h)
         self.result = None
@@ -262,7 +268,7 @@ class ElectronicStructure:
         optimiser pattern, src/md/MD.cpp:108)."""
         x = np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1, 3)
         self.ctx.check(self.ctx.lib.nddo_set_coordinates(self.ctx.h, _dp(x)))
-        self.molecule = Molecule(self.molecule.Z, x)
+        self.molecule = Molecule(self.molecule.Z, x, getattr(self.molecule, "epc", None))
 
     def DoSCF(self, requiresGuess: bool = True, params: SCFParams | None = None):
         sp = params or self.params
@@ -291,6 +297,11 @@ class ElectronicStructure:
     def GetVdWCorrectionEnergy(self) -> float:
         """Empirical dispersion energy, included in GetElectronicEnergy (Cndo2.cpp:825)."""
         return self.result.vdw_energy
+
+    def GetCoreEpcCoulombEnergy(self) -> float:
+        """Coulomb energy of the cores and the environmental point charges,
+        sum Z_A q / R, included in GetElectronicEnergy (Cndo2.cpp:418-426, 1414)."""
+        return self.result.core_epc_coulomb
 
     def GetHeatsFormation(self) -> float:
         return self.result.heat_of_formation
@@ -358,9 +369,12 @@ class ElectronicStructure:
 
 
 def format_scf_text(theory, Z, eps, nocc, trace, energy, core_repulsion, charges, dipole=None, vdw=False,
-                    vdw_energy=0.0, heat_of_formation=0.0, converged=True, seconds=0.0, sum_charges=()) -> str:
+                    vdw_energy=0.0, heat_of_formation=0.0, converged=True, seconds=0.0, sum_charges=(),
+                    core_epc=None) -> str:
     """MolDS's SCF output section from explicit values (nddo_format_scf_text;
-    no GPU needed).  trace: [(iteration, rms, diis_error, diis_on, damping_on)]."""
+    no GPU needed).  trace: [(iteration, rms, diis_error, diis_on, damping_on)];
+    core_epc: the cores' Coulomb energy with environmental point charges (None:
+    the molecule has none, no point-charge lines)."""
     L = load_library()
     th = THEORIES[theory.lower()] if isinstance(theory, str) else int(theory)
     Z = np.ascontiguousarray(Z, dtype=np.int32)
@@ -374,7 +388,7 @@ def format_scf_text(theory, Z, eps, nocc, trace, energy, core_repulsion, charges
     sp = np.ascontiguousarray(np.ravel(np.array(sum_charges, dtype=np.int32).reshape(-1, 2)), dtype=np.int32)
     args = (th, int(Z.size), _ip(Z), int(eps.size), int(nocc), len(trace), _dp(rms), _dp(de), _ip(on), _ip(dm),
             int(bool(converged)), _dp(eps), float(energy), float(core_repulsion), int(bool(vdw)), float(vdw_energy),
-            None if dip is None else _dp(dip), _dp(q), float(heat_of_formation), int(sp.size // 2),
+            int(core_epc is not None), float(core_epc or 0.0), None if dip is None else _dp(dip), _dp(q), float(heat_of_formation), int(sp.size // 2),
             _ip(sp) if sp.size else None, float(seconds))
     need = ctypes.c_size_t()
     rc = L.nddo_format_scf_text(*args, None, 0, ctypes.byref(need))

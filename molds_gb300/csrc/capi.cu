@@ -85,6 +85,7 @@ struct nddo_ctx {
   nddo::ScfSettings last_settings;
   bool has_scf = false;
   std::vector<int> Z;                    // elements of the current molecule (the output text)
+  int n_epc = 0;                         // its environmental point charges
   int theory = 0;
   double scf_seconds = 0.0;              // host wall time of the last nddo_scf
   std::vector<int> sum_pairs;            // SCF option sum_charges (first, last atom index pairs)
@@ -195,13 +196,20 @@ void nddo_destroy(nddo_ctx* ctx) {
 const char* nddo_last_error(const nddo_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* Z, const double* xyz) {
+  return nddo_set_molecule_epc(ctx, theory, n_atoms, Z, xyz, 0, nullptr);
+}
+
+int nddo_set_molecule_epc(nddo_ctx* ctx, int theory, int n_atoms, const int* Z, const double* xyz, int n_epc,
+                          const double* epc) {
   return guarded(ctx, [&]() {
     if (!ctx->engine) return fail(ctx, NDDO_ERR_STATE, "engine not initialised");
     if (n_atoms < 1 || !Z || !xyz) return fail(ctx, NDDO_ERR_ARGUMENT, "need at least one atom");
+    if (n_epc < 0 || (n_epc > 0 && !epc)) return fail(ctx, NDDO_ERR_ARGUMENT, "invalid point charges");
     nddo::MoleculeInput in;
     in.theory = theory;
     in.Z.assign(Z, Z + n_atoms);
     in.xyz.assign(xyz, xyz + 3 * (size_t)n_atoms);
+    if (n_epc > 0) in.epc.assign(epc, epc + 4 * (size_t)n_epc);
     ctx->has_scf = false;
     // The molecule lives in a one-slot pool that is kept between calls: a new
     // molecule that fits the pool's arenas reuses them (no device allocation
@@ -214,7 +222,7 @@ int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* Z, cons
     int slot = -1;
     if (ctx->mol) {
       ctx->mol->release(0);
-      if (nao <= ctx->mol->max_n()) {
+      if (nao <= ctx->mol->max_n() && n_epc <= ctx->mol->epc_capacity()) {
         try {
           slot = ctx->mol->admit(in);
         } catch (...) {
@@ -235,6 +243,7 @@ int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* Z, cons
       c.vec = (nao + 31) / 32 * 32;
       c.max_n = nao;
       c.ws_slots = 1;
+      c.epcs = n_epc;
       std::unique_ptr<nddo::Batch> b(new nddo::Batch(ctx->engine.get(), c, 5, nullptr));
       if (ctx->budget && b->device_bytes() > ctx->budget)
         return fail(ctx, NDDO_ERR_BUDGET, "molecule needs " + std::to_string(b->device_bytes()) + " bytes of HBM, budget is " + std::to_string(ctx->budget));
@@ -244,6 +253,7 @@ int nddo_set_molecule(nddo_ctx* ctx, int theory, int n_atoms, const int* Z, cons
     }
     ctx->mol->integrals(std::vector<int>{0});
     ctx->Z.assign(Z, Z + n_atoms);
+    ctx->n_epc = n_epc;
     ctx->theory = theory;
     return (int)NDDO_OK;
   });
@@ -281,6 +291,7 @@ int nddo_scf(nddo_ctx* ctx, const nddo_scf_params* params, int requires_guess, n
       result->final_diis_error = r[0].final_diis_error;
       for (int k = 0; k < 9; ++k) result->dipole[k] = s.dipole ? r[0].dipole[k] : 0.0;
       result->vdw_energy = r[0].vdw_energy;
+      result->core_epc_coulomb = r[0].core_epc;
     }
     if (r[0].status != nddo::kConverged)
       return fail(ctx, NDDO_NOT_CONVERGED,
@@ -399,6 +410,8 @@ int nddo_scf_output_text(nddo_ctx* ctx, char* out, size_t cap, size_t* needed) {
     t.core_repulsion = r[0].core_repulsion;
     t.vdw = ctx->last_settings.vdw || ctx->theory == NDDO_THEORY_AM1D || ctx->theory == NDDO_THEORY_PM3D;
     t.vdw_energy = r[0].vdw_energy;
+    t.epc = ctx->n_epc > 0;
+    t.core_epc = r[0].core_epc;
     t.dipole = ctx->last_settings.dipole ? r[0].dipole : nullptr;
     t.charges = q.data();
     t.heat_of_formation = r[0].heat_of_formation;
@@ -435,9 +448,9 @@ int nddo_set_sum_charges(nddo_ctx* ctx, int n_pairs, const int* pairs) {
 int nddo_format_scf_text(int theory, int n_atoms, const int* Z, int n_ao, int n_occ, int iterations,
                          const double* rms, const double* diis_error, const int* diis_on, const int* damp_on,
                          int converged, const double* eps, double energy, double core_repulsion, int vdw,
-                         double vdw_energy, const double* dipole, const double* charges, double heat_of_formation,
-                         int n_sum_pairs, const int* sum_pairs, double seconds, char* out, size_t cap,
-                         size_t* needed) {
+                         double vdw_energy, int epc, double core_epc, const double* dipole, const double* charges,
+                         double heat_of_formation, int n_sum_pairs, const int* sum_pairs, double seconds, char* out,
+                         size_t cap, size_t* needed) {
   try {
     if (n_sum_pairs < 0 || (n_sum_pairs > 0 && !sum_pairs)) return NDDO_ERR_ARGUMENT;
     if (n_atoms < 1 || !Z || n_ao < 1 || iterations < 0 || (iterations > 0 && (!rms || !diis_error || !diis_on || !damp_on)) ||
@@ -460,6 +473,8 @@ int nddo_format_scf_text(int theory, int n_atoms, const int* Z, int n_ao, int n_
     t.core_repulsion = core_repulsion;
     t.vdw = vdw;
     t.vdw_energy = vdw_energy;
+    t.epc = epc;
+    t.core_epc = core_epc;
     t.dipole = dipole;
     t.charges = charges;
     t.heat_of_formation = heat_of_formation;
@@ -556,6 +571,7 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
       results[i].final_diis_error = r[i].final_diis_error;
       for (int k = 0; k < 9; ++k) results[i].dipole[k] = s.dipole ? r[i].dipole[k] : 0.0;
       results[i].vdw_energy = r[i].vdw_energy;
+      results[i].core_epc_coulomb = r[i].core_epc;
       if (r[i].status != nddo::kConverged) rc = NDDO_NOT_CONVERGED;
       if (charges) b.copy_charges(i, charges + off);
       off += n_atoms[i];
@@ -643,6 +659,7 @@ int nddo_batch_results(nddo_batch* h, nddo_scf_result* results, double* charges)
       results[i].final_diis_error = r[i].final_diis_error;
       for (int k = 0; k < 9; ++k) results[i].dipole[k] = h->dipole ? r[i].dipole[k] : 0.0;
       results[i].vdw_energy = r[i].vdw_energy;
+      results[i].core_epc_coulomb = r[i].core_epc;
       if (r[i].status != nddo::kConverged) rc = NDDO_NOT_CONVERGED;
       if (charges) h->b->copy_charges((int)i, charges + off);
       off += h->n_atoms[i];

@@ -47,6 +47,7 @@ __global__ void init_state_kernel(const DevMol* __restrict__ mols, const int* __
     s.status = kActive;
     s.requires_guess = requires_guess;
     s.ecore = st[m].ecore;   // computed by the integral pass
+    s.ecore_epc = st[m].ecore_epc;
     st[m] = s;
     if (sweeps) sweeps[m] = 0;
   }
@@ -185,6 +186,16 @@ MolLayout layout_molecule(const MoleculeInput& in) {
   if (nelec % 2) throw std::invalid_argument("Total number of valence electrons is odd. totalNumberValenceElectrons=" + std::to_string(nelec));
   L.nao = ao;
   L.nocc = nelec / 2;
+  // point charges (src/base/InputParser.cpp:626-644): a charge on an atom's
+  // position would make its Coulomb terms infinite
+  if (in.epc.size() % 4) throw std::invalid_argument("point charges need x, y, z and a charge each");
+  for (size_t i = 0; i < in.epc.size(); i += 4) {
+    for (int k = 0; k < 4; ++k)
+      if (!std::isfinite(in.epc[i + k])) throw std::invalid_argument("non-finite point charge");
+    for (const DevAtom& A : L.atoms)
+      if (A.x == in.epc[i] && A.y == in.epc[i + 1] && A.z == in.epc[i + 2])
+        throw std::invalid_argument("a point charge at an atom's position");
+  }
   for (int a = 0; a < na; ++a)
     for (int b = a + 1; b < na; ++b) {
       const DevAtom& A = L.atoms[a];
@@ -241,6 +252,9 @@ Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m, cu
     }
     blk_total_ += L.blocks;
     dm.npairs = (int)L.pairs.size();
+    dm.nepc = (int)(mols[m].epc.size() / 4);
+    dm.epc0 = (long long)(h_epc.size() / 4);
+    h_epc.insert(h_epc.end(), mols[m].epc.begin(), mols[m].epc.end());
     dm.mat0 = mat;
     dm.vec0 = vec;
     mat += round32((long long)L.nao * L.nao);
@@ -255,11 +269,14 @@ Batch::Batch(Engine* eng, const std::vector<MoleculeInput>& mols, int diis_m, cu
   cap.blocks = blk_total_;
   cap.mat = mat;
   cap.vec = vec;
+  cap.epcs = (long long)(h_epc.size() / 4);
   cap.max_n = max_n_;
   cap.ws_slots = cap.slots;
   allocate(cap);
   const int nm = (int)h_mols.size();
   cuda_check(cudaMemcpyAsync(d_atoms, h_atoms.data(), h_atoms.size() * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_), "upload atoms");
+  if (!h_epc.empty())
+    cuda_check(cudaMemcpyAsync(d_epc, h_epc.data(), h_epc.size() * sizeof(double), cudaMemcpyHostToDevice, stream_), "upload point charges");
   if (!h_pairs.empty())
     cuda_check(cudaMemcpyAsync(d_pairs, h_pairs.data(), h_pairs.size() * sizeof(DevPair), cudaMemcpyHostToDevice, stream_), "upload pairs");
   cuda_check(cudaMemcpyAsync(d_mols, h_mols.data(), nm * sizeof(DevMol), cudaMemcpyHostToDevice, stream_), "upload mols");
@@ -275,6 +292,7 @@ Batch::Batch(Engine* eng, const BatchCapacity& cap, int diis_m, cudaStream_t str
   allocate(cap);
   h_atoms.assign(cap.atoms, DevAtom{});
   h_pairs.assign(cap.pairs, DevPair{});
+  h_epc.assign(4 * (size_t)cap.epcs, 0.0);
   DevMol empty;
   std::memset(&empty, 0, sizeof(empty));
   h_mols.assign(cap.slots, empty);
@@ -284,6 +302,7 @@ Batch::Batch(Engine* eng, const BatchCapacity& cap, int diis_m, cudaStream_t str
   a_blocks_.reset(cap.blocks);
   a_mat_.reset(cap.mat);
   a_vec_.reset(cap.vec);
+  a_epc_.reset(cap.epcs);
   for (int k = cap.slots - 1; k >= 0; --k) free_slots_.push_back(k);
   cuda_check(cudaMemcpyAsync(d_mols, h_mols.data(), cap.slots * sizeof(DevMol), cudaMemcpyHostToDevice, stream_), "upload mols");
   cuda_check(cudaStreamSynchronize(stream_), "pool init");
@@ -296,6 +315,7 @@ void Batch::allocate(const BatchCapacity& cap) {
   mat_total_ = mat;
   vec_total_ = vec;
   d_atoms = dalloc<DevAtom>(cap.atoms, &bytes_);
+  d_epc = dalloc<double>(4 * (size_t)cap.epcs, &bytes_);
   d_pairs = dalloc<DevPair>(cap.pairs, &bytes_);
   d_mols = dalloc<DevMol>(nm, &bytes_);
   d_list = dalloc<int>(nm, &bytes_);
@@ -388,6 +408,7 @@ int Batch::admit(const MoleculeInput& in) {
   if (!pool_) throw std::logic_error("admit on a fixed batch");
   MolLayout L = layout_molecule(in);
   if (L.nao > cap_.max_n) throw std::invalid_argument("molecule larger than the pool's largest basis");
+  if ((long long)(in.epc.size() / 4) > cap_.epcs) throw std::invalid_argument("more point charges than the pool holds");
   if (free_slots_.empty()) return -1;
   const long long na = (long long)L.atoms.size(), npr = (long long)L.pairs.size();
   const long long nmat = round32((long long)L.nao * L.nao), nvec = round32(L.nao);
@@ -404,6 +425,13 @@ int Batch::admit(const MoleculeInput& in) {
     a_atoms_.release(oa, na); a_pairs_.release(op, npr); a_blocks_.release(ob, L.blocks); a_mat_.release(om, nmat);
     return -1;
   }
+  const long long ne = (long long)(in.epc.size() / 4);
+  const long long oe = ne > 0 ? a_epc_.alloc(ne) : 0;
+  if (oe < 0) {
+    a_atoms_.release(oa, na); a_pairs_.release(op, npr); a_blocks_.release(ob, L.blocks); a_mat_.release(om, nmat);
+    a_vec_.release(ov, nvec);
+    return -1;
+  }
   const int slot = free_slots_.back();
   free_slots_.pop_back();
   DevMol dm;
@@ -417,7 +445,10 @@ int Batch::admit(const MoleculeInput& in) {
   dm.npairs = (int)npr;
   dm.mat0 = om;
   dm.vec0 = ov;
+  dm.nepc = (int)ne;
+  dm.epc0 = oe;
   for (long long a = 0; a < na; ++a) { DevAtom x = L.atoms[a]; x.mol = slot; h_atoms[oa + a] = x; }
+  std::copy(in.epc.begin(), in.epc.end(), h_epc.begin() + 4 * oe);
   for (long long k = 0; k < npr; ++k) {
     DevPair p = L.pairs[k];
     p.a += (int)oa; p.b += (int)oa; p.mol = slot; p.blk += ob;
@@ -431,6 +462,9 @@ int Batch::admit(const MoleculeInput& in) {
   buckets_.clear();
   cuda_check(cudaMemcpyAsync(d_atoms + oa, &h_atoms[oa], na * sizeof(DevAtom), cudaMemcpyHostToDevice, stream_), "upload atoms");
   if (npr) cuda_check(cudaMemcpyAsync(d_pairs + op, &h_pairs[op], npr * sizeof(DevPair), cudaMemcpyHostToDevice, stream_), "upload pairs");
+  if (ne)
+    cuda_check(cudaMemcpyAsync(d_epc + 4 * oe, &h_epc[4 * oe], 4 * ne * sizeof(double), cudaMemcpyHostToDevice, stream_),
+               "upload point charges");
   cuda_check(cudaMemcpyAsync(d_mols + slot, &h_mols[slot], sizeof(DevMol), cudaMemcpyHostToDevice, stream_), "upload mol");
   return slot;
 }
@@ -444,6 +478,7 @@ void Batch::release(int slot) {
   if (d.npairs > 0) a_blocks_.release(h_pairs[d.pair0].blk, slot_blocks_[slot]);
   a_mat_.release(d.mat0, round32(n * n));
   a_vec_.release(d.vec0, round32(n));
+  if (d.nepc > 0) a_epc_.release(d.epc0, d.nepc);
   std::memset(&d, 0, sizeof(d));
   slot_blocks_[slot] = 0;
   free_slots_.push_back(slot);
@@ -464,7 +499,7 @@ Batch::~Batch() {
   if (h_bj_pending) cudaFreeHost(h_bj_pending);
   if (d_bj_ws) cudaFree(d_bj_ws);
   if (d_diis_ws) cudaFree(d_diis_ws);
-  void* ptrs[] = {d_atoms, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
+  void* ptrs[] = {d_atoms, d_epc, d_pairs, d_mols, d_list, d_blocks, d_ecore_pair, d_H, d_F, d_P, d_Pold, d_C, d_eps,
                   d_hist_dens, d_hist_err, d_G32, d_T32, d_Cf, d_Cnf, d_Ff, d_G64, d_T64, d_jA32, d_jV32, d_jA64, d_jV64,
                   d_state, d_trace, d_charges, d_sweeps, d_count, d_active, d_heavy_pairs, d_light_pairs, d_tc_err, d_dip_ws};
   for (void* p : ptrs) if (p) cudaFree(p);
@@ -859,7 +894,8 @@ void Batch::integrals(const std::vector<int>& which) {
   cuda_check(cudaGetLastError(), "pair_kernel");
   h = prof_begin(kKHcore, 0.0);
   launches_ += 1;
-  launch_hcore_kernel(d_atoms, d_pairs, d_mols, d_list, (int)which.size(), d_blocks, d_ecore_pair, d_H, d_state, stream_);
+  launch_hcore_kernel(d_atoms, d_pairs, d_mols, d_list, (int)which.size(), d_blocks, d_ecore_pair, eng_->eri(), d_epc,
+                      d_H, d_state, stream_);
   prof_end(h);
   cuda_check(cudaGetLastError(), "hcore_kernel");
   // the pageable index vectors above must outlive their copies
@@ -1295,6 +1331,7 @@ void Batch::results(std::vector<MolResult>* out) {
     r.final_diis_error = st[m].diis_err;
     for (int k = 0; k < 9; ++k) r.dipole[k] = st[m].dipole[k];
     r.vdw_energy = st[m].vdw_energy;
+    r.core_epc = st[m].ecore_epc;
   }
 }
 

@@ -14,6 +14,9 @@ struct MoleculeInput {
   int theory = NDDO_PM3;
   std::vector<int> Z;
   std::vector<double> xyz;   // bohr, 3 per atom
+  // environmental point charges (MolDS EPC block): x, y, z in bohr and the
+  // charge, 4 per point charge
+  std::vector<double> epc;
 };
 
 struct ScfSettings {
@@ -54,6 +57,7 @@ struct MolResult {
   double energy = 0, core_repulsion = 0, heat_of_formation = 0, final_rms = 0, final_diis_error = 0;
   double dipole[9] = {};        // total, electronic, core (x, y, z) [a.u.] when ScfSettings::dipole
   double vdw_energy = 0;        // empirical dispersion energy, included in energy
+  double core_epc = 0;          // Coulomb energy of the cores and the point charges, included in energy
 };
 
 class Engine;
@@ -62,6 +66,7 @@ class Engine;
 struct BatchCapacity {
   int slots = 0;               // molecules resident at once
   long long atoms = 0, pairs = 0, blocks = 0, mat = 0, vec = 0;
+  long long epcs = 0;          // environmental point charges
   int max_n = 0;               // largest basis admitted
   int ws_slots = 0;            // molecules per Jacobi launch that need a global-memory workspace
 };
@@ -91,6 +96,7 @@ class Batch {
 
   int size() const { return (int)h_mols.size(); }
   int max_n() const { return cap_.max_n; }
+  long long epc_capacity() const { return cap_.epcs; }
   cudaStream_t stream() const { return stream_; }
 
   // pool mode: place a molecule (slot index, or -1 when an arena or the slot
@@ -178,7 +184,7 @@ class Batch {
   int diis_m_;
   bool pool_ = false;
   BatchCapacity cap_;
-  ArenaAlloc a_atoms_, a_pairs_, a_blocks_, a_mat_, a_vec_;
+  ArenaAlloc a_atoms_, a_pairs_, a_blocks_, a_mat_, a_vec_, a_epc_;
   std::vector<int> free_slots_;
   std::vector<long long> slot_blocks_;   // block-arena length of each occupied slot
   size_t bytes_ = 0;
@@ -186,11 +192,13 @@ class Batch {
   int max_n_ = 0, max_iter_alloc_ = 0;
 
   std::vector<DevAtom> h_atoms;
+  std::vector<double> h_epc;      // point charges, 4 doubles each
   std::vector<DevPair> h_pairs;
   std::vector<DevMol> h_mols;
   long long blk_total_ = 0;
 
   DevAtom* d_atoms = nullptr;
+  double* d_epc = nullptr;
   DevPair* d_pairs = nullptr;
   DevMol* d_mols = nullptr;
   int* d_list = nullptr;

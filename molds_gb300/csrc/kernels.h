@@ -75,8 +75,8 @@ void launch_pair_kernels_split(const DevAtom* atoms, const DevPair* pairs, const
                                const OverlapTable* ovt, double* blocks, double* H, double* ecore_pair,
                                cudaStream_t s);
 void launch_hcore_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
-                         int nlist, const double* blocks, const double* ecore_pair, double* H, MolState* st,
-                         cudaStream_t s);
+                         int nlist, const double* blocks, const double* ecore_pair, const EriTable* eri,
+                         const double* epc, double* H, MolState* st, cudaStream_t s);
 void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
                         int nlist, int max_atoms, const double* blocks, const double* H, const double* P, double* F,
                         double* Pold, const MolState* st, int mode_override, int copy_old, int require_active,

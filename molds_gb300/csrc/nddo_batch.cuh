@@ -32,9 +32,11 @@ struct DevPair {
 
 struct DevMol {
   int natoms, nao, nocc, theory;
-  int atom0, pair0, npairs, pad;
+  int atom0, pair0, npairs;
+  int nepc;         // environmental point charges acting on this molecule
   long long mat0;   // element offset of this molecule's N x N matrices
   long long vec0;   // element offset of this molecule's length-N vectors
+  long long epc0;   // first point charge (x, y, z in bohr, charge: 4 doubles each)
 };
 
 // SCF state machine of one molecule (MolDS Cndo2::DoSCF, src/cndo/Cndo2.cpp:585-729)
@@ -54,6 +56,7 @@ struct MolState {
   double B[kMaxDiis * kMaxDiis];   // <e_i, e_j> over ring slots
   double dipole[9];   // total, electronic, core dipole (x, y, z each) [a.u.] after convergence
   double vdw_energy;  // empirical dispersion energy (0 when off)
+  double ecore_epc;   // Coulomb energy of the cores in the point charges' field
 };
 
 struct TraceEntry {

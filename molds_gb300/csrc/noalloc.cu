@@ -242,7 +242,8 @@ extern "C" int nddo_pair_integrals_noalloc(int device, int theory, int n_atoms, 
       }
     }
     if (ce == cudaSuccess) {
-      launch_hcore_kernel(d_atoms, d_pairs, d_mol, d_list, 1, d_pair_blocks, d_ecore, d_core_hamiltonian, d_state, s);
+      launch_hcore_kernel(d_atoms, d_pairs, d_mol, d_list, 1, d_pair_blocks, d_ecore, d_eri, nullptr,
+                          d_core_hamiltonian, d_state, s);
       ce = cudaGetLastError();
     }
     double ecore = 0.0;

@@ -370,16 +370,45 @@ __device__ __forceinline__ const double* partner_block(const DevPair* __restrict
 
 constexpr int kFockThreads = 256;
 
+// Local integral (A's multipoles | a bare point charge): the slot's terms with
+// both rho set to zero (MolDS Mndo::GetSemiEmpiricalMultipoleInteraction,
+// src/mndo/Mndo.cpp:6602-6613, for an atom-EPC pair) and no charge separation
+// on the point charge, whose only multipole is its monopole.
+__device__ __forceinline__ double epc_slot_value(const EriTable* __restrict__ eri, int slot, double R,
+                                                 const nddo_atom_params& pa) {
+  double v = 0.0;
+  const int nt = eri->nterms[slot];
+  for (int t = 0; t < nt; ++t) {
+    const EriTerm e = eri->terms[slot][t];
+    const double da = e.la == 0 ? pa.d[0] : (e.la == 1 ? pa.d[1] : pa.d[2]);
+    const double l = R + (double)e.c1 * da;
+    const double u = (double)e.c3 * da;
+    const double w = (double)e.c5 * da;
+    v += e.coef * rsqrt(l * l + u * u + w * w);
+  }
+  return v;
+}
+
 // One-centre block of H (U on the diagonal plus the attraction of every other
-// core, -Z_B (mu nu|s_B s_B)) and the molecule's core-core energy.
+// core, -Z_B (mu nu|s_B s_B)) and the molecule's core-core energy.  With
+// environmental point charges each adds -q (mu nu|s s) to the block (MolDS
+// Mndo::GetFockDiagElement / GetFockOffDiagElement, src/mndo/Mndo.cpp:474-484,
+// 546-556, present in every non-guess Fock matrix and so in H = F(P = 0) of
+// the energy, src/cndo/Cndo2.cpp:1324-1416), the block rotated from the local
+// values exactly as a pair with a hydrogen (pair_light_kernel), and the
+// cores' energy in their field, sum Z_A q / R (Mndo.cpp:329-331,
+// Cndo2.cpp:418-426), goes to ecore_epc.
 __global__ void __launch_bounds__(kFockThreads)
 hcore_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pairs, const DevMol* __restrict__ mols,
              const int* __restrict__ mol_list, const double* __restrict__ blocks,
-             const double* __restrict__ ecore_pair, double* __restrict__ H, MolState* __restrict__ st) {
+             const double* __restrict__ ecore_pair, const EriTable* __restrict__ eri,
+             const double* __restrict__ epc, double* __restrict__ H, MolState* __restrict__ st) {
+  __shared__ double s_epc[kFockThreads / 32];
   const int m = mol_list[blockIdx.x];
   const DevMol mol = mols[m];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   const long long ld = mol.nao;
+  double e_epc = 0.0;   // this lane's share of sum Z_A q / R
   for (int ia = warp; ia < mol.natoms; ia += nwarps) {
     const DevAtom A = atoms[mol.atom0 + ia];
     const int dA = A.nao == 4 ? 10 : 1;
@@ -397,6 +426,30 @@ hcore_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pair
       for (int k = 0; k < 10; ++k)
         if (k < dA) acc[k] -= zb * (rows ? blk[k * dB] : blk[k]);
     }
+    if (mol.nepc > 0) {
+      const nddo_atom_params& pa = c_params[A.pidx];
+      for (int i = lane; i < mol.nepc; i += 32) {
+        const double* pc = epc + 4 * (mol.epc0 + i);
+        const double dx = pc[0] - A.x, dy = pc[1] - A.y, dz = pc[2] - A.z, q = pc[3];
+        const double R = sqrt(dx * dx + dy * dy + dz * dz);
+        const double iR = 1.0 / R;
+        e_epc += pa.core_charge * q / R;
+        acc[0] -= q * epc_slot_value(eri, 0, R, pa);
+        if (dA == 10) {
+          const double s3 = epc_slot_value(eri, 3, R, pa);
+          const double s4 = epc_slot_value(eri, 4, R, pa);
+          const double s10 = epc_slot_value(eri, 10, R, pa);
+          const double u[4] = {0.0, dy * iR, dz * iR, dx * iR};   // orbital order s, py, pz, px
+#pragma unroll
+          for (int k = 1; k < 10; ++k) {
+            int mu, nu;
+            unpack_index(k, &mu, &nu);
+            const double v = mu == 0 ? s10 * u[nu] : (mu == nu ? s3 : 0.0) + (s4 - s3) * u[mu] * u[nu];
+            acc[k] -= q * v;
+          }
+        }
+      }
+    }
 #pragma unroll
     for (int k = 0; k < 10; ++k) acc[k] = warp_sum(acc[k]);
     if (lane < dA) {
@@ -411,11 +464,19 @@ hcore_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pair
       H[mol.mat0 + c * ld + r] = v;
     }
   }
+  e_epc = warp_sum(e_epc);
+  if (lane == 0) s_epc[warp] = e_epc;
+  __syncthreads();
   if (warp == 0) {
     double s = 0.0;
     for (int k = lane; k < mol.npairs; k += 32) s += ecore_pair[mol.pair0 + k];
     s = warp_sum(s);
-    if (lane == 0) st[m].ecore = s;
+    if (lane == 0) {
+      st[m].ecore = s;
+      double e = 0.0;
+      for (int w = 0; w < nwarps; ++w) e += s_epc[w];
+      st[m].ecore_epc = e;
+    }
   }
 }
 
@@ -585,10 +646,10 @@ void launch_pair_kernels_split(const DevAtom* atoms, const DevPair* pairs, const
 }
 
 void launch_hcore_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
-                         int nlist, const double* blocks, const double* ecore_pair, double* H, MolState* st,
-                         cudaStream_t s) {
+                         int nlist, const double* blocks, const double* ecore_pair, const EriTable* eri,
+                         const double* epc, double* H, MolState* st, cudaStream_t s) {
   if (nlist <= 0) return;
-  hcore_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, pairs, mols, mol_list, blocks, ecore_pair, H, st);
+  hcore_kernel<<<nlist, kFockThreads, 0, s>>>(atoms, pairs, mols, mol_list, blocks, ecore_pair, eri, epc, H, st);
 }
 
 void launch_fock_kernel(const DevAtom* atoms, const DevPair* pairs, const DevMol* mols, const int* mol_list,
@@ -654,7 +715,7 @@ energy_kernel(const DevAtom* __restrict__ atoms, const DevPair* __restrict__ pai
     MolState* s = st + m;
     s->energy_electronic = e;
     s->vdw_energy = v;
-    s->energy = e + s->ecore + v;
+    s->energy = e + s->ecore + s->ecore_epc + v;
     double hof = s->energy;
     for (int a = 0; a < mol.natoms; ++a) {
       const nddo_atom_params& pa = c_params[atoms[mol.atom0 + a].pidx];

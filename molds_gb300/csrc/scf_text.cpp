@@ -4,7 +4,8 @@
 // (src/cndo/Cndo2.cpp:585-729): the iteration log of
 // SatisfyConvergenceCriterion (:1505-1510), the convergence message, then
 // OutputSCFResults (:1299-1303): OutputMOEnergies (:1063-1078),
-// OutputSCFEnergies (:1080-1124), OutputSCFDipole (:1126-1185),
+// OutputSCFEnergies (:1080-1124, with the point-charge lines :1090-1115),
+// OutputSCFDipole (:1126-1185),
 // OutputSCFMulliken (:1187-1221, with the sum_charges option), for MNDO the heat of formation
 // (src/mndo/Mndo.cpp:412-420), and the elapsed-time line and done banner.
 // The labels and number formats are the reference's, so that its output
@@ -63,10 +64,18 @@ std::string format_scf_text(const ScfText& t) {
   const bool vdw = t.vdw != 0;
   o += "\t\t\t\t|   [a.u.]   |   [eV]   |\n";
   add(&o, "\tElectronic energy(SCF):\t%e\t%e\n", t.energy, t.energy / NDDO_EV2AU);
-  o += vdw ? "\tNote that this electronic energy includes core-repulsions and vdW correction.\n\n"
-           : "\tNote that this electronic energy includes core-repulsions.\n\n";
+  if (t.epc)
+    o += vdw ? "\tNote that this electronic energy includes core-repulsions, core-EPC coulomb, and vdW correction.\n\n"
+             : "\tNote that this electronic energy includes core-repulsions and core-EPC coulomb.\n\n";
+  else
+    o += vdw ? "\tNote that this electronic energy includes core-repulsions and vdW correction.\n\n"
+             : "\tNote that this electronic energy includes core-repulsions.\n\n";
   o += "\t\t\t\t|   [a.u.]   |   [eV]   |\n";
   add(&o, "\tCore repulsion energy:\t%e\t%e\n\n", t.core_repulsion, t.core_repulsion / NDDO_EV2AU);
+  if (t.epc) {
+    o += "\t\t\t\t\t\t\t\t|   [a.u.]   |   [eV]   |\n";
+    add(&o, "\tCoulomb interaction between cores and EPCs energy:\t%e\t%e\n\n", t.core_epc, t.core_epc / NDDO_EV2AU);
+  }
   if (vdw) {
     o += "\t\t\t\t\t\t|   [a.u.]   |   [eV]   |\n";
     add(&o, "\tEmpirical van der Waals correction:\t%e\t%e\n\n", t.vdw_energy, t.vdw_energy / NDDO_EV2AU);

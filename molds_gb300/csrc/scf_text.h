@@ -20,6 +20,8 @@ struct ScfText {
   double core_repulsion = 0.0;
   int vdw = 0;                      // the vdW lines (AM1-D, PM3-D, or the vdW option)
   double vdw_energy = 0.0;
+  int epc = 0;                      // the point-charge lines (the molecule has environmental point charges)
+  double core_epc = 0.0;            // Coulomb energy of the cores and the point charges
   const double* dipole = nullptr;   // 9: total, electronic, core (x, y, z); null: no dipole block
   const double* charges = nullptr;  // Mulliken charges
   int n_sum = 0;                    // SCF option sum_charges: pairs (first, last) of atom indices

@@ -4,8 +4,9 @@ Follows src/base/InputParser.cpp: the file is read as whitespace tokens,
 lower-cased, with ``//`` comments removed (:516-540); the THEORY block selects
 the Hamiltonian (:284-295, 1397-1439), the SCF block sets the SCF parameters
 (:311-325, 646-734), GEOMETRY lists ``El x y z`` in Angstrom converted to bohr
-at parse time (:542-582) and MEMORY sets ``limit_heap`` in MB (:394-396,
-1441-1453).  Other MolDS blocks are rejected: this package implements the
+at parse time (:542-582), EPC lists environmental point charges
+``x y z [charge q]`` in Angstrom (:626-644, charge 0 when omitted) and MEMORY
+sets ``limit_heap`` in MB (:394-396, 1441-1453).  Other MolDS blocks are rejected: this package implements the
 closed-shell NDDO SCF only.
 """
 from __future__ import annotations
@@ -48,9 +49,11 @@ class SCFParams:
 
 @dataclass
 class Molecule:
-    """Atoms in input order; coordinates in bohr."""
+    """Atoms in input order; coordinates in bohr.  epc: environmental point
+    charges, one row of x, y, z (bohr) and charge each, or None."""
     Z: np.ndarray
     xyz: np.ndarray
+    epc: np.ndarray | None = None
 
     @property
     def natoms(self) -> int:
@@ -95,6 +98,7 @@ def parse(text: str) -> InputFile:
     theory = None
     scf = SCFParams()
     atoms = []
+    epcs = []
     limit = 256.0
     i = 0
 
@@ -147,6 +151,22 @@ def parse(text: str) -> InputFile:
                     raise InputError(f"bad coordinate for atom {len(atoms)}") from e
                 atoms.append((SYMBOL_TO_Z[sym], xyz))
                 i += 4
+        elif t == "epc":                         # src/base/InputParser.cpp:626-644
+            i += 1
+            while need(i) != "epc_end":
+                try:
+                    xyz = [float(need(i + k)) * ANG2AU for k in (0, 1, 2)]
+                except ValueError as e:
+                    raise InputError(f"bad coordinate for point charge {len(epcs)}") from e
+                i += 3
+                q = 0.0
+                if need(i) == "charge":
+                    try:
+                        q = float(need(i + 1))
+                    except ValueError as e:
+                        raise InputError(f"bad charge for point charge {len(epcs)}") from e
+                    i += 2
+                epcs.append(xyz + [q])
         elif t == "memory":
             i += 1
             while need(i) != "memory_end":
@@ -164,4 +184,5 @@ def parse(text: str) -> InputFile:
         raise InputError("no GEOMETRY block")
     Z = np.array([a[0] for a in atoms], dtype=np.int32)
     xyz = np.array([a[1] for a in atoms], dtype=np.float64)
-    return InputFile(theory, scf, Molecule(Z, xyz), limit, toks)
+    epc = np.array(epcs, dtype=np.float64).reshape(-1, 4) if epcs else None
+    return InputFile(theory, scf, Molecule(Z, xyz, epc), limit, toks)

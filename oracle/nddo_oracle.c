@@ -470,6 +470,45 @@ int oracle_integrals(int theory, int natoms, const int* Z, const double* xyz,
   return N;
 }
 
+/* Environmental point charges (MolDS EPC).  For every atom A and point
+ * charge (x, y, z, q): V[mu][nu] += -q (mu nu|s s)_{A,EPC} on A's one-centre
+ * block, the integral taken as for an atom pair with the EPC an s-only centre
+ * (src/base/atoms/mm/EnvironmentalPointCharge.cpp:29-35) and both rho set to
+ * zero (src/mndo/Mndo.cpp:3822-3935, 6602-6613); the Fock matrix gets V in
+ * every non-guess build (Mndo.cpp:474-484, 546-556).  *ecore_epc = sum
+ * Z_A q / R (Mndo.cpp:329-331, src/cndo/Cndo2.cpp:418-426).  V is N x N and
+ * is added to.  Returns N or a negative error. */
+int oracle_epc(int theory, int natoms, const int* Z, const double* xyz, int nepc, const double* epc,
+               double* V, double* ecore_epc) {
+  oracle_atom* P = (oracle_atom*)malloc(sizeof(oracle_atom) * (natoms > 0 ? natoms : 1));
+  int* first = (int*)malloc(sizeof(int) * (natoms > 0 ? natoms : 1));
+  int N = fill_params(theory, natoms, Z, P, first);
+  if (N < 0) { free(P); free(first); return -1; }
+  oracle_atom pc;
+  memset(&pc, 0, sizeof(pc));
+  pc.n_ao = 1;
+  double e = 0.0;
+  for (int a = 0; a < natoms; ++a) {
+    oracle_atom A = P[a];
+    A.rho[0] = A.rho[1] = A.rho[2] = 0.0;
+    const double* ra = xyz + 3 * a;
+    for (int i = 0; i < nepc; ++i) {
+      const double* rp = epc + 4 * i;
+      const double q = rp[3];
+      double W[4][4][4][4];
+      pair_eri(&A, ra, &pc, rp, W);
+      for (int m = 0; m < A.n_ao; ++m)
+        for (int n = 0; n < A.n_ao; ++n)
+          V[(size_t)(first[a] + m) * N + first[a] + n] += -1.0 * q * W[m][n][0][0];
+      double dx = rp[0] - ra[0], dy = rp[1] - ra[1], dz = rp[2] - ra[2];
+      e += A.core_charge * q / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+  }
+  *ecore_epc = e;
+  free(P); free(first);
+  return N;
+}
+
 static double coulomb1(const oracle_atom* p, int m, int n) {
   if (m == 0 && n == 0) return p->gss;
   if (m == 0 || n == 0) return p->gsp;

@@ -21,6 +21,9 @@ Reference semantics restated here (file:line in the MolDS tree):
   * E = 1/2 sum P (F + H) + E_core, F and H rebuilt ............. Cndo2.cpp:1324-1416
   * Mulliken q_A = Z_A - sum_mu P_mu,mu ......................... Cndo2.cpp:1187-1199, 1733-1747
   * MNDO heat of formation ...................................... mndo/Mndo.cpp:395-404
+  * environmental point charges: -q (mu nu|s s) in every non-guess Fock,
+    sum Z_A q / R in the energy .................................. mndo/Mndo.cpp:329-331,
+                                                                    474-484, 546-556, 6602-6613
   * dipole: STO-6G Cartesian matrix (C restatement), origin at the
     centre of core mass, -sum P X + origin * sum P S, core part ... Cndo2.cpp:1871-1944,
                                                                     base/Molecule.cpp:396-419
@@ -80,6 +83,7 @@ def lib():
             ip = ctypes.POINTER(ctypes.c_int)
             L.oracle_num_aos.argtypes = [ctypes.c_int, ctypes.c_int, ip]
             L.oracle_integrals.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp, dp, dp]
+            L.oracle_epc.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, ctypes.c_int, dp, dp, dp]
             L.oracle_fock.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp, dp, ctypes.c_int, dp]
             L.oracle_atom_info.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp]
             L.oracle_cartesian.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp]
@@ -133,6 +137,7 @@ class Molecule:
     theory: int
     Z: np.ndarray            # int32 atomic numbers
     xyz: np.ndarray          # (A, 3) bohr
+    epc: np.ndarray | None = None   # (n, 4): point charges x, y, z (bohr), charge
 
     @property
     def natoms(self):
@@ -153,17 +158,36 @@ class SCFResult:
     trace: list = field(default_factory=list)   # (iter, rms, diis_error, diis_on, damp_on)
     dipole: np.ndarray | None = None   # (3, 3): total, electronic, core; x y z [a.u.]
     vdw_energy: float = 0.0            # empirical dispersion energy, included in energy
+    core_epc: float = 0.0              # sum Z_A q / R over cores and point charges, included in energy
 
 
 class NotConverged(RuntimeError):
     pass
 
 
-def make_molecule(theory, Z, xyz_bohr) -> Molecule:
+def make_molecule(theory, Z, xyz_bohr, epc=None) -> Molecule:
     if isinstance(theory, str):
         theory = THEORIES[theory.lower()]
+    if epc is not None:
+        epc = np.ascontiguousarray(epc, dtype=np.float64).reshape(-1, 4)
+        epc = epc if epc.shape[0] else None
     return Molecule(int(theory), np.ascontiguousarray(Z, dtype=np.int32),
-                    np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1, 3))
+                    np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1, 3), epc)
+
+
+def epc_terms(mol: Molecule):
+    """Point-charge terms: V (N x N, the -q (mu nu|s s) one-centre blocks of
+    every non-guess Fock matrix) and sum Z_A q / R."""
+    N = num_aos(mol)
+    V = np.zeros((N, N))
+    e = np.zeros(1)
+    if mol.epc is None:
+        return V, 0.0
+    pc = np.ascontiguousarray(mol.epc, dtype=np.float64)
+    if lib().oracle_epc(mol.theory, mol.natoms, _ip(mol.Z), _dp(mol.xyz), int(pc.shape[0]), _dp(pc),
+                        _dp(V), _dp(e)) < 0:
+        raise ValueError("element without NDDO parameters")
+    return V, float(e[0])
 
 
 def num_aos(mol: Molecule) -> int:
@@ -251,6 +275,8 @@ def fock(mol: Molecule, S, eri, P, guess=False):
     eri_c = np.ascontiguousarray(eri) if eri.size else np.zeros((1, 4, 4, 4, 4))
     lib().oracle_fock(mol.theory, mol.natoms, _ip(mol.Z), _dp(S), _dp(eri_c), _dp(Pc),
                       1 if guess else 0, _dp(F))
+    if mol.epc is not None and not guess:
+        F += epc_terms(mol)[0]
     return F
 
 
@@ -358,7 +384,8 @@ def _properties(mol, S, eri, ecore, P, eps, C, info, iters, trace, params) -> SC
     evdw = 0.0
     if params.vdw or dtheory:
         evdw = vdw_energy(mol, 1.40 if dtheory else params.vdw_s6, 23.0 if dtheory else params.vdw_d)
-    energy = e_elec + ecore + evdw
+    eepc = epc_terms(mol)[1] if mol.epc is not None else 0.0
+    energy = e_elec + ecore + eepc + evdw
     firsts = np.concatenate([[0], np.cumsum(info[:, 1].astype(int))[:-1]])
     diag = np.diag(P)
     pop = np.array([diag[f:f + int(n)].sum() for f, n in zip(firsts, info[:, 1])])
@@ -367,7 +394,7 @@ def _properties(mol, S, eri, ecore, P, eps, C, info, iters, trace, params) -> SC
     if mol.theory == THEORIES["mndo"]:
         hof = energy - float(info[:, 2].sum()) + float(info[:, 3].sum())
     return SCFResult(True, iters, energy, ecore, eps, C, P, charges, hof, trace,
-                     dipole(mol, S, P), evdw)
+                     dipole(mol, S, P), evdw, eepc)
 
 
 # --------------------------------------------------------------------------
@@ -379,7 +406,7 @@ def parse_input(text: str):
     for line in text.splitlines():
         line = line.split("//")[0]
         tokens += line.lower().split()
-    theory, params, atoms = None, SCFParams(), []
+    theory, params, atoms, epcs = None, SCFParams(), [], []
     i = 0
     while i < len(tokens):
         t = tokens[i]
@@ -423,7 +450,18 @@ def parse_input(text: str):
                        float(tokens[i + 3]) * ANG2AU]
                 atoms.append((SYMBOL_TO_Z[sym], xyz))
                 i += 4
+        elif t == "epc":                      # InputParser.cpp:626-644
+            i += 1
+            while tokens[i] != "epc_end":
+                xyz = [float(tokens[i + k]) * ANG2AU for k in range(3)]
+                i += 3
+                q = 0.0
+                if tokens[i] == "charge":
+                    q = float(tokens[i + 1])
+                    i += 2
+                epcs.append(xyz + [q])
+            continue
         i += 1
     Z = np.array([a[0] for a in atoms], dtype=np.int32)
     xyz = np.array([a[1] for a in atoms], dtype=np.float64)
-    return make_molecule(theory, Z, xyz), params
+    return make_molecule(theory, Z, xyz, epcs if epcs else None), params
