@@ -6,6 +6,10 @@ MOLDS_GB300_TUNING, so each candidate is read fresh by the library):
   * tridiag_threads -- the CTA size (256, 512, 1024) of the FP64
     tridiagonalisation, per basis-size class (a batch of 64 molecules of each
     size: (H2O)_k clusters and random alkanes);
+  * vec_smem        -- whether the tridiagonal eigenvector kernel keeps its
+    inverse-iteration factors in shared memory (fewer, larger CTAs per SM) or
+    in the global workspace (up to 32 one-warp CTAs per SM), per basis-size
+    class, in batches run as concurrent molecule groups;
   * groups          -- the number of concurrent molecule groups of a fixed
     batch (1, 2, 3, 4, 6), for batches of 64 and 256 (H2O)32;
   * check_block     -- SCF iterations enqueued per convergence check (1, 2, 4).
@@ -103,7 +107,27 @@ def main():
     tlines = [f"tridiag_threads {nb} {t}" for nb, t in threads_rows]
     tlines[-1] = f"tridiag_threads 1073741824 {threads_rows[-1][1]}"
 
-    # 2. molecule groups per batch size
+    # 2. eigenvector-kernel factor storage per basis-size class, in batches
+    #    split into concurrent groups (the kernel's footprint decides how well
+    #    it shares the SMs with the other groups' kernels)
+    default_groups = ["groups 1 1", "groups 64 3", "groups 256 4"]
+    smem_rows = []
+    for kind, extra, nbasis in classes:
+        nmol = 256 if nbasis <= 192 else (128 if nbasis <= 240 else 64)
+        best = None
+        for v in (1, 0):
+            spec = dict(kind=kind, nmol=nmol, repeats=args.repeats, **extra)
+            dt = _time(tlines + default_groups + [f"vec_smem 1073741824 {v}"], spec)
+            log.append({"sweep": "vec_smem", "basis": nbasis, "molecules": nmol, "smem": v, "s": dt})
+            print(f"vec_smem basis {nbasis:4d} molecules {nmol:4d} smem {v}: {dt * 1e3:8.1f} ms", flush=True)
+            if best is None or dt < best[1]:
+                best = (v, dt)
+        smem_rows.append((nbasis, best[0]))
+    vlines = [f"vec_smem {nb} {v}" for nb, v in smem_rows]
+    vlines[-1] = f"vec_smem 1073741824 {smem_rows[-1][1]}"
+    tlines = tlines + vlines
+
+    # 3. molecule groups per batch size
     group_rows = []
     for nmol in (64, 256):
         best = None
@@ -117,7 +141,7 @@ def main():
         group_rows.append((nmol, best[0]))
     glines = ["groups 1 1"] + [f"groups {nm} {g}" for nm, g in group_rows]
 
-    # 3. iterations per convergence check
+    # 4. iterations per convergence check
     best = None
     for b in (1, 2, 4):
         spec = dict(kind="water32", nmol=256, repeats=args.repeats)

@@ -843,7 +843,7 @@ void launch_tri_vectors(const DevMol* mols, const int* list, int nlist, int max_
   if (nlist <= 0 || max_k <= 0) return;
   hh_set_attributes();
   const int pairs = std::max(1, std::min(kVecPerCta, tuned_vec_pairs(max_n)));
-  const bool vec_smem = tri_vectors_smem_bytes(max_n, true, pairs) <= (size_t)hh_optin_smem();
+  const bool vec_smem = tuned_vec_smem(max_n) && tri_vectors_smem_bytes(max_n, true, pairs) <= (size_t)hh_optin_smem();
   const size_t vsh = tri_vectors_smem_bytes(max_n, vec_smem, pairs);
   dim3 gv(nlist, (max_k + pairs - 1) / pairs);
   tri_vectors_kernel<<<gv, kVecThreads, vsh, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z,

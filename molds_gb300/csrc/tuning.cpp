@@ -7,6 +7,9 @@
 //   check_block <b>               SCF iterations enqueued per convergence check
 //   vec_pairs <n> <p>             bases up to n: p eigenpairs (lane pairs) per CTA of
 //                                 the tridiagonal eigenvector kernel (1..16)
+//   vec_smem <n> <s>              bases up to n: that kernel keeps its inverse-iteration
+//                                 factors in shared memory (1, when they fit) or in
+//                                 the global workspace (0)
 // MOLDS_GB300_TUNING names another table (the autotuner's candidates);
 // missing entries keep the built-in defaults.
 #include <dlfcn.h>
@@ -29,6 +32,7 @@ struct Table {
   std::vector<std::pair<int, int>> groups{{48, 1}, {96, 2}, {144, 3}, {192, 4}};
   std::vector<std::pair<int, int>> tridiag_threads{{1 << 30, 512}};
   std::vector<std::pair<int, int>> vec_pairs{{1 << 30, 16}};
+  std::vector<std::pair<int, int>> vec_smem{{1 << 30, 1}};
   int check_block = 2;
 };
 
@@ -54,7 +58,7 @@ void load() {
   std::ifstream f(env ? std::string(env) : default_path());
   if (!f) return;
   Table t;
-  bool groups = false, threads = false, pairs = false;
+  bool groups = false, threads = false, pairs = false, smem = false;
   std::string line;
   while (std::getline(f, line)) {
     if (line.empty() || line[0] == '#') continue;
@@ -79,11 +83,18 @@ void load() {
       if (!pairs) t.vec_pairs.clear();
       pairs = true;
       t.vec_pairs.emplace_back(a, b);
+    } else if (key == "vec_smem" && a >= 1 && (b == 0 || b == 1)) {
+      if (!smem) t.vec_smem.clear();
+      smem = true;
+      t.vec_smem.emplace_back(a, b);
     }
   }
   std::sort(t.groups.begin(), t.groups.end());
   std::sort(t.tridiag_threads.begin(), t.tridiag_threads.end());
   std::sort(t.vec_pairs.begin(), t.vec_pairs.end());
+  std::sort(t.vec_smem.begin(), t.vec_smem.end());
+  if (t.vec_smem.empty() || t.vec_smem.back().first < (1 << 30))
+    t.vec_smem.emplace_back(1 << 30, t.vec_smem.empty() ? 1 : t.vec_smem.back().second);
   if (t.vec_pairs.empty() || t.vec_pairs.back().first < (1 << 30))
     t.vec_pairs.emplace_back(1 << 30, t.vec_pairs.empty() ? 16 : t.vec_pairs.back().second);
   if (t.tridiag_threads.empty() || t.tridiag_threads.back().first < (1 << 30))
@@ -117,6 +128,12 @@ int tuned_vec_pairs(int n) {
   for (const auto& e : table().vec_pairs)
     if (n <= e.first) return e.second;
   return 16;
+}
+
+bool tuned_vec_smem(int n) {
+  for (const auto& e : table().vec_smem)
+    if (n <= e.first) return e.second != 0;
+  return true;
 }
 
 }  // namespace nddo
