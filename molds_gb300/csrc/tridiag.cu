@@ -336,6 +336,62 @@ __device__ __forceinline__ TriEval pair_eval(const double* __restrict__ d, const
   return out;
 }
 
+// The Sturm count of the FP32 copy of T (df, e2f) at x, split across the lane
+// pair as pair_eval: the same recurrences on FP32's pipe, which has 64 times
+// the FP64 one's throughput.  Such a count is exact for a perturbation of T
+// of some ten eps_32 ||T||, so it only ever proposes starting points; every
+// decision is taken on FP64 counts.
+__device__ __forceinline__ int pair_count_f32(const float* __restrict__ df, const float* __restrict__ e2f, int n,
+                                              int r, int side, float e2r, float x) {
+  float p0 = 1.0f, p1;
+  int s_prev = 0, cnt = 0, sg = 0;
+  auto sgn = [](float v) { const unsigned b = __float_as_uint(v); return (b << 1) == 0 ? -1 : (int)(b >> 31); };
+  auto step = [&](float dd, float ee, bool count) {
+    const float p2 = fmaf(dd - x, p1, -(ee * p0));
+    if (count) {
+      const int sv = sgn(p2);
+      const int sn = sv < 0 ? (s_prev ^ 1) : sv;   // a zero takes the sign opposite to its predecessor's
+      cnt += sn != s_prev;
+      s_prev = sn;
+    }
+    p0 = p1;
+    p1 = p2;
+    const int e0 = (int)((__float_as_uint(p0) >> 23) & 0xff), e1 = (int)((__float_as_uint(p1) >> 23) & 0xff);
+    const int em = e0 > e1 ? e0 : e1;
+    if (em != 0 && (em > 127 + 40 || em < 127 - 40)) {
+      const float scale = __uint_as_float((unsigned)(254 - em) << 23);   // 2^(127 - em)
+      p0 *= scale;
+      p1 *= scale;
+    }
+  };
+  if (side == 0) {
+    p1 = df[0] - x;
+    const int s1 = sgn(p1) < 0 ? 1 : sgn(p1);
+    if (r >= 1) { cnt = s1; s_prev = s1; }
+    for (int i = 1; i < r; ++i) step(df[i], e2f[i - 1], true);
+    if (r >= 1) {
+      sg = s_prev;
+      step(df[r], e2f[r - 1], false);   // (p0, p1) = (P_r, P_{r+1})
+    }
+  } else {
+    p1 = df[n - 1] - x;
+    s_prev = sgn(p1) < 0 ? 1 : sgn(p1);
+    cnt = s_prev;
+    for (int i = n - 2; i > r; --i) step(df[i], e2f[i], true);
+    sg = s_prev;
+  }
+  const int co = __shfl_xor_sync(0xffffffffu, cnt, 1);
+  const int so = __shfl_xor_sync(0xffffffffu, sg, 1);
+  const float w0 = __shfl_xor_sync(0xffffffffu, p0, 1);
+  const float w1 = __shfl_xor_sync(0xffffffffu, p1, 1);
+  const float P0 = side ? w0 : p0, P1 = side ? w1 : p1;
+  const float Q0 = side ? p0 : w0, Q1 = side ? p1 : w1;
+  const int sP = side ? so : sg, sQ = side ? sg : so;
+  const float f = fmaf(Q1, P1, -(e2r * P0 * Q0));
+  const int sf = sgn(f);
+  return cnt + co + (sf < 0 ? 1 : (sf ^ sP ^ sQ));
+}
+
 // uniform pseudo-random value in [-0.5, 0.5): the start vector of inverse iteration
 __device__ __forceinline__ double start_entry(unsigned int idx, unsigned int i) {
   unsigned long long z = ((unsigned long long)idx << 32) ^ (unsigned long long)(i * 0x9E3779B9u) ^ 0x2545F4914F6CDD1DULL;
@@ -442,6 +498,8 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   double* e = d + n;
   double* e2 = e + n;
   double* red = e2 + n;   // 2 * (kVecThreads / 32)
+  float* df = reinterpret_cast<float*>(red + 2 * (kVecThreads / 32));   // FP32 copy of d and e^2: n doubles' room
+  float* e2f = df + n;
   const double* tdd = td + mol.vec0;
   const double* tde = tdd + vstride;
   const int tid = threadIdx.x;
@@ -454,6 +512,8 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
     d[i] = di;
     e[i] = ei;
     e2[i] = ei * ei;
+    df[i] = (float)di;
+    e2f[i] = (float)(ei * ei);
     const double r = fabs(ei) + fabs(em);
     gl = fmin(gl, di - r);
     gu = fmax(gu, di + r);
@@ -480,10 +540,13 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   const int idx = lo + (valid ? c : 0);
   // Eigenvalue idx of T to round-off.  [a, b] always carries the true counts
   // of its ends (count(a) <= idx < count(b)).
-  //  0. warm start: the eigenvalue of the same index from the previous pass of
-  //     this SCF (eps holds it; a cold start stores NaN there).  Its count
-  //     narrows [a, b]; when the count is idx or idx + 1 (no other eigenvalue
-  //     between it and eigenvalue idx), step 2 starts from it directly;
+  //  0. a starting point: bisection on FP32 counts (pair_count_f32) from the
+  //     Gershgorin interval down to about 16 eps_32 ||T||; the eigenvalue of
+  //     the same index from the previous pass of this SCF (eps; NaN after a
+  //     cold start) replaces the interval's midpoint when it lies in the
+  //     interval (it is then at least as close).  The FP64 count at the
+  //     starting point narrows [a, b]; when it is idx or idx + 1 (no other
+  //     eigenvalue between it and eigenvalue idx), step 2 starts from it;
   //  1. otherwise bisection on the count until [a, b] holds eigenvalue idx
   //     alone (count(a) = idx, count(b) = idx + 1), or is below the tolerance
   //     (a cluster: the midpoint is the eigenvalue);
@@ -508,17 +571,28 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
     const int r = n / 2 - 1;
     const double e2r = e2[r];
     int ca = 0, cb = n;
-    bool adj = false;   // lam is a warm start with count idx or idx + 1
+    bool adj = false;   // lam is a starting point with count idx or idx + 1
     {
-      const double x0 = valid ? eps[mol.vec0 + idx] : 0.0;
-      const bool warm = valid && x0 > gl && x0 < gu;   // false for NaN
-      if (__any_sync(0xffffffffu, warm)) {
-        const TriEval ev = pair_eval<false>(d, e2, n, r, side, e2r, warm ? x0 : 0.5 * (gl + gu));
-        if (warm) {
-          if (ev.count > idx) { bnd = x0; cb = ev.count; }
-          else { a = x0; ca = ev.count; }
-          if (ev.count == idx || ev.count == idx + 1) { adj = true; lam = x0; }
+      constexpr double kEps32 = 1.1920928955078125e-07;
+      const float e2rf = e2f[r];
+      double a32 = gl, b32 = gu;
+      for (int it = 0; it < 48; ++it) {
+        const bool go = valid && b32 - a32 > 16.0 * kEps32 * (fabs(a32) + fabs(b32) + tnorm);
+        if (!__any_sync(0xffffffffu, go)) break;
+        const double mid = 0.5 * (a32 + b32);
+        const int c32 = pair_count_f32(df, e2f, n, r, side, e2rf, (float)mid);
+        if (go) {
+          if (c32 > idx) b32 = mid;
+          else a32 = mid;
         }
+      }
+      const double xp = valid ? eps[mol.vec0 + idx] : 0.0;
+      const double x0 = (xp >= a32 && xp <= b32) ? xp : 0.5 * (a32 + b32);   // the midpoint for NaN
+      const TriEval ev = pair_eval<false>(d, e2, n, r, side, e2r, x0);
+      if (valid && x0 > gl && x0 < gu) {
+        if (ev.count > idx) { bnd = x0; cb = ev.count; }
+        else { a = x0; ca = ev.count; }
+        if (ev.count == idx || ev.count == idx + 1) { adj = true; lam = x0; }
       }
     }
     for (int it = 0; it < 80; ++it) {
@@ -575,7 +649,7 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
   const int cl = tid >> 1;   // this pair's slot in the CTA
   if (vec_smem) {
     // factors and vector in shared memory, element i of slot cl at i * pairs + cl
-    double* fl = red + 2 * (kVecThreads / 32);
+    double* fl = red + 2 * (kVecThreads / 32) + n;
     double* fu1i = fl + (long long)n * pairs;
     double* fu2 = fu1i + (long long)n * pairs;
     double* xs = fu2 + (long long)n * pairs;
@@ -784,7 +858,7 @@ static void hh_set_attributes() {
 // tri_vectors_kernel: d, e, e^2 and the reduction slots; with vec_smem also
 // the factors, vector and pivot flags of its `pairs` inverse iterations
 size_t tri_vectors_smem_bytes(int n, bool vec_smem, int pairs) {
-  size_t b = (3 * (size_t)n + 2 * (kVecThreads / 32)) * sizeof(double);
+  size_t b = (4 * (size_t)n + 2 * (kVecThreads / 32)) * sizeof(double);   // d, e, e^2, FP32 d and e^2, slots
   if (vec_smem) b += (size_t)n * pairs * (4 * sizeof(double) + 1);
   return b;
 }
