@@ -599,12 +599,15 @@ void Batch::build_jobs(const std::vector<int>& which) {
   int n_big = 0;
   for (int m : which) n_big += h_mols[m].nao >= kGridShareMinN;
   const bool share = 4 * n_big <= grid_ctas_;
+  // largest basis the per-molecule kernels serve; every larger molecule of the
+  // list is tridiagonalised by the whole-GPU kernels alone
+  hh_served_max_n_ = share ? std::min(per_molecule, kGridShareMinN - 1) : per_molecule;
   for (int m : which) {
     const DevMol& d = h_mols[m];
     const int kd = std::min(d.nocc, d.nao - d.nocc);
     list_max_n_ = std::max(list_max_n_, d.nao);
     hh_max_k_ = std::max(hh_max_k_, kd);
-    if (d.nao <= per_molecule && !(share && d.nao >= kGridShareMinN)) {
+    if (d.nao <= hh_served_max_n_) {
       hh_small_.push_back(m);
       hh_small_max_n_ = std::max(hh_small_max_n_, d.nao);
       hh_small_max_k_ = std::max(hh_small_max_k_, kd);
@@ -684,7 +687,7 @@ void Batch::upload_list(const std::vector<int>& which) {
       if (n > lo && n <= hi) {
         b.push_back(m);
         mx = std::max(mx, n);
-        if (n <= hh_back_max_n()) mx_hh = std::max(mx_hh, n);
+        if (n <= hh_served_max_n_) mx_hh = std::max(mx_hh, n);
       }
     }
     lo = hi;
@@ -1027,7 +1030,7 @@ void Batch::eigen_step(const ScfSettings& s) {
       if (bucket_hh_max_n_[b] == 0) continue;
       launches_ += 1;
       launch_hh_tridiag(d_mols, bucket_dev_[b], (int)buckets_[b].size(), bucket_hh_max_n_[b], d_state, 1, d_F, d_G64,
-                        d_td, vec_total_, d_S[4], hh_back_max_n(), stream_);
+                        d_td, vec_total_, d_S[4], hh_served_max_n_, stream_);
     }
     // the whole-GPU path: each chunk's molecules share one cooperative launch
     for (const GridChunk& c : grid_chunks_) {

@@ -224,6 +224,7 @@ class Batch {
   int hh_small_max_n_ = 0, hh_small_max_k_ = 0;
   int hh_large_max_n_ = 0, hh_large_max_k_ = 0;
   std::vector<int> bucket_hh_max_n_;     // per size bucket: largest basis on the per-molecule kernels
+  int hh_served_max_n_ = 0;              // the per-molecule kernels serve bases up to this; larger: whole-GPU kernels
   // whole-GPU path: the large molecules in chunks of at most one per SM, each
   // chunk one cooperative launch whose CTAs are split over its molecules
   struct GridChunk { int first, count, nctas, map_off, max_k; };

@@ -75,7 +75,7 @@ void load() {
       if (!groups) t.groups.clear();
       groups = true;
       t.groups.emplace_back(a, b);
-    } else if (key == "tridiag_threads" && a >= 1 && (b == 256 || b == 512 || b == 1024)) {
+    } else if (key == "tridiag_threads" && a >= 1 && b >= 32 && b <= 1024 && (b & (b - 1)) == 0) {
       if (!threads) t.tridiag_threads.clear();
       threads = true;
       t.tridiag_threads.emplace_back(a, b);
