@@ -781,14 +781,17 @@ hh_back_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, co
   for (int i = warp; i < n; i += kBackWarps) zs[i * kP + lane] = c < k ? (T)Zm[(long long)i * k + c] : (T)0;
   for (int i = tid; i < n; i += kBackCols * kBackWarps) taus[i] = (T)tt[i];
   __syncthreads();
+  int par = 0;   // parity of the reflectors applied so far (tau == 0 ones are skipped)
   for (int j = n - 3; j >= 0; --j) {
     const T tau = taus[j];
     if (tau == (T)0) continue;
     const double* ug = Wm + (long long)j * n;
     const T* u;
     if (sizeof(T) == 4) {
-      // two staging rows: a warp still updating with reflector j + 1 reads the other one
-      T* ur = urow + (j & 1) * n;
+      // two staging rows: a warp still updating with the previous applied
+      // reflector reads the other one
+      T* ur = urow + par * n;
+      par ^= 1;
       for (int i = j + 1 + tid; i < n; i += kBackCols * kBackWarps) ur[i] = (T)ug[i];
       __syncthreads();
       u = ur;
