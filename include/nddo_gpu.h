@@ -198,6 +198,15 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
 typedef struct nddo_batch nddo_batch;
 int nddo_batch_create(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, const int* atomic_numbers,
                       const double* xyz_bohr, int diis_num_error_vect, nddo_batch** out);
+/* nddo_batch_create with environmental point charges per molecule (as
+ * nddo_set_molecule_epc): n_epc[i] charges for molecule i (n_epc may be
+ * NULL: none), their rows of x, y, z [bohr] and charge concatenated in
+ * molecule order in epc_xyzq.  nddo_batch_set_coordinates moves the atoms
+ * only; nddo_scf_result.core_epc_coulomb carries each molecule's core-EPC
+ * energy. */
+int nddo_batch_create_epc(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, const int* atomic_numbers,
+                          const double* xyz_bohr, const int* n_epc, const double* epc_xyzq, int diis_num_error_vect,
+                          nddo_batch** out);
 /* Integrals + SCF + energies of every molecule, on the device only. */
 int nddo_batch_run(nddo_batch* b, const nddo_scf_params* params);
 /* As nddo_batch_run with DoSCF's requiresGuess: 0 starts every molecule from

@@ -105,6 +105,8 @@ SIGNATURES = {
                                       ctypes.POINTER(ScfResultC), _DP]),
     "nddo_batch_create": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_void_p)]),
+    "nddo_batch_create_epc": (ctypes.c_int, [_CTX, ctypes.c_int, ctypes.c_int, _IP, _IP, _DP, _IP, _DP, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_void_p)]),
     "nddo_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScfParamsC)]),
     "nddo_batch_run_ex": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ScfParamsC), ctypes.c_int]),
     "nddo_batch_set_coordinates": (ctypes.c_int, [ctypes.c_void_p, _DP]),
@@ -417,6 +419,15 @@ def batch_scf(theory, molecules, params: SCFParams | None = None, context: Conte
     Returns (results, charges): a list of dicts and a list of per-molecule
     Mulliken charge arrays."""
     ctx = context or Context()
+    if any(getattr(m, "epc", None) is not None for m in molecules):
+        # molecules with point charges: a resident batch (the context's cached
+        # batch keys on atoms only)
+        b = ResidentBatch(theory, molecules, (params or SCFParams()).diis_num_error_vect, context=ctx)
+        try:
+            b.run(params or SCFParams())
+            return b.results()
+        finally:
+            b.close()
     th = THEORIES[theory.lower()] if isinstance(theory, str) else int(theory)
     nat = np.array([m.natoms for m in molecules], dtype=np.int32)
     Z = np.ascontiguousarray(np.concatenate([m.Z for m in molecules]), dtype=np.int32)
@@ -446,8 +457,18 @@ class ResidentBatch:
         Z = np.ascontiguousarray(np.concatenate([m.Z for m in molecules]), dtype=np.int32)
         xyz = np.ascontiguousarray(np.concatenate([np.asarray(m.xyz).reshape(-1, 3) for m in molecules]))
         h = ctypes.c_void_p()
-        self.ctx.check(self.ctx.lib.nddo_batch_create(self.ctx.h, th, len(molecules), _ip(self.nat), _ip(Z), _dp(xyz),
-                                                      diis_num_error_vect, ctypes.byref(h)))
+        # environmental point charges per molecule (Molecule.epc rows x, y, z, q)
+        epcs = [np.zeros((0, 4)) if getattr(m, "epc", None) is None else np.asarray(m.epc, dtype=np.float64).reshape(-1, 4)
+                for m in molecules]
+        n_epc = np.array([e.shape[0] for e in epcs], dtype=np.int32)
+        if n_epc.any():
+            ep = np.ascontiguousarray(np.concatenate(epcs))
+            self.ctx.check(self.ctx.lib.nddo_batch_create_epc(self.ctx.h, th, len(molecules), _ip(self.nat), _ip(Z),
+                                                              _dp(xyz), _ip(n_epc), _dp(ep), diis_num_error_vect,
+                                                              ctypes.byref(h)))
+        else:
+            self.ctx.check(self.ctx.lib.nddo_batch_create(self.ctx.h, th, len(molecules), _ip(self.nat), _ip(Z),
+                                                          _dp(xyz), diis_num_error_vect, ctypes.byref(h)))
         self.h = h
         self.n = len(molecules)
 
@@ -470,7 +491,8 @@ class ResidentBatch:
         offs = np.concatenate([[0], np.cumsum(self.nat)])
         out = [dict(status=r.status, iterations=r.iterations, energy=r.energy, core_repulsion=r.core_repulsion,
                     heat_of_formation=r.heat_of_formation, final_rms=r.final_rms,
-                    final_diis_error=r.final_diis_error, dipole=_dipole3(r), vdw_energy=r.vdw_energy) for r in res]
+                    final_diis_error=r.final_diis_error, dipole=_dipole3(r), vdw_energy=r.vdw_energy,
+                    core_epc_coulomb=r.core_epc_coulomb) for r in res]
         return out, [ch[offs[i]:offs[i + 1]] for i in range(self.n)]
 
     def device_bytes(self) -> int:

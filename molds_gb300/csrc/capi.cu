@@ -583,6 +583,11 @@ int nddo_batch_scf(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, con
 
 int nddo_batch_create(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, const int* Z, const double* xyz,
                       int diis_m, nddo_batch** out) {
+  return nddo_batch_create_epc(ctx, theory, n_mol, n_atoms, Z, xyz, nullptr, nullptr, diis_m, out);
+}
+
+int nddo_batch_create_epc(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, const int* Z, const double* xyz,
+                          const int* n_epc, const double* epc, int diis_m, nddo_batch** out) {
   return guarded(ctx, [&]() {
     if (!out) return fail(ctx, NDDO_ERR_ARGUMENT, "null output handle");
     *out = nullptr;
@@ -590,13 +595,17 @@ int nddo_batch_create(nddo_ctx* ctx, int theory, int n_mol, const int* n_atoms, 
     if (n_mol < 1 || !n_atoms || !Z || !xyz) return fail(ctx, NDDO_ERR_ARGUMENT, "bad batch arguments");
     if (diis_m < 0 || diis_m > nddo::kMaxDiis) return fail(ctx, NDDO_ERR_ARGUMENT, "diis_num_error_vect must be in 0..8");
     std::vector<nddo::MoleculeInput> mols(n_mol);
-    size_t off = 0;
+    size_t off = 0, eoff = 0;
     for (int i = 0; i < n_mol; ++i) {
       if (n_atoms[i] < 1) return fail(ctx, NDDO_ERR_ARGUMENT, "molecule without atoms");
       mols[i].theory = theory;
       mols[i].Z.assign(Z + off, Z + off + n_atoms[i]);
       mols[i].xyz.assign(xyz + 3 * off, xyz + 3 * (off + n_atoms[i]));
       off += n_atoms[i];
+      const int ne = n_epc ? n_epc[i] : 0;
+      if (ne < 0 || (ne > 0 && !epc)) return fail(ctx, NDDO_ERR_ARGUMENT, "invalid point charges");
+      if (ne > 0) mols[i].epc.assign(epc + 4 * eoff, epc + 4 * (eoff + ne));
+      eoff += ne;
     }
     std::unique_ptr<nddo::GroupedBatch> b(
         new nddo::GroupedBatch(ctx->engine.get(), mols, diis_m, nddo::GroupedBatch::default_groups(n_mol)));

@@ -165,3 +165,41 @@ def test_forces_carry_no_explicit_epc_term(ctx):
             xm[a, k] -= h
             fd[a, k] = -(frozen(xp) - frozen(xm)) / (2 * h)
     assert np.max(np.abs(F - fd)) < 2e-7, np.max(np.abs(F - fd))
+
+
+def test_batch_with_point_charges(ctx):
+    """nddo_batch_create_epc: molecules with and without charges in one
+    resident batch, each against the oracle; new coordinates move the atoms
+    and keep the charges."""
+    names = ["ch4_mndo", "c2h6_mndo", "ch3f_mndo", "ch3cl_mndo"]
+    mols, oms = [], []
+    for i, nm in enumerate(names):
+        mol, p = O.parse_input(FIX[nm]["input"])
+        pc = point_charges(mol.xyz, 2 + 3 * i, 20 + i) if i != 1 else None
+        mols.append(M.Molecule(mol.Z, mol.xyz, pc))
+        oms.append(O.make_molecule(mol.theory, mol.Z, mol.xyz, pc))
+    b = M.ResidentBatch("mndo", mols, context=ctx)
+    b.run(_params(p))
+    res, charges = b.results()
+    for om, r, q in zip(oms, res, charges):
+        ref = O.scf(om, p)
+        assert r["status"] == M.STATUS_CONVERGED and r["iterations"] == ref.iterations
+        assert abs(r["energy"] - ref.energy) < 1e-8
+        assert abs(r["core_epc_coulomb"] - ref.core_epc) < 1e-11
+        assert np.max(np.abs(q - ref.charges)) < 1e-6
+    shift = np.random.default_rng(9).normal(scale=0.03, size=(sum(m.natoms for m in mols), 3))
+    b.set_coordinates(np.concatenate([m.xyz for m in mols]) + shift)
+    b.run(_params(p), requires_guess=False)
+    res, _ = b.results()
+    o = 0
+    for om, r in zip(oms, res):
+        moved = O.make_molecule(om.theory, om.Z, om.xyz + shift[o:o + om.natoms], om.epc)
+        o += om.natoms
+        ref = O.scf(moved, p)
+        assert abs(r["energy"] - ref.energy) < 1e-8
+        assert abs(r["core_epc_coulomb"] - ref.core_epc) < 1e-11
+    b.close()
+    # the one-call wrapper takes the same molecules
+    res2, _ = M.batch_scf("mndo", mols, _params(p), context=ctx)
+    for om, r in zip(oms, res2):
+        assert abs(r["energy"] - O.scf(om, p).energy) < 1e-8
