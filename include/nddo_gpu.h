@@ -273,11 +273,18 @@ typedef struct {
   int lane;
   double energy, core_repulsion, heat_of_formation, final_rms;
   double t_submit, t_admit, t_done;
+  double core_epc_coulomb;     /* core-EPC Coulomb energy [Eh], included in energy (0 without charges) */
 } nddo_serve_result;
 int nddo_server_create(nddo_ctx* ctx, const nddo_scf_params* params, size_t hbm_budget_bytes, int max_basis,
                        nddo_server** out);
 int nddo_server_submit(nddo_server* s, int theory, int n_atoms, const int* atomic_numbers, const double* xyz_bohr,
                        long long* ticket);
+/* nddo_server_submit with environmental point charges (as
+ * nddo_set_molecule_epc): n_epc rows of x, y, z [bohr] and charge.  Each
+ * lane's pool holds as many point charges as atoms; a request with more
+ * than its lane can ever hold is refused with NDDO_ERR_ARGUMENT. */
+int nddo_server_submit_epc(nddo_server* s, int theory, int n_atoms, const int* atomic_numbers, const double* xyz_bohr,
+                           int n_epc, const double* epc_xyzq, long long* ticket);
 int nddo_server_poll(nddo_server* s, int max_wait_us, int max_results, nddo_serve_result* out, double* charges,
                      size_t charges_capacity, int* n_out);
 /* Requests queued (not yet admitted) and molecules in the SCF. */

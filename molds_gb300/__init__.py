@@ -64,7 +64,7 @@ class ServeResultC(ctypes.Structure):
                 ("n_atoms", ctypes.c_int), ("lane", ctypes.c_int), ("energy", ctypes.c_double),
                 ("core_repulsion", ctypes.c_double), ("heat_of_formation", ctypes.c_double),
                 ("final_rms", ctypes.c_double), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double),
-                ("t_done", ctypes.c_double)]
+                ("t_done", ctypes.c_double), ("core_epc_coulomb", ctypes.c_double)]
 
 
 # every entry point of include/nddo_gpu.h with its argument types
@@ -127,6 +127,8 @@ SIGNATURES = {
                                           ctypes.POINTER(ctypes.c_void_p)]),
     "nddo_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _IP, _DP,
                                           ctypes.POINTER(ctypes.c_longlong)]),
+    "nddo_server_submit_epc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _IP, _DP, ctypes.c_int, _DP,
+                                              ctypes.POINTER(ctypes.c_longlong)]),
     "nddo_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ServeResultC), _DP,
                                         ctypes.c_size_t, _IP]),
     "nddo_server_pending": (ctypes.c_int, [ctypes.c_void_p, _IP, _IP]),
@@ -575,7 +577,14 @@ class Server:
         Z = np.ascontiguousarray(molecule.Z, dtype=np.int32)
         xyz = np.ascontiguousarray(molecule.xyz, dtype=np.float64).reshape(-1, 3)
         ticket = ctypes.c_longlong()
-        self.ctx.check(self.lib.nddo_server_submit(self.h, t, int(Z.shape[0]), _ip(Z), _dp(xyz), ctypes.byref(ticket)))
+        epc = getattr(molecule, "epc", None)
+        if epc is not None and np.size(epc):
+            ep = np.ascontiguousarray(epc, dtype=np.float64).reshape(-1, 4)
+            self.ctx.check(self.lib.nddo_server_submit_epc(self.h, t, int(Z.shape[0]), _ip(Z), _dp(xyz),
+                                                           int(ep.shape[0]), _dp(ep), ctypes.byref(ticket)))
+        else:
+            self.ctx.check(self.lib.nddo_server_submit(self.h, t, int(Z.shape[0]), _ip(Z), _dp(xyz),
+                                                       ctypes.byref(ticket)))
         return ticket.value
 
     def poll(self, max_wait_us: int = 1000, max_results: int = 512):
@@ -591,7 +600,7 @@ class Server:
             res.append({"ticket": o.ticket, "status": o.status, "iterations": o.iterations, "energy": o.energy,
                         "core_repulsion": o.core_repulsion, "heat_of_formation": o.heat_of_formation,
                         "final_rms": o.final_rms, "lane": o.lane, "t_submit": o.t_submit, "t_admit": o.t_admit,
-                        "t_done": o.t_done, "charges": q})
+                        "t_done": o.t_done, "core_epc_coulomb": o.core_epc_coulomb, "charges": q})
         return res
 
     def pending(self):

@@ -782,13 +782,20 @@ int nddo_server_create(nddo_ctx* ctx, const nddo_scf_params* params, size_t hbm_
 }
 
 int nddo_server_submit(nddo_server* h, int theory, int n_atoms, const int* Z, const double* xyz, long long* ticket) {
+  return nddo_server_submit_epc(h, theory, n_atoms, Z, xyz, 0, nullptr, ticket);
+}
+
+int nddo_server_submit_epc(nddo_server* h, int theory, int n_atoms, const int* Z, const double* xyz, int n_epc,
+                           const double* epc, long long* ticket) {
   if (!h) return NDDO_ERR_ARGUMENT;
   return guarded(h->ctx, [&]() -> int {
     if (n_atoms < 1 || !Z || !xyz || !ticket) return fail(h->ctx, NDDO_ERR_ARGUMENT, "bad request arguments");
+    if (n_epc < 0 || (n_epc > 0 && !epc)) return fail(h->ctx, NDDO_ERR_ARGUMENT, "invalid point charges");
     nddo::MoleculeInput in;
     in.theory = theory;
     in.Z.assign(Z, Z + n_atoms);
     in.xyz.assign(xyz, xyz + 3 * (size_t)n_atoms);
+    if (n_epc > 0) in.epc.assign(epc, epc + 4 * (size_t)n_epc);
     *ticket = h->s->submit(in);
     return (int)NDDO_OK;
   });
@@ -817,6 +824,7 @@ int nddo_server_poll(nddo_server* h, int max_wait_us, int max_results, nddo_serv
       o.ticket = r.ticket; o.status = r.status; o.iterations = r.iterations; o.n_atoms = r.natoms; o.lane = r.lane;
       o.energy = r.energy; o.core_repulsion = r.core_repulsion; o.heat_of_formation = r.heat_of_formation;
       o.final_rms = r.final_rms; o.t_submit = r.t_submit; o.t_admit = r.t_admit; o.t_done = r.t_done;
+      o.core_epc_coulomb = r.core_epc;
       if (charges) {
         std::copy(r.charges.begin(), r.charges.end(), charges + used);
         used += r.charges.size();

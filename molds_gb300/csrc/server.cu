@@ -12,12 +12,14 @@ namespace {
 // (at most 3.2 N^2 doubles, an all-heavy molecule), pair records, energies and
 // index lists (at most N^2 / 2 pairs), atoms and charges (at most N^2 / 16).
 constexpr double kBlocksPerMat = 3.2, kPairsPerMat = 0.5, kAtomsPerMat = 1.0 / 16.0;
+constexpr double kEpcsPerAtom = 1.0;   // point-charge arena: as many charges as atoms
 constexpr int kSmallLaneMaxN = 194;   // tridiagonalisation in shared memory
 constexpr int kMidLaneMaxN = 400;
 
 BatchCapacity lane_capacity(size_t bytes, int max_n, int min_n, int diis_m, int ws_slots) {
   const double per_mat = (double)Batch::bytes_per_mat_element(diis_m) + kBlocksPerMat * 8.0 +
-                         kPairsPerMat * (sizeof(DevPair) + 8.0 + 8.0) + kAtomsPerMat * (sizeof(DevAtom) + 8.0);
+                         kPairsPerMat * (sizeof(DevPair) + 8.0 + 8.0) +
+                         kAtomsPerMat * (sizeof(DevAtom) + 8.0 + kEpcsPerAtom * 4 * sizeof(double));
   // the Jacobi workspaces come off the top
   const long long np = (max_n + 63) / 64 * 64;
   const double ws_bytes = max_n > 138 ? (double)ws_slots * np * np * (2 * 4 + 3 * 8) : 0.0;
@@ -27,6 +29,7 @@ BatchCapacity lane_capacity(size_t bytes, int max_n, int min_n, int diis_m, int 
   c.blocks = (long long)(kBlocksPerMat * c.mat) + 128;
   c.pairs = (long long)(kPairsPerMat * c.mat) + 64;
   c.atoms = (long long)(kAtomsPerMat * c.mat) + 64;
+  c.epcs = (long long)(kEpcsPerAtom * (double)c.atoms);
   const long long min_mat = std::max<long long>(32, ((long long)min_n * min_n + 31) / 32 * 32);
   c.vec = c.mat / 4 + 1024;
   c.slots = (int)std::max<long long>(1, std::min<long long>(4096, c.mat / min_mat));
@@ -136,8 +139,11 @@ long long Server::submit(const MoleculeInput& in) {
   if ((int)in.xyz.size() != 3 * (int)in.Z.size()) throw std::invalid_argument("coordinate count does not match atom count");
   if (in.theory < 0 || in.theory >= NDDO_NUM_THEORY_SLOTS) throw std::invalid_argument("unknown theory");
   if (nelec % 2) throw std::invalid_argument("Total number of valence electrons is odd. totalNumberValenceElectrons=" + std::to_string(nelec));
+  if (in.epc.size() % 4) throw std::invalid_argument("point charges need x, y, z and a charge each");
   for (auto& L : lanes_) {
     if (nao > L->lo && nao <= L->hi) {
+      if ((long long)(in.epc.size() / 4) > L->b->epc_capacity())
+        throw std::invalid_argument("more point charges than the lane's pool holds");
       const long long t = next_ticket_++;
       ++outstanding_;
       {
@@ -227,9 +233,15 @@ bool Server::lane_step(Lane& L) {
       req = L.queue.front();
       tq = L.queue_t.front();
     }
-    const int slot = b.admit(req.second);
-    if (slot < 0 && L.active.empty() && fresh.empty()) {
-      // cannot fit even into an empty lane: fail the request rather than wait forever
+    int slot = -1;
+    bool invalid = false;
+    try {
+      slot = b.admit(req.second);
+    } catch (const std::invalid_argument&) {
+      invalid = true;   // a molecule its layout rejects (coincident atoms, a charge on an atom, ...)
+    }
+    if (invalid || (slot < 0 && L.active.empty() && fresh.empty())) {
+      // rejected, or cannot fit even into an empty lane: fail the request rather than wait forever
       ServeResult r;
       r.ticket = req.first;
       r.status = kFailed;
@@ -287,6 +299,7 @@ bool Server::lane_step(Lane& L) {
       r.core_repulsion = st.ecore;
       r.heat_of_formation = st.heat_of_formation;
       r.final_rms = st.rms;
+      r.core_epc = st.ecore_epc;
       r.natoms = d.natoms;
       r.lane = L.index;
       r.t_submit = L.slot_tsubmit[m];

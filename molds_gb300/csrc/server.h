@@ -31,6 +31,7 @@ struct ServeResult {
   int status = 0, iterations = 0, natoms = 0, lane = 0;
   double energy = 0, core_repulsion = 0, heat_of_formation = 0, final_rms = 0;
   double t_submit = 0, t_admit = 0, t_done = 0;   // seconds on the server clock
+  double core_epc = 0;                            // core-point-charge Coulomb energy (included in energy)
   std::vector<double> charges;
 };
 

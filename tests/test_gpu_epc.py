@@ -203,3 +203,29 @@ def test_batch_with_point_charges(ctx):
     res2, _ = M.batch_scf("mndo", mols, _params(p), context=ctx)
     for om, r in zip(oms, res2):
         assert abs(r["energy"] - O.scf(om, p).energy) < 1e-8
+
+
+def test_serving_with_point_charges(ctx):
+    """nddo_server_submit_epc: requests with charges in a stream with plain
+    ones, against the oracle; a request with a charge on an atom fails alone
+    without stopping the server."""
+    names = ["ch3f_pm3", "c2h6_pm3", "ch3cl_pm3"]
+    p = O.parse_input(FIX[names[0]]["input"])[1]   # one SCF block for the whole stream
+    srv = M.Server(_params(p), context=ctx, hbm_budget_bytes=2 << 30, max_basis=256)
+    want = {}
+    for i, nm in enumerate(names):
+        mol = O.parse_input(FIX[nm]["input"])[0]
+        pc = point_charges(mol.xyz, 3 + 4 * i, 40 + i) if i != 1 else None
+        t = srv.submit("pm3", M.Molecule(mol.Z, mol.xyz, pc))
+        want[t] = O.scf(O.make_molecule(mol.theory, mol.Z, mol.xyz, pc), p)
+    mol, _ = O.parse_input(FIX["ch4_pm3"]["input"])
+    bad = srv.submit("pm3", M.Molecule(mol.Z, mol.xyz, np.c_[mol.xyz[:1], [0.5]]))
+    res = {r["ticket"]: r for r in srv.drain()}
+    srv.close()
+    assert res[bad]["status"] == M.STATUS_FAILED
+    for t, ref in want.items():
+        r = res[t]
+        assert r["status"] == M.STATUS_CONVERGED and r["iterations"] == ref.iterations
+        assert abs(r["energy"] - ref.energy) < 1e-8
+        assert abs(r["core_epc_coulomb"] - ref.core_epc) < 1e-11
+        assert np.max(np.abs(r["charges"] - ref.charges)) < 1e-6
