@@ -406,13 +406,38 @@ __device__ __forceinline__ double start_entry(unsigned int idx, unsigned int i) 
 // with the row interchanges, then back substitution), in place in x (element
 // i at x[i * ld]).  b is the pseudo-random start vector (start) or scale * x;
 // returns sum y_i^2, so the normalisation costs no extra pass.
+// Both sweeps load the operands of kSolveBlock rows before storing their
+// results: every row reads x only at rows no earlier store of the sweep has
+// written (ld >= 1), so the order is the plain loop's, and the loads of a
+// block overlap instead of each waiting for the previous row's store (the
+// factors and the vector may live in L2, in the global scratch).
+constexpr int kSolveBlock = 8;
+
 template <typename PivT>
 __device__ __forceinline__ double tri_solve(int n, int ld, double* __restrict__ x, const double* __restrict__ fl,
                                             const double* __restrict__ fu1i, const double* __restrict__ fu2,
                                             const PivT* __restrict__ piv, const double* __restrict__ e, bool start,
                                             double scale, unsigned idx) {
   double cb = start ? start_entry(idx, 0) : scale * x[0];
-  for (int i = 0; i + 1 < n; ++i) {
+  int i = 0;
+  for (; i + kSolveBlock < n; i += kSolveBlock) {   // rows i .. i + kSolveBlock - 1, all below n - 1
+    double bn[kSolveBlock], l[kSolveBlock];
+    bool pv[kSolveBlock];
+#pragma unroll
+    for (int u = 0; u < kSolveBlock; ++u) {
+      const long long o = (long long)(i + u) * ld;
+      bn[u] = start ? start_entry(idx, (unsigned)(i + u + 1)) : scale * x[o + ld];
+      l[u] = fl[o];
+      pv[u] = piv[o] != (PivT)0;
+    }
+#pragma unroll
+    for (int u = 0; u < kSolveBlock; ++u) {
+      const long long o = (long long)(i + u) * ld;
+      if (pv[u]) { x[o] = bn[u]; cb = fma(-l[u], bn[u], cb); }
+      else { x[o] = cb; cb = fma(-l[u], cb, bn[u]); }
+    }
+  }
+  for (; i + 1 < n; ++i) {
     const long long o = (long long)i * ld;
     const double bn = start ? start_entry(idx, (unsigned)(i + 1)) : scale * x[o + ld];
     const double l = fl[o];
@@ -423,7 +448,27 @@ __device__ __forceinline__ double tri_solve(int n, int ld, double* __restrict__ 
   double x2 = 0.0, x1 = cb * fu1i[on];
   x[on] = x1;
   double ss = x1 * x1;
-  for (int i = n - 2; i >= 0; --i) {
+  i = n - 2;
+  for (; i - kSolveBlock + 1 >= 0; i -= kSolveBlock) {   // rows i down to i - kSolveBlock + 1
+    double u3[kSolveBlock], f2[kSolveBlock], xv[kSolveBlock], f1[kSolveBlock];
+#pragma unroll
+    for (int u = 0; u < kSolveBlock; ++u) {
+      const long long o = (long long)(i - u) * ld;
+      u3[u] = piv[o] ? e[i - u + 1] : 0.0;
+      f2[u] = fu2[o];
+      xv[u] = x[o];
+      f1[u] = fu1i[o];
+    }
+#pragma unroll
+    for (int u = 0; u < kSolveBlock; ++u) {
+      const double xi = fma(-u3[u], x2, fma(-f2[u], x1, xv[u])) * f1[u];
+      x[(long long)(i - u) * ld] = xi;
+      ss = fma(xi, xi, ss);
+      x2 = x1;
+      x1 = xi;
+    }
+  }
+  for (; i >= 0; --i) {
     const long long o = (long long)i * ld;
     const double u3 = piv[o] ? e[i + 1] : 0.0;
     const double xi = fma(-u3, x2, fma(-fu2[o], x1, x[o])) * fu1i[o];
@@ -472,7 +517,17 @@ __device__ __forceinline__ void inverse_iteration(int n, int ld, const double* _
   const double r1 = s1s > 0.0 ? rsqrt(s1s) : 0.0;
   const double s2s = tri_solve(n, ld, x, fl, fu1i, fu2, piv, e, false, r1, idx);
   const double r2 = s2s > 0.0 ? rsqrt(s2s) : 0.0;
-  for (int i = 0; i < n; ++i) out[(long long)i * out_ld] = x[(long long)i * ld] * r2;
+  // out may be x itself (the global scratch path): each block's loads come
+  // before its stores, and every element is read before it is written
+  int i = 0;
+  for (; i + kSolveBlock <= n; i += kSolveBlock) {
+    double v[kSolveBlock];
+#pragma unroll
+    for (int u = 0; u < kSolveBlock; ++u) v[u] = x[(long long)(i + u) * ld];
+#pragma unroll
+    for (int u = 0; u < kSolveBlock; ++u) out[(long long)(i + u) * out_ld] = v[u] * r2;
+  }
+  for (; i < n; ++i) out[(long long)i * out_ld] = x[(long long)i * ld] * r2;
 }
 
 // grid: (list entry, chunk of `pairs` <= kVecPerCta indices); a lane pair per wanted
