@@ -824,10 +824,11 @@ hh_back_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, co
   if (cb >= k) return;
   constexpr int kP = kBackCols + 1;
   T* zs = reinterpret_cast<T*>(bsm);                                   // n x kP
-  T* red = zs + (long long)n * kP;                                     // kBackWarps x kBackCols
-  T* dotv = red + kBackWarps * kBackCols;                              // kBackCols
-  T* taus = dotv + kBackCols;                                          // n
-  T* urow = taus + n;                                                  // 2 n (FP32: staged reflectors)
+  T* red = zs + (long long)n * kP;                                     // 2 x kBackWarps x kBackCols
+  T* dotv = red + 2 * kBackWarps * kBackCols;                          // 2 x kBackCols
+  T* taus = dotv + 2 * kBackCols;                                      // n
+  T* urow = taus + n;                                                  // 2 n (FP32: staged reflectors;
+                                                                       // FP64: the pairs' u_{j-1}.u_j)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const double* Zm = Z + mol.mat0;
   const double* Wm = W + mol.mat0;
@@ -835,9 +836,66 @@ hh_back_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, co
   const int c = cb + lane;
   for (int i = warp; i < n; i += kBackWarps) zs[i * kP + lane] = c < k ? (T)Zm[(long long)i * k + c] : (T)0;
   for (int i = tid; i < n; i += kBackCols * kBackWarps) taus[i] = (T)tt[i];
+  int jstart = n - 3;
+  if (sizeof(T) == 8) {
+    // FP64: reflectors in pairs (j, j - 1), one reduction round per pair.
+    // With d = u^T z over the unmodified z and c = u_{j-1}^T u_j,
+    //   H_{j-1} H_j z = z - a u_j - b u_{j-1},  a = tau_j d_j,
+    //   b = tau_{j-1} (d_{j-1} - c a),
+    // the same two FMAs per element and reflector as one at a time, with
+    // half the barriers and single-warp sums.  c of every pair first.
+    T* cs = urow;
+    for (int q = warp; n - 3 - 2 * q >= 1; q += kBackWarps) {
+      const int j = n - 3 - 2 * q;
+      const double* uj = Wm + (long long)j * n;          // valid from row j + 1
+      const double* um = Wm + (long long)(j - 1) * n;    // valid from row j
+      double sc = 0.0;
+      for (int i = j + 1 + lane; i < n; i += 32) sc = fma(um[i], uj[i], sc);
+      sc = warp_sum_d(sc);
+      if (lane == 0) cs[q] = (T)sc;
+    }
+    __syncthreads();
+    int j = n - 3;
+    for (; j >= 1; j -= 2) {
+      const T tj = taus[j], tm = taus[j - 1];
+      if (tj == (T)0 && tm == (T)0) continue;   // uniform: both H = I
+      const double* uj = Wm + (long long)j * n;
+      const double* um = Wm + (long long)(j - 1) * n;
+      const int i0 = j + ((warp - j) & (kBackWarps - 1));   // this warp's first row >= j
+      T pj = 0, pm = 0;
+      for (int i = i0; i < n; i += kBackWarps) {
+        const T z = zs[i * kP + lane];
+        const T vj = i > j ? (T)uj[i] : (T)0;
+        pj = fma(vj, z, pj);
+        pm = fma((T)um[i], z, pm);
+      }
+      red[warp * kBackCols + lane] = pj;
+      red[(kBackWarps + warp) * kBackCols + lane] = pm;
+      __syncthreads();
+      if (warp == 0) {
+        T sj = red[lane], sm = red[kBackWarps * kBackCols + lane];
+#pragma unroll
+        for (int q = 1; q < kBackWarps; ++q) {
+          sj += red[q * kBackCols + lane];
+          sm += red[(kBackWarps + q) * kBackCols + lane];
+        }
+        const T a = tj * sj;
+        dotv[lane] = a;
+        dotv[kBackCols + lane] = tm * (sm - cs[(n - 3 - j) >> 1] * a);
+      }
+      __syncthreads();
+      const T a = dotv[lane], b = dotv[kBackCols + lane];
+      for (int i = i0; i < n; i += kBackWarps) {
+        T* zp = zs + i * kP + lane;
+        const T vj = i > j ? (T)uj[i] : (T)0;
+        *zp = fma(-b, (T)um[i], fma(-a, vj, *zp));
+      }
+    }
+    jstart = j;   // 0 when one reflector is left, else -1
+  }
   __syncthreads();
   int par = 0;   // parity of the reflectors applied so far (tau == 0 ones are skipped)
-  for (int j = n - 3; j >= 0; --j) {
+  for (int j = jstart; j >= 0; --j) {
     const T tau = taus[j];
     if (tau == (T)0) continue;
     const double* ug = Wm + (long long)j * n;
@@ -933,7 +991,7 @@ static int hh_optin_smem() {
 }
 
 size_t hh_back_smem_bytes(int n) {
-  return ((size_t)n * (kBackCols + 1) + kBackWarps * kBackCols + kBackCols + 3 * n) * sizeof(double);
+  return ((size_t)n * (kBackCols + 1) + 2 * kBackWarps * kBackCols + 2 * kBackCols + 3 * n) * sizeof(double);
 }
 
 int hh_back_max_n() {
