@@ -1,12 +1,15 @@
 // Drives the C++ host layer (include/nddo_electronic_structure.hpp) the way
 // MolDS's main drives an ElectronicStructure (src/base/MolDS.cpp:165-178):
 // SetMolecule, DoSCF, then the getters.  Input file: the theory number, then
-// one atom per line "Z x y z" in bohr.  Optional arguments: max_iter
+// one atom per line "Z x y z" in bohr, and environmental point charges as
+// lines "epc x y z q" (bohr, charge).  Optional arguments: max_iter
 // rms_density damping_thresh damping_weight diis_num_error_vect
 // diis_start_error diis_end_error.  Exit code 3 when the engine throws.
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <sstream>
+#include <string>
 
 #include "nddo_electronic_structure.hpp"
 
@@ -20,10 +23,18 @@ int main(int argc, char** argv) {
   int theory = 0;
   in >> theory;
   molds_gb300::Molecule mol;
-  int z;
-  double x, y, w;
-  while (in >> z >> x >> y >> w) {
-    mol.atomicNumbers.push_back(z);
+  std::string line;
+  while (std::getline(in, line)) {
+    std::istringstream ls(line);
+    std::string head;
+    if (!(ls >> head)) continue;
+    double x, y, w, q;
+    if (head == "epc") {
+      if (ls >> x >> y >> w >> q) mol.epcs.insert(mol.epcs.end(), {x, y, w, q});
+      continue;
+    }
+    if (!(ls >> x >> y >> w)) continue;
+    mol.atomicNumbers.push_back(std::atoi(head.c_str()));
     mol.xyz.push_back(x);
     mol.xyz.push_back(y);
     mol.xyz.push_back(w);
@@ -45,6 +56,7 @@ int main(int argc, char** argv) {
     std::printf("energy %.15e\n", es.GetElectronicEnergy(0));
     std::printf("core_repulsion %.15e\n", es.GetCoreRepulsionEnergy());
     std::printf("vdw %.15e\n", es.GetVdWCorrectionEnergy());
+    std::printf("core_epc %.15e\n", es.GetCoreEpcCoulombEnergy());
     std::printf("iterations %d\n", es.GetIterations());
     const int n = es.GetTotalNumberAOs();
     std::printf("homo %.15e\n", es.GetEnergiesMO()[0]);

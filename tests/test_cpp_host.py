@@ -35,6 +35,8 @@ def _write_molecule(tmp_path, mol):
     p = tmp_path / "mol.txt"
     lines = [str(int(mol.theory))] + [f"{int(z)} {float(x):.17g} {float(y):.17g} {float(w):.17g}"
                                        for z, (x, y, w) in zip(mol.Z, mol.xyz)]
+    if getattr(mol, "epc", None) is not None:
+        lines += [f"epc {x:.17g} {y:.17g} {w:.17g} {q:.17g}" for x, y, w, q in np.asarray(mol.epc, dtype=float)]
     p.write_text("\n".join(lines) + "\n")
     return str(p)
 
@@ -89,3 +91,28 @@ def test_cpp_host_matches_oracle(tmp_path, name):
     assert int(v["excited_state_error"][0]) == -1
     # MolDS's SCF output text, against the reference's own output file
     assert not compare_scf_text(v["scf_text"][0], case["scf_text"], skip_iterations=p.rms_density < 1e-12)
+
+
+@pytest.mark.gpu
+def test_cpp_host_point_charges(tmp_path):
+    """Environmental point charges through Molecule::epcs and
+    GetCoreEpcCoulombEnergy, against the oracle; the SCF text carries the
+    core-EPC lines."""
+    import molds_gb300 as M
+    exe = _program(tmp_path)
+    mol, p = O.parse_input([c for c in FIX if c["name"] == "ch3f_am1"][0]["input"])
+    pc = np.array([[6.0, 1.0, -2.0, -0.834], [-5.5, 3.0, 1.0, 0.417], [0.5, -6.5, 2.5, 0.417]])
+    om = O.make_molecule(mol.theory, mol.Z, mol.xyz, pc)
+    ref = O.scf(om, p)
+    r = subprocess.run([exe, _write_molecule(tmp_path, om)] + _args(p), capture_output=True, text=True)
+    assert r.returncode == 0, (r.stdout, r.stderr)
+    v = _parse(r.stdout)
+    assert abs(float(v["energy"][0]) - ref.energy) < 1e-8
+    assert abs(float(v["core_epc"][0]) - ref.core_epc) < 1e-11
+    assert int(v["iterations"][0]) == ref.iterations
+    q = np.array([float(x) for x in v["charge"]])
+    assert np.max(np.abs(q - ref.charges)) < 1e-6
+    nocc = int(round(O.atom_info(om)[:, 0].sum())) // 2
+    expect = M.format_scf_text(om.theory, om.Z, ref.eps, nocc, ref.trace, ref.energy, ref.core_repulsion,
+                               ref.charges, dipole=ref.dipole, core_epc=ref.core_epc)
+    assert not compare_scf_text(v["scf_text"][0], expect)
