@@ -229,3 +229,29 @@ def test_serving_with_point_charges(ctx):
         assert abs(r["energy"] - ref.energy) < 1e-8
         assert abs(r["core_epc_coulomb"] - ref.core_epc) < 1e-11
         assert np.max(np.abs(r["charges"] - ref.charges)) < 1e-6
+
+
+def test_edge_cases(ctx):
+    """Charges of zero change nothing, bit for bit; a charge on an atom's
+    position, a non-finite charge and a row count that is not a multiple of
+    four are rejected and leave no molecule set."""
+    mol, p = O.parse_input(FIX["c2h6_am1"]["input"])
+    es = M.ElectronicStructure(mol.theory, _params(p), context=ctx)
+    es.SetMolecule(M.Molecule(mol.Z, mol.xyz))
+    es.DoSCF(True)
+    e0, q0 = es.GetElectronicEnergy(0), es.GetMullikenCharges()
+    zero = np.c_[point_charges(mol.xyz, 5, 3)[:, :3], np.zeros(5)]
+    es.SetMolecule(M.Molecule(mol.Z, mol.xyz, zero))
+    es.DoSCF(True)
+    assert es.GetElectronicEnergy(0) == e0 and es.GetCoreEpcCoulombEnergy() == 0.0
+    assert np.array_equal(es.GetMullikenCharges(), q0)
+    for bad in (np.c_[mol.xyz[1:2], [0.3]], np.array([[5.0, 5.0, 5.0, np.nan]])):
+        with pytest.raises(M.NddoError):
+            es.SetMolecule(M.Molecule(mol.Z, mol.xyz, bad))
+        with pytest.raises(M.NddoError):
+            es.DoSCF(True)   # no molecule is set after a rejected one
+    Z = np.ascontiguousarray(mol.Z, dtype=np.int32)
+    xyz = np.ascontiguousarray(mol.xyz, dtype=np.float64)
+    rc = ctx.lib.nddo_set_molecule_epc(ctx.h, mol.theory, int(Z.size), Z.ctypes.data_as(M._IP),
+                                       xyz.ctypes.data_as(M._DP), -1, None)
+    assert rc == M.ERR_ARGUMENT
