@@ -46,6 +46,7 @@ namespace nddo {
 constexpr int kHhMaxThreads = 1024;   // the CTA size comes from the tuning table (256, 512 or 1024)
 constexpr int kVecThreads = 32;   // one warp: 16 lane pairs, 16 eigenpairs per CTA
 constexpr int kOrthThreads = 256;
+constexpr size_t kOrthStaticSmem = (1024 + kOrthThreads / 32 + 1) * sizeof(double) + 1024;   // and some slack
 constexpr int kBackCols = 32, kBackWarps = 8;
 
 size_t hh_tridiag_smem_bytes(int n, bool a_in_smem) {
@@ -720,11 +721,15 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
 
 // Re-orthogonalisation inside clusters of close eigenvalues: for each vector j
 // of a cluster, z_j <- z_j - sum_{l<j} <z_l, z_j> z_l twice (classical
-// Gram-Schmidt applied twice), then normalised.  One CTA per molecule.
+// Gram-Schmidt applied twice), then normalised.  One CTA per molecule.  When
+// the launch's shared memory holds the molecule's vectors (stage_pitch > 0)
+// and the molecule has a cluster, they are copied there first (row pitch
+// k + 1: column accesses free of bank conflicts) and back at the end.
 __global__ void __launch_bounds__(kOrthThreads)
 tri_orth_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, const MolState* __restrict__ st,
                 int require_active, int final_pass, const double* __restrict__ td, long long vstride,
-                const double* __restrict__ eps, double* __restrict__ Z) {
+                const double* __restrict__ eps, double* __restrict__ Z, int stage) {
+  extern __shared__ __align__(16) double zsm[];
   __shared__ double dots[1024];
   __shared__ double red[kOrthThreads / 32];
   __shared__ double onenrm_s;
@@ -756,6 +761,17 @@ tri_orth_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, c
   const double ortol = 1e-3 * onenrm_s;
   const double* ev = eps + mol.vec0 + lo;
   double* Zm = Z + mol.mat0;
+  bool any = false;   // a pair of neighbours closer than ortol: some cluster to treat
+  for (int c = 1 + tid; c < k; c += kOrthThreads) any = any || (ev[c] - ev[c - 1] < ortol);
+  if (!__syncthreads_or(any)) return;
+  double* Zw = Zm;
+  long long ld = k;
+  if (stage) {
+    Zw = zsm;
+    ld = k + 1;
+    for (long long t = tid; t < (long long)n * k; t += kOrthThreads) zsm[(t / k) * ld + t % k] = Zm[t];
+    __syncthreads();
+  }
   int c0 = 0;
   while (c0 < k) {
     int c1 = c0 + 1;
@@ -770,33 +786,35 @@ tri_orth_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list, c
             for (int q = warp; q < cnt; q += nwarps) {
               const int l = c0 + l0 + q;
               double s = 0.0;
-              for (int i = lane; i < n; i += 32) s = fma(Zm[(long long)i * k + l], Zm[(long long)i * k + j], s);
+              for (int i = lane; i < n; i += 32) s = fma(Zw[(long long)i * ld + l], Zw[(long long)i * ld + j], s);
               s = warp_sum_d(s);
               if (lane == 0) dots[q] = s;
             }
             __syncthreads();
             for (int i = tid; i < n; i += kOrthThreads) {
-              double zj = Zm[(long long)i * k + j];
-              for (int q = 0; q < cnt; ++q) zj = fma(-dots[q], Zm[(long long)i * k + c0 + l0 + q], zj);
-              Zm[(long long)i * k + j] = zj;
+              double zj = Zw[(long long)i * ld + j];
+              for (int q = 0; q < cnt; ++q) zj = fma(-dots[q], Zw[(long long)i * ld + c0 + l0 + q], zj);
+              Zw[(long long)i * ld + j] = zj;
             }
             __syncthreads();
           }
         }
         double s = 0.0;
-        for (int i = tid; i < n; i += kOrthThreads) { const double z = Zm[(long long)i * k + j]; s = fma(z, z, s); }
+        for (int i = tid; i < n; i += kOrthThreads) { const double z = Zw[(long long)i * ld + j]; s = fma(z, z, s); }
         s = warp_sum_d(s);
         if (lane == 0) red[warp] = s;
         __syncthreads();
         double tot = 0.0;
         for (int w = 0; w < nwarps; ++w) tot += red[w];
         const double r = tot > 0.0 ? rsqrt(tot) : 0.0;
-        for (int i = tid; i < n; i += kOrthThreads) Zm[(long long)i * k + j] *= r;
+        for (int i = tid; i < n; i += kOrthThreads) Zw[(long long)i * ld + j] *= r;
         __syncthreads();
       }
     }
     c0 = c1;
   }
+  if (stage)
+    for (long long t = tid; t < (long long)n * k; t += kOrthThreads) Zm[t] = zsm[(t / k) * ld + t % k];
 }
 
 // X = Q Z with Q = H_0 H_1 ... H_{n-3}: H_{n-3} is applied first.  CTA = 32
@@ -968,6 +986,8 @@ static void hh_set_attributes() {
     cudaFuncSetAttribute(hh_back_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaFuncSetAttribute(hh_back_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     cudaFuncSetAttribute(tri_vectors_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncSetAttribute(tri_orth_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         optin - (int)kOrthStaticSmem);
   });
 }
 
@@ -1046,7 +1066,11 @@ void launch_hh_vectors(const DevMol* mols, const int* list, int nlist, int max_n
                        cudaStream_t s) {
   if (nlist <= 0 || max_k <= 0) return;
   launch_tri_vectors(mols, list, nlist, max_n, max_k, st, require_active, final_pass, td, vstride, eps, Z, S4, s);
-  tri_orth_kernel<<<nlist, kOrthThreads, 0, s>>>(mols, list, st, require_active, final_pass, td, vstride, eps, Z);
+  // the vectors of the launch's largest molecule in shared memory when they fit
+  const size_t osh = (size_t)max_n * (max_k + 1) * sizeof(double);
+  const int stage = osh + kOrthStaticSmem <= (size_t)hh_optin_smem() ? 1 : 0;
+  tri_orth_kernel<<<nlist, kOrthThreads, stage ? osh : 0, s>>>(mols, list, st, require_active, final_pass, td,
+                                                                vstride, eps, Z, stage);
   dim3 gb(nlist, (max_k + kBackCols - 1) / kBackCols);
   // mixed precision: FP32 back-transformation for molecules still in the FP32 phase
   const int fp64_phase = (mixed && !final_pass) ? 1 : -1;
