@@ -722,7 +722,7 @@ tri_vectors_kernel(const DevMol* __restrict__ mols, const int* __restrict__ list
 // Re-orthogonalisation inside clusters of close eigenvalues: for each vector j
 // of a cluster, z_j <- z_j - sum_{l<j} <z_l, z_j> z_l twice (classical
 // Gram-Schmidt applied twice), then normalised.  One CTA per molecule.  When
-// the launch's shared memory holds the molecule's vectors (stage_pitch > 0)
+// the launch's shared memory holds the molecule's vectors (stage != 0)
 // and the molecule has a cluster, they are copied there first (row pitch
 // k + 1: column accesses free of bank conflicts) and back at the end.
 __global__ void __launch_bounds__(kOrthThreads)
