@@ -600,6 +600,15 @@ int oracle_atom_info(int theory, int natoms, const int* Z, double* out) {
   return 0;
 }
 
+/* Charge separations D_0..D_2 and additive terms rho_0..rho_2 of one
+ * element's multipoles (out[0..5]), as the pair integrals use them. */
+int oracle_multipole_params(int theory, int Z, double* out) {
+  oracle_atom p;
+  if (oracle_fill(theory, Z, &p) != 0) return -1;
+  for (int l = 0; l < 3; ++l) { out[l] = p.d[l]; out[3 + l] = p.rho[l]; }
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Cartesian (dipole) matrix <mu| r_k |nu> by the STO-6G expansion           */
 /* ------------------------------------------------------------------------ */

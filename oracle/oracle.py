@@ -84,6 +84,7 @@ def lib():
             L.oracle_num_aos.argtypes = [ctypes.c_int, ctypes.c_int, ip]
             L.oracle_integrals.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp, dp, dp]
             L.oracle_epc.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, ctypes.c_int, dp, dp, dp]
+            L.oracle_multipole_params.argtypes = [ctypes.c_int, ctypes.c_int, dp]
             L.oracle_fock.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp, dp, ctypes.c_int, dp]
             L.oracle_atom_info.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp]
             L.oracle_cartesian.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, dp]
@@ -173,6 +174,16 @@ def make_molecule(theory, Z, xyz_bohr, epc=None) -> Molecule:
         epc = epc if epc.shape[0] else None
     return Molecule(int(theory), np.ascontiguousarray(Z, dtype=np.int32),
                     np.ascontiguousarray(xyz_bohr, dtype=np.float64).reshape(-1, 3), epc)
+
+
+def multipole_params(theory, Z):
+    """(D_0, D_1, D_2, rho_0, rho_1, rho_2) of one element [bohr]."""
+    if isinstance(theory, str):
+        theory = THEORIES[theory.lower()]
+    out = np.zeros(6)
+    if lib().oracle_multipole_params(int(theory), int(Z), _dp(out)) != 0:
+        raise ValueError("element without NDDO parameters")
+    return out
 
 
 def epc_terms(mol: Molecule):

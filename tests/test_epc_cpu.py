@@ -138,3 +138,43 @@ def test_output_lines(built, vdw):
     plain = M.format_scf_text("pm3", Z, ref.eps, 4, ref.trace, ref.energy, ref.core_repulsion, ref.charges,
                               dipole=ref.dipole, vdw=vdw, vdw_energy=ref.vdw_energy)
     assert "EPC" not in plain
+
+
+@pytest.mark.parametrize("theory", ["mndo", "am1", "pm3", "pm3/pddg"])
+@pytest.mark.parametrize("Z", [6, 7, 8, 9, 16, 17])
+def test_blocks_are_the_point_charge_model(theory, Z):
+    """An independent restatement of the atom-charge block: MNDO's point-charge
+    model of each orbital product (Dewar & Thiel 1977) with rho = 0 seen from
+    a bare charge q on the local z axis at distance R -- ss a unit charge;
+    s p_sigma +-1/2 at +-D_1 along the axis; p p (the monopole and the linear
+    quadrupole) +1/2 at the centre and +1/4 at +-2 D_2 along the p axis --
+    rotated into the space frame: (s s|ss) = s0, (s p_i|ss) = s10 u_i,
+    (p_i p_j|ss) = s3 delta_ij + (s4 - s3) u_i u_j.  The oracle gets the same
+    block through its general multipole case tree and 4-index rotation."""
+    try:
+        d = O.multipole_params(theory, Z)
+    except ValueError:
+        pytest.skip(f"no {theory} parameters for Z = {Z}")
+    D1, D2 = d[1], d[2]
+    rng = np.random.default_rng(Z * 31 + len(theory))
+    for _ in range(5):
+        at = rng.normal(size=3)
+        v = rng.normal(size=3)
+        pc = at + v / np.linalg.norm(v) * rng.uniform(3.0, 12.0)
+        q = rng.uniform(-1.0, 1.0)
+        V, e = O.epc_terms(O.make_molecule(theory, [Z], at[None, :], [[*pc, q]]))
+        R = float(np.linalg.norm(pc - at))
+        u = (pc - at) / R
+        s0 = 1.0 / R
+        s10 = 0.5 / (R - D1) - 0.5 / (R + D1)
+        s3 = 0.5 / R + 0.5 / np.sqrt(R * R + 4.0 * D2 * D2)          # p_pi p_pi
+        s4 = 0.5 / R + 0.25 / (R - 2.0 * D2) + 0.25 / (R + 2.0 * D2)  # p_sigma p_sigma
+        uo = np.array([0.0, u[1], u[2], u[0]])                        # orbital order s, py, pz, px
+        ref = np.zeros((4, 4))
+        ref[0, 0] = s0
+        for i in range(1, 4):
+            ref[0, i] = ref[i, 0] = s10 * uo[i]
+            for j in range(1, 4):
+                ref[i, j] = (s3 if i == j else 0.0) + (s4 - s3) * uo[i] * uo[j]
+        assert np.max(np.abs(V - (-q) * ref)) < 1e-14 * max(1.0, abs(q) / R)
+        assert abs(e - O.atom_info(O.make_molecule(theory, [Z], at[None, :]))[0, 0] * q / R) < 1e-15
