@@ -7,7 +7,8 @@ import pytest
 import molds_gb300 as M
 
 
-def test_missing_library_raises(tmp_path):
+def test_missing_library_raises(tmp_path, monkeypatch):
+    monkeypatch.setattr(M, "_lib", None)   # another test may have loaded the built library already
     with pytest.raises(ImportError, match="no CPU fallback"):
         M.load_library(str(tmp_path / "libnddo_gb300.so"))
 
